@@ -1,0 +1,381 @@
+#!/usr/bin/env python3
+"""Throughput of the FFTCC-seeded first-order IC-GN path on one GB300.
+
+Workload (one step = one image pair solved end to end): 2048x2048 u8 synthetic speckle, the
+target warped by a smooth field (8 Gaussian bumps per component, |u|,|v| up to ~10 px,
+local strain up to 2 %, noise 2 DN); subset radius 15, POI grid step 4 with margin r+2
+(254 016 POIs).  A step runs reference prep (float plane, Gradient2D4 planes, per-POI
+mean/norm/inverse Hessian), target prep (B-spline table), FFTCC and IC-GN.
+
+value  = POIs / device time per step, inputs resident in HBM (dic_run_device), L2 flushed
+         (256 MB write) before every timed step, CUDA events on the engine stream.
+e2e    = the same through the C ABI with host buffers (dic_set_ref / dic_set_tar /
+         dic_process_pair): pinned host images and POI queue copied in, results copied out.
+--impl reference: the reference's CPU path (the oracle restatement, all host threads).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = {"name": "pair2048_bumps_r15_step4", "width": 2048, "height": 2048, "radius": 15, "step": 4,
+            "seed": 4, "conv": 0.001, "max_iter": 10}
+CPU_SAMPLE_STRIDE = 64          # every 64th POI of the queue for the CPU timings
+L2_FLUSH_BYTES = 256 << 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def load_pair():
+    """The synthetic pair, cached per process tree under $DIC_BENCH_CACHE (default /tmp)."""
+    from fasticgn_gb300 import speckle
+    cache = Path(os.environ.get("DIC_BENCH_CACHE", "/tmp")) / f"gb300_dic_{WORKLOAD['name']}_v1.npz"
+    if cache.exists():
+        d = np.load(cache)
+        return d["ref"], d["tar"]
+    t = time.time()
+    pr = speckle.pair_bumps(seed=WORKLOAD["seed"], width=WORKLOAD["width"], height=WORKLOAD["height"])
+    log(f"generated workload in {time.time() - t:.1f} s")
+    try:
+        tmp = cache.with_suffix(f".tmp{os.getpid()}.npz")
+        np.savez(tmp, ref=pr.ref, tar=pr.tar)
+        os.replace(tmp, cache)
+    except OSError:
+        pass
+    return pr.ref, pr.tar
+
+
+def grid():
+    from fasticgn_gb300 import grid_queue
+    return grid_queue(WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["radius"], WORKLOAD["step"])
+
+
+# ------------------------------------------------------------------------------ CPU legs
+
+def cpu_pair_time(ref, tar, threads):
+    """Reference CPU path on a bounded sample: full-image prep + FFTCC/IC-GN on every 64th POI.
+    Returns (POIs/s extrapolated to the whole queue, detail dict, sample results)."""
+    from oracle import oracle as O
+    w, h, r = WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["radius"]
+    reff, tarf = ref.astype(np.float32), tar.astype(np.float32)
+    pois = O.grid_pois(w, h, r, WORKLOAD["step"])
+    total = len(pois)
+    sample = np.ascontiguousarray(pois[::CPU_SAMPLE_STRIDE])
+    t0 = time.perf_counter()
+    gx, gy = O.gradient(reff, threads)
+    coef = O.bspline_prepare(tarf, threads)
+    t1 = time.perf_counter()
+    O.fftcc2d(reff, tarf, sample, r, threads)
+    t2 = time.perf_counter()
+    O.icgn2d1(reff, gx, gy, coef, sample, r, WORKLOAD["conv"], WORKLOAD["max_iter"], threads)
+    t3 = time.perf_counter()
+    per_poi = (t3 - t1) / len(sample)
+    pair_s = (t1 - t0) + per_poi * total
+    detail = {"prep_s": t1 - t0, "fftcc_s_per_poi": (t2 - t1) / len(sample),
+              "icgn_s_per_poi": (t3 - t2) / len(sample), "sample_pois": len(sample), "pair_s": pair_s}
+    return total / pair_s, detail, sample
+
+
+def run_reference(args):
+    from oracle import oracle as O
+    threads = O.default_threads()
+    ref, tar = load_pair()
+    for _ in range(args.warmup):
+        cpu_pair_time(ref, tar, threads)
+    vals, pair_s = [], []
+    for _ in range(args.steps):
+        v, d, _ = cpu_pair_time(ref, tar, threads)
+        vals.append(v)
+        pair_s.append(d["pair_s"])
+    value = float(np.mean(vals))
+    sample = (f"full-image gradient + B-spline table, then FFTCC + IC-GN on every {CPU_SAMPLE_STRIDE}th POI "
+              f"({d['sample_pois']} of {len(grid())}), extrapolated to the whole queue; own FFT, not FFTW")
+    line = {"impl": "reference", "metric": "POIs/s", "value": value, "unit": "POI/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(pair_s)),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_block(),
+            "cpu_baseline": {"value": value, "unit": "POI/s", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "POI/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_block():
+    return {"workload": WORKLOAD["name"], "image": f"{WORKLOAD['width']}x{WORKLOAD['height']} u8 speckle",
+            "field": "8 Gaussian bumps per component, |u|,|v| <= ~10 px, strain <= 2 %, noise 2 DN",
+            "subset_radius": WORKLOAD["radius"], "poi_step": WORKLOAD["step"], "pois": len(grid()),
+            "seed_method": "FFTCC", "conv_criterion": WORKLOAD["conv"], "max_iteration": WORKLOAD["max_iter"],
+            "l2": "flushed before every timed step (256 MB device write, untimed)",
+            "step": "ref prep + per-POI prep + target B-spline table + FFTCC + IC-GN"}
+
+
+# ------------------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------ GPU arm
+
+def measured_peak_hbm():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel: str):
+    p = ROOT / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    k = d.get("kernels", {}).get(kernel)
+    if not k or d.get("workload") != WORKLOAD["name"]:
+        return None
+    return float(k["dram_bytes_per_launch"])
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import fasticgn_gb300 as dic
+    from fasticgn_gb300 import _build, _lib
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    _build.build_lib()
+
+    ref, tar = load_pair()
+    W, H, R = WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["radius"]
+    tmpl = grid()
+    P = len(tmpl)
+    dev = torch.device("cuda", local)
+    eng = dic.Engine(R, R, WORKLOAD["conv"], WORKLOAD["max_iter"], device=local)
+    stream = torch.cuda.ExternalStream(eng.stream, device=dev)
+    ref_d = torch.from_numpy(ref).to(dev)
+    tar_d = torch.from_numpy(tar).to(dev)
+    tmpl_d = torch.from_numpy(tmpl.view(np.uint8).copy()).to(dev)
+    work_d = torch.empty_like(tmpl_d)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+    flags = _lib.DIC_RUN_FFTCC | _lib.DIC_RUN_ICGN | _lib.DIC_RUN_PREPARE
+
+    def device_step():
+        with torch.cuda.stream(stream):
+            work_d.copy_(tmpl_d)
+        eng.set_ref_device(ref_d.data_ptr(), W, H, W, _lib.DIC_U8)
+        eng.set_tar_device(tar_d.data_ptr(), W, H, W, _lib.DIC_U8)
+        eng.run_device(work_d.data_ptr(), P, flags)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        device_step()
+    barrier()
+    launches0 = eng.stats()["kernel_launches"]
+    times, kern = [], {k: [] for k in ("ms_prepare_ref", "ms_poi_prepare", "ms_prepare_tar", "ms_fftcc", "ms_icgn")}
+    iters = []
+    with ClockSampler(local) as clk:
+        for _ in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.random_(0, 255)           # untimed L2 flush
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+            device_step()
+            with torch.cuda.stream(stream):
+                e.record(stream)
+            e.synchronize()
+            times.append(s.elapsed_time(e))
+            st = eng.stats()
+            for k in kern:
+                kern[k].append(st[k])
+            iters.append(st["icgn_iterations"])
+        barrier()
+    launches = eng.stats()["kernel_launches"] - launches0
+    step_ms = float(np.sum(times)) / args.steps
+    max_ms = step_ms
+    if world > 1:
+        t = torch.tensor([step_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        max_ms = float(t.item())
+    value = world * P / (max_ms * 1e-3)
+    result_dev = work_d.cpu().numpy().view(dic.POI_DTYPE)
+
+    # ---- e2e through the host C ABI (pinned host buffers)
+    ref_h = torch.from_numpy(ref).pin_memory()
+    tar_h = torch.from_numpy(tar).pin_memory()
+    q_h = torch.from_numpy(tmpl.view(np.uint8).copy()).pin_memory()
+    q_np = q_h.numpy().view(dic.POI_DTYPE)
+    tmpl_bytes = tmpl.view(np.uint8)
+
+    def e2e_step():
+        eng.set_ref(ref_h.numpy())
+        eng.set_tar(tar_h.numpy())
+        eng.process_pair(q_np)
+
+    for _ in range(max(1, args.warmup)):
+        q_h.numpy()[:] = tmpl_bytes
+        e2e_step()
+    e2e_times = []
+    for _ in range(args.steps):
+        q_h.numpy()[:] = tmpl_bytes          # the caller's fresh POI queue (untimed)
+        with torch.cuda.stream(stream):
+            flush.random_(0, 255)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        e2e_step()
+        e.record(stream)
+        e.synchronize()
+        e2e_times.append(s.elapsed_time(e))
+    e2e_ms = float(np.mean(e2e_times))
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    assert q_np.tobytes() == result_dev.tobytes(), "host and device entry points disagree"
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # ---- roofline of the dominant kernel (IC-GN gather model, SURVEY-style algorithmic bytes)
+    N = (2 * R + 1) ** 2
+    it_sum = float(np.mean(iters))
+    icgn_ms = float(np.mean(kern["ms_icgn"]))
+    alg_bytes = 64.0 * N * it_sum + P * (12.0 * N + 144 + 8 + 32 + 40)
+    peak, peak_kind = measured_peak_hbm()
+    achieved = alg_bytes / (icgn_ms * 1e-3) / 1e9
+    traffic = profiled_traffic("k_icgn")
+    roofline = {"kernel": "k_icgn", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg_bytes,
+                "model": "64 B B-spline texel per warped sample per iteration + 12 B ref/grad per sample "
+                         "+ 224 B per-POI record/IO"}
+
+    # ---- CPU baseline on a bounded sample, and parity of the GPU result on that sample
+    from oracle import oracle as O
+    threads = O.default_threads()
+    cpu_value, cpu_detail, cpu_sample = cpu_pair_time(ref, tar, threads)
+    g = result_dev[::CPU_SAMPLE_STRIDE]
+    cz, gz = cpu_sample["r"][:, O.R_ZNCC], g["zncc"]
+    both = (cz >= 0) & (gz >= 0) & np.isfinite(cz) & np.isfinite(gz)
+    du = np.abs(cpu_sample["p"][both, O.P_U] - g["u"][both])
+    dv = np.abs(cpu_sample["p"][both, O.P_V] - g["v"][both])
+    parity = {"sample_pois": int(len(g)), "shared_valid": int(both.sum()),
+              "median_du": float(np.median(du)), "median_dv": float(np.median(dv)),
+              "p99_du": float(np.quantile(du, 0.99)), "p99_dv": float(np.quantile(dv, 0.99)),
+              "max_du": float(du.max()), "max_dv": float(dv.max()),
+              "flag_agreement": float(np.mean(np.where(cz < 0, cz, 0) == np.where(gz < 0, gz, 0)))}
+    ok = result_dev["zncc"] >= 0
+    h2d = ref.nbytes + tar.nbytes + tmpl.nbytes
+    line = {
+        "metric": "POIs/s", "value": value, "unit": "POI/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": max_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_block(),
+        "frames_per_s": world * 1e3 / max_ms,
+        "e2e": {"value": world * P / (e2e_ms * 1e-3), "unit": "POI/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(tmpl.nbytes)},
+        "roofline": roofline,
+        "cpu_baseline": {"value": cpu_value, "unit": "POI/s", "cores": threads, "kind": "port",
+                         "sample": f"full-image prep + FFTCC/IC-GN on every {CPU_SAMPLE_STRIDE}th POI "
+                                   f"({cpu_detail['sample_pois']} POIs), extrapolated; own FFT, not FFTW",
+                         "detail": cpu_detail},
+        "clocks": clk.summary(), "gpu_launches": int(launches),
+        "kernels_ms": {k: float(np.mean(v)) for k, v in kern.items()},
+        "iteration_mean": it_sum / P, "valid_ratio": float(ok.mean()),
+        "parity_vs_cpu": parity,
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,655 @@
+// Host engine behind the C ABI of include/dic.h.
+//
+// One dic_engine owns a CUDA stream and the device state of one reference/target pair
+// (see dic_kernels.cuh for the HBM layout).  Calls are synchronous from the caller's
+// point of view except dic_run_device, which only enqueues work on the engine stream.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <set>
+#include <string>
+#include <vector>
+#include <algorithm>
+
+#include "dic_kernels.cuh"
+
+using namespace dic;
+
+namespace
+{
+
+const char* kVersion = "gb300-dic 0.1.0 (sm_103a)";
+
+struct DicError
+{
+  int code;
+  std::string msg;
+};
+
+#define DIC_CUDA(call)                                                                         \
+  do                                                                                           \
+  {                                                                                            \
+    cudaError_t e_ = (call);                                                                   \
+    if (e_ != cudaSuccess)                                                                     \
+      throw DicError{DIC_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};         \
+  } while (0)
+
+int dtype_size(int dtype)
+{
+  switch (dtype)
+  {
+    case DIC_U8: return 1;
+    case DIC_U16: return 2;
+    case DIC_F32: return 4;
+    default: return 0;
+  }
+}
+
+template <typename T>
+struct DevBuf
+{
+  T* ptr = nullptr;
+  size_t cap = 0;  // elements
+  void ensure(size_t n)
+  {
+    if (n <= cap) return;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+    cudaError_t e = cudaMalloc(&ptr, std::max<size_t>(n, 1) * sizeof(T));
+    if (e != cudaSuccess)
+    {
+      ptr = nullptr;
+      throw DicError{DIC_ERR_MEMORY, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+    }
+    cap = n;
+  }
+  void release()
+  {
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    cap = 0;
+  }
+};
+
+std::mutex g_init_mutex;
+std::set<int> g_initialized_devices;
+
+void init_constants(int device)
+{
+  std::lock_guard<std::mutex> lock(g_init_mutex);
+  if (g_initialized_devices.count(device)) return;
+  const float bc[4][4] = DIC_BC_MATRIX;
+  float bc2[256];
+  for (int k = 0; k < 4; ++k)
+    for (int l = 0; l < 4; ++l)
+      for (int m = 0; m < 4; ++m)
+        for (int n = 0; n < 4; ++n) bc2[((k * 4 + l) * 4 + m) * 4 + n] = bc[l][m] * bc[k][n];
+  std::vector<float2> tw(kTwiddleCount);
+  for (int N = 2; N <= kMaxTwiddleN; ++N)
+    for (int k = 0; k < N; ++k)
+    {
+      const double a = -2.0 * M_PI * (double)k / (double)N;
+      tw[tw_offset(N) + k] = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+  DIC_CUDA(cudaMemcpyToSymbol(c_bc2, bc2, sizeof(bc2)));
+  DIC_CUDA(cudaMemcpyToSymbol(c_tw, tw.data(), sizeof(float2) * tw.size()));
+  g_initialized_devices.insert(device);
+}
+
+enum Phase { kPhRef = 0, kPhPoi, kPhTar, kPhFftcc, kPhIcgn, kPhCount };
+
+}  // namespace
+
+struct dic_engine
+{
+  dic_config cfg{};
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+
+  int w = 0, h = 0;
+  int ref_dtype = 0, tar_dtype = 0;
+  bool ref_set = false, tar_set = false;
+  bool ref_dirty = true, tar_dirty = true;
+  DevBuf<unsigned char> raw_ref, raw_tar;
+  DevBuf<float> ref_f32, tar_f32;
+  DevBuf<float4> ref_pack, coef;
+
+  // prepared layout
+  std::vector<int> layout_x, layout_y;   // host copy of a host-defined layout
+  bool layout_ready = false;
+  int64_t layout_count = 0;
+  DevBuf<PoiRef> poi_ref;
+  DevBuf<dic_poi> queue;
+  DevBuf<int64_t> slots;
+  DevBuf<unsigned long long> counters;
+
+  bool timing = true;
+  cudaEvent_t ev[kPhCount][2] = {};
+  bool ev_pending[kPhCount] = {};
+  double ms[kPhCount] = {};
+  long long launches = 0;
+  long long icgn_pois = 0;
+  bool iter_pending = false;
+  unsigned long long iter_sum = 0;
+
+  void check_launch(const char* what)
+  {
+    ++launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw DicError{DIC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+  }
+  void mark(int ph, int which)
+  {
+    if (!timing) return;
+    DIC_CUDA(cudaEventRecord(ev[ph][which], stream));
+    if (which == 1) ev_pending[ph] = true;
+  }
+  void harvest()
+  {
+    for (int p = 0; p < kPhCount; ++p)
+      if (ev_pending[p])
+      {
+        float t = 0.f;
+        DIC_CUDA(cudaEventSynchronize(ev[p][1]));
+        DIC_CUDA(cudaEventElapsedTime(&t, ev[p][0], ev[p][1]));
+        ms[p] = t;
+        ev_pending[p] = false;
+      }
+    if (iter_pending)
+    {
+      DIC_CUDA(cudaMemcpyAsync(&iter_sum, counters.ptr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
+      DIC_CUDA(cudaStreamSynchronize(stream));
+      iter_pending = false;
+    }
+  }
+
+  // ---------------------------------------------------------------- images
+  void set_image(bool is_ref, const void* px, int width, int height, int64_t stride, int dtype, bool device)
+  {
+    const int es = dtype_size(dtype);
+    if (!px || es == 0 || width < 5 || height < 5)
+      throw DicError{DIC_ERR_ARGUMENT, "image: null pixels, unknown dtype or size below 5x5"};
+    if (stride < (int64_t)width * es) throw DicError{DIC_ERR_ARGUMENT, "image: row stride smaller than a row"};
+    const bool other_set = is_ref ? tar_set : ref_set;
+    if (other_set && (width != w || height != h))
+    {
+      // A new size invalidates the other image; the caller must set it again.
+      if (is_ref) tar_set = false; else ref_set = false;
+    }
+    if (w != width || h != height) layout_ready = false;
+    w = width;
+    h = height;
+    auto& raw = is_ref ? raw_ref : raw_tar;
+    raw.ensure((size_t)width * height * es);
+    DIC_CUDA(cudaMemcpy2DAsync(raw.ptr, (size_t)width * es, px, (size_t)stride, (size_t)width * es, height,
+                               device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, stream));
+    if (is_ref)
+    {
+      ref_dtype = dtype;
+      ref_set = true;
+      ref_dirty = true;
+      layout_ready = false;   // setRefImage invalidates the prepared layout's data
+    }
+    else
+    {
+      tar_dtype = dtype;
+      tar_set = true;
+      tar_dirty = true;
+    }
+  }
+
+  float scale() const { return cfg.input_scale == 0.f ? 1.f : cfg.input_scale; }
+
+  template <typename T>
+  void launch_prepare_ref()
+  {
+    dim3 grid((w + kPrepTile - 1) / kPrepTile, (h + kPrepTile - 1) / kPrepTile);
+    k_prepare_ref<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_ref.ptr), w, h, scale(),
+                                               ref_f32.ptr, ref_pack.ptr);
+    check_launch("k_prepare_ref");
+  }
+  template <typename T>
+  void launch_prepare_tar()
+  {
+    dim3 grid((w + kPrepTile - 1) / kPrepTile, (h + kPrepTile - 1) / kPrepTile);
+    k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_tar.ptr), w, h, scale(),
+                                               tar_f32.ptr, coef.ptr);
+    check_launch("k_prepare_tar");
+  }
+
+  void ensure_ref()
+  {
+    if (!ref_set) throw DicError{DIC_ERR_STATE, "reference image must be set first"};
+    if (!ref_dirty) return;
+    const size_t px = (size_t)w * h;
+    ref_f32.ensure(px);
+    ref_pack.ensure(px);
+    mark(kPhRef, 0);
+    switch (ref_dtype)
+    {
+      case DIC_U8: launch_prepare_ref<uint8_t>(); break;
+      case DIC_U16: launch_prepare_ref<uint16_t>(); break;
+      default: launch_prepare_ref<float>(); break;
+    }
+    mark(kPhRef, 1);
+    ref_dirty = false;
+  }
+  void ensure_tar()
+  {
+    if (!tar_set) throw DicError{DIC_ERR_STATE, "target image must be set first"};
+    if (!ref_set) throw DicError{DIC_ERR_STATE, "reference image must be set first"};
+    if (!tar_dirty) return;
+    const size_t px = (size_t)w * h;
+    tar_f32.ensure(px);
+    coef.ensure(px * 4);
+    mark(kPhTar, 0);
+    switch (tar_dtype)
+    {
+      case DIC_U8: launch_prepare_tar<uint8_t>(); break;
+      case DIC_U16: launch_prepare_tar<uint16_t>(); break;
+      default: launch_prepare_tar<float>(); break;
+    }
+    mark(kPhTar, 1);
+    tar_dirty = false;
+  }
+
+  // ---------------------------------------------------------------- layout
+  void upload_queue(const dic_poi* pois, int64_t n)
+  {
+    queue.ensure((size_t)n);
+    DIC_CUDA(cudaMemcpyAsync(queue.ptr, pois, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, stream));
+  }
+  void download_queue(dic_poi* pois, int64_t n)
+  {
+    DIC_CUDA(cudaMemcpyAsync(pois, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, stream));
+    DIC_CUDA(cudaStreamSynchronize(stream));
+  }
+  bool layout_matches(const dic_poi* pois, int64_t n) const
+  {
+    if (!layout_ready || (int64_t)layout_x.size() != n) return false;
+    for (int64_t i = 0; i < n; ++i)
+      if (layout_x[i] != (int)pois[i].x || layout_y[i] != (int)pois[i].y) return false;
+    return true;
+  }
+  void record_layout(const dic_poi* pois, int64_t n)
+  {
+    layout_x.resize(n);
+    layout_y.resize(n);
+    for (int64_t i = 0; i < n; ++i)
+    {
+      layout_x[i] = (int)pois[i].x;
+      layout_y[i] = (int)pois[i].y;
+    }
+  }
+  // Per-POI reference data for the POIs currently in `src` (device records).
+  void prepare_layout_device(const dic_poi* src, int64_t n)
+  {
+    ensure_ref();
+    poi_ref.ensure((size_t)std::max<int64_t>(n, 1));
+    if (n > 0)
+    {
+      mark(kPhPoi, 0);
+      const int wpb = 8;
+      const unsigned blocks = (unsigned)((n + wpb - 1) / wpb);
+      k_poi_prepare<<<blocks, wpb * 32, 0, stream>>>(ref_pack.ptr, w, h, src, n, cfg.subset_radius_x,
+                                                     cfg.subset_radius_y, poi_ref.ptr);
+      check_launch("k_poi_prepare");
+      mark(kPhPoi, 1);
+    }
+    layout_ready = true;
+    layout_count = n;
+  }
+
+  // ---------------------------------------------------------------- solvers
+  void run_fftcc(dic_poi* d_pois, int64_t n)
+  {
+    if (n == 0) return;
+    ensure_ref();
+    ensure_tar();
+    FftccParams p{ref_f32.ptr, tar_f32.ptr, d_pois, n, w, h};
+    const int r = cfg.subset_radius_x;
+    const unsigned blocks = (unsigned)((n + 3) / 4);
+    mark(kPhFftcc, 0);
+    switch (2 * r)
+    {
+#define DIC_FFTCC_CASE(M) \
+  case M: k_fftcc<M><<<blocks, 128, 0, stream>>>(p); break;
+      DIC_FFTCC_CASE(8) DIC_FFTCC_CASE(10) DIC_FFTCC_CASE(12) DIC_FFTCC_CASE(14) DIC_FFTCC_CASE(16)
+      DIC_FFTCC_CASE(18) DIC_FFTCC_CASE(20) DIC_FFTCC_CASE(22) DIC_FFTCC_CASE(24) DIC_FFTCC_CASE(26)
+      DIC_FFTCC_CASE(28) DIC_FFTCC_CASE(30) DIC_FFTCC_CASE(32)
+#undef DIC_FFTCC_CASE
+      default:
+      {
+        if (r < 1 || 2 * r > kMaxTwiddleN)
+          throw DicError{DIC_ERR_ARGUMENT, "FFTCC supports subset radius 1..32 on this engine"};
+        const int m = 2 * r;
+        const size_t smem = (size_t)2 * m * (m + 1) * sizeof(float2);
+        DIC_CUDA(cudaFuncSetAttribute(k_fftcc_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_fftcc_large<<<(unsigned)n, 256, smem, stream>>>(p, m);
+      }
+    }
+    check_launch("k_fftcc");
+    mark(kPhFftcc, 1);
+  }
+
+  void run_icgn(dic_poi* d_pois, int64_t n, const int64_t* d_slots)
+  {
+    if (n == 0) return;
+    ensure_ref();
+    ensure_tar();
+    counters.ensure(1);
+    DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
+    IcgnParams p;
+    p.coef = coef.ptr;
+    p.ref_pack = ref_pack.ptr;
+    p.poi_ref = poi_ref.ptr;
+    p.slot = d_slots;
+    p.pois = d_pois;
+    p.n = n;
+    p.w = w;
+    p.h = h;
+    p.rx = cfg.subset_radius_x;
+    p.ry = cfg.subset_radius_y;
+    p.conv = cfg.conv_criterion;
+    p.max_iter = (float)cfg.max_iteration;
+    p.iter_sum = counters.ptr;
+    const int wpb = 8;
+    mark(kPhIcgn, 0);
+    k_icgn<<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, 0, stream>>>(p);
+    check_launch("k_icgn");
+    mark(kPhIcgn, 1);
+    icgn_pois = n;
+    iter_pending = true;
+  }
+
+  // IC-GN on the device queue `queue` whose host copy is `pois`.
+  void icgn_queue(const dic_poi* host_pois, int64_t n)
+  {
+    if (!layout_matches(host_pois, n))
+    {
+      record_layout(host_pois, n);
+      prepare_layout_device(queue.ptr, n);
+    }
+    run_icgn(queue.ptr, n, nullptr);
+  }
+};
+
+namespace
+{
+
+template <typename F>
+int guarded(dic_engine* e, F&& f)
+{
+  if (!e) return DIC_ERR_ARGUMENT;
+  try
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != e->cfg.device) DIC_CUDA(cudaSetDevice(e->cfg.device));
+    f();
+    e->last_error.clear();
+    return DIC_OK;
+  }
+  catch (const DicError& err)
+  {
+    e->last_error = err.msg;
+    return err.code;
+  }
+  catch (const std::exception& ex)
+  {
+    e->last_error = ex.what();
+    return DIC_ERR_MEMORY;
+  }
+}
+
+bool finite_xy(const dic_poi& p) { return std::isfinite(p.x) && std::isfinite(p.y); }
+
+}  // namespace
+
+extern "C" {
+
+const char* dic_version(void) { return kVersion; }
+int32_t dic_abi_version(void) { return DIC_ABI_VERSION; }
+
+int dic_engine_create(const dic_config* config, dic_engine** out)
+{
+  if (!config || !out) return DIC_ERR_ARGUMENT;
+  *out = nullptr;
+  if (config->subset_radius_x < 1 || config->subset_radius_y < 1 || config->max_iteration < 1 ||
+      !(config->conv_criterion >= 0.f))
+    return DIC_ERR_ARGUMENT;
+  dic_engine* e = new (std::nothrow) dic_engine();
+  if (!e) return DIC_ERR_MEMORY;
+  e->cfg = *config;
+  try
+  {
+    DIC_CUDA(cudaSetDevice(config->device));
+    init_constants(config->device);
+    DIC_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    for (int p = 0; p < kPhCount; ++p)
+      for (int k = 0; k < 2; ++k) DIC_CUDA(cudaEventCreate(&e->ev[p][k]));
+  }
+  catch (const DicError& err)
+  {
+    std::fprintf(stderr, "dic_engine_create: %s\n", err.msg.c_str());
+    delete e;
+    return err.code;
+  }
+  *out = e;
+  return DIC_OK;
+}
+
+void dic_engine_destroy(dic_engine* e)
+{
+  if (!e) return;
+  cudaSetDevice(e->cfg.device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  e->raw_ref.release();
+  e->raw_tar.release();
+  e->ref_f32.release();
+  e->tar_f32.release();
+  e->ref_pack.release();
+  e->coef.release();
+  e->poi_ref.release();
+  e->queue.release();
+  e->slots.release();
+  e->counters.release();
+  for (int p = 0; p < kPhCount; ++p)
+    for (int k = 0; k < 2; ++k)
+      if (e->ev[p][k]) cudaEventDestroy(e->ev[p][k]);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+const char* dic_last_error(const dic_engine* e) { return e ? e->last_error.c_str() : "null engine"; }
+void* dic_stream(dic_engine* e) { return e ? (void*)e->stream : nullptr; }
+
+int dic_set_ref(dic_engine* e, const void* px, int32_t w, int32_t h, int64_t stride, int32_t dtype)
+{
+  return guarded(e, [&] { e->set_image(true, px, w, h, stride, dtype, false); });
+}
+int dic_set_tar(dic_engine* e, const void* px, int32_t w, int32_t h, int64_t stride, int32_t dtype)
+{
+  return guarded(e, [&] {
+    if (e->ref_set && (w != e->w || h != e->h))
+      throw DicError{DIC_ERR_ARGUMENT, "reference and target image sizes must match"};
+    e->set_image(false, px, w, h, stride, dtype, false);
+  });
+}
+int dic_set_ref_device(dic_engine* e, const void* px, int32_t w, int32_t h, int64_t stride, int32_t dtype)
+{
+  return guarded(e, [&] { e->set_image(true, px, w, h, stride, dtype, true); });
+}
+int dic_set_tar_device(dic_engine* e, const void* px, int32_t w, int32_t h, int64_t stride, int32_t dtype)
+{
+  return guarded(e, [&] {
+    if (e->ref_set && (w != e->w || h != e->h))
+      throw DicError{DIC_ERR_ARGUMENT, "reference and target image sizes must match"};
+    e->set_image(false, px, w, h, stride, dtype, true);
+  });
+}
+
+int dic_prepare_ref(dic_engine* e, const dic_poi* pois, int64_t n)
+{
+  return guarded(e, [&] {
+    if (n < 0 || (n > 0 && !pois)) throw DicError{DIC_ERR_ARGUMENT, "prepare_ref: bad queue"};
+    for (int64_t i = 0; i < n; ++i)
+      if (!finite_xy(pois[i])) throw DicError{DIC_ERR_ARGUMENT, "prepare_ref: non-finite POI coordinate"};
+    e->ensure_ref();
+    e->record_layout(pois, n);
+    e->upload_queue(pois, n);
+    e->prepare_layout_device(e->queue.ptr, n);
+    DIC_CUDA(cudaStreamSynchronize(e->stream));
+  });
+}
+
+int dic_prepare_tar(dic_engine* e)
+{
+  return guarded(e, [&] {
+    e->ensure_tar();
+    DIC_CUDA(cudaStreamSynchronize(e->stream));
+  });
+}
+
+int dic_fftcc(dic_engine* e, dic_poi* pois, int64_t n, const int64_t* cache_idx)
+{
+  return guarded(e, [&] {
+    if (n < 0 || (n > 0 && !pois)) throw DicError{DIC_ERR_ARGUMENT, "fftcc: bad queue"};
+    if (e->cfg.subset_radius_x != e->cfg.subset_radius_y)
+      throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D supports positive square radii only"};
+    if (!e->ref_set || !e->tar_set) throw DicError{DIC_ERR_STATE, "FFTCC2D images must be set before compute"};
+    if (cache_idx)
+    {
+      // FFTCC2D::compute(queue, cache_indices) checks (src/oc_fftcc.cpp:498-527).
+      if (n == 0) return;
+      if (!e->layout_ready || e->layout_x.empty())
+        throw DicError{DIC_ERR_STATE, "FFTCC2D indexed compute requires a prepared reference layout"};
+      for (int64_t i = 0; i < n; ++i)
+      {
+        const int64_t k = cache_idx[i];
+        if (k < 0 || k >= (int64_t)e->layout_x.size())
+          throw DicError{DIC_ERR_RANGE, "FFTCC2D reference cache index out of range"};
+        if (!finite_xy(pois[i]) || e->layout_x[k] != (int)pois[i].x || e->layout_y[k] != (int)pois[i].y)
+          throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D reference cache index does not match POI coordinates"};
+      }
+    }
+    if (n == 0) return;
+    e->upload_queue(pois, n);
+    e->run_fftcc(e->queue.ptr, n);
+    e->download_queue(pois, n);
+  });
+}
+
+int dic_icgn(dic_engine* e, dic_poi* pois, int64_t n)
+{
+  return guarded(e, [&] {
+    if (n < 0 || (n > 0 && !pois)) throw DicError{DIC_ERR_ARGUMENT, "icgn: bad queue"};
+    if (!e->ref_set || !e->tar_set) throw DicError{DIC_ERR_STATE, "ICGN images must be set before compute"};
+    if (n == 0) return;
+    e->upload_queue(pois, n);
+    e->icgn_queue(pois, n);
+    e->download_queue(pois, n);
+  });
+}
+
+int dic_process_pair(dic_engine* e, dic_poi* pois, int64_t n)
+{
+  return guarded(e, [&] {
+    if (n < 0 || (n > 0 && !pois)) throw DicError{DIC_ERR_ARGUMENT, "process_pair: bad queue"};
+    if (!e->ref_set || !e->tar_set) throw DicError{DIC_ERR_STATE, "images must be set before compute"};
+    if (e->cfg.subset_radius_x != e->cfg.subset_radius_y)
+      throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D supports positive square radii only"};
+    if (n == 0) return;
+    e->upload_queue(pois, n);
+    if (!e->layout_matches(pois, n))
+    {
+      e->record_layout(pois, n);
+      e->prepare_layout_device(e->queue.ptr, n);
+    }
+    e->run_fftcc(e->queue.ptr, n);
+    e->run_icgn(e->queue.ptr, n, nullptr);
+    e->download_queue(pois, n);
+  });
+}
+
+int dic_run_device(dic_engine* e, dic_poi* d_pois, int64_t n, int32_t flags)
+{
+  return guarded(e, [&] {
+    if (n < 0 || (n > 0 && !d_pois)) throw DicError{DIC_ERR_ARGUMENT, "run_device: bad queue"};
+    if (!e->ref_set || !e->tar_set) throw DicError{DIC_ERR_STATE, "images must be set before compute"};
+    if (n == 0) return;
+    // The device queue defines the layout when asked to (DIC_RUN_PREPARE), when no layout of
+    // this size is resident, or when the reference changed; otherwise it is trusted to hold
+    // the resident layout's integer (x, y).  A device-defined layout has no host copy, so
+    // the next host-queue call prepares its own.
+    if ((flags & DIC_RUN_PREPARE) || !e->layout_ready || e->layout_count != n || e->ref_dirty)
+    {
+      e->layout_x.clear();
+      e->layout_y.clear();
+      e->prepare_layout_device(d_pois, n);
+    }
+    if (flags & DIC_RUN_FFTCC) e->run_fftcc(d_pois, n);
+    if (flags & DIC_RUN_ICGN) e->run_icgn(d_pois, n, nullptr);
+  });
+}
+
+int dic_process_frame(dic_engine* e, dic_poi* pois, int64_t n, const dic_poi* prev,
+                      const dic_frame_policy* policy, dic_frame_report* report)
+{
+  (void)prev;
+  (void)policy;
+  (void)report;
+  (void)pois;
+  (void)n;
+  return guarded(e, [&] { throw DicError{DIC_ERR_STATE, "dic_process_frame: not built yet"}; });
+}
+
+int dic_read_plane(dic_engine* e, int32_t plane, void* dst, int64_t bytes)
+{
+  return guarded(e, [&] {
+    if (!dst) throw DicError{DIC_ERR_ARGUMENT, "read_plane: null destination"};
+    const void* src = nullptr;
+    size_t size = 0;
+    const size_t px = (size_t)e->w * e->h;
+    switch (plane)
+    {
+      case DIC_PLANE_REF: e->ensure_ref(); src = e->ref_f32.ptr; size = px * sizeof(float); break;
+      case DIC_PLANE_REF_PACK: e->ensure_ref(); src = e->ref_pack.ptr; size = px * sizeof(float4); break;
+      case DIC_PLANE_TAR: e->ensure_tar(); src = e->tar_f32.ptr; size = px * sizeof(float); break;
+      case DIC_PLANE_TAR_COEF: e->ensure_tar(); src = e->coef.ptr; size = px * 4 * sizeof(float4); break;
+      default: throw DicError{DIC_ERR_ARGUMENT, "read_plane: unknown plane"};
+    }
+    if ((size_t)bytes != size) throw DicError{DIC_ERR_ARGUMENT, "read_plane: size mismatch"};
+    DIC_CUDA(cudaMemcpyAsync(dst, src, size, cudaMemcpyDeviceToHost, e->stream));
+    DIC_CUDA(cudaStreamSynchronize(e->stream));
+  });
+}
+
+int dic_get_stats(const dic_engine* ce, dic_stats* out)
+{
+  dic_engine* e = const_cast<dic_engine*>(ce);
+  if (!out) return DIC_ERR_ARGUMENT;
+  return guarded(e, [&] {
+    e->harvest();
+    out->ms_prepare_ref = e->ms[kPhRef];
+    out->ms_poi_prepare = e->ms[kPhPoi];
+    out->ms_prepare_tar = e->ms[kPhTar];
+    out->ms_fftcc = e->ms[kPhFftcc];
+    out->ms_icgn = e->ms[kPhIcgn];
+    out->kernel_launches = e->launches;
+    out->icgn_pois = e->icgn_pois;
+    out->icgn_iterations = (int64_t)e->iter_sum;
+  });
+}
+
+int dic_set_timing(dic_engine* e, int32_t enabled)
+{
+  return guarded(e, [&] {
+    e->harvest();
+    e->timing = enabled != 0;
+  });
+}
+
+}  // extern "C"

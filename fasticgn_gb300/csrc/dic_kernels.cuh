@@ -1,0 +1,972 @@
+// GB300 (sm_103a) kernels of the FFTCC -> first-order IC-GN path.
+//
+// Data layout in HBM (one engine):
+//   raw_ref, raw_tar   W*H input pixels as uploaded (u8 / u16 / f32)
+//   ref_f32, tar_f32   W*H float grey levels (FFTCC subsets read these)
+//   ref_pack           W*H float4 {ref, gx, gy, 0}: one 16-byte load per IC-GN sample
+//   tar_coef           W*H*16 float BicubicBspline table, 64 B per texel, texel-major
+//   poi_ref            per prepared POI: PoiRef (224 B), resident across frames
+//   queue              dic_poi records (56 B)
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/dic.h"
+
+namespace dic
+{
+
+constexpr int kWarp = 32;
+constexpr unsigned kFull = 0xffffffffu;
+
+// --------------------------------------------------------------------------------------
+// Per-POI reference record, built once per (reference, layout) by k_poi_prepare.
+// The IC-GN kernel evaluates the ZNSSD terms in a single pass over the warped samples:
+// with tau = t - t0 (t0 = reference subset mean), rc = reference zero-mean value and
+// sd = [gx, gx*lx, gx*ly, gy, gy*lx, gy*ly] it accumulates
+//   A0 = sum tau, A1 = sum tau^2, A2 = sum tau*rc, B_i = sum sd_i * tau
+// and recovers the two-pass quantities of src/oc_icgn.cpp:303-322 exactly in algebra:
+//   |t_c|^2 = A1 - A0*m_t, sum t_c rc = A2 - m_t*sum(rc)      (m_t = A0/N),
+//   num_i   = s*(B_i - m_t*S_i) - G_i      with s = |rc| / |t_c|,
+//   S_i = sum sd_i, G_i = sum sd_i*rc  (per-POI constants kept here).
+// The reference-side constants are formed with the same expressions and the same
+// accumulation order as the target-side sums (rn_sq = sum rc^2 - sum(rc)*m_r with
+// m_r = sum(rc)/N, G_i likewise centred), so a target subset equal to the reference subset
+// reproduces s = 1, ZNSSD = 0 and num = 0 bit for bit, as the CPU's two-pass form does.
+// --------------------------------------------------------------------------------------
+struct __align__(16) PoiRef
+{
+  float t0;          // reference subset mean
+  float ref_norm;    // sqrt(rn_sq)
+  float ref_norm_sq; // rn_sq = sum rc^2 - sum(rc) * m_r
+  float sum_rc;      // sum rc (0 up to rounding)
+  float S[6];
+  float G[6];        // sum sd_i*rc - m_r * S_i
+  float inv_h[36];   // row-major inverse Hessian
+  float valid;       // 1 when the reference subset lies inside the image
+  float pad[3];
+};
+static_assert(sizeof(PoiRef) == 224, "PoiRef layout");
+
+// BicubicBspline BC matrix (src/oc_cubic_bspline.h:52-58)
+#define DIC_BC_MATRIX                                                              \
+  {{-144.0f / 336.0f, 384.0f / 336.0f, -384.0f / 336.0f, 144.0f / 336.0f},        \
+   {342.0f / 336.0f, -702.0f / 336.0f, 450.0f / 336.0f, -90.0f / 336.0f},         \
+   {-198.0f / 336.0f, -18.0f / 336.0f, 270.0f / 336.0f, -54.0f / 336.0f},         \
+   {0.0f, 1.0f, 0.0f, 0.0f}}
+
+// Products BC[l][m] * BC[k][n] rounded to float, indexed [k][l][m][n]; filled by the host.
+// (This header is compiled in exactly one translation unit, dic_engine.cu.)
+__constant__ float c_bc2[256];
+// FFT twiddles: W_N^k = exp(-2 pi i k / N) for N in [2, kMaxTwiddleN], at tw_offset(N).
+constexpr int kMaxTwiddleN = 64;
+__host__ __device__ constexpr int tw_offset(int n) { return n * (n - 1) / 2 - 1; }
+constexpr int kTwiddleCount = tw_offset(kMaxTwiddleN + 1);
+__constant__ float2 c_tw[kTwiddleCount];
+
+template <typename T>
+__device__ __forceinline__ float load_px(const T* p, size_t i, float scale);
+template <>
+__device__ __forceinline__ float load_px<uint8_t>(const uint8_t* p, size_t i, float scale)
+{ return scale == 1.0f ? (float)p[i] : (float)p[i] * scale; }
+template <>
+__device__ __forceinline__ float load_px<uint16_t>(const uint16_t* p, size_t i, float scale)
+{ return scale == 1.0f ? (float)p[i] : (float)p[i] * scale; }
+template <>
+__device__ __forceinline__ float load_px<float>(const float* p, size_t i, float scale)
+{ return scale == 1.0f ? p[i] : p[i] * scale; }
+
+// --------------------------------------------------------------------------------------
+// Reference prep: raw -> float plane, Gradient2D4 (src/oc_gradient.cpp:37-79), packed
+// {ref, gx, gy, 0}.  16x16 output tile per 256-thread block, 2-px halo staged in smem.
+// Stencil term order follows the CPU: -f(c+2)/12 + 2f(c+1)/3 - 2f(c-1)/3 + f(c-2)/12,
+// each product rounded separately (no contraction), so planes are bit-identical.
+// --------------------------------------------------------------------------------------
+constexpr int kPrepTile = 16;
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_prepare_ref(const T* __restrict__ raw, int w, int h, float scale,
+                                                     float* __restrict__ ref_f32,
+                                                     float4* __restrict__ ref_pack)
+{
+  __shared__ float tile[kPrepTile + 4][kPrepTile + 4 + 1];
+  const int bx = blockIdx.x * kPrepTile, by = blockIdx.y * kPrepTile;
+  for (int i = threadIdx.x; i < (kPrepTile + 4) * (kPrepTile + 4); i += blockDim.x)
+  {
+    int ty = i / (kPrepTile + 4), tx = i % (kPrepTile + 4);
+    int gx = bx + tx - 2, gy = by + ty - 2;
+    float v = 0.f;
+    if (gx >= 0 && gx < w && gy >= 0 && gy < h) v = load_px<T>(raw, (size_t)gy * w + gx, scale);
+    tile[ty][tx] = v;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % kPrepTile, ty = threadIdx.x / kPrepTile;
+  const int x = bx + tx, y = by + ty;
+  if (x >= w || y >= h) return;
+  const float c = tile[ty + 2][tx + 2];
+  const float f1 = 1.f / 12.f, f2 = 2.f / 3.f;
+  float gxv = 0.f, gyv = 0.f;
+  if (x >= 2 && x < w - 2)
+  {
+    float r = 0.f;
+    r = __fsub_rn(r, __fmul_rn(tile[ty + 2][tx + 4], f1));
+    r = __fadd_rn(r, __fmul_rn(tile[ty + 2][tx + 3], f2));
+    r = __fsub_rn(r, __fmul_rn(tile[ty + 2][tx + 1], f2));
+    r = __fadd_rn(r, __fmul_rn(tile[ty + 2][tx + 0], f1));
+    gxv = r;
+  }
+  if (y >= 2 && y < h - 2)
+  {
+    float r = 0.f;
+    r = __fsub_rn(r, __fmul_rn(tile[ty + 4][tx + 2], f1));
+    r = __fadd_rn(r, __fmul_rn(tile[ty + 3][tx + 2], f2));
+    r = __fsub_rn(r, __fmul_rn(tile[ty + 1][tx + 2], f2));
+    r = __fadd_rn(r, __fmul_rn(tile[ty + 0][tx + 2], f1));
+    gyv = r;
+  }
+  const size_t o = (size_t)y * w + x;
+  ref_f32[o] = c;
+  ref_pack[o] = make_float4(c, gxv, gyv, 0.f);
+}
+
+// --------------------------------------------------------------------------------------
+// Target prep: raw -> float plane + BicubicBspline table (src/oc_cubic_bspline.cpp:84-132).
+// Texel (r, c) for 1 <= c < w-2, 1 <= r < h-2 holds coef[k][l] = P[3-k][3-l] with
+// P[k][l] = sum_m sum_n BC[l][m] BC[k][n] q[n][m], accumulated in the CPU's m, n order with
+// separate roundings, so the table is bit-identical to the CPU's; other texels are 0.
+// Each thread writes its 64 B texel as four float4 stores.
+// --------------------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, int w, int h, float scale,
+                                                     float* __restrict__ tar_f32,
+                                                     float4* __restrict__ coef)
+{
+  __shared__ float tile[kPrepTile + 3][kPrepTile + 3 + 1];
+  const int bx = blockIdx.x * kPrepTile, by = blockIdx.y * kPrepTile;
+  for (int i = threadIdx.x; i < (kPrepTile + 3) * (kPrepTile + 3); i += blockDim.x)
+  {
+    int ty = i / (kPrepTile + 3), tx = i % (kPrepTile + 3);
+    int gx = bx + tx - 1, gy = by + ty - 1;
+    float v = 0.f;
+    if (gx >= 0 && gx < w && gy >= 0 && gy < h) v = load_px<T>(raw, (size_t)gy * w + gx, scale);
+    tile[ty][tx] = v;
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % kPrepTile, ty = threadIdx.x / kPrepTile;
+  const int x = bx + tx, y = by + ty;
+  if (x >= w || y >= h) return;
+  const size_t o = (size_t)y * w + x;
+  tar_f32[o] = tile[ty + 1][tx + 1];
+  float4* dst = coef + o * 4;
+  if (x < 1 || y < 1 || x >= w - 2 || y >= h - 2)
+  {
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+    dst[0] = z; dst[1] = z; dst[2] = z; dst[3] = z;
+    return;
+  }
+  float q[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) q[i][j] = tile[ty + i][tx + j];
+  float p[4][4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+#pragma unroll
+    for (int l = 0; l < 4; ++l)
+    {
+      float acc = 0.f;
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int n = 0; n < 4; ++n)
+          acc = __fadd_rn(acc, __fmul_rn(c_bc2[((k * 4 + l) * 4 + m) * 4 + n], q[n][m]));
+      p[k][l] = acc;
+    }
+#pragma unroll
+  for (int k = 0; k < 4; ++k)
+    dst[k] = make_float4(p[3 - k][3], p[3 - k][2], p[3 - k][1], p[3 - k][0]);
+}
+
+// --------------------------------------------------------------------------------------
+// Warp helpers
+// --------------------------------------------------------------------------------------
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  return v;
+}
+
+// 6x6 inverse by partial-pivot LU in float (restates Eigen's Matrix6f::inverse, which
+// src/oc_icgn.cpp:234 calls).  Single thread.
+__device__ void inverse6(const float (&a_in)[36], float* inv)
+{
+  float a[36];
+  int perm[6];
+#pragma unroll
+  for (int i = 0; i < 36; ++i) a[i] = a_in[i];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) perm[i] = i;
+  for (int k = 0; k < 6; ++k)
+  {
+    int piv = k;
+    float best = fabsf(a[k * 6 + k]);
+    for (int i = k + 1; i < 6; ++i)
+      if (fabsf(a[i * 6 + k]) > best) { best = fabsf(a[i * 6 + k]); piv = i; }
+    if (piv != k)
+    {
+      for (int j = 0; j < 6; ++j) { float t = a[k * 6 + j]; a[k * 6 + j] = a[piv * 6 + j]; a[piv * 6 + j] = t; }
+      int t = perm[k]; perm[k] = perm[piv]; perm[piv] = t;
+    }
+    for (int i = k + 1; i < 6; ++i)
+    {
+      a[i * 6 + k] = a[i * 6 + k] / a[k * 6 + k];
+      for (int j = k + 1; j < 6; ++j) a[i * 6 + j] -= a[i * 6 + k] * a[k * 6 + j];
+    }
+  }
+  for (int col = 0; col < 6; ++col)
+  {
+    float y[6];
+    for (int i = 0; i < 6; ++i)
+    {
+      float s = (perm[i] == col) ? 1.f : 0.f;
+      for (int j = 0; j < i; ++j) s -= a[i * 6 + j] * y[j];
+      y[i] = s;
+    }
+    for (int i = 5; i >= 0; --i)
+    {
+      float s = y[i];
+      for (int j = i + 1; j < 6; ++j) s -= a[i * 6 + j] * inv[j * 6 + col];
+      inv[i * 6 + col] = s / a[i * 6 + i];
+    }
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// Per-POI reference prep (src/oc_icgn.cpp:197-234): one warp per POI.  Reads the packed
+// {ref, gx, gy} plane, forms mean, zero-mean norm, S, G, the float Hessian and its
+// inverse, and stores a PoiRef.  POIs whose reference subset leaves the image get
+// valid = 0 (the IC-GN entry test rejects them before any of this is read).
+// --------------------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_poi_prepare(const float4* __restrict__ ref_pack, int w, int h,
+                                                     const dic_poi* __restrict__ pois, int64_t n,
+                                                     int rx, int ry, PoiRef* __restrict__ out)
+{
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (i >= n) return;
+  const float px = pois[i].x, py = pois[i].y;
+  PoiRef* rec = out + i;
+  // Entry-test geometry of src/oc_icgn.cpp:184-185.
+  if (!(py - ry >= 0 && px - rx >= 0 && py + ry <= h - 1 && px + rx <= w - 1))
+  {
+    if (lane == 0) rec->valid = 0.f;
+    return;
+  }
+  const int sw = 2 * rx + 1, size = sw * (2 * ry + 1);
+  const int cx = (int)px, cy = (int)py;
+  float sum = 0.f;
+  for (int k = lane; k < size; k += 32)
+  {
+    const int lx = k % sw - rx, ly = k / sw - ry;
+    sum += ref_pack[(size_t)(cy + ly) * w + cx + lx].x;
+  }
+  sum = warp_sum(sum);
+  const float t0 = sum / (float)size;
+  float nsq = 0.f, src = 0.f, S[6] = {0.f}, G[6] = {0.f}, H[21] = {0.f};
+  // Same sample order and the same fmaf forms as the IC-GN kernel's target sums.
+  for (int k = lane; k < size; k += 32)
+  {
+    const int lx = k % sw - rx, ly = k / sw - ry;
+    const float4 v = ref_pack[(size_t)(cy + ly) * w + cx + lx];
+    const float rc = v.x - t0;
+    const float flx = (float)lx, fly = (float)ly;
+    const float sd[6] = {v.y, v.y * flx, v.y * fly, v.z, v.z * flx, v.z * fly};
+    nsq = fmaf(rc, rc, nsq);
+    src += rc;
+    int t = 0;
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+    {
+      S[a] += sd[a];
+      G[a] = fmaf(sd[a], rc, G[a]);
+#pragma unroll
+      for (int b = 0; b <= a; ++b) H[t++] += sd[a] * sd[b];
+    }
+  }
+  nsq = warp_sum(nsq);
+  src = warp_sum(src);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) { S[a] = warp_sum(S[a]); G[a] = warp_sum(G[a]); }
+#pragma unroll
+  for (int t = 0; t < 21; ++t) H[t] = warp_sum(H[t]);
+  if (lane == 0)
+  {
+    float hf[36];
+    int t = 0;
+    for (int a = 0; a < 6; ++a)
+      for (int b = 0; b <= a; ++b) { hf[a * 6 + b] = H[t]; hf[b * 6 + a] = H[t]; ++t; }
+    inverse6(hf, rec->inv_h);
+    const float m_r = src * (1.f / (float)size);
+    const float rn_sq = fmaf(-src, m_r, nsq);
+    rec->t0 = t0;
+    rec->ref_norm = sqrtf(rn_sq);
+    rec->ref_norm_sq = rn_sq;
+    rec->sum_rc = src;
+    for (int a = 0; a < 6; ++a) { rec->S[a] = S[a]; rec->G[a] = fmaf(-m_r, S[a], G[a]); }
+    rec->valid = 1.f;
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// IC-GN iteration (src/oc_icgn.cpp:168-387): one warp per POI.  Per iteration one pass
+// over the (2rx+1)(2ry+1) warped samples: warp the local coordinate, reject on the
+// interpolatable-range test, gather the texel's 16 B-spline coefficients (4 x 16 B),
+// evaluate the bicubic polynomial, and accumulate the nine single-pass sums (PoiRef).
+// The warp then reduces the sums with an xor butterfly, solves dp = invH * num on lanes
+// 0-5, and every lane applies the same inverse-compositional update W <- W * W(dp)^-1.
+// Control flow is warp-uniform; results do not depend on other POIs or on scheduling.
+// --------------------------------------------------------------------------------------
+struct IcgnParams
+{
+  const float4* coef;      // tar B-spline table (4 float4 per texel)
+  const float4* ref_pack;  // {ref, gx, gy, 0}
+  const PoiRef* poi_ref;   // per layout slot
+  const int64_t* slot;     // queue index -> layout slot (nullptr: identity)
+  dic_poi* pois;
+  int64_t n;
+  int w, h, rx, ry;
+  float conv;
+  float max_iter;
+  unsigned long long* iter_sum;  // sum of iterations (nullable)
+};
+
+__device__ __forceinline__ void compose_update(float (&W)[6], const float (&dp)[6])
+{
+  // W(dp) = [[1+dux, duy, du], [dvx, 1+dvy, dv], [0, 0, 1]]; inverse by cofactors
+  // (Eigen compute_inverse_size3 restated), then W <- W * inv.
+  const float m0 = 1.f + dp[1], m1 = dp[2], m2 = dp[0];
+  const float m3 = dp[4], m4 = 1.f + dp[5], m5 = dp[3];
+  const float c00 = m4 * 1.f - m5 * 0.f;
+  const float c10 = m5 * 0.f - m3 * 1.f;
+  const float c20 = m3 * 0.f - m4 * 0.f;
+  const float det = m0 * c00 + m1 * c10 + m2 * c20;
+  const float id = 1.f / det;
+  const float i0 = c00 * id, i1 = (m2 * 0.f - m1 * 1.f) * id, i2 = (m1 * m5 - m2 * m4) * id;
+  const float i3 = c10 * id, i4 = (m0 * 1.f - m2 * 0.f) * id, i5 = (m2 * m3 - m0 * m5) * id;
+  const float i6 = c20 * id, i7 = (m1 * 0.f - m0 * 0.f) * id, i8 = (m0 * m4 - m1 * m3) * id;
+  const float a0 = W[0], a1 = W[1], a2 = W[2], a3 = W[3], a4 = W[4], a5 = W[5];
+  W[0] = a0 * i0 + a1 * i3 + a2 * i6;
+  W[1] = a0 * i1 + a1 * i4 + a2 * i7;
+  W[2] = a0 * i2 + a1 * i5 + a2 * i8;
+  W[3] = a3 * i0 + a4 * i3 + a5 * i6;
+  W[4] = a3 * i1 + a4 * i4 + a5 * i7;
+  W[5] = a3 * i2 + a4 * i5 + a5 * i8;
+}
+
+__global__ void __launch_bounds__(256) k_icgn(IcgnParams P)
+{
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (i >= P.n) return;
+  dic_poi* poi = P.pois + i;
+  const float px = poi->x, py = poi->y;
+  const float u_in = poi->u, ux_in = poi->ux, uy_in = poi->uy;
+  const float v_in = poi->v, vx_in = poi->vx, vy_in = poi->vy;
+  const float zncc_in = poi->zncc;
+  const int w = P.w, h = P.h, rx = P.rx, ry = P.ry;
+  // Entry test (src/oc_icgn.cpp:184-191).
+  if (py - ry < 0 || px - rx < 0 || py + ry > h - 1 || px + rx > w - 1 || fabsf(u_in) >= w ||
+      fabsf(v_in) >= h || zncc_in < 0 || isnan(u_in) || isnan(v_in))
+  {
+    if (lane == 0) poi->zncc = zncc_in >= 0 ? -3.f : zncc_in;
+    return;
+  }
+  const PoiRef* R = P.poi_ref + (P.slot ? P.slot[i] : i);
+  const float t0 = R->t0, ref_norm = R->ref_norm, ref_norm_sq = R->ref_norm_sq, sum_rc = R->sum_rc;
+  float S_l = 0.f, G_l = 0.f, invh_row[6];
+  if (lane < 6)
+  {
+    S_l = R->S[lane];
+    G_l = R->G[lane];
+#pragma unroll
+    for (int c = 0; c < 6; ++c) invh_row[c] = R->inv_h[lane * 6 + c];
+  }
+  const int sw = 2 * rx + 1, size = sw * (2 * ry + 1);
+  const float inv_size = 1.f / (float)size;
+  const int cx = (int)px, cy = (int)py;
+  const int step_x = 32 % sw, step_y = 32 / sw;
+  const int lx0 = lane % sw - rx, ly0 = lane / sw - ry;
+  // warp matrix rows (Deformation2D1::setWarp, src/oc_deformation.cpp:116-128)
+  float W[6] = {1.f + ux_in, uy_in, u_in, vx_in, 1.f + vy_in, v_in};
+  const float rx2 = (float)(rx * rx), ry2 = (float)(ry * ry);
+  int it = 0;
+  float conv = 0.f, znssd = 0.f;
+  int status = 0;  // 0 ok, -3 out of range, -5 NaN coordinate
+  do
+  {
+    ++it;
+    float A0 = 0.f, A1 = 0.f, A2 = 0.f, B[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool oob = false, nan_seen = false;
+    int lx = lx0, ly = ly0;
+    for (int k = lane; k < size; k += 32)
+    {
+      const float flx = (float)lx, fly = (float)ly;
+      const float gxp = px + (W[0] * flx + W[1] * fly + W[2]);
+      const float gyp = py + (W[3] * flx + W[4] * fly + W[5]);
+      if (gxp < 1.f || gyp < 1.f || gxp >= (float)(w - 2) || gyp >= (float)(h - 2))
+        oob = true;
+      else if (isnan(gxp) || isnan(gyp))
+        nan_seen = true;
+      else
+      {
+        const float fx = floorf(gxp), fy = floorf(gyp);
+        const int xi = (int)fx, yi = (int)fy;
+        const float dx = gxp - fx, dy = gyp - fy;
+        const float4* c = P.coef + ((size_t)yi * w + xi) * 4;
+        const float4 c0 = __ldg(c + 0), c1 = __ldg(c + 1), c2 = __ldg(c + 2), c3 = __ldg(c + 3);
+        const float r0 = fmaf(fmaf(fmaf(c0.w, dx, c0.z), dx, c0.y), dx, c0.x);
+        const float r1 = fmaf(fmaf(fmaf(c1.w, dx, c1.z), dx, c1.y), dx, c1.x);
+        const float r2 = fmaf(fmaf(fmaf(c2.w, dx, c2.z), dx, c2.y), dx, c2.x);
+        const float r3 = fmaf(fmaf(fmaf(c3.w, dx, c3.z), dx, c3.y), dx, c3.x);
+        const float t = fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
+        const float4 rv = __ldg(P.ref_pack + (size_t)(cy + ly) * w + (cx + lx));
+        const float tau = t - t0;
+        const float rc = rv.x - t0;
+        A0 += tau;
+        A1 = fmaf(tau, tau, A1);
+        A2 = fmaf(tau, rc, A2);
+        B[0] = fmaf(rv.y, tau, B[0]);
+        B[1] = fmaf(rv.y * flx, tau, B[1]);
+        B[2] = fmaf(rv.y * fly, tau, B[2]);
+        B[3] = fmaf(rv.z, tau, B[3]);
+        B[4] = fmaf(rv.z * flx, tau, B[4]);
+        B[5] = fmaf(rv.z * fly, tau, B[5]);
+      }
+      lx += step_x;
+      ly += step_y;
+      if (lx > rx) { lx -= sw; ly += 1; }
+    }
+    if (__any_sync(kFull, oob)) { status = -3; break; }
+    if (__any_sync(kFull, nan_seen)) { status = -5; break; }
+    A0 = warp_sum(A0);
+    A1 = warp_sum(A1);
+    A2 = warp_sum(A2);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) B[a] = warp_sum(B[a]);
+    const float mean_tau = A0 * inv_size;
+    const float tnorm_sq = fmaf(-A0, mean_tau, A1);
+    // A flat target subset has zero norm; the CPU then divides by zero and the POI ends
+    // as NaN (-5).  Rounding can leave a tiny residue here, so force the same outcome.
+    const float tar_norm = tnorm_sq > 0.f ? sqrtf(tnorm_sq) : __int_as_float(0x7fc00000);
+    const float s = ref_norm / tar_norm;
+    const float tc_rc = fmaf(-mean_tau, sum_rc, A2);
+    const float esq = s * s * tnorm_sq - 2.f * s * tc_rc + ref_norm_sq;
+    znssd = esq / (ref_norm * ref_norm);
+    // lane a < 6: num_a, then dp_a = invH row a . num
+    float num_l = 0.f;
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+      if (lane == a) num_l = s * fmaf(-mean_tau, S_l, B[a]) - G_l;
+    float dp_l = 0.f;
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+    {
+      const float nc = __shfl_sync(kFull, num_l, c);
+      if (lane < 6) dp_l += invh_row[c] * nc;
+    }
+    float dp[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) dp[a] = __shfl_sync(kFull, dp_l, a);
+    compose_update(W, dp);
+    conv = sqrtf(dp[0] * dp[0] + dp[1] * dp[1] * rx2 + dp[2] * dp[2] * ry2 + dp[3] * dp[3] +
+                 dp[4] * dp[4] * rx2 + dp[5] * dp[5] * ry2);
+  } while ((float)it < P.max_iter && conv >= P.conv);
+
+  if (lane != 0) return;
+  if (P.iter_sum) atomicAdd(P.iter_sum, (unsigned long long)it);
+  if (status == -3) { poi->zncc = -3.f; return; }   // src/oc_icgn.cpp:285-289
+  if (status == -5) { poi->zncc = -5.f; return; }   // :297-301
+  float u = W[2], ux = W[0] - 1.f, uy = W[1], v = W[5], vx = W[3], vy = W[4] - 1.f;
+  float zncc = 0.5f * (2.f - znssd);
+  if (conv >= P.conv && (float)it >= P.max_iter) zncc = -4.f;
+  if (isnan(zncc) || isnan(u) || isnan(v))
+  {
+    u = u_in;
+    v = v_in;
+    zncc = -5.f;
+  }
+  poi->u = u; poi->ux = ux; poi->uy = uy;
+  poi->v = v; poi->vx = vx; poi->vy = vy;
+  poi->u0 = u_in;
+  poi->v0 = v_in;
+  poi->zncc = zncc;
+  poi->iteration = (float)it;
+  poi->convergence = conv;
+}
+
+// --------------------------------------------------------------------------------------
+// Register FFT of compile-time length N (mixed radix 2/3/4/5 + generic primes), one
+// transform per thread.  Four-step decomposition N = N1*N2 with n = N2*n1 + n2,
+// k = k1 + N1*k2.  After full unrolling every twiddle index is a constant, so twiddles are
+// read straight from the constant bank.
+// --------------------------------------------------------------------------------------
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{ return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // -i * a
+
+__host__ __device__ constexpr bool is_prime(int n)
+{
+  if (n < 2) return false;
+  for (int d = 2; d * d <= n; ++d)
+    if (n % d == 0) return false;
+  return true;
+}
+__host__ __device__ constexpr int first_factor(int n)
+{
+  if (n <= 5 || is_prime(n)) return n;
+  if (n % 4 == 0) return 4;
+  if (n % 2 == 0) return 2;
+  if (n % 3 == 0) return 3;
+  if (n % 5 == 0) return 5;
+  for (int d = 7; d <= n; d += 2)
+    if (n % d == 0) return d;
+  return n;
+}
+
+template <int N>
+__device__ __forceinline__ float2 twiddle_mul(float2 v, int e)
+{
+  const int r = e % N;
+  if (r == 0) return v;
+  return cmul(v, c_tw[tw_offset(N) + r]);
+}
+
+template <int N>
+struct Dft
+{
+  // generic prime length: direct DFT with table twiddles
+  __device__ __forceinline__ static void run(const float2 (&in)[N], float2 (&out)[N])
+  {
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+    {
+      float2 acc = in[0];
+#pragma unroll
+      for (int j = 1; j < N; ++j) acc = cadd(acc, twiddle_mul<N>(in[j], j * k));
+      out[k] = acc;
+    }
+  }
+};
+template <>
+struct Dft<1>
+{
+  __device__ __forceinline__ static void run(const float2 (&in)[1], float2 (&out)[1]) { out[0] = in[0]; }
+};
+template <>
+struct Dft<2>
+{
+  __device__ __forceinline__ static void run(const float2 (&in)[2], float2 (&out)[2])
+  {
+    out[0] = cadd(in[0], in[1]);
+    out[1] = csub(in[0], in[1]);
+  }
+};
+template <>
+struct Dft<3>
+{
+  __device__ __forceinline__ static void run(const float2 (&in)[3], float2 (&out)[3])
+  {
+    const float k = 0.86602540378443864676f;  // sin(2 pi / 3)
+    const float2 s = cadd(in[1], in[2]), d = csub(in[1], in[2]);
+    const float2 m = make_float2(in[0].x - 0.5f * s.x, in[0].y - 0.5f * s.y);
+    const float2 rot = mul_mi(cscale(d, k));
+    out[0] = cadd(in[0], s);
+    out[1] = cadd(m, rot);
+    out[2] = csub(m, rot);
+  }
+};
+template <>
+struct Dft<4>
+{
+  __device__ __forceinline__ static void run(const float2 (&in)[4], float2 (&out)[4])
+  {
+    const float2 a = cadd(in[0], in[2]), b = csub(in[0], in[2]);
+    const float2 c = cadd(in[1], in[3]), d = mul_mi(csub(in[1], in[3]));
+    out[0] = cadd(a, c);
+    out[2] = csub(a, c);
+    out[1] = cadd(b, d);
+    out[3] = csub(b, d);
+  }
+};
+template <>
+struct Dft<5>
+{
+  __device__ __forceinline__ static void run(const float2 (&in)[5], float2 (&out)[5])
+  {
+    const float c1 = 0.30901699437494742410f;   // cos(2 pi / 5)
+    const float c2 = -0.80901699437494742410f;  // cos(4 pi / 5)
+    const float s1 = 0.95105651629515357212f;   // sin(2 pi / 5)
+    const float s2 = 0.58778525229247312917f;   // sin(4 pi / 5)
+    const float2 a1 = cadd(in[1], in[4]), b1 = csub(in[1], in[4]);
+    const float2 a2 = cadd(in[2], in[3]), b2 = csub(in[2], in[3]);
+    out[0] = cadd(in[0], cadd(a1, a2));
+    const float2 m1 = make_float2(in[0].x + c1 * a1.x + c2 * a2.x, in[0].y + c1 * a1.y + c2 * a2.y);
+    const float2 m2 = make_float2(in[0].x + c2 * a1.x + c1 * a2.x, in[0].y + c2 * a1.y + c1 * a2.y);
+    const float2 r1 = mul_mi(make_float2(s1 * b1.x + s2 * b2.x, s1 * b1.y + s2 * b2.y));
+    const float2 r2 = mul_mi(make_float2(s2 * b1.x - s1 * b2.x, s2 * b1.y - s1 * b2.y));
+    out[1] = cadd(m1, r1);
+    out[4] = csub(m1, r1);
+    out[2] = cadd(m2, r2);
+    out[3] = csub(m2, r2);
+  }
+};
+
+template <int N, int N1 = first_factor(N)>
+struct Fft
+{
+  static constexpr int N2 = N / N1;
+  __device__ __forceinline__ static void run(const float2 (&in)[N], float2 (&out)[N])
+  {
+    float2 y[N];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2)
+    {
+      float2 a[N1], b[N1];
+#pragma unroll
+      for (int n1 = 0; n1 < N1; ++n1) a[n1] = in[N2 * n1 + n2];
+      Fft<N1>::run(a, b);
+#pragma unroll
+      for (int k1 = 0; k1 < N1; ++k1) y[k1 * N2 + n2] = twiddle_mul<N>(b[k1], n2 * k1);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1)
+    {
+      float2 a[N2], b[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; ++n2) a[n2] = y[k1 * N2 + n2];
+      Fft<N2>::run(a, b);
+#pragma unroll
+      for (int k2 = 0; k2 < N2; ++k2) out[k1 + N1 * k2] = b[k2];
+    }
+  }
+};
+template <int N>
+struct Fft<N, N>
+{
+  __device__ __forceinline__ static void run(const float2 (&in)[N], float2 (&out)[N]) { Dft<N>::run(in, out); }
+};
+
+// --------------------------------------------------------------------------------------
+// FFTCC (src/oc_fftcc.cpp:396-496), one warp per POI, M = 2r <= 32.
+// The zero-mean reference and target subsets are packed as z = ref + i*tar and
+// transformed once (rows then columns, one lane per line).  With Z[-k] read back from
+// shared memory, R = (Z[k] + conj Z[-k]) / 2 and T = (Z[k] - conj Z[-k]) / 2i are the two
+// real-input spectra, X = conj(R) * T is the cross-power spectrum FFTW's r2c/c2r pair
+// produces, and the inverse transform (columns then rows) gives the unnormalised
+// correlation map.  Argmax: strict '>' from index 0, i.e. the largest value and, among
+// equal values, the lowest row-major index, reduced as (value, index) pairs.
+// --------------------------------------------------------------------------------------
+struct FftccParams
+{
+  const float* ref;
+  const float* tar;
+  dic_poi* pois;
+  int64_t n;
+  int w, h;
+};
+
+template <int M>
+__global__ void __launch_bounds__(128) k_fftcc(FftccParams P)
+{
+  constexpr int R = M / 2;
+  constexpr int S = (M % 2 == 0) ? M + 1 : M;  // odd row stride: conflict-free float2 rows
+  constexpr int kWarpsPerBlock = 4;
+  __shared__ float2 smem[kWarpsPerBlock][M * S];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t i = (int64_t)blockIdx.x * kWarpsPerBlock + warp;
+  if (i >= P.n) return;
+  float2* z = smem[warp];
+  dic_poi* poi = P.pois + i;
+  const float px = poi->x, py = poi->y, u_init = poi->u, v_init = poi->v;
+  const int w = P.w, h = P.h;
+  if ((int)px < R || (int)px >= w - R || (int)py < R || (int)py >= h - R ||
+      int(px + u_init) < R || int(px + u_init) >= w - R || int(py + v_init) < R ||
+      int(py + v_init) >= h - R)
+    return;  // untouched, as the CPU leaves it
+  // subsets: lane c < M reads column c of every row (coordinates as the CPU forms them)
+  float rv[M], tv[M];
+  float rsum = 0.f, tsum = 0.f;
+  if (lane < M)
+  {
+    const float fxr = __fsub_rn(__fadd_rn(px, (float)lane), (float)R);
+    const int xr = (int)fxr, xt = (int)__fadd_rn(fxr, u_init);
+#pragma unroll
+    for (int r = 0; r < M; ++r)
+    {
+      const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
+      const int yr = (int)fyr, yt = (int)__fadd_rn(fyr, v_init);
+      rv[r] = P.ref[(size_t)yr * w + xr];
+      tv[r] = P.tar[(size_t)yt * w + xt];
+      rsum += rv[r];
+      tsum += tv[r];
+    }
+  }
+  rsum = warp_sum(rsum);
+  tsum = warp_sum(tsum);
+  const float rmean = rsum / (float)(M * M), tmean = tsum / (float)(M * M);
+  float rn = 0.f, tn = 0.f;
+  if (lane < M)
+  {
+#pragma unroll
+    for (int r = 0; r < M; ++r)
+    {
+      rv[r] -= rmean;
+      tv[r] -= tmean;
+      rn += rv[r] * rv[r];
+      tn += tv[r] * tv[r];
+      z[r * S + lane] = make_float2(rv[r], tv[r]);
+    }
+  }
+  rn = warp_sum(rn);
+  tn = warp_sum(tn);
+  __syncwarp();
+  float2 a[M], b[M];
+  // forward rows
+  if (lane < M)
+  {
+#pragma unroll
+    for (int k = 0; k < M; ++k) a[k] = z[lane * S + k];
+    Fft<M>::run(a, b);
+#pragma unroll
+    for (int k = 0; k < M; ++k) z[lane * S + k] = b[k];
+  }
+  __syncwarp();
+  // forward columns; keep column `lane` of Z in b[]
+  if (lane < M)
+  {
+#pragma unroll
+    for (int k = 0; k < M; ++k) a[k] = z[k * S + lane];
+    Fft<M>::run(a, b);
+  }
+  __syncwarp();
+  if (lane < M)
+  {
+#pragma unroll
+    for (int k = 0; k < M; ++k) z[k * S + lane] = b[k];
+  }
+  __syncwarp();
+  // cross-power spectrum, conjugated for the inverse transform: conj(X)
+  if (lane < M)
+  {
+    const int cm = (M - lane) % M;
+#pragma unroll
+    for (int k = 0; k < M; ++k)
+    {
+      const float2 A = b[k];
+      const float2 zm = z[((M - k) % M) * S + cm];
+      const float2 B = make_float2(zm.x, -zm.y);
+      const float2 Rk = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y + B.y));
+      const float2 D = csub(A, B);
+      const float2 Tk = make_float2(0.5f * D.y, -0.5f * D.x);  // D / (2i)
+      const float2 X = make_float2(Rk.x * Tk.x + Rk.y * Tk.y, Rk.x * Tk.y - Rk.y * Tk.x);
+      a[k] = make_float2(X.x, -X.y);  // inverse via conj(FFT(conj(X)))
+    }
+    Fft<M>::run(a, b);
+  }
+  __syncwarp();
+  if (lane < M)
+  {
+#pragma unroll
+    for (int k = 0; k < M; ++k) z[k * S + lane] = b[k];
+  }
+  __syncwarp();
+  float best = -2.f;
+  int best_idx = 0;
+  if (lane < M)
+  {
+#pragma unroll
+    for (int k = 0; k < M; ++k) a[k] = z[lane * S + k];
+    Fft<M>::run(a, b);
+    // real part of conj(FFT(conj(.))) is the real part of the FFT output
+#pragma unroll
+    for (int k = 0; k < M; ++k)
+      if (b[k].x > best) { best = b[k].x; best_idx = lane * M + k; }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    const float ov = __shfl_xor_sync(kFull, best, o);
+    const int oi = __shfl_xor_sync(kFull, best_idx, o);
+    if (ov > best || (ov == best && oi < best_idx)) { best = ov; best_idx = oi; }
+  }
+  if (lane == 0)
+  {
+    int lu = best_idx % M, lv = best_idx / M;
+    if (lu > R) lu -= M;
+    if (lv > R) lv -= M;
+    poi->u = (float)lu + u_init;
+    poi->v = (float)lv + v_init;
+    poi->u0 = u_init;
+    poi->v0 = v_init;
+    poi->zncc = best / (sqrtf(rn * tn) * (float)(M * M));
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// FFTCC for 32 < M <= 64 (subset radius 17..32): one 256-thread CTA per POI.  Same packing
+// and cross-power algebra as k_fftcc; each 1-D transform is a direct DFT over one line,
+// with (line, bin) outputs spread over the CTA and twiddles from the constant table.
+// --------------------------------------------------------------------------------------
+__device__ __forceinline__ void block_argmax(float& v, int& idx, float* sv, int* si)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    const float ov = __shfl_xor_sync(kFull, v, o);
+    const int oi = __shfl_xor_sync(kFull, idx, o);
+    if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) { sv[warp] = v; si[warp] = idx; }
+  __syncthreads();
+  if (warp == 0)
+  {
+    v = lane < (int)(blockDim.x >> 5) ? sv[lane] : -2.f;
+    idx = lane < (int)(blockDim.x >> 5) ? si[lane] : 0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      const float ov = __shfl_xor_sync(kFull, v, o);
+      const int oi = __shfl_xor_sync(kFull, idx, o);
+      if (ov > v || (ov == v && oi < idx)) { v = ov; idx = oi; }
+    }
+  }
+}
+
+__device__ __forceinline__ float block_sum(float v, float* sbuf)
+{
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) sbuf[warp] = v;
+  __syncthreads();
+  float t = lane < (int)(blockDim.x >> 5) ? sbuf[lane] : 0.f;
+  return warp_sum(t);
+}
+
+// out[line][k] = sum_j in[line][j] W^(j k) along rows (by_rows) or columns; conj twiddles
+// when inverse.  in/out are m x s float2 arrays (row stride s).
+__device__ void dft_lines(const float2* in, float2* out, int m, int s, bool by_rows, bool inverse)
+{
+  const float2* tw = c_tw + tw_offset(m);
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x)
+  {
+    const int line = t / m, k = t % m;
+    float re = 0.f, im = 0.f;
+    int e = 0;
+    for (int j = 0; j < m; ++j)
+    {
+      const float2 a = by_rows ? in[line * s + j] : in[j * s + line];
+      float2 wv = tw[e];
+      if (inverse) wv.y = -wv.y;
+      re += a.x * wv.x - a.y * wv.y;
+      im += a.x * wv.y + a.y * wv.x;
+      e += k;
+      if (e >= m) e -= m;
+    }
+    if (by_rows) out[line * s + k] = make_float2(re, im);
+    else out[k * s + line] = make_float2(re, im);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_fftcc_large(FftccParams P, int m)
+{
+  extern __shared__ float2 dyn[];
+  __shared__ float s_red[32];
+  __shared__ int s_idx[32];
+  const int s = m + 1;
+  float2* za = dyn;
+  float2* zb = dyn + m * s;
+  const int64_t i = blockIdx.x;
+  if (i >= P.n) return;
+  dic_poi* poi = P.pois + i;
+  const float px = poi->x, py = poi->y, u_init = poi->u, v_init = poi->v;
+  const int w = P.w, h = P.h, R = m / 2;
+  if ((int)px < R || (int)px >= w - R || (int)py < R || (int)py >= h - R ||
+      int(px + u_init) < R || int(px + u_init) >= w - R || int(py + v_init) < R ||
+      int(py + v_init) >= h - R)
+    return;
+  float rsum = 0.f, tsum = 0.f;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x)
+  {
+    const int r = t / m, c = t % m;
+    const float fxr = __fsub_rn(__fadd_rn(px, (float)c), (float)R);
+    const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
+    const float rv = P.ref[(size_t)(int)fyr * w + (int)fxr];
+    const float tv = P.tar[(size_t)(int)__fadd_rn(fyr, v_init) * w + (int)__fadd_rn(fxr, u_init)];
+    za[r * s + c] = make_float2(rv, tv);
+    rsum += rv;
+    tsum += tv;
+  }
+  rsum = block_sum(rsum, s_red);
+  tsum = block_sum(tsum, s_red);
+  const float rmean = rsum / (float)(m * m), tmean = tsum / (float)(m * m);
+  float rn = 0.f, tn = 0.f;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x)
+  {
+    const int r = t / m, c = t % m;
+    float2 v = za[r * s + c];
+    v.x -= rmean;
+    v.y -= tmean;
+    rn += v.x * v.x;
+    tn += v.y * v.y;
+    za[r * s + c] = v;
+  }
+  rn = block_sum(rn, s_red);
+  tn = block_sum(tn, s_red);
+  __syncthreads();
+  dft_lines(za, zb, m, s, true, false);    // rows
+  dft_lines(zb, za, m, s, false, false);   // columns -> Z in za
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x)
+  {
+    const int k1 = t / m, k2 = t % m;
+    const float2 A = za[k1 * s + k2];
+    const float2 zm = za[((m - k1) % m) * s + (m - k2) % m];
+    const float2 B = make_float2(zm.x, -zm.y);
+    const float2 Rk = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y + B.y));
+    const float2 D = csub(A, B);
+    const float2 Tk = make_float2(0.5f * D.y, -0.5f * D.x);
+    zb[k1 * s + k2] = make_float2(Rk.x * Tk.x + Rk.y * Tk.y, Rk.x * Tk.y - Rk.y * Tk.x);
+  }
+  __syncthreads();
+  dft_lines(zb, za, m, s, false, true);    // inverse columns
+  dft_lines(za, zb, m, s, true, true);     // inverse rows -> correlation in zb (real part)
+  float best = -2.f;
+  int best_idx = 0;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x)
+  {
+    const float v = zb[(t / m) * s + t % m].x;
+    if (v > best) { best = v; best_idx = t; }
+  }
+  block_argmax(best, best_idx, s_red, s_idx);
+  if (threadIdx.x == 0)
+  {
+    int lu = best_idx % m, lv = best_idx / m;
+    if (lu > R) lu -= m;
+    if (lv > R) lv -= m;
+    poi->u = (float)lu + u_init;
+    poi->v = (float)lv + v_init;
+    poi->u0 = u_init;
+    poi->v0 = v_init;
+    poi->zncc = best / (sqrtf(rn * tn) * (float)(m * m));
+  }
+}
+
+}  // namespace dic

@@ -1,0 +1,246 @@
+"""Python face of the GB300 DIC engine, mirroring the reference's solver classes.
+
+``ICGN2D1`` mirrors ICGN2D1CudaMvp / OpenCorr ICGN2D1 (src/icgn2d1_cuda_mvp.h:98-143,
+src/oc_icgn.h:45-77) and ``FFTCC2D`` mirrors FFTCC2DCuda / FFTCC2D (src/fftcc2d_cuda.h:85-109,
+src/oc_fftcc.h:56-100): same constructor arguments, the same set / prepare / compute verbs
+over a POI queue, and the same exceptions (ValueError for std::invalid_argument,
+IndexError for std::out_of_range, RuntimeError for std::logic_error).  A POI queue is a
+numpy structured array of ``POI_DTYPE`` (struct dic_poi).  ``Engine`` is the direct handle
+on one dic_engine; both classes hold one.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import POI_DTYPE, DicConfig, DicStats
+
+_DTYPES = {np.dtype(np.uint8): _lib.DIC_U8, np.dtype(np.uint16): _lib.DIC_U16,
+           np.dtype(np.float32): _lib.DIC_F32}
+
+
+def make_queue(xs, ys) -> np.ndarray:
+    q = np.zeros(len(xs), dtype=POI_DTYPE)
+    q["x"] = xs
+    q["y"] = ys
+    return q
+
+
+def grid_queue(width: int, height: int, radius: int, step: int, lines=None) -> np.ndarray:
+    """buildPoiQueue (opencorr_cli_cuda_mvp.cpp:2439-2472): margin r+2, y outer, x inner;
+    with ``lines`` only those rows (in the order given, edge rows skipped)."""
+    margin = radius + 2
+    xs_line = np.arange(margin, width - margin, step, dtype=np.float32)
+    if lines:
+        rows = [y for y in lines if margin <= y < height - margin]
+    else:
+        rows = list(range(margin, height - margin, step))
+    xs = np.tile(xs_line, len(rows))
+    ys = np.repeat(np.asarray(rows, dtype=np.float32), len(xs_line))
+    return make_queue(xs, ys)
+
+
+def _check_queue(q: np.ndarray) -> np.ndarray:
+    if not isinstance(q, np.ndarray) or q.dtype != POI_DTYPE or q.ndim != 1:
+        raise TypeError("a POI queue is a 1-D numpy array of POI_DTYPE")
+    if not q.flags.c_contiguous:
+        raise ValueError("POI queue must be C-contiguous")
+    return q
+
+
+class Engine:
+    """One dic_engine: one GPU, one stream, resident reference state."""
+
+    def __init__(self, subset_radius_x: int, subset_radius_y: int | None = None,
+                 conv_criterion: float = 0.001, max_iteration: int = 10, device: int = 0,
+                 input_scale: float = 1.0):
+        self._L = _lib.load()
+        cfg = DicConfig(int(subset_radius_x), int(subset_radius_y if subset_radius_y is not None else subset_radius_x),
+                        float(conv_criterion), int(max_iteration), int(device), float(input_scale))
+        h = ctypes.c_void_p()
+        rc = self._L.dic_engine_create(ctypes.byref(cfg), ctypes.byref(h))
+        if rc != _lib.DIC_OK:
+            if rc == _lib.DIC_ERR_ARGUMENT:
+                raise ValueError("invalid DIC engine configuration")
+            raise _lib.DicError(rc, "dic_engine_create failed (is a CUDA device available?)")
+        self._h = h
+        self.config = cfg
+
+    # ------------------------------------------------------------------ lifetime
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.dic_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _call(self, rc: int) -> None:
+        _lib.raise_for(rc, self._h)
+
+    @property
+    def stream(self) -> int:
+        return int(self._L.dic_stream(self._h) or 0)
+
+    # ------------------------------------------------------------------ images
+    @staticmethod
+    def _image(img: np.ndarray):
+        img = np.asarray(img)
+        if img.ndim != 2 or img.dtype not in _DTYPES:
+            raise ValueError("an image is a 2-D uint8, uint16 or float32 array")
+        if img.strides[1] != img.itemsize:
+            img = np.ascontiguousarray(img)
+        return img, _DTYPES[img.dtype]
+
+    def set_ref(self, img: np.ndarray) -> None:
+        img, dt = self._image(img)
+        self._call(self._L.dic_set_ref(self._h, img.ctypes.data, img.shape[1], img.shape[0], img.strides[0], dt))
+
+    def set_tar(self, img: np.ndarray) -> None:
+        img, dt = self._image(img)
+        self._call(self._L.dic_set_tar(self._h, img.ctypes.data, img.shape[1], img.shape[0], img.strides[0], dt))
+
+    def set_ref_device(self, ptr: int, width: int, height: int, stride: int, dtype: int) -> None:
+        self._call(self._L.dic_set_ref_device(self._h, ptr, width, height, stride, dtype))
+
+    def set_tar_device(self, ptr: int, width: int, height: int, stride: int, dtype: int) -> None:
+        self._call(self._L.dic_set_tar_device(self._h, ptr, width, height, stride, dtype))
+
+    # ------------------------------------------------------------------ solvers
+    def prepare_ref(self, queue: np.ndarray | None = None) -> None:
+        if queue is None:
+            self._call(self._L.dic_prepare_ref(self._h, None, 0))
+        else:
+            q = _check_queue(queue)
+            self._call(self._L.dic_prepare_ref(self._h, q.ctypes.data, len(q)))
+
+    def prepare_tar(self) -> None:
+        self._call(self._L.dic_prepare_tar(self._h))
+
+    def fftcc(self, queue: np.ndarray, cache_indices=None) -> np.ndarray:
+        q = _check_queue(queue)
+        idx_ptr = None
+        if cache_indices is not None:
+            idx = np.ascontiguousarray(cache_indices, dtype=np.int64)
+            if idx.shape != (len(q),):
+                raise ValueError("FFTCC2D::compute requires one cache index per POI")
+            idx_ptr = idx.ctypes.data
+        self._call(self._L.dic_fftcc(self._h, q.ctypes.data, len(q), idx_ptr))
+        return q
+
+    def icgn(self, queue: np.ndarray) -> np.ndarray:
+        q = _check_queue(queue)
+        self._call(self._L.dic_icgn(self._h, q.ctypes.data, len(q)))
+        return q
+
+    def process_pair(self, queue: np.ndarray) -> np.ndarray:
+        q = _check_queue(queue)
+        self._call(self._L.dic_process_pair(self._h, q.ctypes.data, len(q)))
+        return q
+
+    def process_frame(self, queue: np.ndarray, prev: np.ndarray | None, skip_fftcc: bool = True,
+                      poi_fallback: bool = True, zncc_threshold: float = 0.8,
+                      frame_fallback_ratio: float = float("inf")):
+        q = _check_queue(queue)
+        prev_ptr = None
+        if prev is not None:
+            prev = _check_queue(prev)
+            if len(prev) != len(q):
+                raise ValueError("previous results must have one record per POI")
+            prev_ptr = prev.ctypes.data
+        pol = _lib.DicFramePolicy(int(skip_fftcc), int(poi_fallback), float(zncc_threshold),
+                                  float(frame_fallback_ratio))
+        rep = _lib.DicFrameReport()
+        self._call(self._L.dic_process_frame(self._h, q.ctypes.data, len(q), prev_ptr, ctypes.byref(pol),
+                                             ctypes.byref(rep)))
+        return q, {f: getattr(rep, f) for f, _ in rep._fields_}
+
+    def run_device(self, device_pois: int, count: int, flags: int) -> None:
+        self._call(self._L.dic_run_device(self._h, device_pois, count, flags))
+
+    def read_plane(self, plane: int, width: int, height: int) -> np.ndarray:
+        shape = {_lib.DIC_PLANE_REF: (height, width), _lib.DIC_PLANE_TAR: (height, width),
+                 _lib.DIC_PLANE_REF_PACK: (height, width, 4), _lib.DIC_PLANE_TAR_COEF: (height, width, 16)}[plane]
+        out = np.empty(shape, dtype=np.float32)
+        self._call(self._L.dic_read_plane(self._h, plane, out.ctypes.data, out.nbytes))
+        return out
+
+    def set_timing(self, enabled: bool) -> None:
+        self._call(self._L.dic_set_timing(self._h, int(bool(enabled))))
+
+    def stats(self) -> dict:
+        s = DicStats()
+        self._call(self._L.dic_get_stats(self._h, ctypes.byref(s)))
+        return {f: getattr(s, f) for f, _ in s._fields_}
+
+
+class ICGN2D1:
+    """ICGN2D1CudaMvp(rx, ry, conv_criterion, stop_condition, device) on the GB300 engine."""
+
+    def __init__(self, subset_radius_x: int, subset_radius_y: int, conv_criterion: float = 0.001,
+                 stop_condition: int = 10, device: int = 0, input_scale: float = 1.0):
+        self.engine = Engine(subset_radius_x, subset_radius_y, conv_criterion, int(stop_condition), device,
+                             input_scale)
+
+    def setImages(self, ref_img, tar_img):
+        self.setRefImage(ref_img)
+        self.setTarImage(tar_img)
+
+    def setRefImage(self, ref_img):
+        self.engine.set_ref(ref_img)
+
+    def setTarImage(self, tar_img):
+        self.engine.set_tar(tar_img)
+
+    def prepareRef(self, poi_queue: np.ndarray | None = None):
+        self.engine.prepare_ref(poi_queue)
+
+    def prepareTar(self):
+        self.engine.prepare_tar()
+
+    def prepare(self):
+        self.prepareRef()
+        self.prepareTar()
+
+    def compute(self, poi_queue: np.ndarray) -> np.ndarray:
+        return self.engine.icgn(poi_queue)
+
+
+class FFTCC2D:
+    """FFTCC2DCuda(rx, ry, device) on the GB300 engine (square radii only, as the reference)."""
+
+    def __init__(self, subset_radius_x: int, subset_radius_y: int, device: int = 0, input_scale: float = 1.0):
+        if subset_radius_x <= 0 or subset_radius_x != subset_radius_y or subset_radius_x > 23170:
+            raise ValueError("FFTCC2D supports positive square radii only (1..23170); "
+                             "rectangular FFTs are unsupported")
+        self.engine = Engine(subset_radius_x, subset_radius_y, device=device, input_scale=input_scale)
+
+    def setImages(self, ref_img, tar_img):
+        self.setRefImage(ref_img)
+        self.setTarImage(tar_img)
+
+    def setRefImage(self, ref_img):
+        self.engine.set_ref(ref_img)
+
+    def setTarImage(self, tar_img):
+        self.engine.set_tar(tar_img)
+
+    def prepareRef(self, poi_queue: np.ndarray):
+        self.engine.prepare_ref(poi_queue)
+
+    def prepareTar(self):
+        self.engine.prepare_tar()
+
+    def compute(self, poi_queue: np.ndarray, cache_indices=None) -> np.ndarray:
+        return self.engine.fftcc(poi_queue, cache_indices)

@@ -1,0 +1,201 @@
+"""Seeded synthetic speckle pairs with exact displacement truth.
+
+Images are sums of Gaussian speckles rendered analytically: the target pixel x' is mapped
+back to its material point X (x' = X + d(X), solved by fixed-point iteration, which
+converges because the displacement gradients stay far below 1) and the reference pattern
+is evaluated at X.  No image is resampled, so the truth d(X) at every reference POI is
+exact and a first-order subset shape function sees no model error for affine fields.
+
+Workload shapes (all sizes in px, values in grey levels):
+
+* ``pair_affine``: 512x512 u8, background 40, ~3000 speckles with sigma ~ U(1.5, 3) and
+  peak ~ U(80, 200), translation (2.37, -1.61) plus uniform strain 1e-3, noise 1 DN.
+* ``pair_bumps``: 2048x2048 u8, the same speckle density, displacement = sum of 8 Gaussian
+  bumps scaled to |u|, |v| <= 12 px and local strain <= 2 %, noise 2 DN.
+* ``stream_frame``: 2048x2048 12-bit in u16, affine strain ramp + a sinusoidal
+  displacement of wavelength 256 px, noise 8 DN.
+* ``crack_frame``: 1024x1024 12-bit in u16, uniform strain + a displacement jump across a
+  line.
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+SPECKLES_PER_PX = 3000.0 / (512.0 * 512.0)
+
+
+@dataclasses.dataclass
+class Speckles:
+    x: np.ndarray
+    y: np.ndarray
+    sigma: np.ndarray
+    peak: np.ndarray
+
+
+def make_speckles(rng: np.random.Generator, width: int, height: int, pad: float,
+                  density: float = SPECKLES_PER_PX, sigma=(1.5, 3.0), peak=(80.0, 200.0)) -> Speckles:
+    area = (width + 2 * pad) * (height + 2 * pad)
+    n = int(round(density * area))
+    return Speckles(x=rng.uniform(-pad, width + pad, n), y=rng.uniform(-pad, height + pad, n),
+                    sigma=rng.uniform(sigma[0], sigma[1], n), peak=rng.uniform(peak[0], peak[1], n))
+
+
+def render(width: int, height: int, sp: Speckles, field=None, background: float = 40.0,
+           chunk: int = 2048) -> np.ndarray:
+    """Float64 image of the speckle pattern carried by ``field`` (None = reference).
+
+    ``field(X, Y) -> (u, v)`` is the displacement of the material point at reference (X, Y).
+    """
+    yy, xx = np.meshgrid(np.arange(height, dtype=np.float64), np.arange(width, dtype=np.float64),
+                         indexing="ij")
+    if field is None:
+        bx, by = xx, yy
+        fx, fy = sp.x, sp.y
+    else:
+        bx, by = xx.copy(), yy.copy()
+        # X = x' - d(X); the error contracts by max|grad d| <= 0.02 per pass, so six passes
+        # leave < 1e-8 px for a 12 px field.
+        for _ in range(6):
+            u, v = field(bx, by)
+            bx, by = xx - u, yy - v
+        su, sv = field(sp.x, sp.y)
+        fx, fy = sp.x + su, sp.y + sv
+    img = np.full(width * height, background, dtype=np.float64)
+    reach = int(math.ceil(4.0 * float(sp.sigma.max()) + 2.0))
+    off = np.arange(-reach, reach + 1)
+    oy, ox = np.meshgrid(off, off, indexing="ij")
+    oy, ox = oy.ravel(), ox.ravel()
+    bxf, byf = bx.ravel(), by.ravel()
+    for s in range(0, len(sp.x), chunk):
+        cx = np.rint(fx[s:s + chunk]).astype(np.int64)
+        cy = np.rint(fy[s:s + chunk]).astype(np.int64)
+        px = cx[:, None] + ox[None, :]
+        py = cy[:, None] + oy[None, :]
+        inside = (px >= 0) & (px < width) & (py >= 0) & (py < height)
+        idx = np.where(inside, py * width + px, 0)
+        dx = bxf[idx] - sp.x[s:s + chunk, None]
+        dy = byf[idx] - sp.y[s:s + chunk, None]
+        sig = sp.sigma[s:s + chunk, None]
+        val = sp.peak[s:s + chunk, None] * np.exp(-(dx * dx + dy * dy) / (2.0 * sig * sig))
+        val = np.where(inside, val, 0.0)
+        img += np.bincount(idx.ravel(), weights=val.ravel(), minlength=width * height)
+    return img.reshape(height, width)
+
+
+def quantize(img: np.ndarray, rng: np.random.Generator, noise: float, max_value: int,
+             dtype) -> np.ndarray:
+    out = img + (rng.normal(0.0, noise, img.shape) if noise > 0 else 0.0)
+    return np.clip(np.rint(out), 0, max_value).astype(dtype)
+
+
+# --------------------------------------------------------------------------- fields
+
+def affine_field(u0, v0, ux, uy, vx, vy, xc, yc):
+    def f(x, y):
+        return (u0 + ux * (x - xc) + uy * (y - yc), v0 + vx * (x - xc) + vy * (y - yc))
+    f.params = (u0, v0, ux, uy, vx, vy, xc, yc)
+    return f
+
+
+def bumps_field(rng: np.random.Generator, width: int, height: int, n: int = 8,
+                max_disp: float = 12.0, max_strain: float = 0.02):
+    """Sum of n Gaussian bumps per component, scaled to the displacement/strain limits."""
+    cx = rng.uniform(0, width, (2, n))
+    cy = rng.uniform(0, height, (2, n))
+    s = rng.uniform(0.15, 0.35, (2, n)) * max(width, height)
+    a = rng.uniform(-1.0, 1.0, (2, n))
+
+    def raw(x, y, k):
+        out = np.zeros(np.broadcast(x, y).shape)
+        for j in range(n):
+            out = out + a[k, j] * np.exp(-((x - cx[k, j]) ** 2 + (y - cy[k, j]) ** 2) / (2 * s[k, j] ** 2))
+        return out
+
+    gy, gx = np.meshgrid(np.linspace(0, height - 1, 257), np.linspace(0, width - 1, 257), indexing="ij")
+    scale = 1.0
+    for k in range(2):
+        f = raw(gx, gy, k)
+        du_dy, du_dx = np.gradient(f, gy[:, 0], gx[0, :])
+        disp = np.abs(f).max()
+        strain = max(np.abs(du_dx).max(), np.abs(du_dy).max())
+        scale = min(scale, max_disp / disp, max_strain / strain)
+
+    def field(x, y):
+        return scale * raw(x, y, 0), scale * raw(x, y, 1)
+    return field
+
+
+def sine_field(amp: float, wavelength: float, strain: float, xc: float, yc: float):
+    def field(x, y):
+        return (strain * (x - xc) + amp * np.sin(2 * np.pi * x / wavelength),
+                strain * (y - yc) + amp * np.sin(2 * np.pi * y / wavelength))
+    return field
+
+
+def crack_field(strain: float, jump: float, p0, direction, xc: float, yc: float):
+    nx, ny = -direction[1], direction[0]
+
+    def field(x, y):
+        side = ((x - p0[0]) * nx + (y - p0[1]) * ny) > 0
+        return (strain * (x - xc) + np.where(side, jump * nx, 0.0),
+                strain * (y - yc) + np.where(side, jump * ny, 0.0))
+    return field
+
+
+# --------------------------------------------------------------------------- workloads
+
+@dataclasses.dataclass
+class Pair:
+    ref: np.ndarray          # raw pixels (u8 or u16)
+    tar: np.ndarray
+    field: object            # truth: field(x, y) -> (u, v) at reference positions
+    max_value: int
+
+
+def pair_affine(seed: int = 1, width: int = 512, height: int = 512, noise: float = 1.0) -> Pair:
+    rng = np.random.default_rng(seed)
+    xc, yc = (width - 1) / 2.0, (height - 1) / 2.0
+    field = affine_field(2.37, -1.61, 1e-3, 0.0, 0.0, 1e-3, xc, yc)
+    sp = make_speckles(rng, width, height, pad=16.0)
+    ref = quantize(render(width, height, sp), rng, noise, 255, np.uint8)
+    tar = quantize(render(width, height, sp, field), rng, noise, 255, np.uint8)
+    return Pair(ref, tar, field, 255)
+
+
+def pair_bumps(seed: int = 4, width: int = 2048, height: int = 2048, noise: float = 2.0,
+               max_disp: float = 12.0, max_strain: float = 0.02) -> Pair:
+    rng = np.random.default_rng(seed)
+    field = bumps_field(rng, width, height, max_disp=max_disp, max_strain=max_strain)
+    sp = make_speckles(rng, width, height, pad=max_disp + 16.0)
+    ref = quantize(render(width, height, sp), rng, noise, 255, np.uint8)
+    tar = quantize(render(width, height, sp, field), rng, noise, 255, np.uint8)
+    return Pair(ref, tar, field, 255)
+
+
+def stream_frames(seed: int = 2, width: int = 2048, height: int = 2048, frames: int = 200,
+                  which=None, noise: float = 8.0):
+    """Reference + the requested frames of the 12-bit sine/strain stream (frame k of `frames`)."""
+    rng = np.random.default_rng(seed)
+    sp = make_speckles(rng, width, height, pad=24.0, peak=(80.0 * 4095 / 255, 200.0 * 4095 / 255))
+    bg = 40.0 * 4095 / 255
+    ref = quantize(render(width, height, sp, background=bg), rng, noise, 4095, np.uint16)
+    out = []
+    xc, yc = (width - 1) / 2.0, (height - 1) / 2.0
+    for k in (which if which is not None else range(frames)):
+        frac = (k + 1) / frames
+        field = sine_field(0.5 * frac, 256.0, 5e-3 * frac, xc, yc)
+        frng = np.random.default_rng(seed * 100003 + k)
+        tar = quantize(render(width, height, sp, field, background=bg), frng, noise, 4095, np.uint16)
+        out.append((k, tar, field))
+    return ref, out
+
+
+def grid_xy(width: int, height: int, radius: int, step: int):
+    """POI grid of buildPoiQueue (opencorr_cli_cuda_mvp.cpp:2439-2472): margin r+2, y outer."""
+    margin = radius + 2
+    ys, xs = np.meshgrid(np.arange(margin, height - margin, step), np.arange(margin, width - margin, step),
+                         indexing="ij")
+    return xs.ravel().astype(np.float32), ys.ravel().astype(np.float32)

@@ -1,0 +1,189 @@
+/*
+ * dic.h -- C ABI of the GB300 2D-DIC engine (FFTCC seed + first-order IC-GN).
+ *
+ * One engine = one GPU, one host thread, one CUDA stream.  It holds the reference image,
+ * its gradients and the per-POI reference data (mean, norms, inverse Hessian) resident
+ * on the device across frames, and rebuilds only the target B-spline table per frame.
+ *
+ * The entry points replace the C++ solver classes of FastICGN / OpenCorr:
+ *   ICGN2D1CudaMvp  (src/icgn2d1_cuda_mvp.h:98-143)  and  ICGN2D1  (src/oc_icgn.h:45-77)
+ *   FFTCC2DCuda     (src/fftcc2d_cuda.h:85-109)      and  FFTCC2D  (src/oc_fftcc.h:56-100)
+ * One engine serves both solvers, so a target frame is uploaded once instead of twice.
+ *
+ * Conventions: no exceptions cross this boundary.  Every call returns DIC_OK (0) or a
+ * negative dic_status and leaves a message for dic_last_error().  Host buffers are
+ * caller-owned and are only read/written during the call.  Results follow the CPU
+ * OpenCorr rules (src/oc_icgn.cpp:168-387): zncc carries -3 (rejected before or during
+ * iteration because the subset left the image or the seed was unusable), -4 (no
+ * convergence within max_iteration) or -5 (non-finite result), exactly where the CPU path
+ * assigns them.
+ */
+#ifndef GB300_DIC_H
+#define GB300_DIC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DIC_ABI_VERSION 1
+
+typedef enum dic_status
+{
+  DIC_OK = 0,
+  DIC_ERR_ARGUMENT = -1,   /* std::invalid_argument in the reference */
+  DIC_ERR_STATE = -2,      /* std::logic_error: a required set/prepare step is missing */
+  DIC_ERR_RANGE = -3,      /* std::out_of_range: cache index outside the prepared layout */
+  DIC_ERR_CUDA = -4,       /* a CUDA runtime call failed */
+  DIC_ERR_MEMORY = -5      /* device or pinned allocation failed */
+} dic_status;
+
+typedef enum dic_dtype
+{
+  DIC_U8 = 1,    /* 8-bit grey levels (Image2D Compat8) */
+  DIC_U16 = 2,   /* 12- or 16-bit grey levels stored in uint16 */
+  DIC_F32 = 3    /* already-converted float grey levels */
+} dic_dtype;
+
+/* Solver configuration: ICGN2D1CudaMvp(rx, ry, conv, max_iter, device) and
+ * FFTCC2DCuda(rx, ry, device).  FFTCC needs rx == ry (src/oc_fftcc.cpp:162-164). */
+typedef struct dic_config
+{
+  int32_t subset_radius_x;
+  int32_t subset_radius_y;
+  float conv_criterion;     /* |dp| threshold; OpenCorr CLI default 0.001 */
+  int32_t max_iteration;    /* stop_condition; OpenCorr CLI default 10 */
+  int32_t device;           /* CUDA device ordinal */
+  float input_scale;        /* raw -> float scale applied on upload (cv::Mat::convertTo);
+                               0 means 1.  1/16 reads left-aligned 12-bit data. */
+} dic_config;
+
+/* One point of interest: opencorr::POI2D (src/oc_poi.h:102-136) reduced to the
+ * first-order fields this path reads and writes.  56 bytes. */
+typedef struct dic_poi
+{
+  float x, y;                        /* reference position (px) */
+  float u, ux, uy, v, vx, vy;        /* deformation.p[0..2], p[6..8] */
+  float u0, v0, zncc, iteration, convergence, feature;   /* result.r[0..5] */
+} dic_poi;
+
+/* Frame policy for dic_process_frame (opencorr_cli_cuda_mvp.cpp:3024-3210). */
+typedef struct dic_frame_policy
+{
+  int32_t skip_fftcc;            /* seed from prev_results instead of running FFTCC */
+  int32_t poi_fallback;          /* POI-level FFTCC repair of bad POIs */
+  float zncc_threshold;          /* bad = zncc < threshold and != -3 (default 0.8) */
+  float frame_fallback_ratio;    /* whole-frame FFTCC+IC-GN when bad ratio exceeds this */
+} dic_frame_policy;
+
+typedef struct dic_frame_report
+{
+  int64_t pois;
+  int64_t bad_before_repair;
+  int64_t bad_after_repair;
+  int64_t repaired_candidates;
+  int32_t frame_fallback_used;
+  int32_t fftcc_used;
+  double iteration_mean;
+} dic_frame_report;
+
+/* Device timings (CUDA events on the engine stream) of the most recent call of each
+ * phase, in milliseconds, plus counters. */
+typedef struct dic_stats
+{
+  double ms_prepare_ref;     /* raw -> float reference + Gradient2D4 planes */
+  double ms_poi_prepare;     /* per-POI mean, norms, inverse Hessian */
+  double ms_prepare_tar;     /* raw -> float target + BicubicBspline table */
+  double ms_fftcc;
+  double ms_icgn;
+  int64_t kernel_launches;   /* kernels launched by this engine since creation */
+  int64_t icgn_pois;         /* POIs of the last IC-GN call */
+  int64_t icgn_iterations;   /* sum of IC-GN iterations over those POIs */
+} dic_stats;
+
+typedef struct dic_engine dic_engine;
+
+const char* dic_version(void);
+int32_t dic_abi_version(void);
+
+/* ICGN2D1CudaMvp::ICGN2D1CudaMvp / FFTCC2DCuda::FFTCC2DCuda (src/icgn2d1_cuda_mvp.h:98-100,
+ * src/fftcc2d_cuda.h:85). */
+int dic_engine_create(const dic_config* config, dic_engine** out);
+/* ~ICGN2D1CudaMvp / ~FFTCC2DCuda. */
+void dic_engine_destroy(dic_engine* engine);
+/* Message of the last failed call on this engine ("" after a success). */
+const char* dic_last_error(const dic_engine* engine);
+/* The engine's CUDA stream (a cudaStream_t), for callers that order their own work. */
+void* dic_stream(dic_engine* engine);
+
+/* setRefImage / setTarImage (src/icgn2d1_cuda_mvp.h:106-107, src/fftcc2d_cuda.h:91-92):
+ * copy a host image (row_stride_bytes >= width * element size) to the device.  Setting
+ * the reference invalidates the prepared reference state; setting the target invalidates
+ * the B-spline table.  Reference and target must have the same size. */
+int dic_set_ref(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
+                int64_t row_stride_bytes, int32_t dtype);
+int dic_set_tar(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
+                int64_t row_stride_bytes, int32_t dtype);
+/* The same from device memory (device-to-device copy on the engine stream). */
+int dic_set_ref_device(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
+                       int64_t row_stride_bytes, int32_t dtype);
+int dic_set_tar_device(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
+                       int64_t row_stride_bytes, int32_t dtype);
+
+/* prepareRef(queue) (src/icgn2d1_cuda_mvp.h:121, src/fftcc2d_cuda.h:97): reference
+ * float plane, Gradient2D4 planes and the per-POI reference data for this POI layout
+ * (keyed by integer x, y), resident until the reference or the layout changes. */
+int dic_prepare_ref(dic_engine* engine, const dic_poi* pois, int64_t count);
+/* prepareTar (src/icgn2d1_cuda_mvp.h:122): target float plane + B-spline table. */
+int dic_prepare_tar(dic_engine* engine);
+
+/* FFTCC2DCuda::compute(queue) / compute(queue, cache_indices)
+ * (src/fftcc2d_cuda.h:103-108; src/oc_fftcc.cpp:396-557).  With cache_indices, entry i
+ * must name a prepared-layout slot whose integer (x, y) equals that of pois[i]. */
+int dic_fftcc(dic_engine* engine, dic_poi* pois, int64_t count, const int64_t* cache_indices);
+/* ICGN2D1CudaMvp::compute(queue) (src/icgn2d1_cuda_mvp.h:125; src/oc_icgn.cpp:168-397).
+ * Uses the prepared layout when the queue's integer (x, y) match it, else prepares one. */
+int dic_icgn(dic_engine* engine, dic_poi* pois, int64_t count);
+/* FFTCC seed then IC-GN on one queue with one upload and one download
+ * (opencorr_cli_cuda_mvp.cpp:3187-3196, the non-skip branch of processFrame). */
+int dic_process_pair(dic_engine* engine, dic_poi* pois, int64_t count);
+
+/* processFrame (opencorr_cli_cuda_mvp.cpp:3024-3210): with policy->skip_fftcc and
+ * prev_results (count entries) the queue is seeded from the previous frame and solved by
+ * IC-GN alone, then repaired per POI or per frame as the policy says; otherwise FFTCC +
+ * IC-GN.  pois holds the POI template on entry and the results on return. */
+int dic_process_frame(dic_engine* engine, dic_poi* pois, int64_t count, const dic_poi* prev_results,
+                      const dic_frame_policy* policy, dic_frame_report* report);
+
+/* Device-resident variant: pois points to device memory (count records) and the call only
+ * enqueues work on the engine stream (dic_get_stats or a stream sync waits for it).  flags
+ * selects the phases, run in this order: DIC_RUN_PREPARE (take this queue's integer (x, y)
+ * as the prepared layout; implied when no layout of this size is resident or the reference
+ * changed), DIC_RUN_FFTCC, DIC_RUN_ICGN. */
+#define DIC_RUN_FFTCC 1
+#define DIC_RUN_ICGN 2
+#define DIC_RUN_PREPARE 4
+int dic_run_device(dic_engine* engine, dic_poi* device_pois, int64_t count, int32_t flags);
+
+/* Copy one resident device plane to host memory (bytes must equal the plane size):
+ * DIC_PLANE_REF       W*H float reference grey levels
+ * DIC_PLANE_REF_PACK  W*H float4 {ref, gx, gy, 0} (Gradient2D4 planes, src/oc_gradient.cpp)
+ * DIC_PLANE_TAR       W*H float target grey levels
+ * DIC_PLANE_TAR_COEF  W*H*16 float BicubicBspline table (src/oc_cubic_bspline.cpp:84-132)
+ * Prepares the plane first if its image changed.  For inspection and tests. */
+#define DIC_PLANE_REF 1
+#define DIC_PLANE_REF_PACK 2
+#define DIC_PLANE_TAR 3
+#define DIC_PLANE_TAR_COEF 4
+int dic_read_plane(dic_engine* engine, int32_t plane, void* host_dst, int64_t bytes);
+
+int dic_get_stats(const dic_engine* engine, dic_stats* out);
+/* Turns per-phase CUDA-event timing on (1) or off (0).  On by default. */
+int dic_set_timing(dic_engine* engine, int32_t enabled);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300_DIC_H */

@@ -1,0 +1,147 @@
+"""CPU tests of the oracle: pinned to the reference's golden cases and known answers.
+
+The oracle (oracle/dic_oracle.cpp) restates OpenCorr's CPU path; the reference itself cannot
+be built here (Eigen, OpenCV and FFTW are absent), so it is pinned by
+  * the sub-pixel accuracy gate's cases and limits (smoke/run_subpixel_accuracy_gate.py),
+  * whole-pixel shift sequences with exact truth (smoke/generate_synthetic_dic.py),
+  * the closed-form out-of-range band (smoke/run_oob_rejection_gate.py),
+  * the zero-texture rule for the CPU backend (smoke/run_zero_texture_gate.py: -5 inside a
+    constant block, exact self-match outside),
+  * its own FFT against numpy's DFT.
+"""
+import json
+
+import numpy as np
+import pytest
+
+import dic_checks as C
+
+
+def run_oracle_pair(O, ref, tar, radius, step, threads=None):
+    h, w = ref.shape
+    pois = O.grid_pois(w, h, radius, step)
+    O.run_pair(ref.astype(np.float32), tar.astype(np.float32), pois, radius, threads=threads)
+    return pois
+
+
+def as_fields(O, pois):
+    p, r = pois["p"], pois["r"]
+    return {"x": pois["x"], "y": pois["y"], "u": p[:, O.P_U], "v": p[:, O.P_V], "ux": p[:, O.P_UX],
+            "uy": p[:, O.P_UY], "vx": p[:, O.P_VX], "vy": p[:, O.P_VY], "zncc": r[:, O.R_ZNCC],
+            "iteration": r[:, O.R_ITER]}
+
+
+@pytest.mark.parametrize("case", ["s15", "s15_lowsnr", "s63"])
+def test_oracle_subpixel_accuracy_gate(oracle_mod, golden, case):
+    """Every frame of the gate's cases meets its accuracy limits (single-pair FFTCC + IC-GN)."""
+    O = oracle_mod
+    g = golden(case)
+    limits = json.loads(str(g["limits"]))
+    ref, radius, grid = g["ref"], int(g["radius"]), int(g["grid"])
+    h, w = ref.shape
+    for k, motion in enumerate(g["motions"]):
+        res = as_fields(O, run_oracle_pair(O, ref, g["tars"][k], radius, grid))
+        m = C.accuracy(res, motion, g["centre"], w, h, radius)
+        errs = C.check_accuracy(m, limits)
+        assert not errs, f"{case} frame {k}: {errs} {m}"
+
+
+def test_oracle_whole_pixel_shifts_exact(oracle_mod, golden):
+    """A noise-free whole-pixel shift is recovered exactly (u = dx, v = dy, zncc 1)."""
+    O = oracle_mod
+    g = golden("shift")
+    ref, radius = g["ref"], int(g["radius"])
+    h, w = ref.shape
+    for (dx, dy), tar in zip(g["shifts"], g["tars"]):
+        res = as_fields(O, run_oracle_pair(O, ref, tar, radius, 1))
+        x, y = res["x"], res["y"]
+        # subsets whose target footprint stays inside the unfilled part of the shifted image
+        inside = (x - radius - 2 >= dx + 1) & (y - radius - 2 >= dy + 1) & \
+                 (x + dx + radius + 3 < w) & (y + dy + radius + 3 < h)
+        assert inside.sum() > 100
+        assert np.all(np.abs(res["u"][inside] - dx) <= 1e-4)
+        assert np.all(np.abs(res["v"][inside] - dy) <= 1e-4)
+        assert np.all(res["zncc"][inside] >= 0.9999)
+
+
+def test_oracle_oob_band(oracle_mod, golden):
+    """Every POI the 10-px shift pushes off the image is -3; the rest stay valid."""
+    O = oracle_mod
+    g = golden("oob")
+    ref, tar, radius, shift = g["ref"], g["tar"], int(g["radius"]), int(g["shift"])
+    h, w = ref.shape
+    pois = O.grid_pois(w, h, radius, 1)
+    # seed with the known shift, as the gate's FFTCC does for interior POIs
+    pois["p"][:, O.P_U] = shift
+    gx, gy = O.gradient(ref.astype(np.float32))
+    coef = O.bspline_prepare(tar.astype(np.float32))
+    O.icgn2d1(ref.astype(np.float32), gx, gy, coef, pois, radius)
+    res = as_fields(O, pois)
+    band = C.oob_band(res["x"], res["y"], radius, w, h, shift, 0)
+    assert band.sum() > 0 and (~band).sum() > 0
+    assert np.all(res["zncc"][band] == -3.0)
+    # the incoming guess is kept on rejection
+    assert np.all(res["u"][band] == shift)
+    assert np.all(res["zncc"][~band] != -3.0)
+
+
+def test_oracle_zero_texture(oracle_mod, golden):
+    """CPU rule: -5 with u = v = 0 inside a constant block; exact self-match outside."""
+    O = oracle_mod
+    g = golden("zero_texture")
+    ref, radius = g["ref"], int(g["radius"])
+    h, w = ref.shape
+    res = as_fields(O, run_oracle_pair(O, ref, ref, radius, 1))
+    rel = C.block_relation(res["x"], res["y"], radius, g["block_x"], int(g["block_y"]), int(g["block_side"]))
+    inside, outside = rel == 2, rel == 0
+    assert inside.sum() > 0
+    assert np.all(res["zncc"][inside] == -5.0)
+    assert np.all(res["u"][inside] == 0.0) and np.all(res["v"][inside] == 0.0)
+    assert np.all(res["zncc"][outside] == 1.0)
+    assert np.all(np.abs(res["u"][outside]) <= 1e-4) and np.all(np.abs(res["v"][outside]) <= 1e-4)
+
+
+def test_oracle_fft_matches_dft(oracle_mod):
+    """The oracle's own FFT gives the unnormalised correlation map FFTW's r2c/c2r pair does."""
+    O = oracle_mod
+    rng = np.random.default_rng(7)
+    for radius in (5, 12, 15):
+        m = 2 * radius
+        ref = rng.uniform(0, 255, (64, 64)).astype(np.float32)
+        tar = np.roll(ref, (2, -3), axis=(0, 1)) + rng.normal(0, 1, ref.shape).astype(np.float32)
+        cmap = O.fftcc2d_map(ref, tar, radius, 32.0, 32.0)
+        rs = ref[32 - radius:32 + radius, 32 - radius:32 + radius].astype(np.float64)
+        ts = tar[32 - radius:32 + radius, 32 - radius:32 + radius].astype(np.float64)
+        rs -= rs.mean()
+        ts -= ts.mean()
+        want = np.fft.ifft2(np.conj(np.fft.fft2(rs)) * np.fft.fft2(ts)).real * m * m
+        np.testing.assert_allclose(cmap, want, rtol=0, atol=2e-5 * np.abs(want).max())
+
+
+def test_oracle_fftcc_integer_shift(oracle_mod):
+    O = oracle_mod
+    rng = np.random.default_rng(3)
+    ref = rng.uniform(0, 255, (96, 96)).astype(np.float32)
+    for dx, dy in [(0, 0), (3, -2), (-7, 5), (15, 0)]:
+        tar = np.roll(ref, (dy, dx), axis=(0, 1))
+        pois = O.make_pois([48.0], [48.0])
+        O.fftcc2d(ref, tar, pois, 15)
+        assert pois["p"][0, O.P_U] == dx and pois["p"][0, O.P_V] == dy
+        # windows overlap only partly once shifted, so zncc is 1 only for the zero shift
+        if dx == 0 and dy == 0:
+            assert abs(pois["r"][0, O.R_ZNCC] - 1.0) < 1e-5
+        else:
+            assert 0.3 < pois["r"][0, O.R_ZNCC] < 1.0
+
+
+def test_oracle_bspline_integer_nodes(oracle_mod):
+    """At integer positions the table's c[0][0] term returns the pixel value exactly."""
+    O = oracle_mod
+    rng = np.random.default_rng(5)
+    img = rng.integers(0, 256, (20, 24)).astype(np.float32)
+    coef = O.bspline_prepare(img)
+    for y in range(1, 17):
+        for x in range(1, 21):
+            assert O.bspline_value(coef, float(x), float(y)) == img[y, x]
+    assert O.bspline_value(coef, 0.5, 5.0) == -1.0      # x < 1
+    assert O.bspline_value(coef, 5.0, 18.0) == -1.0     # y >= h - 2
