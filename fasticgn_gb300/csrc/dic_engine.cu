@@ -291,7 +291,7 @@ struct dic_engine
     if (n > 0)
     {
       mark(kPhPoi, 0);
-      const int wpb = 8;
+      const int wpb = 4;
       const unsigned blocks = (unsigned)((n + wpb - 1) / wpb);
       k_poi_prepare<<<blocks, wpb * 32, 0, stream>>>(ref_pack.ptr, w, h, src, n, cfg.subset_radius_x,
                                                      cfg.subset_radius_y, poi_ref.ptr);
@@ -355,9 +355,12 @@ struct dic_engine
     p.conv = cfg.conv_criterion;
     p.max_iter = (float)cfg.max_iteration;
     p.iter_sum = counters.ptr;
-    const int wpb = 8;
+    const int wpb = 4;
     mark(kPhIcgn, 0);
-    k_icgn<<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, 0, stream>>>(p);
+    if (2 * p.rx + 1 <= 32)
+      k_icgn<true><<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, 0, stream>>>(p);
+    else
+      k_icgn<false><<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, 0, stream>>>(p);
     check_launch("k_icgn");
     mark(kPhIcgn, 1);
     icgn_pois = n;

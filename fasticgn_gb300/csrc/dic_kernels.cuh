@@ -4,7 +4,7 @@
 //   raw_ref, raw_tar   W*H input pixels as uploaded (u8 / u16 / f32)
 //   ref_f32, tar_f32   W*H float grey levels (FFTCC subsets read these)
 //   ref_pack           W*H float4 {ref, gx, gy, 0}: one 16-byte load per IC-GN sample
-//   tar_coef           W*H*16 float BicubicBspline table, 64 B per texel, texel-major
+//   tar_coef           BicubicBspline table: 4 planes of W*H float4 (coefficient rows)
 //   poi_ref            per prepared POI: PoiRef (224 B), resident across frames
 //   queue              dic_poi records (56 B)
 #pragma once
@@ -135,7 +135,9 @@ __global__ void __launch_bounds__(256) k_prepare_ref(const T* __restrict__ raw, 
 // Texel (r, c) for 1 <= c < w-2, 1 <= r < h-2 holds coef[k][l] = P[3-k][3-l] with
 // P[k][l] = sum_m sum_n BC[l][m] BC[k][n] q[n][m], accumulated in the CPU's m, n order with
 // separate roundings, so the table is bit-identical to the CPU's; other texels are 0.
-// Each thread writes its 64 B texel as four float4 stores.
+// Layout: four planes of W*H float4, plane k holding coefficient row k of every texel, so a
+// warp reading row k of 32 neighbouring texels touches one contiguous 512 B run (the
+// texel-major 64 B layout spreads the same warp load over 16 cache lines).
 // --------------------------------------------------------------------------------------
 template <typename T>
 __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, int w, int h, float scale,
@@ -158,11 +160,12 @@ __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, 
   if (x >= w || y >= h) return;
   const size_t o = (size_t)y * w + x;
   tar_f32[o] = tile[ty + 1][tx + 1];
-  float4* dst = coef + o * 4;
+  const size_t plane = (size_t)w * h;
+  float4* dst = coef + o;
   if (x < 1 || y < 1 || x >= w - 2 || y >= h - 2)
   {
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
-    dst[0] = z; dst[1] = z; dst[2] = z; dst[3] = z;
+    dst[0] = z; dst[plane] = z; dst[2 * plane] = z; dst[3 * plane] = z;
     return;
   }
   float q[4][4];
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, 
     }
 #pragma unroll
   for (int k = 0; k < 4; ++k)
-    dst[k] = make_float4(p[3 - k][3], p[3 - k][2], p[3 - k][1], p[3 - k][0]);
+    dst[k * plane] = make_float4(p[3 - k][3], p[3 - k][2], p[3 - k][1], p[3 - k][0]);
 }
 
 // --------------------------------------------------------------------------------------
@@ -200,57 +203,112 @@ __device__ __forceinline__ float warp_sum(float v)
 }
 
 // 6x6 inverse by partial-pivot LU in float (restates Eigen's Matrix6f::inverse, which
-// src/oc_icgn.cpp:234 calls).  Single thread.
-__device__ void inverse6(const float (&a_in)[36], float* inv)
+// src/oc_icgn.cpp:234 calls).  Fully unrolled with static indices, so the matrix lives in
+// registers; row swaps are predicated.
+__device__ __forceinline__ void inverse6(float (&a)[6][6], float (&inv)[6][6])
 {
-  float a[36];
-  int perm[6];
+  int perm[6] = {0, 1, 2, 3, 4, 5};
 #pragma unroll
-  for (int i = 0; i < 36; ++i) a[i] = a_in[i];
-#pragma unroll
-  for (int i = 0; i < 6; ++i) perm[i] = i;
   for (int k = 0; k < 6; ++k)
   {
     int piv = k;
-    float best = fabsf(a[k * 6 + k]);
+    float best = fabsf(a[k][k]);
+#pragma unroll
     for (int i = k + 1; i < 6; ++i)
-      if (fabsf(a[i * 6 + k]) > best) { best = fabsf(a[i * 6 + k]); piv = i; }
-    if (piv != k)
+      if (fabsf(a[i][k]) > best) { best = fabsf(a[i][k]); piv = i; }
+#pragma unroll
+    for (int i = k + 1; i < 6; ++i)
     {
-      for (int j = 0; j < 6; ++j) { float t = a[k * 6 + j]; a[k * 6 + j] = a[piv * 6 + j]; a[piv * 6 + j] = t; }
-      int t = perm[k]; perm[k] = perm[piv]; perm[piv] = t;
+      const bool sw = (piv == i);
+#pragma unroll
+      for (int j = 0; j < 6; ++j)
+      {
+        const float ak = a[k][j], ai = a[i][j];
+        a[k][j] = sw ? ai : ak;
+        a[i][j] = sw ? ak : ai;
+      }
+      const int pk = perm[k], pi = perm[i];
+      perm[k] = sw ? pi : pk;
+      perm[i] = sw ? pk : pi;
     }
+#pragma unroll
     for (int i = k + 1; i < 6; ++i)
     {
-      a[i * 6 + k] = a[i * 6 + k] / a[k * 6 + k];
-      for (int j = k + 1; j < 6; ++j) a[i * 6 + j] -= a[i * 6 + k] * a[k * 6 + j];
+      a[i][k] = a[i][k] / a[k][k];
+#pragma unroll
+      for (int j = k + 1; j < 6; ++j) a[i][j] -= a[i][k] * a[k][j];
     }
   }
+#pragma unroll
   for (int col = 0; col < 6; ++col)
   {
     float y[6];
+#pragma unroll
     for (int i = 0; i < 6; ++i)
     {
       float s = (perm[i] == col) ? 1.f : 0.f;
-      for (int j = 0; j < i; ++j) s -= a[i * 6 + j] * y[j];
+#pragma unroll
+      for (int j = 0; j < i; ++j) s -= a[i][j] * y[j];
       y[i] = s;
     }
+#pragma unroll
     for (int i = 5; i >= 0; --i)
     {
       float s = y[i];
-      for (int j = i + 1; j < 6; ++j) s -= a[i * 6 + j] * inv[j * 6 + col];
-      inv[i * 6 + col] = s / a[i * 6 + i];
+#pragma unroll
+      for (int j = i + 1; j < 6; ++j) s -= a[i][j] * inv[j][col];
+      inv[i][col] = s / a[i][i];
     }
   }
 }
+
+// --------------------------------------------------------------------------------------
+// Subset walk shared by the per-POI prep and the IC-GN kernel, so both visit the samples
+// of a subset in the same lane and the same per-lane order (the exact self-match property
+// of PoiRef depends on it).  For subsets at most 32 columns wide lane l owns column
+// lx = l - rx and walks the rows, so every warp-wide load reads one row of neighbouring
+// texels; wider subsets use the flat order k = l + 32 j.
+// --------------------------------------------------------------------------------------
+#define DIC_FOR_EACH_SAMPLE(LANE, RX, RY, ...)                                   \
+  {                                                                              \
+    const int sw_ = 2 * (RX) + 1;                                                \
+    if (sw_ <= 32)                                                               \
+    {                                                                            \
+      if ((LANE) < sw_)                                                          \
+      {                                                                          \
+        const int lx = (LANE) - (RX);                                            \
+        for (int ly = -(RY); ly <= (RY); ++ly) { __VA_ARGS__ }                   \
+      }                                                                          \
+    }                                                                            \
+    else                                                                         \
+    {                                                                            \
+      const int size_ = sw_ * (2 * (RY) + 1);                                    \
+      int lx_ = (LANE) % sw_ - (RX), ly_ = (LANE) / sw_ - (RY);                  \
+      for (int k_ = (LANE); k_ < size_; k_ += 32)                                \
+      {                                                                          \
+        {                                                                        \
+          const int lx = lx_, ly = ly_;                                          \
+          __VA_ARGS__                                                            \
+        }                                                                        \
+        lx_ += 32;                                                               \
+        if (lx_ > (RX)) { lx_ -= sw_; ly_ += 1; }                                \
+      }                                                                          \
+    }                                                                            \
+  }
 
 // --------------------------------------------------------------------------------------
 // Per-POI reference prep (src/oc_icgn.cpp:197-234): one warp per POI.  Reads the packed
 // {ref, gx, gy} plane, forms mean, zero-mean norm, S, G, the float Hessian and its
 // inverse, and stores a PoiRef.  POIs whose reference subset leaves the image get
 // valid = 0 (the IC-GN entry test rejects them before any of this is read).
+//
+// Column walk (subset at most 32 wide): lane l owns column lx = l - rx, so every factor
+// lx is constant within a lane and comes out of the row loop.  The lane accumulates
+// row moments sum g*g'*ly^k (k = 0, 1, 2; g, g' in {gx, gy}) and forms its share of the
+// 21 Hessian entries from them once; S and G likewise (S_1 = lx * sum gx, ...).  The
+// target-side sums of k_icgn use the same forms, which keeps the exact self-match.
 // --------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_poi_prepare(const float4* __restrict__ ref_pack, int w, int h,
+__global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ ref_pack, int w, int h,
                                                      const dic_poi* __restrict__ pois, int64_t n,
                                                      int rx, int ry, PoiRef* __restrict__ out)
 {
@@ -268,33 +326,91 @@ __global__ void __launch_bounds__(256) k_poi_prepare(const float4* __restrict__ 
   const int sw = 2 * rx + 1, size = sw * (2 * ry + 1);
   const int cx = (int)px, cy = (int)py;
   float sum = 0.f;
-  for (int k = lane; k < size; k += 32)
-  {
-    const int lx = k % sw - rx, ly = k / sw - ry;
-    sum += ref_pack[(size_t)(cy + ly) * w + cx + lx].x;
-  }
-  sum = warp_sum(sum);
-  const float t0 = sum / (float)size;
-  float nsq = 0.f, src = 0.f, S[6] = {0.f}, G[6] = {0.f}, H[21] = {0.f};
-  // Same sample order and the same fmaf forms as the IC-GN kernel's target sums.
-  for (int k = lane; k < size; k += 32)
-  {
-    const int lx = k % sw - rx, ly = k / sw - ry;
-    const float4 v = ref_pack[(size_t)(cy + ly) * w + cx + lx];
-    const float rc = v.x - t0;
-    const float flx = (float)lx, fly = (float)ly;
-    const float sd[6] = {v.y, v.y * flx, v.y * fly, v.z, v.z * flx, v.z * fly};
-    nsq = fmaf(rc, rc, nsq);
-    src += rc;
-    int t = 0;
+  float nsq = 0.f, src = 0.f, S[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, G[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  float H[21];
 #pragma unroll
-    for (int a = 0; a < 6; ++a)
+  for (int t = 0; t < 21; ++t) H[t] = 0.f;
+  if (sw <= 32)
+  {
+    const float4* col = ref_pack + (size_t)(cy - ry) * w + cx + (lane - rx);
+    if (lane < sw)
+      for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&col[(size_t)r * w].x);
+    sum = warp_sum(sum);
+    const float t0 = sum / (float)size;
+    float Qxx[3] = {0.f, 0.f, 0.f}, Qyy[3] = {0.f, 0.f, 0.f}, Qxy[3] = {0.f, 0.f, 0.f};
+    if (lane < sw)
     {
-      S[a] += sd[a];
-      G[a] = fmaf(sd[a], rc, G[a]);
-#pragma unroll
-      for (int b = 0; b <= a; ++b) H[t++] += sd[a] * sd[b];
+      for (int r = 0; r < 2 * ry + 1; ++r)
+      {
+        const float fly = (float)(r - ry);
+        const float4 v = __ldg(&col[(size_t)r * w]);
+        const float rc = v.x - t0;
+        nsq = fmaf(rc, rc, nsq);
+        src += rc;
+        const float grc = __fmul_rn(v.y, rc), hrc = __fmul_rn(v.z, rc);
+        G[0] = __fadd_rn(G[0], grc);
+        G[2] = fmaf(grc, fly, G[2]);
+        G[3] = __fadd_rn(G[3], hrc);
+        G[5] = fmaf(hrc, fly, G[5]);
+        S[0] += v.y;
+        S[2] = fmaf(v.y, fly, S[2]);
+        S[3] += v.z;
+        S[5] = fmaf(v.z, fly, S[5]);
+        const float xx = v.y * v.y, yy = v.z * v.z, xy = v.y * v.z;
+        const float xxl = xx * fly, yyl = yy * fly, xyl = xy * fly;
+        Qxx[0] += xx; Qxx[1] += xxl; Qxx[2] = fmaf(xxl, fly, Qxx[2]);
+        Qyy[0] += yy; Qyy[1] += yyl; Qyy[2] = fmaf(yyl, fly, Qyy[2]);
+        Qxy[0] += xy; Qxy[1] += xyl; Qxy[2] = fmaf(xyl, fly, Qxy[2]);
+      }
     }
+    const float lx = (float)(lane - rx), lx2 = lx * lx;
+    G[1] = lx * G[0];
+    G[4] = lx * G[3];
+    S[1] = lx * S[0];
+    S[4] = lx * S[3];
+    // sd = [gx, gx lx, gx ly, gy, gy lx, gy ly]; H lower triangle, row-major (a >= b).
+    // Factor of sd_a sd_b by (f_a, f_b) with f in {1, lx, ly}:
+    //   (1,1) Q0, (lx,1) lx Q0, (lx,lx) lx^2 Q0, (ly,1) Q1, (ly,lx) lx Q1, (ly,ly) Q2.
+    H[0] = Qxx[0];                                   // (0,0)
+    H[1] = lx * Qxx[0];  H[2] = lx2 * Qxx[0];        // (1,0) (1,1)
+    H[3] = Qxx[1];  H[4] = lx * Qxx[1];  H[5] = Qxx[2];   // (2,0) (2,1) (2,2)
+    H[6] = Qxy[0];  H[7] = lx * Qxy[0];  H[8] = Qxy[1];  H[9] = Qyy[0];                 // (3,*)
+    H[10] = lx * Qxy[0];  H[11] = lx2 * Qxy[0];  H[12] = lx * Qxy[1];                   // (4,0..2)
+    H[13] = lx * Qyy[0];  H[14] = lx2 * Qyy[0];                                          // (4,3) (4,4)
+    H[15] = Qxy[1];  H[16] = lx * Qxy[1];  H[17] = Qxy[2];                               // (5,0..2)
+    H[18] = Qyy[1];  H[19] = lx * Qyy[1];  H[20] = Qyy[2];                               // (5,3..5)
+    if (lane >= sw)
+    {
+#pragma unroll
+      for (int t = 0; t < 21; ++t) H[t] = 0.f;
+#pragma unroll
+      for (int a = 0; a < 6; ++a) { S[a] = 0.f; G[a] = 0.f; }
+    }
+    if (lane == 0) rec->t0 = t0;
+  }
+  else
+  {
+    DIC_FOR_EACH_SAMPLE(lane, rx, ry, sum += __ldg(&ref_pack[(size_t)(cy + ly) * w + cx + lx].x);)
+    sum = warp_sum(sum);
+    const float t0 = sum / (float)size;
+    DIC_FOR_EACH_SAMPLE(lane, rx, ry,
+      const float4 v = __ldg(&ref_pack[(size_t)(cy + ly) * w + cx + lx]);
+      const float rc = v.x - t0;
+      const float flx = (float)lx, fly = (float)ly;
+      const float sd[6] = {v.y, v.y * flx, v.y * fly, v.z, v.z * flx, v.z * fly};
+      nsq = fmaf(rc, rc, nsq);
+      src += rc;
+      int t = 0;
+#pragma unroll
+      for (int a = 0; a < 6; ++a)
+      {
+        S[a] += sd[a];
+        G[a] = fmaf(sd[a], rc, G[a]);
+#pragma unroll
+        for (int b = 0; b <= a; ++b) H[t++] += sd[a] * sd[b];
+      }
+    )
+    if (lane == 0) rec->t0 = t0;
   }
   nsq = warp_sum(nsq);
   src = warp_sum(src);
@@ -304,34 +420,45 @@ __global__ void __launch_bounds__(256) k_poi_prepare(const float4* __restrict__ 
   for (int t = 0; t < 21; ++t) H[t] = warp_sum(H[t]);
   if (lane == 0)
   {
-    float hf[36];
+    float hf[6][6], inv[6][6];
     int t = 0;
+#pragma unroll
     for (int a = 0; a < 6; ++a)
-      for (int b = 0; b <= a; ++b) { hf[a * 6 + b] = H[t]; hf[b * 6 + a] = H[t]; ++t; }
-    inverse6(hf, rec->inv_h);
+#pragma unroll
+      for (int b = 0; b <= a; ++b) { hf[a][b] = H[t]; hf[b][a] = H[t]; ++t; }
+    inverse6(hf, inv);
     const float m_r = src * (1.f / (float)size);
     const float rn_sq = fmaf(-src, m_r, nsq);
-    rec->t0 = t0;
     rec->ref_norm = sqrtf(rn_sq);
     rec->ref_norm_sq = rn_sq;
     rec->sum_rc = src;
+#pragma unroll
     for (int a = 0; a < 6; ++a) { rec->S[a] = S[a]; rec->G[a] = fmaf(-m_r, S[a], G[a]); }
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+#pragma unroll
+      for (int b = 0; b < 6; ++b) rec->inv_h[a * 6 + b] = inv[a][b];
     rec->valid = 1.f;
   }
 }
 
 // --------------------------------------------------------------------------------------
 // IC-GN iteration (src/oc_icgn.cpp:168-387): one warp per POI.  Per iteration one pass
-// over the (2rx+1)(2ry+1) warped samples: warp the local coordinate, reject on the
-// interpolatable-range test, gather the texel's 16 B-spline coefficients (4 x 16 B),
-// evaluate the bicubic polynomial, and accumulate the nine single-pass sums (PoiRef).
-// The warp then reduces the sums with an xor butterfly, solves dp = invH * num on lanes
-// 0-5, and every lane applies the same inverse-compositional update W <- W * W(dp)^-1.
-// Control flow is warp-uniform; results do not depend on other POIs or on scheduling.
+// over the (2rx+1)(2ry+1) warped samples: warp the local coordinate, test the
+// interpolatable range, gather the texel's 16 B-spline coefficients (one float4 from each
+// coefficient-row plane), evaluate the bicubic polynomial, and accumulate the nine
+// single-pass sums (PoiRef).  The warp then reduces the sums with an xor butterfly, solves
+// dp = invH * num on lanes 0-5, and every lane applies the same inverse-compositional
+// update W <- W * W(dp)^-1.  Control flow is warp-uniform; results do not depend on other
+// POIs or on scheduling.
+//
+// The per-sample test is one combined range test (a NaN coordinate fails it too); only
+// when some sample fails does the warp re-walk the subset to apply the CPU's order, out of
+// range (-3) before NaN (-5).
 // --------------------------------------------------------------------------------------
 struct IcgnParams
 {
-  const float4* coef;      // tar B-spline table (4 float4 per texel)
+  const float4* coef;      // tar B-spline table: 4 planes of W*H float4
   const float4* ref_pack;  // {ref, gx, gy, 0}
   const PoiRef* poi_ref;   // per layout slot
   const int64_t* slot;     // queue index -> layout slot (nullptr: identity)
@@ -366,7 +493,23 @@ __device__ __forceinline__ void compose_update(float (&W)[6], const float (&dp)[
   W[5] = a3 * i2 + a4 * i5 + a5 * i8;
 }
 
-__global__ void __launch_bounds__(256) k_icgn(IcgnParams P)
+// Bicubic value at a warped sample from the coefficient-row planes (texel floor(x, y)).
+__device__ __forceinline__ float sample_bspline(const float4* __restrict__ coef, size_t plane, int w,
+                                                float gxp, float gyp)
+{
+  const float fx = floorf(gxp), fy = floorf(gyp);
+  const float4* c = coef + ((size_t)((int)fy * w + (int)fx));
+  const float dx = gxp - fx, dy = gyp - fy;
+  const float4 c0 = __ldg(c), c1 = __ldg(c + plane), c2 = __ldg(c + 2 * plane), c3 = __ldg(c + 3 * plane);
+  const float r0 = fmaf(fmaf(fmaf(c0.w, dx, c0.z), dx, c0.y), dx, c0.x);
+  const float r1 = fmaf(fmaf(fmaf(c1.w, dx, c1.z), dx, c1.y), dx, c1.x);
+  const float r2 = fmaf(fmaf(fmaf(c2.w, dx, c2.z), dx, c2.y), dx, c2.x);
+  const float r3 = fmaf(fmaf(fmaf(c3.w, dx, c3.z), dx, c3.y), dx, c3.x);
+  return fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
+}
+
+template <bool kColumn>
+__global__ void __launch_bounds__(128, 7) k_icgn(IcgnParams P)
 {
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
@@ -384,24 +527,24 @@ __global__ void __launch_bounds__(256) k_icgn(IcgnParams P)
     if (lane == 0) poi->zncc = zncc_in >= 0 ? -3.f : zncc_in;
     return;
   }
+  // Only t0 stays live across the sample loop; the other per-POI constants are re-read
+  // (L1-resident) after each reduction, which keeps the loop within 64 registers.
   const PoiRef* R = P.poi_ref + (P.slot ? P.slot[i] : i);
-  const float t0 = R->t0, ref_norm = R->ref_norm, ref_norm_sq = R->ref_norm_sq, sum_rc = R->sum_rc;
-  float S_l = 0.f, G_l = 0.f, invh_row[6];
-  if (lane < 6)
-  {
-    S_l = R->S[lane];
-    G_l = R->G[lane];
-#pragma unroll
-    for (int c = 0; c < 6; ++c) invh_row[c] = R->inv_h[lane * 6 + c];
-  }
+  const float t0 = R->t0;
   const int sw = 2 * rx + 1, size = sw * (2 * ry + 1);
   const float inv_size = 1.f / (float)size;
   const int cx = (int)px, cy = (int)py;
-  const int step_x = 32 % sw, step_y = 32 / sw;
-  const int lx0 = lane % sw - rx, ly0 = lane / sw - ry;
+  const size_t plane = (size_t)w * h;
+  const float4* __restrict__ coef = P.coef;
+  const float4* __restrict__ ref_pack = P.ref_pack;
   // warp matrix rows (Deformation2D1::setWarp, src/oc_deformation.cpp:116-128)
   float W[6] = {1.f + ux_in, uy_in, u_in, vx_in, 1.f + vy_in, v_in};
   const float rx2 = (float)(rx * rx), ry2 = (float)(ry * ry);
+  const float xmax = (float)(w - 2), ymax = (float)(h - 2);
+  constexpr bool column_walk = kColumn;   // the host picks kColumn = (2 rx + 1 <= 32)
+  const bool col_active = lane < sw;
+  const float flx_col = (float)(lane - rx);
+  const float4* ref_col = ref_pack + (size_t)(cy - ry) * w + cx + (lane - rx);
   int it = 0;
   float conv = 0.f, znssd = 0.f;
   int status = 0;  // 0 ok, -3 out of range, -5 NaN coordinate
@@ -409,53 +552,101 @@ __global__ void __launch_bounds__(256) k_icgn(IcgnParams P)
   {
     ++it;
     float A0 = 0.f, A1 = 0.f, A2 = 0.f, B[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    bool oob = false, nan_seen = false;
-    int lx = lx0, ly = ly0;
-    for (int k = lane; k < size; k += 32)
+    bool bad = false;
+    if constexpr (column_walk)
     {
-      const float flx = (float)lx, fly = (float)ly;
-      const float gxp = px + (W[0] * flx + W[1] * fly + W[2]);
-      const float gyp = py + (W[3] * flx + W[4] * fly + W[5]);
-      if (gxp < 1.f || gyp < 1.f || gxp >= (float)(w - 2) || gyp >= (float)(h - 2))
-        oob = true;
-      else if (isnan(gxp) || isnan(gyp))
-        nan_seen = true;
+      if (col_active)
+      {
+        const float ax = fmaf(W[0], flx_col, W[2]), ay = fmaf(W[3], flx_col, W[5]);
+#pragma unroll 1
+        for (int r = 0; r < 2 * ry + 1; ++r)
+        {
+          const float fly = (float)(r - ry);
+          const float gxp = px + fmaf(W[1], fly, ax);
+          const float gyp = py + fmaf(W[4], fly, ay);
+          if (!(gxp >= 1.f && gyp >= 1.f && gxp < xmax && gyp < ymax))
+          {
+            bad = true;
+            continue;
+          }
+          const float t = sample_bspline(coef, plane, w, gxp, gyp);
+          const float4 rv = __ldg(ref_col + (size_t)r * w);
+          const float tau = t - t0;
+          const float rc = rv.x - t0;
+          A0 += tau;
+          A1 = fmaf(tau, tau, A1);
+          A2 = fmaf(tau, rc, A2);
+          // __fmul_rn / __fadd_rn: never contracted, so these match k_poi_prepare's G bit for bit
+          const float gt = __fmul_rn(rv.y, tau), ht = __fmul_rn(rv.z, tau);
+          B[0] = __fadd_rn(B[0], gt);
+          B[2] = fmaf(gt, fly, B[2]);
+          B[3] = __fadd_rn(B[3], ht);
+          B[5] = fmaf(ht, fly, B[5]);
+        }
+      }
+      B[1] = flx_col * B[0];
+      B[4] = flx_col * B[3];
+    }
+    else
+    {
+      DIC_FOR_EACH_SAMPLE(lane, rx, ry,
+        const float flx = (float)lx, fly = (float)ly;
+        const float gxp = px + (W[0] * flx + W[1] * fly + W[2]);
+        const float gyp = py + (W[3] * flx + W[4] * fly + W[5]);
+        if (!(gxp >= 1.f && gyp >= 1.f && gxp < xmax && gyp < ymax))
+          bad = true;
+        else
+        {
+          const float t = sample_bspline(coef, plane, w, gxp, gyp);
+          const float4 rv = __ldg(ref_pack + (size_t)(cy + ly) * w + (cx + lx));
+          const float tau = t - t0;
+          const float rc = rv.x - t0;
+          A0 += tau;
+          A1 = fmaf(tau, tau, A1);
+          A2 = fmaf(tau, rc, A2);
+          B[0] = fmaf(rv.y, tau, B[0]);
+          B[1] = fmaf(rv.y * flx, tau, B[1]);
+          B[2] = fmaf(rv.y * fly, tau, B[2]);
+          B[3] = fmaf(rv.z, tau, B[3]);
+          B[4] = fmaf(rv.z * flx, tau, B[4]);
+          B[5] = fmaf(rv.z * fly, tau, B[5]);
+        }
+      )
+    }
+    if (__any_sync(kFull, bad))
+    {
+      // Rare path: classify with the CPU's order (src/oc_icgn.cpp:266-301).
+      bool oob = false;
+      if constexpr (column_walk)
+      {
+        if (col_active)
+        {
+          const float ax = fmaf(W[0], flx_col, W[2]), ay = fmaf(W[3], flx_col, W[5]);
+          for (int r = 0; r < 2 * ry + 1; ++r)
+          {
+            const float fly = (float)(r - ry);
+            const float gxp = px + fmaf(W[1], fly, ax), gyp = py + fmaf(W[4], fly, ay);
+            if (gxp < 1.f || gyp < 1.f || gxp >= xmax || gyp >= ymax) oob = true;
+          }
+        }
+      }
       else
       {
-        const float fx = floorf(gxp), fy = floorf(gyp);
-        const int xi = (int)fx, yi = (int)fy;
-        const float dx = gxp - fx, dy = gyp - fy;
-        const float4* c = P.coef + ((size_t)yi * w + xi) * 4;
-        const float4 c0 = __ldg(c + 0), c1 = __ldg(c + 1), c2 = __ldg(c + 2), c3 = __ldg(c + 3);
-        const float r0 = fmaf(fmaf(fmaf(c0.w, dx, c0.z), dx, c0.y), dx, c0.x);
-        const float r1 = fmaf(fmaf(fmaf(c1.w, dx, c1.z), dx, c1.y), dx, c1.x);
-        const float r2 = fmaf(fmaf(fmaf(c2.w, dx, c2.z), dx, c2.y), dx, c2.x);
-        const float r3 = fmaf(fmaf(fmaf(c3.w, dx, c3.z), dx, c3.y), dx, c3.x);
-        const float t = fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
-        const float4 rv = __ldg(P.ref_pack + (size_t)(cy + ly) * w + (cx + lx));
-        const float tau = t - t0;
-        const float rc = rv.x - t0;
-        A0 += tau;
-        A1 = fmaf(tau, tau, A1);
-        A2 = fmaf(tau, rc, A2);
-        B[0] = fmaf(rv.y, tau, B[0]);
-        B[1] = fmaf(rv.y * flx, tau, B[1]);
-        B[2] = fmaf(rv.y * fly, tau, B[2]);
-        B[3] = fmaf(rv.z, tau, B[3]);
-        B[4] = fmaf(rv.z * flx, tau, B[4]);
-        B[5] = fmaf(rv.z * fly, tau, B[5]);
+        DIC_FOR_EACH_SAMPLE(lane, rx, ry,
+          const float gxp = px + (W[0] * (float)lx + W[1] * (float)ly + W[2]);
+          const float gyp = py + (W[3] * (float)lx + W[4] * (float)ly + W[5]);
+          if (gxp < 1.f || gyp < 1.f || gxp >= xmax || gyp >= ymax) oob = true;
+        )
       }
-      lx += step_x;
-      ly += step_y;
-      if (lx > rx) { lx -= sw; ly += 1; }
+      status = __any_sync(kFull, oob) ? -3 : -5;
+      break;
     }
-    if (__any_sync(kFull, oob)) { status = -3; break; }
-    if (__any_sync(kFull, nan_seen)) { status = -5; break; }
     A0 = warp_sum(A0);
     A1 = warp_sum(A1);
     A2 = warp_sum(A2);
 #pragma unroll
     for (int a = 0; a < 6; ++a) B[a] = warp_sum(B[a]);
+    const float ref_norm = R->ref_norm, ref_norm_sq = R->ref_norm_sq, sum_rc = R->sum_rc;
     const float mean_tau = A0 * inv_size;
     const float tnorm_sq = fmaf(-A0, mean_tau, A1);
     // A flat target subset has zero norm; the CPU then divides by zero and the POI ends
@@ -466,6 +657,8 @@ __global__ void __launch_bounds__(256) k_icgn(IcgnParams P)
     const float esq = s * s * tnorm_sq - 2.f * s * tc_rc + ref_norm_sq;
     znssd = esq / (ref_norm * ref_norm);
     // lane a < 6: num_a, then dp_a = invH row a . num
+    const int row = lane < 6 ? lane : 0;
+    const float S_l = R->S[row], G_l = R->G[row];
     float num_l = 0.f;
 #pragma unroll
     for (int a = 0; a < 6; ++a)
@@ -475,7 +668,7 @@ __global__ void __launch_bounds__(256) k_icgn(IcgnParams P)
     for (int c = 0; c < 6; ++c)
     {
       const float nc = __shfl_sync(kFull, num_l, c);
-      if (lane < 6) dp_l += invh_row[c] * nc;
+      dp_l += R->inv_h[row * 6 + c] * nc;
     }
     float dp[6];
 #pragma unroll
@@ -492,16 +685,19 @@ __global__ void __launch_bounds__(256) k_icgn(IcgnParams P)
   float u = W[2], ux = W[0] - 1.f, uy = W[1], v = W[5], vx = W[3], vy = W[4] - 1.f;
   float zncc = 0.5f * (2.f - znssd);
   if (conv >= P.conv && (float)it >= P.max_iter) zncc = -4.f;
+  // The incoming guess is re-read here (the record is still unmodified) rather than kept
+  // live across the iteration loop.
+  const float u_init = poi->u, v_init = poi->v;
   if (isnan(zncc) || isnan(u) || isnan(v))
   {
-    u = u_in;
-    v = v_in;
+    u = u_init;
+    v = v_init;
     zncc = -5.f;
   }
   poi->u = u; poi->ux = ux; poi->uy = uy;
   poi->v = v; poi->vx = vx; poi->vy = vy;
-  poi->u0 = u_in;
-  poi->v0 = v_in;
+  poi->u0 = u_init;
+  poi->v0 = v_init;
   poi->zncc = zncc;
   poi->iteration = (float)it;
   poi->convergence = conv;

@@ -171,7 +171,7 @@ class Engine:
 
     def read_plane(self, plane: int, width: int, height: int) -> np.ndarray:
         shape = {_lib.DIC_PLANE_REF: (height, width), _lib.DIC_PLANE_TAR: (height, width),
-                 _lib.DIC_PLANE_REF_PACK: (height, width, 4), _lib.DIC_PLANE_TAR_COEF: (height, width, 16)}[plane]
+                 _lib.DIC_PLANE_REF_PACK: (height, width, 4), _lib.DIC_PLANE_TAR_COEF: (4, height, width, 4)}[plane]
         out = np.empty(shape, dtype=np.float32)
         self._call(self._L.dic_read_plane(self._h, plane, out.ctypes.data, out.nbytes))
         return out
