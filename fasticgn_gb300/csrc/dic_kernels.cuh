@@ -401,12 +401,12 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
       nsq = fmaf(rc, rc, nsq);
       src += rc;
       int t = 0;
-#pragma unroll
+      _Pragma("unroll")
       for (int a = 0; a < 6; ++a)
       {
         S[a] += sd[a];
         G[a] = fmaf(sd[a], rc, G[a]);
-#pragma unroll
+        _Pragma("unroll")
         for (int b = 0; b <= a; ++b) H[t++] += sd[a] * sd[b];
       }
     )
