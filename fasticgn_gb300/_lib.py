@@ -83,6 +83,8 @@ SIGNATURES = {
     "dic_read_plane": (ctypes.c_int, [_vp, _i32, _vp, _i64]),
     "dic_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(DicStats)]),
     "dic_set_timing": (ctypes.c_int, [_vp, _i32]),
+    "dic_process_pair_noalloc": (ctypes.c_int, [ctypes.POINTER(DicConfig), _vp, _vp, _i32, _i32, _i32, _vp, _i64,
+                                                _vp, ctypes.c_char_p, _i64]),
 }
 
 _lib = None

@@ -656,3 +656,155 @@ int dic_set_timing(dic_engine* e, int32_t enabled)
 }
 
 }  // extern "C"
+
+// --------------------------------------------------------------------------------------
+// Allocation-free pair solve.
+//
+// Some callers cannot call cudaMalloc: a host application that reserves the device memory
+// up front and hands its plug-ins only buffers it owns, or an acquisition loop in which
+// the implicit device synchronisation of an allocation would stall the camera's stream.
+// dic_process_pair_noalloc serves them.  The caller passes the two images and the POI queue
+// in device memory; everything else the pair needs (float planes, Gradient2D4 planes,
+// B-spline table, per-POI reference records) is carved from the fixed array below, which
+// every GPU that loads this library holds until the process exits.
+// --------------------------------------------------------------------------------------
+namespace
+{
+constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;   // 32 MiB
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mutex;
+std::vector<void*> g_noalloc_base;   // per device: device address of g_noalloc_scratch
+
+size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+void noalloc_error(char* text, int64_t cap, const std::string& msg)
+{
+  if (text && cap > 0)
+  {
+    const size_t n = std::min<size_t>(msg.size(), (size_t)cap - 1);
+    std::memcpy(text, msg.data(), n);
+    text[n] = '\0';
+  }
+}
+
+template <typename T>
+void noalloc_prepare(const void* ref, const void* tar, int w, int h, float scale, float* ref_f32,
+                     float4* ref_pack, float* tar_f32, float4* coef, cudaStream_t s)
+{
+  dim3 grid((w + kPrepTile - 1) / kPrepTile, (h + kPrepTile - 1) / kPrepTile);
+  k_prepare_ref<T><<<grid, 256, 0, s>>>(static_cast<const T*>(ref), w, h, scale, ref_f32, ref_pack);
+  k_prepare_tar<T><<<grid, 256, 0, s>>>(static_cast<const T*>(tar), w, h, scale, tar_f32, coef);
+}
+}  // namespace
+
+extern "C" int dic_process_pair_noalloc(const dic_config* cfg, const void* d_ref, const void* d_tar,
+                                        int32_t w, int32_t h, int32_t dtype, dic_poi* d_pois, int64_t n,
+                                        void* stream, char* error_text, int64_t error_capacity)
+{
+  if (!cfg || !d_ref || !d_tar || (n > 0 && !d_pois) || n < 0)
+  {
+    noalloc_error(error_text, error_capacity, "dic_process_pair_noalloc: null pointer or negative count");
+    return DIC_ERR_ARGUMENT;
+  }
+  const int r = cfg->subset_radius_x;
+  if (r < 1 || cfg->subset_radius_y != r || 2 * r > kMaxTwiddleN || cfg->max_iteration < 1 || w < 5 || h < 5 ||
+      dtype_size(dtype) == 0)
+  {
+    noalloc_error(error_text, error_capacity,
+                  "dic_process_pair_noalloc: needs a square subset radius 1..32, max_iteration >= 1, "
+                  "an image of at least 5x5 and dtype u8, u16 or f32");
+    return DIC_ERR_ARGUMENT;
+  }
+  const size_t px = (size_t)w * h;
+  const size_t off_ref = 0, off_pack = off_ref + align256(px * sizeof(float));
+  const size_t off_tar = off_pack + align256(px * sizeof(float4));
+  const size_t off_coef = off_tar + align256(px * sizeof(float));
+  const size_t off_poi = off_coef + align256(px * 4 * sizeof(float4));
+  const size_t need = off_poi + align256((size_t)n * sizeof(PoiRef));
+  if (need > kNoAllocScratchBytes)
+  {
+    noalloc_error(error_text, error_capacity,
+                  "dic_process_pair_noalloc: " + std::to_string(w) + "x" + std::to_string(h) + " with " +
+                      std::to_string(n) + " POIs needs " + std::to_string(need) +
+                      " bytes of scratch; the fixed scratch holds " + std::to_string(kNoAllocScratchBytes) +
+                      " (88 bytes per pixel + 224 bytes per POI, each plane rounded up to 256 bytes)");
+    return DIC_ERR_ARGUMENT;
+  }
+  try
+  {
+    int dev = 0;
+    DIC_CUDA(cudaGetDevice(&dev));
+    unsigned char* base = nullptr;
+    {
+      std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+      if ((int)g_noalloc_base.size() <= dev) g_noalloc_base.resize(dev + 1, nullptr);
+      if (!g_noalloc_base[dev])
+      {
+        // One-time set-up on this device (the current one): the array's device address,
+        // the constant tables, and the large-FFTCC shared-memory opt-in.
+        void* addr = nullptr;
+        DIC_CUDA(cudaGetSymbolAddress(&addr, g_noalloc_scratch));
+        init_constants(dev);
+        DIC_CUDA(cudaFuncSetAttribute(k_fftcc_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)(2 * kMaxTwiddleN * (kMaxTwiddleN + 1) * sizeof(float2))));
+        g_noalloc_base[dev] = addr;
+      }
+      base = static_cast<unsigned char*>(g_noalloc_base[dev]);
+    }
+    if (n == 0) return DIC_OK;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    float* ref_f32 = reinterpret_cast<float*>(base + off_ref);
+    float4* ref_pack = reinterpret_cast<float4*>(base + off_pack);
+    float* tar_f32 = reinterpret_cast<float*>(base + off_tar);
+    float4* coef = reinterpret_cast<float4*>(base + off_coef);
+    PoiRef* poi_ref = reinterpret_cast<PoiRef*>(base + off_poi);
+    const float scale = cfg->input_scale == 0.f ? 1.f : cfg->input_scale;
+    switch (dtype)
+    {
+      case DIC_U8: noalloc_prepare<uint8_t>(d_ref, d_tar, w, h, scale, ref_f32, ref_pack, tar_f32, coef, s); break;
+      case DIC_U16: noalloc_prepare<uint16_t>(d_ref, d_tar, w, h, scale, ref_f32, ref_pack, tar_f32, coef, s); break;
+      default: noalloc_prepare<float>(d_ref, d_tar, w, h, scale, ref_f32, ref_pack, tar_f32, coef, s); break;
+    }
+    const int wpb = 4;
+    const unsigned blocks = (unsigned)((n + wpb - 1) / wpb);
+    k_poi_prepare<<<blocks, wpb * 32, 0, s>>>(ref_pack, w, h, d_pois, n, r, r, poi_ref);
+    FftccParams fp{ref_f32, tar_f32, d_pois, n, w, h};
+    switch (2 * r)
+    {
+#define DIC_NOALLOC_FFTCC(M) \
+  case M: k_fftcc<M><<<(unsigned)((n + 3) / 4), 128, 0, s>>>(fp); break;
+      DIC_NOALLOC_FFTCC(8) DIC_NOALLOC_FFTCC(10) DIC_NOALLOC_FFTCC(12) DIC_NOALLOC_FFTCC(14) DIC_NOALLOC_FFTCC(16)
+      DIC_NOALLOC_FFTCC(18) DIC_NOALLOC_FFTCC(20) DIC_NOALLOC_FFTCC(22) DIC_NOALLOC_FFTCC(24)
+      DIC_NOALLOC_FFTCC(26) DIC_NOALLOC_FFTCC(28) DIC_NOALLOC_FFTCC(30) DIC_NOALLOC_FFTCC(32)
+#undef DIC_NOALLOC_FFTCC
+      default:
+        k_fftcc_large<<<(unsigned)n, 256, (size_t)2 * (2 * r) * (2 * r + 1) * sizeof(float2), s>>>(fp, 2 * r);
+    }
+    IcgnParams ip;
+    ip.coef = coef;
+    ip.ref_pack = ref_pack;
+    ip.poi_ref = poi_ref;
+    ip.slot = nullptr;
+    ip.pois = d_pois;
+    ip.n = n;
+    ip.w = w;
+    ip.h = h;
+    ip.rx = r;
+    ip.ry = r;
+    ip.conv = cfg->conv_criterion;
+    ip.max_iter = (float)cfg->max_iteration;
+    ip.iter_sum = nullptr;
+    if (2 * r + 1 <= 32)
+      k_icgn<true><<<blocks, wpb * 32, 0, s>>>(ip);
+    else
+      k_icgn<false><<<blocks, wpb * 32, 0, s>>>(ip);
+    DIC_CUDA(cudaGetLastError());
+  }
+  catch (const DicError& err)
+  {
+    noalloc_error(error_text, error_capacity, err.msg);
+    return err.code;
+  }
+  return DIC_OK;
+}

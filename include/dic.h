@@ -183,6 +183,34 @@ int dic_get_stats(const dic_engine* engine, dic_stats* out);
 /* Turns per-phase CUDA-event timing on (1) or off (0).  On by default. */
 int dic_set_timing(dic_engine* engine, int32_t enabled);
 
+/* Allocation-free pair solve (FFTCC seed + IC-GN).  No counterpart in the reference: its
+ * solvers allocate their device buffers themselves.
+ *
+ * For callers that cannot call cudaMalloc -- a host application that reserves device
+ * memory up front and hands its plug-ins only buffers it owns, or an acquisition loop in
+ * which an allocation's implicit device synchronisation would stall the camera stream.
+ * The caller passes the reference and target images (device memory, dense rows of width
+ * pixels of dtype) and the POI queue (device memory, updated in place, same result fields
+ * as dic_process_pair); all intermediate planes and per-POI records live in one fixed
+ * 32 MiB device array inside this library, held by every GPU that loads it until the
+ * process exits.  Limit: 88 bytes per pixel plus 224 bytes per POI (each plane rounded up
+ * to 256 bytes) must fit in 32 MiB, e.g. 512x512 with up to 46 811 POIs; larger calls are
+ * rejected with DIC_ERR_ARGUMENT and a message in error_text (nullable, error_capacity
+ * bytes).  The subset radius must be square, 1..32.
+ *
+ * The call enqueues its kernels on `stream` (a cudaStream_t, 0 = legacy default stream)
+ * and returns without waiting; it makes no cudaMalloc, cudaFree or other allocating call.
+ * The first call on a device (the current device) also performs one-time set-up -- it
+ * looks up the scratch array's device address and loads the constant tables -- so that
+ * first call should come before any stream capture.  Every call shares the one scratch
+ * array, which keeps the last call's contents; each call writes every scratch byte it
+ * later reads, so nothing needs clearing, but calls that overlap on the GPU (on different
+ * streams, or from different threads) race on the scratch and must be serialised by the
+ * caller. */
+int dic_process_pair_noalloc(const dic_config* config, const void* device_ref, const void* device_tar,
+                             int32_t width, int32_t height, int32_t dtype, dic_poi* device_pois,
+                             int64_t count, void* stream, char* error_text, int64_t error_capacity);
+
 #ifdef __cplusplus
 }
 #endif
