@@ -54,7 +54,7 @@ class DicFrameReport(ctypes.Structure):
 class DicStats(ctypes.Structure):
     _fields_ = [("ms_prepare_ref", ctypes.c_double), ("ms_poi_prepare", ctypes.c_double),
                 ("ms_prepare_tar", ctypes.c_double), ("ms_fftcc", ctypes.c_double),
-                ("ms_icgn", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
+                ("ms_icgn", ctypes.c_double), ("ms_frame", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
                 ("icgn_pois", ctypes.c_int64), ("icgn_iterations", ctypes.c_int64)]
 
 
@@ -80,6 +80,10 @@ SIGNATURES = {
     "dic_process_frame": (ctypes.c_int, [_vp, _vp, _i64, _vp, ctypes.POINTER(DicFramePolicy),
                                          ctypes.POINTER(DicFrameReport)]),
     "dic_run_device": (ctypes.c_int, [_vp, _vp, _i64, _i32]),
+    "dic_sequence_begin": (ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(DicFramePolicy)]),
+    "dic_sequence_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32, _i32, _vp,
+                                          ctypes.POINTER(DicFrameReport)]),
+    "dic_set_graphs": (ctypes.c_int, [_vp, _i32]),
     "dic_read_plane": (ctypes.c_int, [_vp, _i32, _vp, _i64]),
     "dic_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(DicStats)]),
     "dic_set_timing": (ctypes.c_int, [_vp, _i32]),

@@ -98,7 +98,7 @@ void init_constants(int device)
   g_initialized_devices.insert(device);
 }
 
-enum Phase { kPhRef = 0, kPhPoi, kPhTar, kPhFftcc, kPhIcgn, kPhCount };
+enum Phase { kPhRef = 0, kPhPoi, kPhTar, kPhFftcc, kPhIcgn, kPhFrame, kPhCount };
 
 }  // namespace
 
@@ -303,12 +303,14 @@ struct dic_engine
   }
 
   // ---------------------------------------------------------------- solvers
-  void run_fftcc(dic_poi* d_pois, int64_t n)
+  void run_fftcc(dic_poi* d_pois, int64_t n, const int64_t* n_dev = nullptr, const int* enable = nullptr)
   {
     if (n == 0) return;
     ensure_ref();
     ensure_tar();
     FftccParams p{ref_f32.ptr, tar_f32.ptr, d_pois, n, w, h};
+    p.n_dev = n_dev;
+    p.enable = enable;
     const int r = cfg.subset_radius_x;
     const unsigned blocks = (unsigned)((n + 3) / 4);
     mark(kPhFftcc, 0);
@@ -326,7 +328,6 @@ struct dic_engine
           throw DicError{DIC_ERR_ARGUMENT, "FFTCC supports subset radius 1..32 on this engine"};
         const int m = 2 * r;
         const size_t smem = (size_t)2 * m * (m + 1) * sizeof(float2);
-        DIC_CUDA(cudaFuncSetAttribute(k_fftcc_large, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_fftcc_large<<<(unsigned)n, 256, smem, stream>>>(p, m);
       }
     }
@@ -334,14 +335,17 @@ struct dic_engine
     mark(kPhFftcc, 1);
   }
 
-  void run_icgn(dic_poi* d_pois, int64_t n, const int64_t* d_slots)
+  void run_icgn(dic_poi* d_pois, int64_t n, const int64_t* d_slots, const int64_t* n_dev = nullptr,
+                const int* enable = nullptr, bool reset_iterations = true)
   {
     if (n == 0) return;
     ensure_ref();
     ensure_tar();
     counters.ensure(1);
-    DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
+    if (reset_iterations) DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
     IcgnParams p;
+    p.n_dev = n_dev;
+    p.enable = enable;
     p.coef = coef.ptr;
     p.ref_pack = ref_pack.ptr;
     p.poi_ref = poi_ref.ptr;
@@ -365,6 +369,104 @@ struct dic_engine
     mark(kPhIcgn, 1);
     icgn_pois = n;
     iter_pending = true;
+  }
+
+  // ---------------------------------------------------------------- frames
+  // Device queues of the frame policy: tmpl (layout template), prev (previous frame's
+  // results), queue (current frame), scratch (whole-frame pass), fq (repair candidates).
+  DevBuf<dic_poi> tmpl, prev, scratch, fq;
+  DevBuf<int64_t> cand;
+  DevBuf<FrameCounters> fcount;
+  DevBuf<float> baseline;         // sequence: first frame's bad ratio + margin
+  dic_frame_policy seq_policy{};
+  int64_t seq_n = 0;
+  long long seq_frame = 0;
+  bool use_graphs = true;
+  cudaGraphExec_t seq_graph = nullptr;
+  int seq_graph_kernels = 0;
+
+  void ensure_frame_buffers(int64_t n)
+  {
+    tmpl.ensure((size_t)n);
+    prev.ensure((size_t)n);
+    scratch.ensure((size_t)n);
+    fq.ensure((size_t)n);
+    cand.ensure((size_t)n);
+    queue.ensure((size_t)n);
+    fcount.ensure(1);
+    baseline.ensure(1);
+  }
+
+  // Enqueue one frame on the device queues (no host synchronisation).  The layout must be
+  // tmpl's.  use_skip: seed from prev and run the policy; otherwise FFTCC + IC-GN from the
+  // template.  frame_threshold: device pointer (sequence) or host value.
+  void enqueue_frame(int64_t n, bool use_skip, const dic_frame_policy& pol, const float* threshold_dev,
+                     float threshold_host)
+  {
+    const unsigned tb = 256, nb = (unsigned)((n + tb - 1) / tb);
+    const float thr = pol.zncc_threshold;
+    DIC_CUDA(cudaMemsetAsync(fcount.ptr, 0, sizeof(FrameCounters), stream));
+    DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
+    if (!use_skip)
+    {
+      DIC_CUDA(cudaMemcpyAsync(queue.ptr, tmpl.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, stream));
+      run_fftcc(queue.ptr, n);
+      run_icgn(queue.ptr, n, nullptr, nullptr, nullptr, false);
+      k_count_bad<<<nb, tb, 0, stream>>>(queue.ptr, thr, &fcount.ptr->bad, n);
+      check_launch("k_count_bad");
+      k_count_bad<<<nb, tb, 0, stream>>>(queue.ptr, thr, &fcount.ptr->bad_after, n);
+      check_launch("k_count_bad");
+      return;
+    }
+    k_seed_from_previous<<<nb, tb, 0, stream>>>(tmpl.ptr, prev.ptr, queue.ptr, n);
+    check_launch("k_seed_from_previous");
+    run_icgn(queue.ptr, n, nullptr, nullptr, nullptr, false);
+    k_scan_bad<<<nb, tb, 0, stream>>>(queue.ptr, prev.ptr, thr, pol.poi_fallback, fcount.ptr, cand.ptr, n);
+    check_launch("k_scan_bad");
+    if (threshold_dev)
+      k_decide_dev<<<1, 32, 0, stream>>>(fcount.ptr, n, threshold_dev, pol.poi_fallback);
+    else
+      k_decide<<<1, 32, 0, stream>>>(fcount.ptr, n, threshold_host, pol.poi_fallback);
+    check_launch("k_decide");
+    // whole-frame pass: FFTCC + IC-GN from the template, merged per POI
+    const int* ff = &fcount.ptr->frame_fallback;
+    k_copy_queue<<<nb, tb, 0, stream>>>(tmpl.ptr, scratch.ptr, ff, n);
+    check_launch("k_copy_queue");
+    run_fftcc(scratch.ptr, n, nullptr, ff);
+    run_icgn(scratch.ptr, n, nullptr, nullptr, ff, false);
+    k_merge_frame<<<nb, tb, 0, stream>>>(queue.ptr, scratch.ptr, fcount.ptr, thr, n);
+    check_launch("k_merge_frame");
+    // POI-level repair of the candidates (layout slots = template indices)
+    const int* pr = &fcount.ptr->poi_repair;
+    const int64_t* cn = &fcount.ptr->candidate_count;
+    k_gather_candidates<<<nb, tb, 0, stream>>>(tmpl.ptr, cand.ptr, fcount.ptr, fq.ptr, n);
+    check_launch("k_gather_candidates");
+    run_fftcc(fq.ptr, n, cn, pr);
+    run_icgn(fq.ptr, n, cand.ptr, cn, pr, false);
+    k_merge_repair<<<nb, tb, 0, stream>>>(queue.ptr, fq.ptr, cand.ptr, fcount.ptr, thr, n);
+    check_launch("k_merge_repair");
+    k_count_bad<<<nb, tb, 0, stream>>>(queue.ptr, thr, &fcount.ptr->bad_after, n);
+    check_launch("k_count_bad");
+  }
+
+  void fill_report(dic_frame_report* r, int64_t n, bool use_skip, const dic_poi* host_results)
+  {
+    if (!r) return;
+    FrameCounters c{};
+    DIC_CUDA(cudaMemcpyAsync(&c, fcount.ptr, sizeof(c), cudaMemcpyDeviceToHost, stream));
+    DIC_CUDA(cudaStreamSynchronize(stream));
+    r->pois = n;
+    r->bad_before_repair = (int64_t)c.bad;
+    r->bad_after_repair = (int64_t)c.bad_after;
+    r->repaired_candidates = use_skip && c.poi_repair ? (int64_t)c.candidates : 0;
+    r->frame_fallback_used = use_skip ? c.frame_fallback : 0;
+    r->fftcc_used = (!use_skip || c.frame_fallback || c.poi_repair) ? 1 : 0;
+    double it = 0.0;
+    int64_t valid = 0;
+    if (host_results)
+      for (int64_t i = 0; i < n; ++i)
+        if (host_results[i].zncc >= 0.f) { it += host_results[i].iteration; ++valid; }
+    r->iteration_mean = valid ? it / (double)valid : 0.0;
   }
 
   // IC-GN on the device queue `queue` whose host copy is `pois`.
@@ -431,6 +533,8 @@ int dic_engine_create(const dic_config* config, dic_engine** out)
     DIC_CUDA(cudaSetDevice(config->device));
     init_constants(config->device);
     DIC_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    DIC_CUDA(cudaFuncSetAttribute(k_fftcc_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)(2 * kMaxTwiddleN * (kMaxTwiddleN + 1) * sizeof(float2))));
     for (int p = 0; p < kPhCount; ++p)
       for (int k = 0; k < 2; ++k) DIC_CUDA(cudaEventCreate(&e->ev[p][k]));
   }
@@ -459,6 +563,14 @@ void dic_engine_destroy(dic_engine* e)
   e->queue.release();
   e->slots.release();
   e->counters.release();
+  if (e->seq_graph) cudaGraphExecDestroy(e->seq_graph);
+  e->tmpl.release();
+  e->prev.release();
+  e->scratch.release();
+  e->fq.release();
+  e->cand.release();
+  e->fcount.release();
+  e->baseline.release();
   for (int p = 0; p < kPhCount; ++p)
     for (int k = 0; k < 2; ++k)
       if (e->ev[p][k]) cudaEventDestroy(e->ev[p][k]);
@@ -601,12 +713,154 @@ int dic_run_device(dic_engine* e, dic_poi* d_pois, int64_t n, int32_t flags)
 int dic_process_frame(dic_engine* e, dic_poi* pois, int64_t n, const dic_poi* prev,
                       const dic_frame_policy* policy, dic_frame_report* report)
 {
-  (void)prev;
-  (void)policy;
-  (void)report;
-  (void)pois;
-  (void)n;
-  return guarded(e, [&] { throw DicError{DIC_ERR_STATE, "dic_process_frame: not built yet"}; });
+  return guarded(e, [&] {
+    if (n < 0 || (n > 0 && !pois) || !policy) throw DicError{DIC_ERR_ARGUMENT, "process_frame: bad arguments"};
+    if (!e->ref_set || !e->tar_set) throw DicError{DIC_ERR_STATE, "images must be set before compute"};
+    if (e->cfg.subset_radius_x != e->cfg.subset_radius_y)
+      throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D supports positive square radii only"};
+    if (report) *report = dic_frame_report{};
+    if (n == 0) return;
+    e->ensure_frame_buffers(n);
+    e->counters.ensure(1);
+    DIC_CUDA(cudaMemcpyAsync(e->tmpl.ptr, pois, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, e->stream));
+    const bool use_skip = policy->skip_fftcc && prev != nullptr;
+    if (use_skip)
+      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, prev, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, e->stream));
+    if (!e->layout_matches(pois, n))
+    {
+      e->record_layout(pois, n);
+      e->prepare_layout_device(e->tmpl.ptr, n);
+    }
+    e->enqueue_frame(n, use_skip, *policy, nullptr, policy->frame_fallback_ratio);
+    e->iter_pending = true;
+    e->download_queue(pois, n);
+    e->fill_report(report, n, use_skip, pois);
+  });
+}
+
+int dic_sequence_begin(dic_engine* e, const dic_poi* pois, int64_t n, const dic_frame_policy* policy)
+{
+  return guarded(e, [&] {
+    if (n <= 0 || !pois || !policy) throw DicError{DIC_ERR_ARGUMENT, "sequence_begin: bad arguments"};
+    if (!e->ref_set) throw DicError{DIC_ERR_STATE, "reference image must be set before a sequence"};
+    if (e->cfg.subset_radius_x != e->cfg.subset_radius_y)
+      throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D supports positive square radii only"};
+    for (int64_t i = 0; i < n; ++i)
+      if (!finite_xy(pois[i])) throw DicError{DIC_ERR_ARGUMENT, "sequence_begin: non-finite POI coordinate"};
+    if (e->seq_graph)
+    {
+      cudaGraphExecDestroy(e->seq_graph);
+      e->seq_graph = nullptr;
+    }
+    e->ensure_frame_buffers(n);
+    e->counters.ensure(1);
+    DIC_CUDA(cudaMemcpyAsync(e->tmpl.ptr, pois, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, e->stream));
+    e->record_layout(pois, n);
+    e->prepare_layout_device(e->tmpl.ptr, n);
+    const float inf = INFINITY;
+    DIC_CUDA(cudaMemcpyAsync(e->baseline.ptr, &inf, sizeof(float), cudaMemcpyHostToDevice, e->stream));
+    DIC_CUDA(cudaStreamSynchronize(e->stream));
+    e->seq_policy = *policy;
+    e->seq_n = n;
+    e->seq_frame = 0;
+  });
+}
+
+int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int64_t stride, int32_t dtype,
+                       int32_t pixels_on_device, dic_poi* results, dic_frame_report* report)
+{
+  return guarded(e, [&] {
+    if (e->seq_n <= 0) throw DicError{DIC_ERR_STATE, "dic_sequence_begin must come first"};
+    if (w != e->w || h != e->h) throw DicError{DIC_ERR_ARGUMENT, "reference and target image sizes must match"};
+    if (report) *report = dic_frame_report{};
+    const int64_t n = e->seq_n;
+    if (e->ref_dirty || !e->layout_ready || e->layout_count != n)
+      throw DicError{DIC_ERR_STATE, "the reference or the POI layout changed; call dic_sequence_begin again"};
+    const int64_t launches_before = e->launches;
+    e->set_image(false, px, w, h, stride, dtype, pixels_on_device != 0);
+    const dic_frame_policy& pol = e->seq_policy;
+    const bool use_skip = pol.skip_fftcc && e->seq_frame > 0;
+    e->mark(kPhFrame, 0);
+    if (!use_skip)
+    {
+      e->ensure_tar();
+      e->enqueue_frame(n, false, pol, nullptr, INFINITY);
+      if (pol.skip_fftcc && e->seq_frame == 0)
+      {
+        k_set_baseline<<<1, 32, 0, e->stream>>>(e->fcount.ptr, n, pol.frame_fallback_ratio, e->baseline.ptr);
+        e->check_launch("k_set_baseline");
+      }
+      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+    }
+    else if (e->use_graphs)
+    {
+      if (!e->seq_graph)
+      {
+        // Capture the steady-state frame once: target table, seed, IC-GN, scan, decide,
+        // both repair paths behind device switches, merge, count, results -> prev.
+        const bool timing = e->timing;
+        e->timing = false;
+        e->tar_dirty = true;
+        const int64_t l0 = e->launches;
+        cudaGraph_t g = nullptr;
+        DIC_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        try
+        {
+          e->ensure_tar();
+          e->enqueue_frame(n, true, pol, e->baseline.ptr, 0.f);
+          DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+        }
+        catch (...)
+        {
+          cudaStreamEndCapture(e->stream, &g);
+          if (g) cudaGraphDestroy(g);
+          e->timing = timing;
+          throw;
+        }
+        DIC_CUDA(cudaStreamEndCapture(e->stream, &g));
+        e->timing = timing;
+        e->seq_graph_kernels = (int)(e->launches - l0);
+        e->launches = l0;
+        cudaError_t ie = cudaGraphInstantiate(&e->seq_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess)
+        {
+          e->seq_graph = nullptr;
+          throw DicError{DIC_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie)};
+        }
+      }
+      DIC_CUDA(cudaGraphLaunch(e->seq_graph, e->stream));
+      e->launches += e->seq_graph_kernels;
+      e->tar_dirty = false;
+    }
+    else
+    {
+      e->ensure_tar();
+      e->enqueue_frame(n, true, pol, e->baseline.ptr, 0.f);
+      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+    }
+    e->mark(kPhFrame, 1);
+    e->iter_pending = true;
+    e->icgn_pois = n;
+    (void)launches_before;
+    if (results)
+      DIC_CUDA(cudaMemcpyAsync(results, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, e->stream));
+    if (results || report) DIC_CUDA(cudaStreamSynchronize(e->stream));
+    e->fill_report(report, n, use_skip, results);
+    ++e->seq_frame;
+  });
+}
+
+int dic_set_graphs(dic_engine* e, int32_t enabled)
+{
+  return guarded(e, [&] {
+    e->use_graphs = enabled != 0;
+    if (!e->use_graphs && e->seq_graph)
+    {
+      cudaGraphExecDestroy(e->seq_graph);
+      e->seq_graph = nullptr;
+    }
+  });
 }
 
 int dic_read_plane(dic_engine* e, int32_t plane, void* dst, int64_t bytes)
@@ -641,6 +895,7 @@ int dic_get_stats(const dic_engine* ce, dic_stats* out)
     out->ms_prepare_tar = e->ms[kPhTar];
     out->ms_fftcc = e->ms[kPhFftcc];
     out->ms_icgn = e->ms[kPhIcgn];
+    out->ms_frame = e->ms[kPhFrame];
     out->kernel_launches = e->launches;
     out->icgn_pois = e->icgn_pois;
     out->icgn_iterations = (int64_t)e->iter_sum;

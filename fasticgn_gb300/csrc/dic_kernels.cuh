@@ -468,7 +468,20 @@ struct IcgnParams
   float conv;
   float max_iter;
   unsigned long long* iter_sum;  // sum of iterations (nullable)
+  const int64_t* n_dev = nullptr;   // device-side queue length (overrides n when set)
+  const int* enable = nullptr;      // device-side switch: the launch does nothing when 0
 };
+
+// Queue-slot guard shared by the solver kernels: launches sized for the largest possible
+// queue take their real length and an on/off switch from device memory, so a frame's
+// whole launch sequence can be enqueued (or captured in a graph) before its data-dependent
+// branches are known.
+template <class Params>
+__device__ __forceinline__ bool queue_slot_active(const Params& P, int64_t i)
+{
+  if (P.enable && *P.enable == 0) return false;
+  return i < (P.n_dev ? *P.n_dev : P.n);
+}
 
 __device__ __forceinline__ void compose_update(float (&W)[6], const float (&dp)[6])
 {
@@ -513,7 +526,7 @@ __global__ void __launch_bounds__(128, 7) k_icgn(IcgnParams P)
 {
   const int lane = threadIdx.x & 31;
   const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (i >= P.n) return;
+  if (!queue_slot_active(P, i)) return;
   dic_poi* poi = P.pois + i;
   const float px = poi->x, py = poi->y;
   const float u_in = poi->u, ux_in = poi->ux, uy_in = poi->uy;
@@ -875,6 +888,8 @@ struct FftccParams
   dic_poi* pois;
   int64_t n;
   int w, h;
+  const int64_t* n_dev = nullptr;   // device-side queue length (overrides n when set)
+  const int* enable = nullptr;      // device-side switch: the launch does nothing when 0
 };
 
 template <int M>
@@ -886,7 +901,7 @@ __global__ void __launch_bounds__(128) k_fftcc(FftccParams P)
   __shared__ float2 smem[kWarpsPerBlock][M * S];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t i = (int64_t)blockIdx.x * kWarpsPerBlock + warp;
-  if (i >= P.n) return;
+  if (!queue_slot_active(P, i)) return;
   float2* z = smem[warp];
   dic_poi* poi = P.pois + i;
   const float px = poi->x, py = poi->y, u_init = poi->u, v_init = poi->v;
@@ -1091,7 +1106,7 @@ __global__ void __launch_bounds__(256) k_fftcc_large(FftccParams P, int m)
   float2* za = dyn;
   float2* zb = dyn + m * s;
   const int64_t i = blockIdx.x;
-  if (i >= P.n) return;
+  if (!queue_slot_active(P, i)) return;
   dic_poi* poi = P.pois + i;
   const float px = poi->x, py = poi->y, u_init = poi->u, v_init = poi->v;
   const int w = P.w, h = P.h, R = m / 2;
@@ -1163,6 +1178,171 @@ __global__ void __launch_bounds__(256) k_fftcc_large(FftccParams P, int m)
     poi->v0 = v_init;
     poi->zncc = best / (sqrtf(rn * tn) * (float)(m * m));
   }
+}
+
+// --------------------------------------------------------------------------------------
+// Frame policy (processFrame, opencorr_cli_cuda_mvp.cpp:3024-3210) on the device.
+// A frame is one fixed launch sequence: seed from the previous frame, IC-GN, scan for bad
+// POIs, decide, then either the whole-frame FFTCC + IC-GN pass with a per-POI merge or
+// the POI-level repair (FFTCC + IC-GN on the candidates only, through the layout slots),
+// each gated by a device-side switch.  The per-POI rules are the reference's own:
+//   bad        isBadPoiForFallback            (:490-494)
+//   candidate  isPoiLevelFallbackCandidate    (:541-558)
+//   replace    shouldReplacePoiWithFallback   (:503-515)
+//   take       shouldTakeFrameFallbackResult  (:524-539)
+// --------------------------------------------------------------------------------------
+struct FrameCounters
+{
+  unsigned long long bad;         // bad POIs after the skip attempt
+  unsigned long long candidates;  // POI-level repair candidates
+  unsigned long long recovered;   // repaired POIs that are no longer bad
+  unsigned long long bad_after;   // bad POIs in the final result
+  int64_t candidate_count;        // = candidates, as a queue length for the repair launches
+  int frame_fallback;             // 1: whole-frame pass runs
+  int poi_repair;                 // 1: POI-level repair runs
+};
+
+__device__ __forceinline__ bool is_bad_poi(float z, float thr) { return z != -3.f && (!isfinite(z) || z < thr); }
+
+__device__ __forceinline__ bool replace_with_fallback(float cur_z, float fb_z)
+{
+  if (!isfinite(fb_z) || fb_z == -3.f) return false;
+  if (!isfinite(cur_z)) return true;
+  return fb_z >= cur_z;
+}
+
+// seedPoiQueueFromPrevious (:560-624) without temporal extrapolation: the template record,
+// with the previous frame's six first-order parameters where that result is valid and
+// its result fields cleared.
+__global__ void k_seed_from_previous(const dic_poi* __restrict__ tmpl, const dic_poi* __restrict__ prev,
+                                     dic_poi* __restrict__ cur, int64_t n)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  dic_poi q = tmpl[i];
+  const dic_poi p = prev[i];
+  if (isfinite(p.zncc) && p.zncc >= 0.f)
+  {
+    q.u = p.u; q.ux = p.ux; q.uy = p.uy;
+    q.v = p.v; q.vx = p.vx; q.vy = p.vy;
+    q.u0 = 0.f; q.v0 = 0.f; q.zncc = 0.f; q.iteration = 0.f; q.convergence = 0.f; q.feature = 0.f;
+  }
+  cur[i] = q;
+}
+
+__global__ void k_scan_bad(const dic_poi* __restrict__ cur, const dic_poi* __restrict__ prev, float thr,
+                           int poi_fallback, FrameCounters* __restrict__ c, int64_t* __restrict__ cand, int64_t n)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool bad = false, candidate = false;
+  if (i < n)
+  {
+    const float z = cur[i].zncc;
+    bad = is_bad_poi(z, thr);
+    if (bad && poi_fallback)
+    {
+      if (!isfinite(z) || z < 0.f)
+        candidate = true;
+      else if (!prev || prev[i].x != cur[i].x || prev[i].y != cur[i].y || !isfinite(prev[i].zncc))
+        candidate = true;
+      else
+        candidate = prev[i].zncc >= thr;
+    }
+  }
+  const unsigned bad_mask = __ballot_sync(kFull, bad);
+  if ((threadIdx.x & 31) == 0 && bad_mask) atomicAdd(&c->bad, (unsigned long long)__popc(bad_mask));
+  if (candidate)
+  {
+    // Slot order depends on scheduling; every candidate is solved and merged on its own,
+    // so the frame's result does not.
+    const unsigned long long k = atomicAdd(&c->candidates, 1ull);
+    cand[k] = i;
+  }
+}
+
+__global__ void k_decide(FrameCounters* c, int64_t n, float frame_threshold, int poi_fallback)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  // computeBadZnccRatioFromCount (:626-634), then the > test of :3115
+  const float ratio = n > 0 ? (float)c->bad / (float)n : 0.f;
+  c->frame_fallback = ratio > frame_threshold ? 1 : 0;
+  c->poi_repair = (!c->frame_fallback && poi_fallback && c->candidates > 0) ? 1 : 0;
+  c->candidate_count = (int64_t)c->candidates;
+}
+
+// The same with the threshold in device memory (fixed-reference sequences).
+__global__ void k_decide_dev(FrameCounters* c, int64_t n, const float* frame_threshold, int poi_fallback)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const float ratio = n > 0 ? (float)c->bad / (float)n : 0.f;
+  c->frame_fallback = ratio > *frame_threshold ? 1 : 0;
+  c->poi_repair = (!c->frame_fallback && poi_fallback && c->candidates > 0) ? 1 : 0;
+  c->candidate_count = (int64_t)c->candidates;
+}
+
+// First frame of a sequence: fallback threshold = its bad ratio + margin (:4275-4279).
+__global__ void k_set_baseline(const FrameCounters* c, int64_t n, float margin, float* threshold)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const float ratio = n > 0 ? (float)c->bad / (float)n : 0.f;
+  *threshold = ratio + margin;
+}
+
+__global__ void k_copy_queue(const dic_poi* __restrict__ src, dic_poi* __restrict__ dst, const int* enable, int64_t n)
+{
+  if (enable && *enable == 0) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) dst[i] = src[i];
+}
+
+__global__ void k_gather_candidates(const dic_poi* __restrict__ tmpl, const int64_t* __restrict__ cand,
+                                    const FrameCounters* c, dic_poi* __restrict__ fq, int64_t n_max)
+{
+  if (c->poi_repair == 0) return;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < c->candidate_count && k < n_max) fq[k] = tmpl[cand[k]];
+}
+
+// runPoiLevelFallback merge (:3003-3017)
+__global__ void k_merge_repair(dic_poi* __restrict__ cur, const dic_poi* __restrict__ fq,
+                               const int64_t* __restrict__ cand, FrameCounters* c, float thr, int64_t n_max)
+{
+  if (c->poi_repair == 0) return;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c->candidate_count || k >= n_max) return;
+  const int64_t idx = cand[k];
+  const dic_poi f = fq[k];
+  if (replace_with_fallback(cur[idx].zncc, f.zncc))
+  {
+    if (!is_bad_poi(f.zncc, thr)) atomicAdd(&c->recovered, 1ull);
+    cur[idx] = f;
+  }
+}
+
+// Whole-frame merge (:3141-3149, shouldTakeFrameFallbackResult)
+__global__ void k_merge_frame(dic_poi* __restrict__ cur, const dic_poi* __restrict__ scratch,
+                              const FrameCounters* c, float thr, int64_t n)
+{
+  if (c->frame_fallback == 0) return;
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float sk = cur[i].zncc, sc = scratch[i].zncc;
+  bool take;
+  if (sk == -3.f)
+    take = isfinite(sc) && sc != -3.f && sc >= thr;
+  else if (is_bad_poi(sk, thr))
+    take = replace_with_fallback(sk, sc);
+  else
+    take = false;
+  if (take) cur[i] = scratch[i];
+}
+
+__global__ void k_count_bad(const dic_poi* __restrict__ cur, float thr, unsigned long long* out, int64_t n)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const bool bad = i < n && is_bad_poi(cur[i].zncc, thr);
+  const unsigned m = __ballot_sync(kFull, bad);
+  if ((threadIdx.x & 31) == 0 && m) atomicAdd(out, (unsigned long long)__popc(m));
 }
 
 }  // namespace dic

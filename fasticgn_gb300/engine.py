@@ -166,6 +166,39 @@ class Engine:
                                              ctypes.byref(rep)))
         return q, {f: getattr(rep, f) for f, _ in rep._fields_}
 
+    def sequence_begin(self, template: np.ndarray, skip_fftcc: bool = True, poi_fallback: bool = True,
+                       zncc_threshold: float = 0.8, frame_fallback_margin: float = 0.03) -> None:
+        q = _check_queue(template)
+        pol = _lib.DicFramePolicy(int(skip_fftcc), int(poi_fallback), float(zncc_threshold),
+                                  float(frame_fallback_margin))
+        self._call(self._L.dic_sequence_begin(self._h, q.ctypes.data, len(q), ctypes.byref(pol)))
+        self._seq_n = len(q)
+
+    def sequence_frame(self, tar, results: np.ndarray | None = None, device_ptr: int | None = None,
+                       width: int = 0, height: int = 0, dtype: int = _lib.DIC_U8):
+        """Solve one target frame of the sequence; ``tar`` is a host image, or None with
+        ``device_ptr`` (dense rows) for a frame already on the device."""
+        rep = _lib.DicFrameReport()
+        out_ptr = None
+        if results is not None:
+            results = _check_queue(results)
+            if len(results) != self._seq_n:
+                raise ValueError("results must hold one record per template POI")
+            out_ptr = results.ctypes.data
+        if tar is not None:
+            img, dt = self._image(tar)
+            rc = self._L.dic_sequence_frame(self._h, img.ctypes.data, img.shape[1], img.shape[0], img.strides[0], dt,
+                                            0, out_ptr, ctypes.byref(rep))
+        else:
+            es = {_lib.DIC_U8: 1, _lib.DIC_U16: 2, _lib.DIC_F32: 4}[dtype]
+            rc = self._L.dic_sequence_frame(self._h, device_ptr, width, height, width * es, dtype, 1, out_ptr,
+                                            ctypes.byref(rep))
+        self._call(rc)
+        return {f: getattr(rep, f) for f, _ in rep._fields_}
+
+    def set_graphs(self, enabled: bool) -> None:
+        self._call(self._L.dic_set_graphs(self._h, int(bool(enabled))))
+
     def run_device(self, device_pois: int, count: int, flags: int) -> None:
         self._call(self._L.dic_run_device(self._h, device_pois, count, flags))
 

@@ -97,6 +97,7 @@ typedef struct dic_stats
   double ms_prepare_tar;     /* raw -> float target + BicubicBspline table */
   double ms_fftcc;
   double ms_icgn;
+  double ms_frame;           /* whole frame of dic_sequence_frame (upload excluded) */
   int64_t kernel_launches;   /* kernels launched by this engine since creation */
   int64_t icgn_pois;         /* POIs of the last IC-GN call */
   int64_t icgn_iterations;   /* sum of IC-GN iterations over those POIs */
@@ -155,6 +156,24 @@ int dic_process_pair(dic_engine* engine, dic_poi* pois, int64_t count);
  * IC-GN.  pois holds the POI template on entry and the results on return. */
 int dic_process_frame(dic_engine* engine, dic_poi* pois, int64_t count, const dic_poi* prev_results,
                       const dic_frame_policy* policy, dic_frame_report* report);
+
+/* Fixed-reference sequence (runMultiFrame, opencorr_cli_cuda_mvp.cpp:3834-4516).
+ * dic_sequence_begin takes the POI template (buildPoiQueue order) and the policy, builds the
+ * resident per-POI reference data for it and resets the history; the reference image must
+ * be set.  Each dic_sequence_frame uploads one target (host memory, or device memory when
+ * pixels_on_device) and solves it: the first frame, and every frame when
+ * policy->skip_fftcc is 0, by FFTCC + IC-GN from the template; later frames by IC-GN seeded
+ * from the previous frame's results, with POI-level repair and the whole-frame fallback.
+ * In a sequence policy->frame_fallback_ratio is the margin added to the first frame's bad
+ * ratio (kSkipFftccBadRatioMargin = 0.03 in the reference), as the CLI does
+ * (:4275-4279).  The previous results stay on the device; the steady-state frame is one
+ * captured CUDA graph (dic_set_graphs(engine, 0) launches kernels one by one instead).
+ * results (nullable, count records) receives the frame's results. */
+int dic_sequence_begin(dic_engine* engine, const dic_poi* pois, int64_t count, const dic_frame_policy* policy);
+int dic_sequence_frame(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
+                       int64_t row_stride_bytes, int32_t dtype, int32_t pixels_on_device, dic_poi* results,
+                       dic_frame_report* report);
+int dic_set_graphs(dic_engine* engine, int32_t enabled);
 
 /* Device-resident variant: pois points to device memory (count records) and the call only
  * enqueues work on the engine stream (dic_get_stats or a stream sync waits for it).  flags
