@@ -198,11 +198,26 @@ def profiled_traffic(kernel: str):
     return float(k["dram_bytes_per_launch"])
 
 
+def parity_vs_cpu(result, cpu_sample):
+    """Reference parity-gate statistics of GPU results on the CPU sample's POIs."""
+    from oracle import oracle as O
+    g = result[::CPU_SAMPLE_STRIDE]
+    cz, gz = cpu_sample["r"][:, O.R_ZNCC], g["zncc"]
+    both = (cz >= 0) & (gz >= 0) & np.isfinite(cz) & np.isfinite(gz)
+    du = np.abs(cpu_sample["p"][both, O.P_U] - g["u"][both])
+    dv = np.abs(cpu_sample["p"][both, O.P_V] - g["v"][both])
+    return {"sample_pois": int(len(g)), "shared_valid": int(both.sum()),
+            "median_du": float(np.median(du)), "median_dv": float(np.median(dv)),
+            "p99_du": float(np.quantile(du, 0.99)), "p99_dv": float(np.quantile(dv, 0.99)),
+            "max_du": float(du.max()), "max_dv": float(dv.max()),
+            "cpu_valid_gpu_valid_agreement": float(np.mean((cz >= 0) == (gz >= 0)))}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
     import fasticgn_gb300 as dic
-    from fasticgn_gb300 import _build, _lib
+    from fasticgn_gb300 import _build, _lib, proposal
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -218,6 +233,13 @@ def run_ours(args):
     P = len(tmpl)
     dev = torch.device("cuda", local)
     eng = dic.Engine(R, R, WORKLOAD["conv"], WORKLOAD["max_iter"], device=local)
+    net = None
+    modes = ["fftcc"]
+    if proposal.WEIGHTS.exists():
+        net = proposal.ProposalNet.load(device=local)
+        eng.set_proposal(net)
+        modes.append("learned")
+    headline = args.seed if args.seed in modes else modes[-1]
     stream = torch.cuda.ExternalStream(eng.stream, device=dev)
     ref_d = torch.from_numpy(ref).to(dev)
     tar_d = torch.from_numpy(tar).to(dev)
@@ -225,53 +247,68 @@ def run_ours(args):
     work_d = torch.empty_like(tmpl_d)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
     torch.cuda.synchronize()
-    flags = _lib.DIC_RUN_FFTCC | _lib.DIC_RUN_ICGN | _lib.DIC_RUN_PREPARE
+    flag_of = {"fftcc": _lib.DIC_RUN_FFTCC | _lib.DIC_RUN_ICGN | _lib.DIC_RUN_PREPARE,
+               "learned": _lib.DIC_RUN_LEARNED | _lib.DIC_RUN_PREPARE}
 
-    def device_step():
+    def device_step(mode):
         with torch.cuda.stream(stream):
             work_d.copy_(tmpl_d)
         eng.set_ref_device(ref_d.data_ptr(), W, H, W, _lib.DIC_U8)
         eng.set_tar_device(tar_d.data_ptr(), W, H, W, _lib.DIC_U8)
-        eng.run_device(work_d.data_ptr(), P, flags)
+        eng.run_device(work_d.data_ptr(), P, flag_of[mode])
 
     def barrier():
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        device_step()
-    barrier()
-    launches0 = eng.stats()["kernel_launches"]
-    times, kern = [], {k: [] for k in ("ms_prepare_ref", "ms_poi_prepare", "ms_prepare_tar", "ms_fftcc", "ms_icgn")}
-    iters = []
-    with ClockSampler(local) as clk:
-        for _ in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.random_(0, 255)           # untimed L2 flush
-                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                s.record(stream)
-            device_step()
-            with torch.cuda.stream(stream):
-                e.record(stream)
-            e.synchronize()
-            times.append(s.elapsed_time(e))
-            st = eng.stats()
-            for k in kern:
-                kern[k].append(st[k])
-            iters.append(st["icgn_iterations"])
-        barrier()
-    launches = eng.stats()["kernel_launches"] - launches0
-    step_ms = float(np.sum(times)) / args.steps
-    max_ms = step_ms
-    if world > 1:
-        t = torch.tensor([step_ms], device=dev)
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], device=dev)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        max_ms = float(t.item())
-    value = world * P / (max_ms * 1e-3)
-    result_dev = work_d.cpu().numpy().view(dic.POI_DTYPE)
+        return float(t.item())
 
-    # ---- e2e through the host C ABI (pinned host buffers)
+    kernel_keys = ("ms_prepare_ref", "ms_poi_prepare", "ms_prepare_tar", "ms_fftcc", "ms_proposal", "ms_icgn")
+    res = {}
+    clk = None
+    for mode in modes:
+        for _ in range(args.warmup):
+            device_step(mode)
+        barrier()
+        launches0 = eng.stats()["kernel_launches"]
+        times, kern, iters = [], {k: [] for k in kernel_keys}, []
+        sampler = ClockSampler(local) if mode == headline else None
+        if sampler:
+            sampler.__enter__()
+        try:
+            for _ in range(args.steps):
+                with torch.cuda.stream(stream):
+                    flush.random_(0, 255)           # untimed L2 flush
+                    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    s.record(stream)
+                device_step(mode)
+                with torch.cuda.stream(stream):
+                    e.record(stream)
+                e.synchronize()
+                times.append(s.elapsed_time(e))
+                st = eng.stats()
+                for k in kern:
+                    kern[k].append(st[k])
+                iters.append(st["icgn_iterations"])
+            barrier()
+        finally:
+            if sampler:
+                sampler.__exit__(None, None, None)
+                clk = sampler
+        ms = max_over_ranks(float(np.sum(times)) / args.steps)
+        res[mode] = {"ms_per_step": ms, "value": world * P / (ms * 1e-3),
+                     "launches_per_step": (eng.stats()["kernel_launches"] - launches0) / args.steps,
+                     "kernels_ms": {k: float(np.mean(v)) for k, v in kern.items()},
+                     "icgn_iterations": float(np.mean(iters)),
+                     "result": work_d.cpu().numpy().view(dic.POI_DTYPE).copy()}
+
+    # ---- e2e through the host C ABI (pinned host buffers), headline mode
     ref_h = torch.from_numpy(ref).pin_memory()
     tar_h = torch.from_numpy(tar).pin_memory()
     q_h = torch.from_numpy(tmpl.view(np.uint8).copy()).pin_memory()
@@ -281,7 +318,10 @@ def run_ours(args):
     def e2e_step():
         eng.set_ref(ref_h.numpy())
         eng.set_tar(tar_h.numpy())
-        eng.process_pair(q_np)
+        if headline == "learned":
+            eng.process_pair_learned(q_np)
+        else:
+            eng.process_pair(q_np)
 
     for _ in range(max(1, args.warmup)):
         q_h.numpy()[:] = tmpl_bytes
@@ -298,23 +338,19 @@ def run_ours(args):
         e.record(stream)
         e.synchronize()
         e2e_times.append(s.elapsed_time(e))
-    e2e_ms = float(np.mean(e2e_times))
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    assert q_np.tobytes() == result_dev.tobytes(), "host and device entry points disagree"
+    e2e_ms = max_over_ranks(float(np.mean(e2e_times)))
+    assert q_np.tobytes() == res[headline]["result"].tobytes(), "host and device entry points disagree"
 
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel (IC-GN gather model, SURVEY-style algorithmic bytes)
+    # ---- roofline of the dominant kernel (IC-GN; gather model of SURVEY section 8d)
     N = (2 * R + 1) ** 2
-    it_sum = float(np.mean(iters))
-    icgn_ms = float(np.mean(kern["ms_icgn"]))
-    alg_bytes = 64.0 * N * it_sum + P * (12.0 * N + 144 + 8 + 32 + 40)
+    H0 = res[headline]
+    icgn_ms = H0["kernels_ms"]["ms_icgn"]
+    alg_bytes = 64.0 * N * H0["icgn_iterations"] + P * (12.0 * N + 144 + 8 + 32 + 40)
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / (icgn_ms * 1e-3) / 1e9
     traffic = profiled_traffic("k_icgn")
@@ -322,29 +358,28 @@ def run_ours(args):
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg_bytes,
                 "model": "64 B B-spline texel per warped sample per iteration + 12 B ref/grad per sample "
-                         "+ 224 B per-POI record/IO"}
+                         "+ 224 B per-POI record/IO; the gathers are served on chip, see profiles/"}
 
-    # ---- CPU baseline on a bounded sample, and parity of the GPU result on that sample
+    # ---- CPU baseline on a bounded sample, and parity of each GPU mode on that sample
     from oracle import oracle as O
     threads = O.default_threads()
     cpu_value, cpu_detail, cpu_sample = cpu_pair_time(ref, tar, threads)
-    g = result_dev[::CPU_SAMPLE_STRIDE]
-    cz, gz = cpu_sample["r"][:, O.R_ZNCC], g["zncc"]
-    both = (cz >= 0) & (gz >= 0) & np.isfinite(cz) & np.isfinite(gz)
-    du = np.abs(cpu_sample["p"][both, O.P_U] - g["u"][both])
-    dv = np.abs(cpu_sample["p"][both, O.P_V] - g["v"][both])
-    parity = {"sample_pois": int(len(g)), "shared_valid": int(both.sum()),
-              "median_du": float(np.median(du)), "median_dv": float(np.median(dv)),
-              "p99_du": float(np.quantile(du, 0.99)), "p99_dv": float(np.quantile(dv, 0.99)),
-              "max_du": float(du.max()), "max_dv": float(dv.max()),
-              "flag_agreement": float(np.mean(np.where(cz < 0, cz, 0) == np.where(gz < 0, gz, 0)))}
-    ok = result_dev["zncc"] >= 0
+    seed_modes = {}
+    for mode, r in res.items():
+        ok = r["result"]["zncc"] >= 0
+        seed_modes[mode] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "kernels_ms": r["kernels_ms"],
+                            "icgn_iterations_per_poi": r["icgn_iterations"] / P, "valid_ratio": float(ok.mean()),
+                            "kernel_launches_per_step": r["launches_per_step"],
+                            "parity_vs_cpu": parity_vs_cpu(r["result"], cpu_sample)}
     h2d = ref.nbytes + tar.nbytes + tmpl.nbytes
+    cfg = config_block()
+    cfg["seed_method"] = {"fftcc": "FFTCC", "learned": "learned proposal CNN (FFTCC fallback)"}[headline]
     line = {
-        "metric": "POIs/s", "value": value, "unit": "POI/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": max_ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config_block(),
-        "frames_per_s": world * 1e3 / max_ms,
+        "metric": "POIs/s", "value": H0["value"], "unit": "POI/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": H0["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (IC-GN, FFTCC); bf16 tensor-core with f32 accumulation (proposal CNN)",
+        "data": "synthetic", "config": cfg,
+        "frames_per_s": world * 1e3 / H0["ms_per_step"],
         "e2e": {"value": world * P / (e2e_ms * 1e-3), "unit": "POI/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(tmpl.nbytes)},
         "roofline": roofline,
@@ -352,10 +387,11 @@ def run_ours(args):
                          "sample": f"full-image prep + FFTCC/IC-GN on every {CPU_SAMPLE_STRIDE}th POI "
                                    f"({cpu_detail['sample_pois']} POIs), extrapolated; own FFT, not FFTW",
                          "detail": cpu_detail},
-        "clocks": clk.summary(), "gpu_launches": int(launches),
-        "kernels_ms": {k: float(np.mean(v)) for k, v in kern.items()},
-        "iteration_mean": it_sum / P, "valid_ratio": float(ok.mean()),
-        "parity_vs_cpu": parity,
+        "clocks": clk.summary() if clk else None,
+        "gpu_launches": int(round(H0["launches_per_step"] * args.steps)),
+        "seed_modes": seed_modes,
+        "learned_vs_fftcc": (seed_modes["learned"]["value"] / seed_modes["fftcc"]["value"]) if "learned" in seed_modes else None,
+        "parity_vs_cpu": seed_modes[headline]["parity_vs_cpu"],
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -365,9 +401,11 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--seed", choices=["fftcc", "learned"], default="fftcc",
+                    help="seed method of the headline value (both are measured when the proposal weights exist)")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

@@ -20,7 +20,7 @@ DIC_ERR_CUDA = -4
 DIC_ERR_MEMORY = -5
 
 DIC_U8, DIC_U16, DIC_F32 = 1, 2, 3
-DIC_RUN_FFTCC, DIC_RUN_ICGN, DIC_RUN_PREPARE = 1, 2, 4
+DIC_RUN_FFTCC, DIC_RUN_ICGN, DIC_RUN_PREPARE, DIC_RUN_LEARNED = 1, 2, 4, 8
 DIC_PLANE_REF, DIC_PLANE_REF_PACK, DIC_PLANE_TAR, DIC_PLANE_TAR_COEF = 1, 2, 3, 4
 
 # struct dic_poi (include/dic.h), 56 bytes
@@ -54,7 +54,8 @@ class DicFrameReport(ctypes.Structure):
 class DicStats(ctypes.Structure):
     _fields_ = [("ms_prepare_ref", ctypes.c_double), ("ms_poi_prepare", ctypes.c_double),
                 ("ms_prepare_tar", ctypes.c_double), ("ms_fftcc", ctypes.c_double),
-                ("ms_icgn", ctypes.c_double), ("ms_frame", ctypes.c_double), ("kernel_launches", ctypes.c_int64),
+                ("ms_icgn", ctypes.c_double), ("ms_frame", ctypes.c_double), ("ms_proposal", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64),
                 ("icgn_pois", ctypes.c_int64), ("icgn_iterations", ctypes.c_int64)]
 
 
@@ -87,6 +88,19 @@ SIGNATURES = {
     "dic_read_plane": (ctypes.c_int, [_vp, _i32, _vp, _i64]),
     "dic_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(DicStats)]),
     "dic_set_timing": (ctypes.c_int, [_vp, _i32]),
+    "dic_cnn_param_count": (_i64, []),
+    "dic_cnn_create": (ctypes.c_int, [_i32, ctypes.POINTER(_vp)]),
+    "dic_cnn_destroy": (None, [_vp]),
+    "dic_cnn_last_error": (ctypes.c_char_p, [_vp]),
+    "dic_cnn_set_params": (ctypes.c_int, [_vp, _vp, _i64]),
+    "dic_cnn_get_params": (ctypes.c_int, [_vp, _vp, _i64]),
+    "dic_cnn_input": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _vp, _i64, _vp]),
+    "dic_cnn_forward": (ctypes.c_int, [_vp, _vp, _i64, _vp]),
+    "dic_cnn_seed": (ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _vp, _i64]),
+    "dic_cnn_gradient": (ctypes.c_int, [_vp, _vp, _vp, _i64, _vp, ctypes.POINTER(ctypes.c_float)]),
+    "dic_cnn_train_step": (ctypes.c_int, [_vp, _vp, _vp, _i64, ctypes.c_float, ctypes.POINTER(ctypes.c_float)]),
+    "dic_set_proposal": (ctypes.c_int, [_vp, _vp]),
+    "dic_process_pair_learned": (ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(DicFrameReport)]),
     "dic_process_pair_noalloc": (ctypes.c_int, [ctypes.POINTER(DicConfig), _vp, _vp, _i32, _i32, _i32, _vp, _i64,
                                                 _vp, ctypes.c_char_p, _i64]),
 }

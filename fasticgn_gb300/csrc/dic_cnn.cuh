@@ -1,0 +1,826 @@
+// Proposal network: a small CNN that maps a reference/target subset pair to the six
+// first-order warp parameters, so IC-GN starts close to the answer.  No counterpart in the
+// reference; the architecture is the one the learned-seed workload names:
+//
+//   x0  [2, 31, 31]  reference and target windows at the POI, each zero-mean, unit-variance
+//   c1  3x3 stride 2 pad 1, 2 -> 32, ReLU      -> [32, 16, 16]
+//   c2  3x3 stride 2 pad 1, 32 -> 32, ReLU     -> [32, 8, 8]
+//   c3  3x3 stride 2 pad 1, 32 -> 32, ReLU     -> [32, 4, 4]
+//   c4  3x3 stride 2 pad 1, 32 -> 32, ReLU     -> [32, 2, 2]
+//   f1  128 -> 256, ReLU
+//   f2  256 -> 6: (u, v, 100 ux, 100 uy, 100 vx, 100 vy)
+//
+// Activations are BF16 in NHWC order (channels fastest), weights are kept in FP32 (master)
+// with BF16 working copies, and every product runs on the tensor cores through
+// mma.sync.m16n8k16 bf16 with FP32 accumulation.  One GEMM kernel serves all layers and
+// all passes; an operand functor gathers its A and B tiles (implicit im2col for the
+// convolutions) and an epilogue functor stores the result.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cstdint>
+
+namespace dic
+{
+namespace cnn
+{
+
+constexpr int kWin = 31;          // input window side
+constexpr int kCh = 32;           // conv channels
+constexpr int kHidden = 256;
+constexpr int kOut = 6;
+constexpr int kOutPad = 8;
+constexpr int kC1K = 32;          // conv1 K = 3*3*2 = 18, padded to 32
+
+// Spatial sides: input 31, then 16, 8, 4, 2.
+__host__ __device__ constexpr int side_of(int layer) { return layer == 0 ? 31 : (32 >> layer); }
+
+// FP32 master parameter layout (offsets in floats).  Conv weights are [co][ky][kx][ci].
+struct ParamLayout
+{
+  static constexpr int w1 = 0, b1 = w1 + 32 * 9 * 2;
+  static constexpr int w2 = b1 + 32, b2 = w2 + 32 * 9 * 32;
+  static constexpr int w3 = b2 + 32, b3 = w3 + 32 * 9 * 32;
+  static constexpr int w4 = b3 + 32, b4 = w4 + 32 * 9 * 32;
+  static constexpr int w5 = b4 + 32, b5 = w5 + kHidden * 128;   // [256][128], k = (y, x, c)
+  static constexpr int w6 = b5 + kHidden, b6 = w6 + kOut * kHidden;  // [6][256]
+  static constexpr int count = b6 + kOut;
+};
+static_assert(ParamLayout::count == 62918, "parameter count");
+
+// BF16 working copies, B operands stored [n][k] with k contiguous and K padded:
+//   c1: [32][32], c2..c4: [32][288], f1: [256][128], f2: [8][256] (rows 6, 7 zero).
+struct WeightLayout
+{
+  static constexpr int c1 = 0, c2 = c1 + 32 * kC1K, c3 = c2 + 32 * 288, c4 = c3 + 32 * 288;
+  static constexpr int f1 = c4 + 32 * 288, f2 = f1 + kHidden * 128;
+  static constexpr int count = f2 + kOutPad * kHidden;
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi)
+{
+  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
+{
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// --------------------------------------------------------------------------------------
+// Generic GEMM: C[M x N] = A[M x K] * B[K x N] over k in [k_lo, k_hi) of this split.
+// CTA tile 64 x 32 x 32, 4 warps, each warp 16 rows x 32 columns (four m16n8k16 per
+// k16 step).  Op supplies M, N, K, splits, a(m, k), b(k, n) (BF16, 0 outside), and
+// store(split, m, n, value) for the FP32 accumulator.
+// --------------------------------------------------------------------------------------
+constexpr int BM = 64, BN = 32, BK = 32;
+
+template <class Op>
+__global__ void __launch_bounds__(128) k_gemm(Op op)
+{
+  __shared__ __nv_bfloat16 As[BM][BK + 8];
+  __shared__ __nv_bfloat16 Bs[BN][BK + 8];
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int split = blockIdx.z;
+  const int64_t kper = ((op.K + BK - 1) / BK + op.splits - 1) / op.splits * BK;
+  const int64_t k_lo = (int64_t)split * kper;
+  const int64_t k_hi = k_lo + kper < op.K ? k_lo + kper : op.K;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
+  float acc[4][4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[j][q] = 0.f;
+  for (int64_t k0 = k_lo; k0 < k_hi; k0 += BK)
+  {
+    for (int e = threadIdx.x; e < BM * BK; e += blockDim.x)
+    {
+      const int r = e / BK, c = e % BK;
+      const int64_t k = k0 + c;
+      As[r][c] = (k < k_hi) ? op.a(m0 + r, k) : __float2bfloat16(0.f);
+    }
+    for (int e = threadIdx.x; e < BN * BK; e += blockDim.x)
+    {
+      const int r = e / BK, c = e % BK;
+      const int64_t k = k0 + c;
+      Bs[r][c] = (k < k_hi) ? op.b(k, n0 + r) : __float2bfloat16(0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < BK; kk += 16)
+    {
+      const int r = warp * 16 + g, c = kk + t4 * 2;
+      uint32_t a[4];
+      a[0] = pack_bf16(As[r][c], As[r][c + 1]);
+      a[1] = pack_bf16(As[r + 8][c], As[r + 8][c + 1]);
+      a[2] = pack_bf16(As[r][c + 8], As[r][c + 9]);
+      a[3] = pack_bf16(As[r + 8][c + 8], As[r + 8][c + 9]);
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+      {
+        const int nn = j * 8 + g;
+        uint32_t b[2];
+        b[0] = pack_bf16(Bs[nn][c], Bs[nn][c + 1]);
+        b[1] = pack_bf16(Bs[nn][c + 8], Bs[nn][c + 9]);
+        mma_bf16_16816(acc[j], a, b);
+      }
+    }
+    __syncthreads();
+  }
+  const int r0 = m0 + warp * 16 + g;
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+  {
+    const int c = n0 + j * 8 + t4 * 2;
+    op.store(split, r0, c, acc[j][0]);
+    op.store(split, r0, c + 1, acc[j][1]);
+    op.store(split, r0 + 8, c, acc[j][2]);
+    op.store(split, r0 + 8, c + 1, acc[j][3]);
+  }
+}
+
+__device__ __forceinline__ __nv_bfloat16 bz() { return __float2bfloat16(0.f); }
+
+// Convolution geometry: input side si, channels ci; output side so = si / 2 rounded up
+// (3x3, stride 2, pad 1).  Activations NHWC: act[((n * s + y) * s + x) * c + ch].
+struct ConvGeom
+{
+  int si, so, ci, co;
+  int kdim() const { return 9 * ci; }
+};
+
+// Forward: A[m = (n, oy, ox)][k = (ky, kx, ci)] = in[n, 2oy+ky-1, 2ox+kx-1, ci],
+// B[k][n = co] = W[co][k]; store z + bias, ReLU, BF16.
+struct ConvFwdOp
+{
+  const __nv_bfloat16* in;
+  const __nv_bfloat16* w;   // [co][kpad]
+  const float* bias;
+  __nv_bfloat16* out;
+  int64_t M;
+  int N, splits;
+  int64_t K;                // padded K
+  int si, so, ci, kreal, kpad;
+  __device__ __nv_bfloat16 a(int64_t m, int64_t k) const
+  {
+    if (m >= M || k >= kreal) return bz();
+    const int64_t n = m / (so * so);
+    const int p = (int)(m % (so * so)), oy = p / so, ox = p % so;
+    const int c = (int)(k % ci), kk = (int)(k / ci), ky = kk / 3, kx = kk % 3;
+    const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+    if (iy < 0 || ix < 0 || iy >= si || ix >= si) return bz();
+    return in[((n * si + iy) * si + ix) * ci + c];
+  }
+  __device__ __nv_bfloat16 b(int64_t k, int n) const { return n < N ? w[(int64_t)n * kpad + k] : bz(); }
+  __device__ void store(int, int64_t m, int n, float v) const
+  {
+    if (m >= M || n >= N) return;
+    out[m * N + n] = __float2bfloat16(fmaxf(v + bias[n], 0.f));
+  }
+};
+
+// Backward data: dIn[m = (n, iy, ix)][c] = sum over (ky, kx, co) of
+// dZ[n, oy, ox, co] W[co][ky][kx][c] with iy = 2oy+ky-1; then the ReLU mask of the input
+// activation (act > 0), stored BF16 as the previous layer's dZ.
+struct ConvBwdDataOp
+{
+  const __nv_bfloat16* dz;    // [N][so][so][co]
+  const __nv_bfloat16* w;     // [co][kpad], k = (ky, kx, ci)
+  const __nv_bfloat16* act;   // input activation [N][si][si][ci] (ReLU output)
+  __nv_bfloat16* dzin;        // [N][si][si][ci]
+  int64_t M;
+  int N, splits;
+  int64_t K;                  // 9 * co
+  int si, so, ci, co, kpad;
+  __device__ __nv_bfloat16 a(int64_t m, int64_t k) const
+  {
+    if (m >= M || k >= K) return bz();
+    const int64_t n = m / (si * si);
+    const int p = (int)(m % (si * si)), iy = p / si, ix = p % si;
+    const int o = (int)(k % co), kk = (int)(k / co), ky = kk / 3, kx = kk % 3;
+    const int ty = iy + 1 - ky, tx = ix + 1 - kx;
+    if (ty < 0 || tx < 0 || (ty & 1) || (tx & 1)) return bz();
+    const int oy = ty >> 1, ox = tx >> 1;
+    if (oy >= so || ox >= so) return bz();
+    return dz[((n * so + oy) * so + ox) * co + o];
+  }
+  __device__ __nv_bfloat16 b(int64_t k, int c) const
+  {
+    if (c >= N || k >= K) return bz();
+    const int o = (int)(k % co), kk = (int)(k / co);
+    return w[(int64_t)o * kpad + kk * ci + c];
+  }
+  __device__ void store(int, int64_t m, int c, float v) const
+  {
+    if (m >= M || c >= N) return;
+    const int64_t i = m * N + c;
+    dzin[i] = __float2bfloat16(__bfloat162float(act[i]) > 0.f ? v : 0.f);
+  }
+};
+
+// Backward weights: dW[co][k = (ky, kx, ci)] = sum over (n, oy, ox) of dZ[n, oy, ox, co] *
+// in[n, 2oy+ky-1, 2ox+kx-1, ci]; split-K partials go to part[split][co][kpad] (FP32) and
+// k_reduce_splits sums them in a fixed order.
+struct ConvBwdWeightOp
+{
+  const __nv_bfloat16* dz;    // [Nb][so][so][co]
+  const __nv_bfloat16* in;    // [Nb][si][si][ci]
+  float* part;
+  int64_t M;                  // co
+  int N, splits;              // N = kpad columns
+  int64_t K;                  // Nb * so * so
+  int si, so, ci, co, kreal, kpad;
+  __device__ __nv_bfloat16 a(int64_t m, int64_t k) const
+  {
+    if (m >= M || k >= K) return bz();
+    return dz[k * co + m];
+  }
+  __device__ __nv_bfloat16 b(int64_t k, int col) const
+  {
+    if (col >= kreal || k >= K) return bz();
+    const int64_t n = k / (so * so);
+    const int p = (int)(k % (so * so)), oy = p / so, ox = p % so;
+    const int c = col % ci, kk = col / ci, ky = kk / 3, kx = kk % 3;
+    const int iy = 2 * oy + ky - 1, ix = 2 * ox + kx - 1;
+    if (iy < 0 || ix < 0 || iy >= si || ix >= si) return bz();
+    return in[((n * si + iy) * si + ix) * ci + c];
+  }
+  __device__ void store(int split, int64_t m, int col, float v) const
+  {
+    if (m >= M || col >= N) return;
+    part[((int64_t)split * M + m) * N + col] = v;
+  }
+};
+
+// Dense forward: out[m][n] = act(sum_k in[m][k] W[n][k] + bias[n]).
+struct LinearFwdOp
+{
+  const __nv_bfloat16* in;    // [M][K]
+  const __nv_bfloat16* w;     // [Npad][K]
+  const float* bias;
+  __nv_bfloat16* out_bf;      // ReLU layer output (nullable)
+  float* out_f;               // linear output (nullable), [M][ld]
+  int64_t M;
+  int N, splits;
+  int64_t K;
+  int ld;
+  __device__ __nv_bfloat16 a(int64_t m, int64_t k) const { return m < M ? in[m * K + k] : bz(); }
+  __device__ __nv_bfloat16 b(int64_t k, int n) const { return n < N ? w[(int64_t)n * K + k] : bz(); }
+  __device__ void store(int, int64_t m, int n, float v) const
+  {
+    if (m >= M || n >= N) return;
+    const float z = v + bias[n];
+    if (out_bf) out_bf[m * N + n] = __float2bfloat16(fmaxf(z, 0.f));
+    if (out_f) out_f[m * ld + n] = z;
+  }
+};
+
+// Dense backward data: dIn[m][k] = sum_n dZ[m][n] W[n][k], masked by act[m][k] > 0.
+struct LinearBwdDataOp
+{
+  const __nv_bfloat16* dz;    // [M][Nout]
+  const __nv_bfloat16* w;     // [Npad][Kin]
+  const __nv_bfloat16* act;   // [M][Kin]
+  __nv_bfloat16* dzin;        // [M][Kin]
+  int64_t M;
+  int N, splits;              // N = Kin
+  int64_t K;                  // Nout
+  int nout_pad;
+  __device__ __nv_bfloat16 a(int64_t m, int64_t k) const { return (m < M && k < K) ? dz[m * nout_pad + k] : bz(); }
+  __device__ __nv_bfloat16 b(int64_t k, int c) const { return (c < N && k < K) ? w[k * N + c] : bz(); }
+  __device__ void store(int, int64_t m, int c, float v) const
+  {
+    if (m >= M || c >= N) return;
+    const int64_t i = m * N + c;
+    dzin[i] = __float2bfloat16(__bfloat162float(act[i]) > 0.f ? v : 0.f);
+  }
+};
+
+// Dense backward weights: dW[n][k] = sum_m dZ[m][n] in[m][k]; split-K partials.
+struct LinearBwdWeightOp
+{
+  const __nv_bfloat16* dz;    // [Mb][ldz]
+  const __nv_bfloat16* in;    // [Mb][Kin]
+  float* part;                // [split][Nout][Kin]
+  int64_t M;                  // Nout
+  int N, splits;              // Kin
+  int64_t K;                  // batch
+  int ldz;
+  __device__ __nv_bfloat16 a(int64_t m, int64_t k) const { return (m < M && k < K) ? dz[k * ldz + m] : bz(); }
+  __device__ __nv_bfloat16 b(int64_t k, int c) const { return (c < N && k < K) ? in[k * N + c] : bz(); }
+  __device__ void store(int split, int64_t m, int c, float v) const
+  {
+    if (m >= M || c >= N) return;
+    part[((int64_t)split * M + m) * N + c] = v;
+  }
+};
+
+// --------------------------------------------------------------------------------------
+// Element kernels
+// --------------------------------------------------------------------------------------
+
+// Network input of one POI: the 31x31 reference and target windows centred on the POI's
+// integer position (the target window is NOT shifted by any guess), each normalised to
+// zero mean and unit variance.  Window pixels outside the image repeat the edge.  One warp
+// per POI; x0 is NHWC [n][31][31][2].
+__global__ void k_extract_input(const float* __restrict__ ref, const float* __restrict__ tar, int w, int h,
+                                const dic_poi* __restrict__ pois, int64_t n, __nv_bfloat16* __restrict__ x0)
+{
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (i >= n) return;
+  const int cx = (int)pois[i].x, cy = (int)pois[i].y;
+  constexpr int R = kWin / 2, NPIX = kWin * kWin;
+  float sr = 0.f, st = 0.f;
+  for (int k = lane; k < NPIX; k += 32)
+  {
+    const int x = min(max(cx + k % kWin - R, 0), w - 1), y = min(max(cy + k / kWin - R, 0), h - 1);
+    sr += ref[(size_t)y * w + x];
+    st += tar[(size_t)y * w + x];
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    sr += __shfl_xor_sync(0xffffffffu, sr, o);
+    st += __shfl_xor_sync(0xffffffffu, st, o);
+  }
+  const float mr = sr / NPIX, mt = st / NPIX;
+  float vr = 0.f, vt = 0.f;
+  for (int k = lane; k < NPIX; k += 32)
+  {
+    const int x = min(max(cx + k % kWin - R, 0), w - 1), y = min(max(cy + k / kWin - R, 0), h - 1);
+    const float a = ref[(size_t)y * w + x] - mr, b = tar[(size_t)y * w + x] - mt;
+    vr += a * a;
+    vt += b * b;
+  }
+  for (int o = 16; o > 0; o >>= 1)
+  {
+    vr += __shfl_xor_sync(0xffffffffu, vr, o);
+    vt += __shfl_xor_sync(0xffffffffu, vt, o);
+  }
+  const float ir = vr > 0.f ? rsqrtf(vr / NPIX) : 1.f, it = vt > 0.f ? rsqrtf(vt / NPIX) : 1.f;
+  __nv_bfloat16* out = x0 + i * NPIX * 2;
+  for (int k = lane; k < NPIX; k += 32)
+  {
+    const int x = min(max(cx + k % kWin - R, 0), w - 1), y = min(max(cy + k / kWin - R, 0), h - 1);
+    out[2 * k] = __float2bfloat16((ref[(size_t)y * w + x] - mr) * ir);
+    out[2 * k + 1] = __float2bfloat16((tar[(size_t)y * w + x] - mt) * it);
+  }
+}
+
+// FP32 master parameters -> BF16 working weights (padded GEMM layouts).
+__global__ void k_pack_weights(const float* __restrict__ p, __nv_bfloat16* __restrict__ wb)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  using P = ParamLayout;
+  using L = WeightLayout;
+  if (i < 32 * kC1K)
+  {
+    const int co = i / kC1K, k = i % kC1K;
+    wb[L::c1 + i] = __float2bfloat16(k < 18 ? p[P::w1 + co * 18 + k] : 0.f);
+  }
+  if (i < 32 * 288)
+  {
+    wb[L::c2 + i] = __float2bfloat16(p[P::w2 + i]);
+    wb[L::c3 + i] = __float2bfloat16(p[P::w3 + i]);
+    wb[L::c4 + i] = __float2bfloat16(p[P::w4 + i]);
+  }
+  if (i < kHidden * 128) wb[L::f1 + i] = __float2bfloat16(p[P::w5 + i]);
+  if (i < kOutPad * kHidden)
+  {
+    const int r = i / kHidden;
+    wb[L::f2 + i] = __float2bfloat16(r < kOut ? p[P::w6 + i] : 0.f);
+  }
+}
+
+// Output scaling: the network predicts (u, v, 100 ux, 100 uy, 100 vx, 100 vy).
+__host__ __device__ constexpr float out_scale(int j) { return j < 2 ? 1.f : 100.f; }
+
+// MSE over the six scaled outputs, mean over batch and outputs.  dout = dL/dout (BF16),
+// per-row loss partial into row_loss (summed on the host side in a fixed order).
+__global__ void k_loss_grad(const float* __restrict__ out, const float* __restrict__ target, int64_t n,
+                            __nv_bfloat16* __restrict__ dout, float* __restrict__ row_loss)
+{
+  const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= n) return;
+  float l = 0.f;
+  const float scale = 2.f / (float)(n * kOut);
+#pragma unroll
+  for (int j = 0; j < kOutPad; ++j)
+  {
+    float g = 0.f;
+    if (j < kOut)
+    {
+      const float d = out[m * kOutPad + j] - target[m * kOut + j] * out_scale(j);
+      l += d * d;
+      g = d * scale;
+    }
+    dout[m * kOutPad + j] = __float2bfloat16(g);
+  }
+  row_loss[m] = l;
+}
+
+// Bias gradient: db[c] = sum over rows of dz[row][c] (BF16 rows of width ld), fixed order.
+__global__ void k_bias_grad(const __nv_bfloat16* __restrict__ dz, int64_t rows, int ld, int ncol, float* __restrict__ db)
+{
+  const int c = blockIdx.x;
+  if (c >= ncol) return;
+  float s = 0.f;
+  for (int64_t r = threadIdx.x; r < rows; r += blockDim.x) s += __bfloat162float(dz[r * ld + c]);
+  __shared__ float red[256];
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1)
+  {
+    if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) db[c] = red[0];
+}
+
+// Sum split-K partials part[s][rows][cols] in split order into out[r * out_ld + c] for
+// c < keep (the unpadded columns).
+__global__ void k_reduce_splits(const float* __restrict__ part, int splits, int rows, int cols, int keep,
+                                float* __restrict__ out, int out_ld)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows * keep) return;
+  const int r = i / keep, c = i % keep;
+  float s = 0.f;
+  for (int k = 0; k < splits; ++k) s += part[((int64_t)k * rows + r) * cols + c];
+  out[(int64_t)r * out_ld + c] = s;
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master parameters.
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       int n, float lr, float b1, float b2, float eps, float c1, float c2)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// Network output -> queue seed (u, ux, uy, v, vx, vy); result fields cleared.
+__global__ void k_write_seeds(const float* __restrict__ out, dic_poi* __restrict__ pois, int64_t n)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* o = out + i * kOutPad;
+  dic_poi q = pois[i];
+  q.u = o[0];
+  q.v = o[1];
+  q.ux = o[2] / out_scale(2);
+  q.uy = o[3] / out_scale(3);
+  q.vx = o[4] / out_scale(4);
+  q.vy = o[5] / out_scale(5);
+  q.u0 = 0.f; q.v0 = 0.f; q.zncc = 0.f; q.iteration = 0.f; q.convergence = 0.f; q.feature = 0.f;
+  pois[i] = q;
+}
+
+// --------------------------------------------------------------------------------------
+// Fused inference: the whole network for kT POIs per tile in one CTA, activations
+// resident in shared memory, writing the seeds straight into the POI queue.  Persistent
+// grid (tiles strided over CTAs).  Same arithmetic as the GEMM path (BF16 operands, FP32
+// accumulation, BF16 ReLU outputs), so both give the same seeds up to accumulation order.
+//
+// Shared memory (bytes): W1 [32][32] 2 KB; W2..W4 [32][296] 57 KB (row padded to 37
+// 16-byte chunks: conflict-free ldmatrix); x0p [4][33][33][2] 17 KB (zero border);
+// a1p [4][18][18][40] 104 KB and a2p [4][10][10][40] 32 KB (zero border, pixel stride 80 B
+// so the stride-2 im2col rows of an ldmatrix spread over the banks); a3p, a4, a5 overlay
+// x0p once conv1 has consumed it.
+// --------------------------------------------------------------------------------------
+constexpr int kT = 4;
+constexpr int kFusedThreads = 512;
+constexpr int kPix = 40;                        // padded channel stride (80 B) of a1p/a2p/a3p
+constexpr int kWRow = 296;                      // padded row of W2..W4 (288 + 8)
+constexpr int kSmX0 = kT * 33 * 33 * 2 * 2;     // 17424
+constexpr int kSmA1 = kT * 18 * 18 * kPix * 2;  // 103680
+constexpr int kSmA2 = kT * 10 * 10 * kPix * 2;  // 32000
+constexpr int kSmW1 = 32 * 32 * 2;              // 2048
+constexpr int kSmW = 3 * 32 * kWRow * 2;        // 56832
+constexpr int kSmOut = kT * 8 * 4;              // 128
+constexpr int kSmTotal = kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmOut;
+static_assert(kT * 6 * 6 * kPix * 2 + kT * 128 * 2 + kT * 256 * 2 <= kSmX0, "overlay fits");
+static_assert(kSmTotal <= 227 * 1024, "shared memory");
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], uint32_t addr)
+{
+  asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+               : "r"(addr));
+}
+
+// One 3x3 stride-2 conv layer from padded NHWC smem (pixel stride kPix) to the interior of
+// the next padded buffer, K = 288 (ci = 32).  Tasks = (m-tile, pair of n-tiles).
+template <int SIP, int SO, int SOP>
+__device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloat16* out, const __nv_bfloat16* W,
+                                             const float* __restrict__ bias, int nt, int warp, int lane)
+{
+  constexpr int M = kT * SO * SO;
+  constexpr int MT = (M + 15) / 16;
+  const int g = lane >> 2, t4 = lane & 3;
+  for (int task = warp; task < MT * 2; task += kFusedThreads / 32)
+  {
+    const int mt = task >> 1, nh = task & 1;
+    // ldmatrix A addresses: lane -> row (q & 1) * 8 + (lane & 7), k offset (q >> 1) * 8
+    const int q = lane >> 3;
+    const int arow = mt * 16 + (q & 1) * 8 + (lane & 7);
+    const int rr = arow < M ? arow : M - 1;
+    const int p = rr / (SO * SO), oy = (rr % (SO * SO)) / SO, ox = rr % SO;
+    const __nv_bfloat16* abase = in + ((p * SIP + 2 * oy) * SIP + 2 * ox) * kPix + (q >> 1) * 8;
+    // ldmatrix B addresses: lane -> n row (q >> 1) * 8 + (lane & 7), k offset (q & 1) * 8
+    const __nv_bfloat16* bbase = W + (nh * 16 + (q >> 1) * 8 + (lane & 7)) * kWRow + (q & 1) * 8;
+    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+    for (int kk = 0; kk < 9; ++kk)
+    {
+      const int ky = kk / 3, kx = kk % 3;
+#pragma unroll
+      for (int half = 0; half < 2; ++half)
+      {
+        uint32_t a[4], b[4];
+        ldsm_x4(a, smem_u32(abase + (ky * SIP + kx) * kPix + half * 16));
+        ldsm_x4(b, smem_u32(bbase + kk * 32 + half * 16));
+        const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+        mma_bf16_16816(acc[0], a, b0);
+        mma_bf16_16816(acc[1], a, b1);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+    {
+      const int co = nh * 16 + j * 8 + t4 * 2;
+      const float bb0 = bias[co], bb1 = bias[co + 1];
+#pragma unroll
+      for (int h2 = 0; h2 < 2; ++h2)
+      {
+        const int row = mt * 16 + g + h2 * 8;
+        if (row >= M) continue;
+        const int pp = row / (SO * SO), y = (row % (SO * SO)) / SO, x = row % SO;
+        __nv_bfloat16* dst = out + ((pp * SOP + y + 1) * SOP + x + 1) * kPix + co;
+        *reinterpret_cast<uint32_t*>(dst) =
+            pack_bf16(__float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)), __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
+      }
+    }
+  }
+  (void)nt;
+}
+
+__global__ void __launch_bounds__(kFusedThreads, 1)
+    k_proposal_fused(const float* __restrict__ ref, const float* __restrict__ tar, int w, int h,
+                     dic_poi* __restrict__ pois, int64_t n, const __nv_bfloat16* __restrict__ wb,
+                     const float* __restrict__ params)
+{
+  extern __shared__ __align__(16) unsigned char sm[];
+  __nv_bfloat16* W1s = reinterpret_cast<__nv_bfloat16*>(sm);
+  __nv_bfloat16* W2s = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1);
+  __nv_bfloat16* W3s = W2s + 32 * kWRow;
+  __nv_bfloat16* W4s = W3s + 32 * kWRow;
+  __nv_bfloat16* x0p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW);
+  __nv_bfloat16* a1p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0);
+  __nv_bfloat16* a2p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1);
+  float* outs = reinterpret_cast<float*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2);
+  __nv_bfloat16* a3p = x0p;                                   // [4][6][6][kPix]
+  __nv_bfloat16* a4 = x0p + kT * 6 * 6 * kPix;                // [4][128]
+  __nv_bfloat16* a5 = a4 + kT * 128;                          // [4][256]
+  using L = WeightLayout;
+  using P = ParamLayout;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
+  // weights and zero borders, once per CTA
+  for (int i = tid; i < 32 * 32; i += kFusedThreads) W1s[i] = wb[L::c1 + i];
+  for (int i = tid; i < 3 * 32 * kWRow; i += kFusedThreads)
+  {
+    const int l = i / (32 * kWRow), r = (i / kWRow) % 32, c = i % kWRow;
+    W2s[i] = c < 288 ? wb[L::c2 + l * 32 * 288 + r * 288 + c] : bz();
+  }
+  for (int i = tid; i < (kSmX0 + kSmA1 + kSmA2) / 4; i += kFusedThreads)
+    reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
+  __syncthreads();
+  const int64_t tiles = (n + kT - 1) / kT;
+  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+  {
+    const int64_t p0 = tile * kT;
+    // a3p/a4/a5 of the previous tile overlay x0p: clear it so its border reads as padding
+    for (int i = tid; i < kSmX0 / 4; i += kFusedThreads) reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
+    __syncthreads();
+    // ---- input windows: warp 2p + c stages channel c (0 ref, 1 tar) of POI p.  Lane l holds
+    // column l of the 31x31 window in registers (coalesced row loads, one pass), the warp
+    // reduces mean and variance, and writes the normalised values into x0p's interior.
+    if (warp < 2 * kT)
+    {
+      const int p = warp >> 1, ch = warp & 1;
+      const int64_t i = p0 + p;
+      if (i < n)
+      {
+        const float* img = ch ? tar : ref;
+        const int cx = (int)pois[i].x, cy = (int)pois[i].y;
+        constexpr int R = kWin / 2, NPIX = kWin * kWin;
+        const int x = min(max(cx + lane - R, 0), w - 1);
+        float v[kWin];
+        float s = 0.f;
+        if (lane < kWin)
+        {
+#pragma unroll
+          for (int r = 0; r < kWin; ++r)
+          {
+            const int y = min(max(cy + r - R, 0), h - 1);
+            v[r] = __ldg(img + (size_t)y * w + x);
+          }
+#pragma unroll
+          for (int r = 0; r < kWin; ++r) s += v[r];
+        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const float mean = s / NPIX;
+        float q = 0.f;
+        if (lane < kWin)
+        {
+#pragma unroll
+          for (int r = 0; r < kWin; ++r) q += (v[r] - mean) * (v[r] - mean);
+        }
+        for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+        const float inv = q > 0.f ? rsqrtf(q / NPIX) : 1.f;
+        if (lane < kWin)
+        {
+          __nv_bfloat16* dst = x0p + (p * 33 * 33 + 33 + lane + 1) * 2 + ch;
+#pragma unroll
+          for (int r = 0; r < kWin; ++r) dst[r * 33 * 2] = __float2bfloat16((v[r] - mean) * inv);
+        }
+      }
+    }
+    __syncthreads();
+    // ---- conv1: M = kT * 256 rows, K = 18 (padded 32), A gathered as (ci0, ci1) pairs
+    {
+      constexpr int M = kT * 256;
+      for (int mt = warp; mt < M / 16; mt += kFusedThreads / 32)
+      {
+        int rbase[2];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2)
+        {
+          const int row = mt * 16 + g + h2 * 8;
+          const int p = row >> 8, oy = (row >> 4) & 15, ox = row & 15;
+          rbase[h2] = ((p * 33 + 2 * oy) * 33 + 2 * ox) * 2;
+        }
+        float acc[4][4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
+#pragma unroll
+        for (int ks = 0; ks < 2; ++ks)
+        {
+          uint32_t a[4];
+#pragma unroll
+          for (int r = 0; r < 4; ++r)
+          {
+            const int kk = ks * 8 + (r >> 1) * 4 + t4;   // (ky, kx) index of k = ks*16 + (r>>1)*8 + 2 t4
+            const int h2 = r & 1;
+            a[r] = kk < 9 ? *reinterpret_cast<const uint32_t*>(x0p + rbase[h2] + ((kk / 3) * 33 + kk % 3) * 2) : 0u;
+          }
+#pragma unroll
+          for (int j = 0; j < 4; ++j)
+          {
+            const __nv_bfloat16* wr = W1s + (j * 8 + g) * 32 + ks * 16 + t4 * 2;
+            const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8)};
+            mma_bf16_16816(acc[j], a, b);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+        {
+          const int co = j * 8 + t4 * 2;
+          const float bb0 = params[P::b1 + co], bb1 = params[P::b1 + co + 1];
+#pragma unroll
+          for (int h2 = 0; h2 < 2; ++h2)
+          {
+            const int row = mt * 16 + g + h2 * 8;
+            const int p = row >> 8, y = (row >> 4) & 15, x = row & 15;
+            __nv_bfloat16* dst = a1p + ((p * 18 + y + 1) * 18 + x + 1) * kPix + co;
+            *reinterpret_cast<uint32_t*>(dst) = pack_bf16(__float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)),
+                                                          __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
+          }
+        }
+      }
+    }
+    __syncthreads();
+    // x0p is free: zero the a3p region (its border must read as zero padding)
+    for (int i = tid; i < kT * 6 * 6 * kPix / 2; i += kFusedThreads) reinterpret_cast<uint32_t*>(a3p)[i] = 0u;
+    fused_conv32<18, 8, 10>(a1p, a2p, W2s, params + P::b2, 0, warp, lane);
+    __syncthreads();
+    fused_conv32<10, 4, 6>(a2p, a3p, W3s, params + P::b3, 0, warp, lane);
+    __syncthreads();
+    // ---- conv4: 4x4 -> 2x2, M = kT*4 = 16 rows (one m-tile), written unpadded to a4 [p][y][x][c]
+    if (warp < 2)
+    {
+      constexpr int SIP = 6, SO = 2, M = kT * SO * SO;
+      const int nh = warp, q = lane >> 3;
+      const int arow = (q & 1) * 8 + (lane & 7);
+      const int p = arow / 4, oy = (arow % 4) / 2, ox = arow % 2;
+      const __nv_bfloat16* abase = a3p + ((p * SIP + 2 * oy) * SIP + 2 * ox) * kPix + (q >> 1) * 8;
+      const __nv_bfloat16* bbase = W4s + (nh * 16 + (q >> 1) * 8 + (lane & 7)) * kWRow + (q & 1) * 8;
+      float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+#pragma unroll
+      for (int kk = 0; kk < 9; ++kk)
+#pragma unroll
+        for (int half = 0; half < 2; ++half)
+        {
+          uint32_t a[4], b[4];
+          ldsm_x4(a, smem_u32(abase + ((kk / 3) * SIP + kk % 3) * kPix + half * 16));
+          ldsm_x4(b, smem_u32(bbase + kk * 32 + half * 16));
+          const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+          mma_bf16_16816(acc[0], a, b0);
+          mma_bf16_16816(acc[1], a, b1);
+        }
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+      {
+        const int co = nh * 16 + j * 8 + t4 * 2;
+        const float bb0 = params[P::b4 + co], bb1 = params[P::b4 + co + 1];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2)
+        {
+          const int row = g + h2 * 8;
+          if (row >= M) continue;
+          *reinterpret_cast<uint32_t*>(a4 + row * 32 + co) = pack_bf16(
+              __float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)), __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
+        }
+      }
+    }
+    __syncthreads();
+    // ---- f1: [kT x 128] x W5^T -> [kT x 256]; rows >= kT are zero; B fragments from global (L1)
+    for (int nt = warp; nt < kHidden / 8; nt += kFusedThreads / 32)
+    {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int ks = 0; ks < 8; ++ks)
+      {
+        const int c = ks * 16 + t4 * 2;
+        uint32_t a[4];
+        a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * 128 + c) : 0u;
+        a[1] = 0u;
+        a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * 128 + c + 8) : 0u;
+        a[3] = 0u;
+        const __nv_bfloat16* wr = wb + L::f1 + (nt * 8 + g) * 128 + c;
+        const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)), __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
+        mma_bf16_16816(acc, a, b);
+      }
+      const int co = nt * 8 + t4 * 2;
+      if (g < kT)
+        *reinterpret_cast<uint32_t*>(a5 + g * 256 + co) =
+            pack_bf16(__float2bfloat16(fmaxf(acc[0] + params[P::b5 + co], 0.f)),
+                      __float2bfloat16(fmaxf(acc[1] + params[P::b5 + co + 1], 0.f)));
+    }
+    __syncthreads();
+    // ---- f2: [kT x 256] x W6^T -> [kT x 6] (n padded to 8), one warp
+    if (warp == 0)
+    {
+      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+      for (int ks = 0; ks < 16; ++ks)
+      {
+        const int c = ks * 16 + t4 * 2;
+        uint32_t a[4];
+        a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * 256 + c) : 0u;
+        a[1] = 0u;
+        a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * 256 + c + 8) : 0u;
+        a[3] = 0u;
+        const __nv_bfloat16* wr = wb + L::f2 + g * 256 + c;
+        const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)), __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
+        mma_bf16_16816(acc, a, b);
+      }
+      const int co = t4 * 2;
+      if (g < kT)
+      {
+        outs[g * 8 + co] = acc[0] + (co < kOut ? params[P::b6 + co] : 0.f);
+        outs[g * 8 + co + 1] = acc[1] + (co + 1 < kOut ? params[P::b6 + co + 1] : 0.f);
+      }
+    }
+    __syncthreads();
+    if (tid < kT && p0 + tid < n)
+    {
+      const float* o = outs + tid * 8;
+      dic_poi* dst = pois + p0 + tid;
+      dst->u = o[0];
+      dst->v = o[1];
+      dst->ux = o[2] / out_scale(2);
+      dst->uy = o[3] / out_scale(3);
+      dst->vx = o[4] / out_scale(4);
+      dst->vy = o[5] / out_scale(5);
+      dst->u0 = 0.f; dst->v0 = 0.f; dst->zncc = 0.f; dst->iteration = 0.f; dst->convergence = 0.f; dst->feature = 0.f;
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace cnn
+}  // namespace dic

@@ -13,6 +13,7 @@
 #include <algorithm>
 
 #include "dic_kernels.cuh"
+#include "dic_cnn.cuh"
 
 using namespace dic;
 
@@ -98,9 +99,176 @@ void init_constants(int device)
   g_initialized_devices.insert(device);
 }
 
-enum Phase { kPhRef = 0, kPhPoi, kPhTar, kPhFftcc, kPhIcgn, kPhFrame, kPhCount };
+enum Phase { kPhRef = 0, kPhPoi, kPhTar, kPhFftcc, kPhIcgn, kPhFrame, kPhProposal, kPhCount };
 
 }  // namespace
+
+
+// ======================================================================================
+// Proposal network host side (see dic_cnn.cuh for the architecture and the kernels).
+// ======================================================================================
+struct dic_cnn
+{
+  int device = 0;
+  cudaStream_t stream = nullptr;   // own stream; an engine borrows the network on its stream
+  std::string last_error;
+  DevBuf<float> params, grads, adam_m, adam_v, out, part, row_loss;
+  DevBuf<__nv_bfloat16> wb, x0, a1, a2, a3, a4, a5, d1, d2, d3, d4, d5, dout;
+  int64_t cap = 0;
+  long long adam_t = 0;
+  long long launches = 0;
+
+  void check(const char* what)
+  {
+    ++launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) throw DicError{DIC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e)};
+  }
+
+  void ensure_batch(int64_t n)
+  {
+    if (n <= cap) return;
+    x0.ensure((size_t)n * 31 * 31 * 2);
+    a1.ensure((size_t)n * 256 * 32); d1.ensure((size_t)n * 256 * 32);
+    a2.ensure((size_t)n * 64 * 32);  d2.ensure((size_t)n * 64 * 32);
+    a3.ensure((size_t)n * 16 * 32);  d3.ensure((size_t)n * 16 * 32);
+    a4.ensure((size_t)n * 128);      d4.ensure((size_t)n * 128);
+    a5.ensure((size_t)n * 256);      d5.ensure((size_t)n * 256);
+    out.ensure((size_t)n * cnn::kOutPad);
+    dout.ensure((size_t)n * cnn::kOutPad);
+    row_loss.ensure((size_t)n);
+    DIC_CUDA(cudaMemsetAsync(out.ptr, 0, sizeof(float) * n * cnn::kOutPad, stream));
+    cap = n;
+  }
+
+  void pack()
+  {
+    const int n = cnn::kHidden * 128;
+    cnn::k_pack_weights<<<(n + 255) / 256, 256, 0, stream>>>(params.ptr, wb.ptr);
+    check("k_pack_weights");
+  }
+
+  template <class Op>
+  void gemm(const Op& op, int64_t m_rows, int n_cols)
+  {
+    dim3 grid((unsigned)((m_rows + cnn::BM - 1) / cnn::BM), (unsigned)((n_cols + cnn::BN - 1) / cnn::BN),
+              (unsigned)op.splits);
+    cnn::k_gemm<Op><<<grid, 128, 0, stream>>>(op);
+    check("k_gemm");
+  }
+
+  static int splits_for(int64_t k) { return (int)std::min<int64_t>(128, std::max<int64_t>(1, k / 2048)); }
+
+  // Forward on x0 (already in this->x0 or given), batch n; logits into out [n][8].
+  void forward(const __nv_bfloat16* in, int64_t n)
+  {
+    using L = cnn::WeightLayout;
+    using P = cnn::ParamLayout;
+    const __nv_bfloat16* acts_in[4] = {in, a1.ptr, a2.ptr, a3.ptr};
+    __nv_bfloat16* acts_out[4] = {a1.ptr, a2.ptr, a3.ptr, a4.ptr};
+    const int woff[4] = {L::c1, L::c2, L::c3, L::c4};
+    const int boff[4] = {P::b1, P::b2, P::b3, P::b4};
+    for (int l = 0; l < 4; ++l)
+    {
+      const int si = cnn::side_of(l), so = cnn::side_of(l + 1), ci = l == 0 ? 2 : 32;
+      cnn::ConvFwdOp op;
+      op.in = acts_in[l];
+      op.w = wb.ptr + woff[l];
+      op.bias = params.ptr + boff[l];
+      op.out = acts_out[l];
+      op.M = n * so * so;
+      op.N = 32;
+      op.splits = 1;
+      op.kreal = 9 * ci;
+      op.kpad = l == 0 ? cnn::kC1K : 288;
+      op.K = op.kpad;
+      op.si = si;
+      op.so = so;
+      op.ci = ci;
+      gemm(op, op.M, 32);
+    }
+    cnn::LinearFwdOp f1{a4.ptr, wb.ptr + L::f1, params.ptr + P::b5, a5.ptr, nullptr, n, cnn::kHidden, 1, 128, 0};
+    gemm(f1, n, cnn::kHidden);
+    cnn::LinearFwdOp f2{a5.ptr, wb.ptr + L::f2, params.ptr + P::b6, nullptr, out.ptr, n, cnn::kOut, 1, cnn::kHidden,
+                        cnn::kOutPad};
+    gemm(f2, n, cnn::kOutPad);
+  }
+
+  void reduce_into(int splits, int rows, int cols, int keep, float* dst, int ld)
+  {
+    const int total = rows * keep;
+    cnn::k_reduce_splits<<<(total + 255) / 256, 256, 0, stream>>>(part.ptr, splits, rows, cols, keep, dst, ld);
+    check("k_reduce_splits");
+  }
+
+  void bias_grad(const __nv_bfloat16* dz, int64_t rows, int ld, int ncol, float* db)
+  {
+    cnn::k_bias_grad<<<ncol, 256, 0, stream>>>(dz, rows, ld, ncol, db);
+    check("k_bias_grad");
+  }
+
+  // Backward after forward(in, n) with targets [n][6]; gradients into grads (param layout).
+  void backward(const __nv_bfloat16* in, const float* target, int64_t n)
+  {
+    using L = cnn::WeightLayout;
+    using P = cnn::ParamLayout;
+    cnn::k_loss_grad<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(out.ptr, target, n, dout.ptr, row_loss.ptr);
+    check("k_loss_grad");
+    // f2
+    {
+      const int S = splits_for(n);
+      cnn::LinearBwdWeightOp op{dout.ptr, a5.ptr, part.ptr, cnn::kOut, cnn::kHidden, S, n, cnn::kOutPad};
+      gemm(op, cnn::kOut, cnn::kHidden);
+      reduce_into(S, cnn::kOut, cnn::kHidden, cnn::kHidden, grads.ptr + P::w6, cnn::kHidden);
+      bias_grad(dout.ptr, n, cnn::kOutPad, cnn::kOut, grads.ptr + P::b6);
+      cnn::LinearBwdDataOp dop{dout.ptr, wb.ptr + L::f2, a5.ptr, d5.ptr, n, cnn::kHidden, 1, cnn::kOut, cnn::kOutPad};
+      gemm(dop, n, cnn::kHidden);
+    }
+    // f1
+    {
+      const int S = splits_for(n);
+      cnn::LinearBwdWeightOp op{d5.ptr, a4.ptr, part.ptr, cnn::kHidden, 128, S, n, cnn::kHidden};
+      gemm(op, cnn::kHidden, 128);
+      reduce_into(S, cnn::kHidden, 128, 128, grads.ptr + P::w5, 128);
+      bias_grad(d5.ptr, n, cnn::kHidden, cnn::kHidden, grads.ptr + P::b5);
+      cnn::LinearBwdDataOp dop{d5.ptr, wb.ptr + L::f1, a4.ptr, d4.ptr, n, 128, 1, cnn::kHidden, cnn::kHidden};
+      gemm(dop, n, 128);
+    }
+    // conv4 .. conv1
+    const __nv_bfloat16* acts_in[4] = {in, a1.ptr, a2.ptr, a3.ptr};
+    __nv_bfloat16* dz_out[4] = {d1.ptr, d2.ptr, d3.ptr, d4.ptr};
+    const int woff[4] = {L::c1, L::c2, L::c3, L::c4};
+    const int wpo[4] = {P::w1, P::w2, P::w3, P::w4};
+    const int bpo[4] = {P::b1, P::b2, P::b3, P::b4};
+    for (int l = 3; l >= 0; --l)
+    {
+      const int si = cnn::side_of(l), so = cnn::side_of(l + 1), ci = l == 0 ? 2 : 32;
+      const int kreal = 9 * ci, kpad = l == 0 ? cnn::kC1K : 288;
+      const int64_t K = n * so * so;
+      const int S = splits_for(K);
+      cnn::ConvBwdWeightOp wop{dz_out[l], acts_in[l], part.ptr, 32, kpad, S, K, si, so, ci, 32, kreal, kpad};
+      gemm(wop, 32, kpad);
+      reduce_into(S, 32, kpad, kreal, grads.ptr + wpo[l], kreal);
+      bias_grad(dz_out[l], K, 32, 32, grads.ptr + bpo[l]);
+      if (l > 0)
+      {
+        cnn::ConvBwdDataOp dop{dz_out[l], wb.ptr + woff[l], acts_in[l], dz_out[l - 1], n * si * si, ci, 1, 9 * 32,
+                               si, so, ci, 32, kpad};
+        gemm(dop, n * si * si, ci);
+      }
+    }
+  }
+
+  float loss(int64_t n)
+  {
+    std::vector<float> h((size_t)n);
+    DIC_CUDA(cudaMemcpyAsync(h.data(), row_loss.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost, stream));
+    DIC_CUDA(cudaStreamSynchronize(stream));
+    double s = 0.0;
+    for (float v : h) s += v;
+    return (float)(s / ((double)n * cnn::kOut));
+  }
+};
 
 struct dic_engine
 {
@@ -125,8 +293,12 @@ struct dic_engine
   DevBuf<int64_t> slots;
   DevBuf<unsigned long long> counters;
 
+  // Per-phase CUDA events; a phase launched several times in one call (the learned path's
+  // two IC-GN passes) reports the sum of its launches.
+  static constexpr int kMarks = 8;
   bool timing = true;
-  cudaEvent_t ev[kPhCount][2] = {};
+  cudaEvent_t ev[kPhCount][kMarks][2] = {};
+  int ev_used[kPhCount] = {};
   bool ev_pending[kPhCount] = {};
   double ms[kPhCount] = {};
   long long launches = 0;
@@ -142,19 +314,33 @@ struct dic_engine
   }
   void mark(int ph, int which)
   {
-    if (!timing) return;
-    DIC_CUDA(cudaEventRecord(ev[ph][which], stream));
-    if (which == 1) ev_pending[ph] = true;
+    if (!timing || ev_used[ph] >= kMarks) return;
+    DIC_CUDA(cudaEventRecord(ev[ph][ev_used[ph]][which], stream));
+    if (which == 1)
+    {
+      ++ev_used[ph];
+      ev_pending[ph] = true;
+    }
+  }
+  // A new API call starts a new measurement (pending events of the previous call are dropped).
+  void begin_call()
+  {
+    for (int p = 0; p < kPhCount; ++p) ev_used[p] = 0;
   }
   void harvest()
   {
     for (int p = 0; p < kPhCount; ++p)
       if (ev_pending[p])
       {
-        float t = 0.f;
-        DIC_CUDA(cudaEventSynchronize(ev[p][1]));
-        DIC_CUDA(cudaEventElapsedTime(&t, ev[p][0], ev[p][1]));
-        ms[p] = t;
+        double tot = 0.0;
+        for (int k = 0; k < ev_used[p]; ++k)
+        {
+          float t = 0.f;
+          DIC_CUDA(cudaEventSynchronize(ev[p][k][1]));
+          DIC_CUDA(cudaEventElapsedTime(&t, ev[p][k][0], ev[p][k][1]));
+          tot += t;
+        }
+        ms[p] = tot;
         ev_pending[p] = false;
       }
     if (iter_pending)
@@ -336,7 +522,7 @@ struct dic_engine
   }
 
   void run_icgn(dic_poi* d_pois, int64_t n, const int64_t* d_slots, const int64_t* n_dev = nullptr,
-                const int* enable = nullptr, bool reset_iterations = true)
+                const int* enable = nullptr, bool reset_iterations = true, int max_iter_override = 0)
   {
     if (n == 0) return;
     ensure_ref();
@@ -357,7 +543,7 @@ struct dic_engine
     p.rx = cfg.subset_radius_x;
     p.ry = cfg.subset_radius_y;
     p.conv = cfg.conv_criterion;
-    p.max_iter = (float)cfg.max_iteration;
+    p.max_iter = (float)(max_iter_override > 0 ? max_iter_override : cfg.max_iteration);
     p.iter_sum = counters.ptr;
     const int wpb = 4;
     mark(kPhIcgn, 0);
@@ -449,6 +635,51 @@ struct dic_engine
     check_launch("k_count_bad");
   }
 
+  // ---------------------------------------------------------------- learned seed
+  dic_cnn* proposal = nullptr;
+  static constexpr int kLearnedMaxIter = 6;      // IC-GN budget from the proposal's seed
+  static constexpr float kLearnedAccept = 0.9f;  // ZNCC the proposal's result must reach
+  static constexpr int64_t kProposalBatch = 32768;
+
+  // Queue `queue` holds the template (x, y); layout is this queue's.  Proposal seeds, IC-GN
+  // capped at kLearnedMaxIter, then FFTCC + IC-GN (full budget) for the POIs that fail.
+  void enqueue_learned(int64_t n)
+  {
+    if (!proposal) throw DicError{DIC_ERR_STATE, "no proposal network attached (dic_set_proposal)"};
+    ensure_ref();
+    ensure_tar();
+    ensure_frame_buffers(n);
+    const unsigned tb = 256, nb = (unsigned)((n + tb - 1) / tb);
+    DIC_CUDA(cudaMemsetAsync(fcount.ptr, 0, sizeof(FrameCounters), stream));
+    DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
+    DIC_CUDA(cudaMemcpyAsync(tmpl.ptr, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, stream));
+    mark(kPhProposal, 0);
+    {
+      // fused inference: one persistent CTA per SM, kT POIs per tile, seeds into the queue
+      int sms = 0;
+      DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+      const int64_t tiles = (n + cnn::kT - 1) / cnn::kT;
+      const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
+      cnn::k_proposal_fused<<<grid, cnn::kFusedThreads, cnn::kSmTotal, stream>>>(
+          ref_f32.ptr, tar_f32.ptr, w, h, queue.ptr, n, proposal->wb.ptr, proposal->params.ptr);
+      check_launch("k_proposal_fused");
+    }
+    mark(kPhProposal, 1);
+    run_icgn(queue.ptr, n, nullptr, nullptr, nullptr, false, std::min(kLearnedMaxIter, cfg.max_iteration));
+    k_scan_learned<<<nb, tb, 0, stream>>>(queue.ptr, kLearnedAccept, fcount.ptr, cand.ptr, n);
+    check_launch("k_scan_learned");
+    k_enable_candidates<<<1, 32, 0, stream>>>(fcount.ptr);
+    check_launch("k_enable_candidates");
+    const int* pr = &fcount.ptr->poi_repair;
+    const int64_t* cn = &fcount.ptr->candidate_count;
+    k_gather_candidates<<<nb, tb, 0, stream>>>(tmpl.ptr, cand.ptr, fcount.ptr, fq.ptr, n);
+    check_launch("k_gather_candidates");
+    run_fftcc(fq.ptr, n, cn, pr);
+    run_icgn(fq.ptr, n, cand.ptr, cn, pr, false);
+    k_merge_fallback<<<nb, tb, 0, stream>>>(queue.ptr, fq.ptr, cand.ptr, fcount.ptr, n);
+    check_launch("k_merge_fallback");
+  }
+
   void fill_report(dic_frame_report* r, int64_t n, bool use_skip, const dic_poi* host_results)
   {
     if (!r) return;
@@ -485,7 +716,7 @@ namespace
 {
 
 template <typename F>
-int guarded(dic_engine* e, F&& f)
+int guarded(dic_engine* e, F&& f, bool new_call = true)
 {
   if (!e) return DIC_ERR_ARGUMENT;
   try
@@ -493,6 +724,7 @@ int guarded(dic_engine* e, F&& f)
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev != e->cfg.device) DIC_CUDA(cudaSetDevice(e->cfg.device));
+    if (new_call) e->begin_call();
     f();
     e->last_error.clear();
     return DIC_OK;
@@ -535,8 +767,10 @@ int dic_engine_create(const dic_config* config, dic_engine** out)
     DIC_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
     DIC_CUDA(cudaFuncSetAttribute(k_fftcc_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)(2 * kMaxTwiddleN * (kMaxTwiddleN + 1) * sizeof(float2))));
+    DIC_CUDA(cudaFuncSetAttribute(cnn::k_proposal_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cnn::kSmTotal));
     for (int p = 0; p < kPhCount; ++p)
-      for (int k = 0; k < 2; ++k) DIC_CUDA(cudaEventCreate(&e->ev[p][k]));
+      for (int m = 0; m < dic_engine::kMarks; ++m)
+        for (int k = 0; k < 2; ++k) DIC_CUDA(cudaEventCreate(&e->ev[p][m][k]));
   }
   catch (const DicError& err)
   {
@@ -572,8 +806,9 @@ void dic_engine_destroy(dic_engine* e)
   e->fcount.release();
   e->baseline.release();
   for (int p = 0; p < kPhCount; ++p)
-    for (int k = 0; k < 2; ++k)
-      if (e->ev[p][k]) cudaEventDestroy(e->ev[p][k]);
+    for (int m = 0; m < dic_engine::kMarks; ++m)
+      for (int k = 0; k < 2; ++k)
+        if (e->ev[p][m][k]) cudaEventDestroy(e->ev[p][m][k]);
   if (e->stream) cudaStreamDestroy(e->stream);
   delete e;
 }
@@ -704,6 +939,16 @@ int dic_run_device(dic_engine* e, dic_poi* d_pois, int64_t n, int32_t flags)
       e->layout_x.clear();
       e->layout_y.clear();
       e->prepare_layout_device(d_pois, n);
+    }
+    if (flags & DIC_RUN_LEARNED)
+    {
+      // the learned path works on the engine queue; device records are copied in and out
+      e->queue.ensure((size_t)n);
+      DIC_CUDA(cudaMemcpyAsync(e->queue.ptr, d_pois, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+      e->enqueue_learned(n);
+      DIC_CUDA(cudaMemcpyAsync(d_pois, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+      e->iter_pending = true;
+      return;
     }
     if (flags & DIC_RUN_FFTCC) e->run_fftcc(d_pois, n);
     if (flags & DIC_RUN_ICGN) e->run_icgn(d_pois, n, nullptr);
@@ -851,6 +1096,39 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
   });
 }
 
+int dic_set_proposal(dic_engine* e, dic_cnn* net)
+{
+  return guarded(e, [&] {
+    if (net && net->device != e->cfg.device)
+      throw DicError{DIC_ERR_ARGUMENT, "the proposal network lives on another device"};
+    e->proposal = net;
+  });
+}
+
+int dic_process_pair_learned(dic_engine* e, dic_poi* pois, int64_t n, dic_frame_report* report)
+{
+  return guarded(e, [&] {
+    if (n < 0 || (n > 0 && !pois)) throw DicError{DIC_ERR_ARGUMENT, "process_pair_learned: bad queue"};
+    if (!e->ref_set || !e->tar_set) throw DicError{DIC_ERR_STATE, "images must be set before compute"};
+    if (e->cfg.subset_radius_x != e->cfg.subset_radius_y)
+      throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D supports positive square radii only"};
+    if (report) *report = dic_frame_report{};
+    if (n == 0) return;
+    e->counters.ensure(1);
+    e->upload_queue(pois, n);
+    if (!e->layout_matches(pois, n))
+    {
+      e->record_layout(pois, n);
+      e->prepare_layout_device(e->queue.ptr, n);
+    }
+    e->enqueue_learned(n);
+    e->iter_pending = true;
+    e->icgn_pois = n;
+    e->download_queue(pois, n);
+    e->fill_report(report, n, true, pois);
+  });
+}
+
 int dic_set_graphs(dic_engine* e, int32_t enabled)
 {
   return guarded(e, [&] {
@@ -896,10 +1174,11 @@ int dic_get_stats(const dic_engine* ce, dic_stats* out)
     out->ms_fftcc = e->ms[kPhFftcc];
     out->ms_icgn = e->ms[kPhIcgn];
     out->ms_frame = e->ms[kPhFrame];
+    out->ms_proposal = e->ms[kPhProposal];
     out->kernel_launches = e->launches;
     out->icgn_pois = e->icgn_pois;
     out->icgn_iterations = (int64_t)e->iter_sum;
-  });
+  }, false);
 }
 
 int dic_set_timing(dic_engine* e, int32_t enabled)
@@ -907,6 +1186,192 @@ int dic_set_timing(dic_engine* e, int32_t enabled)
   return guarded(e, [&] {
     e->harvest();
     e->timing = enabled != 0;
+  }, false);
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- proposal network ABI
+namespace
+{
+template <typename F>
+int cnn_guarded(dic_cnn* c, F&& f)
+{
+  if (!c) return DIC_ERR_ARGUMENT;
+  try
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev != c->device) DIC_CUDA(cudaSetDevice(c->device));
+    f();
+    c->last_error.clear();
+    return DIC_OK;
+  }
+  catch (const DicError& err)
+  {
+    c->last_error = err.msg;
+    return err.code;
+  }
+  catch (const std::exception& ex)
+  {
+    c->last_error = ex.what();
+    return DIC_ERR_MEMORY;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+int64_t dic_cnn_param_count(void) { return cnn::ParamLayout::count; }
+
+int dic_cnn_create(int32_t device, dic_cnn** out)
+{
+  if (!out) return DIC_ERR_ARGUMENT;
+  *out = nullptr;
+  dic_cnn* c = new (std::nothrow) dic_cnn();
+  if (!c) return DIC_ERR_MEMORY;
+  c->device = device;
+  try
+  {
+    DIC_CUDA(cudaSetDevice(device));
+    DIC_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    const size_t np = cnn::ParamLayout::count;
+    c->params.ensure(np);
+    c->grads.ensure(np);
+    c->adam_m.ensure(np);
+    c->adam_v.ensure(np);
+    c->wb.ensure(cnn::WeightLayout::count);
+    c->part.ensure((size_t)128 * cnn::kHidden * 128);
+    DIC_CUDA(cudaMemsetAsync(c->params.ptr, 0, sizeof(float) * np, c->stream));
+    DIC_CUDA(cudaMemsetAsync(c->grads.ptr, 0, sizeof(float) * np, c->stream));
+    DIC_CUDA(cudaMemsetAsync(c->adam_m.ptr, 0, sizeof(float) * np, c->stream));
+    DIC_CUDA(cudaMemsetAsync(c->adam_v.ptr, 0, sizeof(float) * np, c->stream));
+    c->pack();
+    DIC_CUDA(cudaStreamSynchronize(c->stream));
+  }
+  catch (const DicError& err)
+  {
+    std::fprintf(stderr, "dic_cnn_create: %s\n", err.msg.c_str());
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return err.code;
+  }
+  *out = c;
+  return DIC_OK;
+}
+
+void dic_cnn_destroy(dic_cnn* c)
+{
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto* b : {&c->params, &c->grads, &c->adam_m, &c->adam_v, &c->out, &c->part, &c->row_loss}) b->release();
+  for (auto* b : {&c->wb, &c->x0, &c->a1, &c->a2, &c->a3, &c->a4, &c->a5, &c->d1, &c->d2, &c->d3, &c->d4, &c->d5,
+                  &c->dout})
+    b->release();
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* dic_cnn_last_error(const dic_cnn* c) { return c ? c->last_error.c_str() : "null network"; }
+
+int dic_cnn_set_params(dic_cnn* c, const float* host, int64_t n)
+{
+  return cnn_guarded(c, [&] {
+    if (!host || n != cnn::ParamLayout::count) throw DicError{DIC_ERR_ARGUMENT, "set_params: wrong parameter count"};
+    DIC_CUDA(cudaMemcpyAsync(c->params.ptr, host, sizeof(float) * n, cudaMemcpyHostToDevice, c->stream));
+    DIC_CUDA(cudaMemsetAsync(c->adam_m.ptr, 0, sizeof(float) * n, c->stream));
+    DIC_CUDA(cudaMemsetAsync(c->adam_v.ptr, 0, sizeof(float) * n, c->stream));
+    c->adam_t = 0;
+    c->pack();
+    DIC_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int dic_cnn_get_params(dic_cnn* c, float* host, int64_t n)
+{
+  return cnn_guarded(c, [&] {
+    if (!host || n != cnn::ParamLayout::count) throw DicError{DIC_ERR_ARGUMENT, "get_params: wrong parameter count"};
+    DIC_CUDA(cudaMemcpyAsync(host, c->params.ptr, sizeof(float) * n, cudaMemcpyDeviceToHost, c->stream));
+    DIC_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int dic_cnn_input(dic_cnn* c, const float* d_ref, const float* d_tar, int32_t w, int32_t h, const dic_poi* d_pois,
+                  int64_t n, void* d_x0)
+{
+  return cnn_guarded(c, [&] {
+    if (!d_ref || !d_tar || !d_x0 || (n > 0 && !d_pois) || w < 1 || h < 1)
+      throw DicError{DIC_ERR_ARGUMENT, "cnn_input: bad arguments"};
+    if (n == 0) return;
+    cnn::k_extract_input<<<(unsigned)((n + 3) / 4), 128, 0, c->stream>>>(d_ref, d_tar, w, h, d_pois, n,
+                                                                        static_cast<__nv_bfloat16*>(d_x0));
+    c->check("k_extract_input");
+    DIC_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int dic_cnn_seed(dic_cnn* c, const float* d_ref, const float* d_tar, int32_t w, int32_t h, dic_poi* d_pois, int64_t n)
+{
+  return cnn_guarded(c, [&] {
+    if (!d_ref || !d_tar || (n > 0 && !d_pois) || w < 1 || h < 1) throw DicError{DIC_ERR_ARGUMENT, "cnn_seed: bad arguments"};
+    if (n == 0) return;
+    int sms = 0;
+    DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+    DIC_CUDA(cudaFuncSetAttribute(cnn::k_proposal_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cnn::kSmTotal));
+    const int64_t tiles = (n + cnn::kT - 1) / cnn::kT;
+    cnn::k_proposal_fused<<<(unsigned)std::min<int64_t>(tiles, sms), cnn::kFusedThreads, cnn::kSmTotal, c->stream>>>(
+        d_ref, d_tar, w, h, d_pois, n, c->wb.ptr, c->params.ptr);
+    c->check("k_proposal_fused");
+    DIC_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int dic_cnn_forward(dic_cnn* c, const void* d_x0, int64_t n, float* d_out)
+{
+  return cnn_guarded(c, [&] {
+    if (!d_x0 || !d_out || n < 0) throw DicError{DIC_ERR_ARGUMENT, "cnn_forward: bad arguments"};
+    if (n == 0) return;
+    c->ensure_batch(n);
+    c->forward(static_cast<const __nv_bfloat16*>(d_x0), n);
+    DIC_CUDA(cudaMemcpyAsync(d_out, c->out.ptr, sizeof(float) * n * cnn::kOutPad, cudaMemcpyDeviceToDevice, c->stream));
+    DIC_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int dic_cnn_gradient(dic_cnn* c, const void* d_x0, const float* d_target, int64_t n, float* d_grad, float* loss)
+{
+  return cnn_guarded(c, [&] {
+    if (!d_x0 || !d_target || !d_grad || n <= 0) throw DicError{DIC_ERR_ARGUMENT, "cnn_gradient: bad arguments"};
+    c->ensure_batch(n);
+    const __nv_bfloat16* in = static_cast<const __nv_bfloat16*>(d_x0);
+    c->forward(in, n);
+    c->backward(in, d_target, n);
+    DIC_CUDA(cudaMemcpyAsync(d_grad, c->grads.ptr, sizeof(float) * cnn::ParamLayout::count,
+                             cudaMemcpyDeviceToDevice, c->stream));
+    const float l = c->loss(n);
+    if (loss) *loss = l;
+  });
+}
+
+int dic_cnn_train_step(dic_cnn* c, const void* d_x0, const float* d_target, int64_t n, float lr, float* loss)
+{
+  return cnn_guarded(c, [&] {
+    if (!d_x0 || !d_target || n <= 0 || !(lr > 0.f)) throw DicError{DIC_ERR_ARGUMENT, "cnn_train_step: bad arguments"};
+    c->ensure_batch(n);
+    const __nv_bfloat16* in = static_cast<const __nv_bfloat16*>(d_x0);
+    c->forward(in, n);
+    c->backward(in, d_target, n);
+    ++c->adam_t;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.f - std::pow(b1, (float)c->adam_t), c2 = 1.f - std::pow(b2, (float)c->adam_t);
+    const int np = cnn::ParamLayout::count;
+    cnn::k_adam<<<(np + 255) / 256, 256, 0, c->stream>>>(c->params.ptr, c->grads.ptr, c->adam_m.ptr, c->adam_v.ptr,
+                                                         np, lr, b1, b2, 1e-8f, c1, c2);
+    c->check("k_adam");
+    c->pack();
+    if (loss) *loss = c->loss(n);
+    else DIC_CUDA(cudaStreamSynchronize(c->stream));
   });
 }
 

@@ -1337,6 +1337,40 @@ __global__ void k_merge_frame(dic_poi* __restrict__ cur, const dic_poi* __restri
   if (take) cur[i] = scratch[i];
 }
 
+// Learned-seed fallback: a POI whose IC-GN from the proposal did not converge within the
+// capped iteration budget (-4), was rejected (-3, -5), or ended with ZNCC below the
+// acceptance threshold goes to FFTCC + IC-GN.  Slots are compacted as in k_scan_bad.
+__global__ void k_scan_learned(const dic_poi* __restrict__ cur, float accept, FrameCounters* __restrict__ c,
+                               int64_t* __restrict__ cand, int64_t n)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float z = cur[i].zncc;
+  if (!(z >= accept))
+  {
+    const unsigned long long k = atomicAdd(&c->candidates, 1ull);
+    cand[k] = i;
+  }
+}
+
+__global__ void k_enable_candidates(FrameCounters* c)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  c->candidate_count = (int64_t)c->candidates;
+  c->poi_repair = c->candidates > 0 ? 1 : 0;
+  c->frame_fallback = 0;
+}
+
+// The fallback result replaces the learned attempt for every candidate.
+__global__ void k_merge_fallback(dic_poi* __restrict__ cur, const dic_poi* __restrict__ fq,
+                                 const int64_t* __restrict__ cand, const FrameCounters* c, int64_t n_max)
+{
+  if (c->poi_repair == 0) return;
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= c->candidate_count || k >= n_max) return;
+  cur[cand[k]] = fq[k];
+}
+
 __global__ void k_count_bad(const dic_poi* __restrict__ cur, float thr, unsigned long long* out, int64_t n)
 {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -196,6 +196,17 @@ class Engine:
         self._call(rc)
         return {f: getattr(rep, f) for f, _ in rep._fields_}
 
+    def set_proposal(self, net) -> None:
+        """Attach a ProposalNet (or None) for process_pair_learned / DIC_RUN_LEARNED."""
+        self._proposal = net
+        self._call(self._L.dic_set_proposal(self._h, net.handle if net is not None else None))
+
+    def process_pair_learned(self, queue: np.ndarray):
+        q = _check_queue(queue)
+        rep = _lib.DicFrameReport()
+        self._call(self._L.dic_process_pair_learned(self._h, q.ctypes.data, len(q), ctypes.byref(rep)))
+        return q, {f: getattr(rep, f) for f, _ in rep._fields_}
+
     def set_graphs(self, enabled: bool) -> None:
         self._call(self._L.dic_set_graphs(self._h, int(bool(enabled))))
 

@@ -98,6 +98,7 @@ typedef struct dic_stats
   double ms_fftcc;
   double ms_icgn;
   double ms_frame;           /* whole frame of dic_sequence_frame (upload excluded) */
+  double ms_proposal;        /* proposal network: input windows + forward + seeds */
   int64_t kernel_launches;   /* kernels launched by this engine since creation */
   int64_t icgn_pois;         /* POIs of the last IC-GN call */
   int64_t icgn_iterations;   /* sum of IC-GN iterations over those POIs */
@@ -183,6 +184,7 @@ int dic_set_graphs(dic_engine* engine, int32_t enabled);
 #define DIC_RUN_FFTCC 1
 #define DIC_RUN_ICGN 2
 #define DIC_RUN_PREPARE 4
+#define DIC_RUN_LEARNED 8   /* proposal-network seeds instead of FFTCC (see below) */
 int dic_run_device(dic_engine* engine, dic_poi* device_pois, int64_t count, int32_t flags);
 
 /* Copy one resident device plane to host memory (bytes must equal the plane size):
@@ -197,6 +199,39 @@ int dic_run_device(dic_engine* engine, dic_poi* device_pois, int64_t count, int3
 #define DIC_PLANE_TAR 3
 #define DIC_PLANE_TAR_COEF 4
 int dic_read_plane(dic_engine* engine, int32_t plane, void* host_dst, int64_t bytes);
+
+/* Proposal network (no counterpart in the reference): a CNN mapping the 31x31 reference and
+ * target windows at a POI to (u, v, ux, uy, vx, vy), so IC-GN starts close.  Trained on the
+ * GPU by its own BF16 tensor-core forward/backward kernels with FP32 accumulation.
+ * Parameters are FP32, dic_cnn_param_count() of them, in the layout of
+ * fasticgn_gb300/csrc/dic_cnn.cuh.  Device pointers: x0 is BF16 [n][31][31][2] (NHWC),
+ * targets FP32 [n][6] (u, v, ux, uy, vx, vy), outputs FP32 [n][8] (u, v, 100ux, 100uy,
+ * 100vx, 100vy, 0, 0), gradients FP32 [param_count]. */
+typedef struct dic_cnn dic_cnn;
+int64_t dic_cnn_param_count(void);
+int dic_cnn_create(int32_t device, dic_cnn** out);
+void dic_cnn_destroy(dic_cnn* net);
+const char* dic_cnn_last_error(const dic_cnn* net);
+int dic_cnn_set_params(dic_cnn* net, const float* host_params, int64_t count);
+int dic_cnn_get_params(dic_cnn* net, float* host_params, int64_t count);
+int dic_cnn_input(dic_cnn* net, const float* device_ref, const float* device_tar, int32_t width, int32_t height,
+                  const dic_poi* device_pois, int64_t count, void* device_x0);
+int dic_cnn_forward(dic_cnn* net, const void* device_x0, int64_t count, float* device_out);
+/* Fused inference (the whole network per POI tile in shared memory): writes the proposal's
+ * (u, ux, uy, v, vx, vy) into device_pois and clears their result fields. */
+int dic_cnn_seed(dic_cnn* net, const float* device_ref, const float* device_tar, int32_t width, int32_t height,
+                 dic_poi* device_pois, int64_t count);
+int dic_cnn_gradient(dic_cnn* net, const void* device_x0, const float* device_target, int64_t count,
+                     float* device_grad, float* loss);
+int dic_cnn_train_step(dic_cnn* net, const void* device_x0, const float* device_target, int64_t count,
+                       float learning_rate, float* loss);
+
+/* Attach (or with NULL detach) a proposal network to an engine on the same device. */
+int dic_set_proposal(dic_engine* engine, dic_cnn* net);
+/* Learned-seed pair solve: proposal seeds, IC-GN capped at 6 iterations, and FFTCC + IC-GN
+ * (the full budget) for every POI that does not converge there or ends with ZNCC < 0.9.
+ * report->repaired_candidates counts those fallback POIs. */
+int dic_process_pair_learned(dic_engine* engine, dic_poi* pois, int64_t count, dic_frame_report* report);
 
 int dic_get_stats(const dic_engine* engine, dic_stats* out);
 /* Turns per-phase CUDA-event timing on (1) or off (0).  On by default. */
