@@ -51,6 +51,26 @@ class DicFrameReport(ctypes.Structure):
                 ("iteration_mean", ctypes.c_double)]
 
 
+class DicJob(ctypes.Structure):
+    _fields_ = [("ref", ctypes.c_void_p), ("tar", ctypes.c_void_p), ("width", ctypes.c_int32),
+                ("height", ctypes.c_int32), ("row_stride_bytes", ctypes.c_int64), ("dtype", ctypes.c_int32),
+                ("subset_radius", ctypes.c_int32), ("pois", ctypes.c_void_p), ("count", ctypes.c_int64)]
+
+
+class DicBatchReport(ctypes.Structure):
+    _fields_ = [("pois", ctypes.c_int64), ("valid", ctypes.c_int64), ("jobs", ctypes.c_int32),
+                ("graph", ctypes.c_int32)]
+
+
+class DicLaunchShape(ctypes.Structure):
+    _fields_ = [("warps_per_cta", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("tuned", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
+
+
+class DicTuning(ctypes.Structure):
+    _fields_ = [("icgn", DicLaunchShape * 2), ("batch", DicLaunchShape * 2)]
+
+
 class DicStats(ctypes.Structure):
     _fields_ = [("ms_prepare_ref", ctypes.c_double), ("ms_poi_prepare", ctypes.c_double),
                 ("ms_prepare_tar", ctypes.c_double), ("ms_fftcc", ctypes.c_double),
@@ -85,6 +105,9 @@ SIGNATURES = {
     "dic_sequence_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32, _i32, _vp,
                                           ctypes.POINTER(DicFrameReport)]),
     "dic_set_graphs": (ctypes.c_int, [_vp, _i32]),
+    "dic_batch_process": (ctypes.c_int, [_vp, ctypes.POINTER(DicJob), _i32, _i32, ctypes.POINTER(DicBatchReport)]),
+    "dic_set_autotune": (ctypes.c_int, [_vp, _i32]),
+    "dic_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(DicTuning)]),
     "dic_read_plane": (ctypes.c_int, [_vp, _i32, _vp, _i64]),
     "dic_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(DicStats)]),
     "dic_set_timing": (ctypes.c_int, [_vp, _i32]),

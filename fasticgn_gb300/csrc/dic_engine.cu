@@ -6,6 +6,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <mutex>
 #include <set>
 #include <string>
@@ -488,7 +489,184 @@ struct dic_engine
     layout_count = n;
   }
 
+  // ---------------------------------------------------------------- launch shapes
+  // IC-GN runs one warp per POI; what can be tuned is how many POIs a CTA holds (2, 4 or
+  // 8 warps) and, for the persistent batch kernel, how many CTAs per SM it launches.
+  // Per-POI results do not depend on either.  shape[persistent][column walk].
+  struct IcgnShape
+  {
+    int warps = 4;
+    int ctas_per_sm = 7;
+    float ms = 0.f;
+  };
+  static constexpr int64_t kTuneMinPois = 2048;
+  bool autotune = false;
+  IcgnShape shape[2][2];
+  bool tuned[2][2] = {};
+  DevBuf<dic_poi> tune_q;
+  cudaEvent_t tune_ev[2] = {};
+
+  bool capturing()
+  {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    DIC_CUDA(cudaStreamIsCapturing(stream, &st));
+    return st != cudaStreamCaptureStatusNone;
+  }
+  template <bool C, int W>
+  static int max_ctas(bool persistent)
+  {
+    int b = 0;
+    if (persistent)
+      DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch<C, W>, W * 32, 0));
+    else
+      DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn<C, W>, W * 32, 0));
+    return std::max(b, 1);
+  }
+  static int occupancy(bool persistent, bool column, int warps)
+  {
+    if (column) return warps == 2 ? max_ctas<true, 2>(persistent) : warps == 8 ? max_ctas<true, 8>(persistent)
+                                                                                : max_ctas<true, 4>(persistent);
+    return warps == 2 ? max_ctas<false, 2>(persistent) : warps == 8 ? max_ctas<false, 8>(persistent)
+                                                                     : max_ctas<false, 4>(persistent);
+  }
+  void launch_icgn(const IcgnParams& p, bool column, int warps)
+  {
+    const unsigned blocks = (unsigned)((p.n + warps - 1) / warps);
+#define DIC_ICGN_LAUNCH(C, W) k_icgn<C, W><<<blocks, W * 32, 0, stream>>>(p)
+    if (column)
+    {
+      if (warps == 2) DIC_ICGN_LAUNCH(true, 2);
+      else if (warps == 8) DIC_ICGN_LAUNCH(true, 8);
+      else DIC_ICGN_LAUNCH(true, 4);
+    }
+    else
+    {
+      if (warps == 2) DIC_ICGN_LAUNCH(false, 2);
+      else if (warps == 8) DIC_ICGN_LAUNCH(false, 8);
+      else DIC_ICGN_LAUNCH(false, 4);
+    }
+#undef DIC_ICGN_LAUNCH
+  }
+  struct BatchLaunch
+  {
+    const BatchJob* jobs;
+    int njobs;
+    dic_poi* pois;
+    const PoiRef* poi_ref;
+    int64_t begin, end;
+    unsigned long long* next;
+    unsigned long long* iter_sum;
+  };
+  void launch_batch(const BatchLaunch& b, bool column, const IcgnShape& sh)
+  {
+    int sms = 0;
+    DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+    const unsigned grid = (unsigned)(sms * sh.ctas_per_sm);
+    const float mi = (float)cfg.max_iteration;
+#define DIC_BATCH_LAUNCH(C, W)                                                                                     \
+  k_icgn_batch<C, W><<<grid, W * 32, 0, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,       \
+                                                  cfg.conv_criterion, mi, b.iter_sum)
+    if (column)
+    {
+      if (sh.warps == 2) DIC_BATCH_LAUNCH(true, 2);
+      else if (sh.warps == 8) DIC_BATCH_LAUNCH(true, 8);
+      else DIC_BATCH_LAUNCH(true, 4);
+    }
+    else
+    {
+      if (sh.warps == 2) DIC_BATCH_LAUNCH(false, 2);
+      else if (sh.warps == 8) DIC_BATCH_LAUNCH(false, 8);
+      else DIC_BATCH_LAUNCH(false, 4);
+    }
+#undef DIC_BATCH_LAUNCH
+    check_launch("k_icgn_batch");
+  }
+  float time_once(const std::function<void()>& f)
+  {
+    if (!tune_ev[0])
+      for (auto& ev : tune_ev) DIC_CUDA(cudaEventCreate(&ev));
+    DIC_CUDA(cudaEventRecord(tune_ev[0], stream));
+    f();
+    DIC_CUDA(cudaEventRecord(tune_ev[1], stream));
+    DIC_CUDA(cudaEventSynchronize(tune_ev[1]));
+    float ms = 0.f;
+    DIC_CUDA(cudaEventElapsedTime(&ms, tune_ev[0], tune_ev[1]));
+    return ms;
+  }
+  // Times every candidate shape on a copy of the seeded queue (best of two runs) and keeps
+  // the fastest.  The queue itself is not touched.
+  void tune_icgn(const IcgnParams& p0, bool column)
+  {
+    tune_q.ensure((size_t)p0.n);
+    IcgnParams p = p0;
+    p.pois = tune_q.ptr;
+    p.iter_sum = nullptr;
+    IcgnShape best;
+    best.ms = INFINITY;
+    for (int warps : {2, 4, 8})
+    {
+      float t = INFINITY;
+      for (int rep = 0; rep < 2; ++rep)
+      {
+        DIC_CUDA(cudaMemcpyAsync(tune_q.ptr, p0.pois, sizeof(dic_poi) * p0.n, cudaMemcpyDeviceToDevice, stream));
+        t = std::min(t, time_once([&] { launch_icgn(p, column, warps); }));
+      }
+      if (t < best.ms) best = IcgnShape{warps, 0, t};
+    }
+    shape[0][column] = best;
+    tuned[0][column] = true;
+  }
+  void tune_batch(const BatchLaunch& b0, bool column, int64_t total)
+  {
+    tune_q.ensure((size_t)total);
+    BatchLaunch b = b0;
+    b.pois = tune_q.ptr;
+    b.iter_sum = nullptr;
+    IcgnShape best;
+    best.ms = INFINITY;
+    for (int warps : {2, 4, 8})
+    {
+      const int full = occupancy(true, column, warps);
+      for (int ctas : {full, std::max(1, (3 * full) / 4)})
+      {
+        const IcgnShape sh{warps, ctas, 0.f};
+        float t = INFINITY;
+        for (int rep = 0; rep < 2; ++rep)
+        {
+          DIC_CUDA(cudaMemcpyAsync(tune_q.ptr + b.begin, b0.pois + b.begin, sizeof(dic_poi) * (b.end - b.begin),
+                                   cudaMemcpyDeviceToDevice, stream));
+          DIC_CUDA(cudaMemsetAsync(b.next, 0, sizeof(unsigned long long), stream));
+          t = std::min(t, time_once([&] { launch_batch(b, column, sh); }));
+        }
+        if (t < best.ms) best = IcgnShape{warps, ctas, t};
+      }
+    }
+    shape[1][column] = best;
+    tuned[1][column] = true;
+    DIC_CUDA(cudaMemsetAsync(b0.next, 0, sizeof(unsigned long long), stream));
+  }
+
   // ---------------------------------------------------------------- solvers
+  // FFTCC launch for an explicit plane pair and (square) radius.
+  void fftcc_launch(const FftccParams& p, int r)
+  {
+    const unsigned blocks = (unsigned)((p.n + 3) / 4);
+    switch (2 * r)
+    {
+#define DIC_FFTCC_CASE2(M) \
+  case M: k_fftcc<M><<<blocks, 128, 0, stream>>>(p); break;
+      DIC_FFTCC_CASE2(8) DIC_FFTCC_CASE2(10) DIC_FFTCC_CASE2(12) DIC_FFTCC_CASE2(14) DIC_FFTCC_CASE2(16)
+      DIC_FFTCC_CASE2(18) DIC_FFTCC_CASE2(20) DIC_FFTCC_CASE2(22) DIC_FFTCC_CASE2(24) DIC_FFTCC_CASE2(26)
+      DIC_FFTCC_CASE2(28) DIC_FFTCC_CASE2(30) DIC_FFTCC_CASE2(32)
+#undef DIC_FFTCC_CASE2
+      default:
+        if (r < 1 || 2 * r > kMaxTwiddleN)
+          throw DicError{DIC_ERR_ARGUMENT, "FFTCC supports subset radius 1..32 on this engine"};
+        k_fftcc_large<<<(unsigned)p.n, 256, (size_t)2 * (2 * r) * (2 * r + 1) * sizeof(float2), stream>>>(p, 2 * r);
+    }
+    check_launch("k_fftcc");
+  }
+
   void run_fftcc(dic_poi* d_pois, int64_t n, const int64_t* n_dev = nullptr, const int* enable = nullptr)
   {
     if (n == 0) return;
@@ -497,27 +675,8 @@ struct dic_engine
     FftccParams p{ref_f32.ptr, tar_f32.ptr, d_pois, n, w, h};
     p.n_dev = n_dev;
     p.enable = enable;
-    const int r = cfg.subset_radius_x;
-    const unsigned blocks = (unsigned)((n + 3) / 4);
     mark(kPhFftcc, 0);
-    switch (2 * r)
-    {
-#define DIC_FFTCC_CASE(M) \
-  case M: k_fftcc<M><<<blocks, 128, 0, stream>>>(p); break;
-      DIC_FFTCC_CASE(8) DIC_FFTCC_CASE(10) DIC_FFTCC_CASE(12) DIC_FFTCC_CASE(14) DIC_FFTCC_CASE(16)
-      DIC_FFTCC_CASE(18) DIC_FFTCC_CASE(20) DIC_FFTCC_CASE(22) DIC_FFTCC_CASE(24) DIC_FFTCC_CASE(26)
-      DIC_FFTCC_CASE(28) DIC_FFTCC_CASE(30) DIC_FFTCC_CASE(32)
-#undef DIC_FFTCC_CASE
-      default:
-      {
-        if (r < 1 || 2 * r > kMaxTwiddleN)
-          throw DicError{DIC_ERR_ARGUMENT, "FFTCC supports subset radius 1..32 on this engine"};
-        const int m = 2 * r;
-        const size_t smem = (size_t)2 * m * (m + 1) * sizeof(float2);
-        k_fftcc_large<<<(unsigned)n, 256, smem, stream>>>(p, m);
-      }
-    }
-    check_launch("k_fftcc");
+    fftcc_launch(p, cfg.subset_radius_x);
     mark(kPhFftcc, 1);
   }
 
@@ -545,12 +704,10 @@ struct dic_engine
     p.conv = cfg.conv_criterion;
     p.max_iter = (float)(max_iter_override > 0 ? max_iter_override : cfg.max_iteration);
     p.iter_sum = counters.ptr;
-    const int wpb = 4;
+    const bool column = 2 * p.rx + 1 <= 32;
+    if (autotune && !tuned[0][column] && n >= kTuneMinPois && !capturing()) tune_icgn(p, column);
     mark(kPhIcgn, 0);
-    if (2 * p.rx + 1 <= 32)
-      k_icgn<true><<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, 0, stream>>>(p);
-    else
-      k_icgn<false><<<(unsigned)((n + wpb - 1) / wpb), wpb * 32, 0, stream>>>(p);
+    launch_icgn(p, column, shape[0][column].warps);
     check_launch("k_icgn");
     mark(kPhIcgn, 1);
     icgn_pois = n;
@@ -680,6 +837,225 @@ struct dic_engine
     check_launch("k_merge_fallback");
   }
 
+  // ---------------------------------------------------------------- uneven batches
+  struct JobBufs
+  {
+    DevBuf<unsigned char> raw_ref, raw_tar;
+    DevBuf<float> ref_f32, tar_f32;
+    DevBuf<float4> ref_pack, coef;
+    void release()
+    {
+      raw_ref.release(); raw_tar.release(); ref_f32.release(); tar_f32.release(); ref_pack.release(); coef.release();
+    }
+  };
+  std::vector<JobBufs> jobs_mem;
+  DevBuf<dic_poi> bq;
+  DevBuf<PoiRef> bpoi;
+  DevBuf<BatchJob> bjobs;
+  DevBuf<unsigned long long> bnext;
+
+  template <typename T>
+  void prep_planes(const unsigned char* raw_r, const unsigned char* raw_t, int bw, int bh, JobBufs& J)
+  {
+    dim3 grid((bw + kPrepTile - 1) / kPrepTile, (bh + kPrepTile - 1) / kPrepTile);
+    k_prepare_ref<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_r), bw, bh, scale(), J.ref_f32.ptr,
+                                               J.ref_pack.ptr);
+    check_launch("k_prepare_ref");
+    k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_t), bw, bh, scale(), J.tar_f32.ptr,
+                                               J.coef.ptr);
+    check_launch("k_prepare_tar");
+  }
+
+  // Batch plan: column-walk jobs (2r + 1 <= 32) first, then wider subsets, stable otherwise.
+  std::vector<int> b_order;
+  std::vector<int64_t> b_first;
+  int64_t b_total = 0, b_col_end = 0;
+  std::vector<dic_job> b_key;           // jobs of the captured batch graph (device pointers)
+  bool b_key_seen = false;
+  cudaGraphExec_t batch_graph = nullptr;
+  int batch_graph_kernels = 0;
+
+  void plan_batch(const dic_job* jobs, int nj)
+  {
+    b_order.resize(nj);
+    for (int j = 0; j < nj; ++j) b_order[j] = j;
+    std::stable_sort(b_order.begin(), b_order.end(), [&](int a, int b) {
+      return (2 * jobs[a].subset_radius + 1 <= 32) > (2 * jobs[b].subset_radius + 1 <= 32);
+    });
+    b_first.assign(nj, 0);
+    b_total = 0;
+    b_col_end = 0;
+    for (int k = 0; k < nj; ++k)
+    {
+      const dic_job& J = jobs[b_order[k]];
+      b_first[k] = b_total;
+      b_total += J.count;
+      if (2 * J.subset_radius + 1 <= 32) b_col_end = b_total;
+    }
+    if ((int)jobs_mem.size() < nj) jobs_mem.resize(nj);
+    bq.ensure((size_t)std::max<int64_t>(b_total, 1));
+    bpoi.ensure((size_t)std::max<int64_t>(b_total, 1));
+    bjobs.ensure((size_t)nj);
+    bnext.ensure(2);
+    counters.ensure(1);
+    std::vector<BatchJob> table(nj);
+    for (int k = 0; k < nj; ++k)
+    {
+      const dic_job& J = jobs[b_order[k]];
+      JobBufs& M = jobs_mem[k];
+      const int es = dtype_size(J.dtype);
+      const size_t px = (size_t)J.width * J.height;
+      M.raw_ref.ensure(px * es);
+      M.raw_tar.ensure(px * es);
+      M.ref_f32.ensure(px);
+      M.tar_f32.ensure(px);
+      M.ref_pack.ensure(px);
+      M.coef.ensure(px * 4);
+      table[k] = BatchJob{M.coef.ptr, M.ref_pack.ptr, b_first[k], J.width, J.height, J.subset_radius,
+                          J.subset_radius};
+    }
+    DIC_CUDA(cudaMemcpyAsync(bjobs.ptr, table.data(), sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, stream));
+  }
+
+  // Everything from pixel upload to results, on the engine stream (capturable when the
+  // pixels and queues are device memory).
+  void enqueue_batch(const dic_job* jobs, int nj, bool on_device)
+  {
+    const cudaMemcpyKind in_kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    mark(kPhFrame, 0);
+    DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
+    for (int k = 0; k < nj; ++k)
+    {
+      const dic_job& J = jobs[b_order[k]];
+      JobBufs& M = jobs_mem[k];
+      const int es = dtype_size(J.dtype);
+      DIC_CUDA(cudaMemcpy2DAsync(M.raw_ref.ptr, (size_t)J.width * es, J.ref, (size_t)J.row_stride_bytes,
+                                 (size_t)J.width * es, J.height, in_kind, stream));
+      DIC_CUDA(cudaMemcpy2DAsync(M.raw_tar.ptr, (size_t)J.width * es, J.tar, (size_t)J.row_stride_bytes,
+                                 (size_t)J.width * es, J.height, in_kind, stream));
+      switch (J.dtype)
+      {
+        case DIC_U8: prep_planes<uint8_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M); break;
+        case DIC_U16: prep_planes<uint16_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M); break;
+        default: prep_planes<float>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M); break;
+      }
+      if (J.count == 0) continue;
+      const int r = J.subset_radius;
+      dic_poi* q = bq.ptr + b_first[k];
+      DIC_CUDA(cudaMemcpyAsync(q, J.pois, sizeof(dic_poi) * J.count, in_kind, stream));
+      k_poi_prepare<<<(unsigned)((J.count + 3) / 4), 128, 0, stream>>>(M.ref_pack.ptr, J.width, J.height, q,
+                                                                      J.count, r, r, bpoi.ptr + b_first[k]);
+      check_launch("k_poi_prepare");
+      FftccParams fp{M.ref_f32.ptr, M.tar_f32.ptr, q, J.count, J.width, J.height};
+      fftcc_launch(fp, r);
+    }
+    DIC_CUDA(cudaMemsetAsync(bnext.ptr, 0, 2 * sizeof(unsigned long long), stream));
+    BatchLaunch col{bjobs.ptr, nj, bq.ptr, bpoi.ptr, 0, b_col_end, bnext.ptr, counters.ptr};
+    BatchLaunch flat{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_col_end, b_total, bnext.ptr + 1, counters.ptr};
+    const bool cap = capturing();
+    if (autotune && !cap)
+    {
+      if (b_col_end >= kTuneMinPois && !tuned[1][1]) tune_batch(col, true, b_total);
+      if (b_total - b_col_end >= kTuneMinPois && !tuned[1][0]) tune_batch(flat, false, b_total);
+    }
+    mark(kPhIcgn, 0);
+    if (b_col_end > 0) launch_batch(col, true, shape[1][1]);
+    if (b_total > b_col_end) launch_batch(flat, false, shape[1][0]);
+    mark(kPhIcgn, 1);
+    for (int k = 0; k < nj; ++k)
+    {
+      const dic_job& J = jobs[b_order[k]];
+      if (J.count == 0) continue;
+      DIC_CUDA(cudaMemcpyAsync(J.pois, bq.ptr + b_first[k], sizeof(dic_poi) * J.count,
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, stream));
+    }
+    mark(kPhFrame, 1);
+  }
+
+  static bool same_jobs(const std::vector<dic_job>& a, const dic_job* b, int nb)
+  {
+    if ((int)a.size() != nb) return false;
+    for (int j = 0; j < nb; ++j)
+      if (a[j].ref != b[j].ref || a[j].tar != b[j].tar || a[j].width != b[j].width || a[j].height != b[j].height ||
+          a[j].row_stride_bytes != b[j].row_stride_bytes || a[j].dtype != b[j].dtype ||
+          a[j].subset_radius != b[j].subset_radius || a[j].pois != b[j].pois || a[j].count != b[j].count)
+        return false;
+    return true;
+  }
+  void drop_batch_graph()
+  {
+    if (batch_graph) cudaGraphExecDestroy(batch_graph);
+    batch_graph = nullptr;
+  }
+
+  // With device-resident pixels and queues and graphs enabled, a batch whose jobs repeat
+  // (same pointers, sizes, radii and counts) is captured on its second call and replayed
+  // from the third on; host-memory batches always run eagerly.
+  void run_batch(const dic_job* jobs, int nj, bool on_device, dic_batch_report* rep)
+  {
+    const bool repeat = on_device && use_graphs && b_key_seen && same_jobs(b_key, jobs, nj);
+    if (!repeat)
+    {
+      drop_batch_graph();
+      b_key.assign(jobs, jobs + nj);
+      b_key_seen = on_device && use_graphs;
+      plan_batch(jobs, nj);
+      enqueue_batch(jobs, nj, on_device);
+    }
+    else
+    {
+      if (!batch_graph)
+      {
+        plan_batch(jobs, nj);   // buffers already have their sizes: no allocation below
+        const bool t = timing;
+        timing = false;
+        const long long l0 = launches;
+        cudaGraph_t g = nullptr;
+        DIC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+        try
+        {
+          enqueue_batch(jobs, nj, on_device);
+        }
+        catch (...)
+        {
+          cudaStreamEndCapture(stream, &g);
+          if (g) cudaGraphDestroy(g);
+          timing = t;
+          throw;
+        }
+        DIC_CUDA(cudaStreamEndCapture(stream, &g));
+        timing = t;
+        batch_graph_kernels = (int)(launches - l0);
+        launches = l0;
+        cudaError_t ie = cudaGraphInstantiate(&batch_graph, g, 0);
+        cudaGraphDestroy(g);
+        if (ie != cudaSuccess)
+        {
+          batch_graph = nullptr;
+          throw DicError{DIC_ERR_CUDA, std::string("cudaGraphInstantiate: ") + cudaGetErrorString(ie)};
+        }
+      }
+      mark(kPhFrame, 0);
+      DIC_CUDA(cudaGraphLaunch(batch_graph, stream));
+      mark(kPhFrame, 1);
+      launches += batch_graph_kernels;
+    }
+    DIC_CUDA(cudaStreamSynchronize(stream));
+    iter_pending = true;
+    icgn_pois = b_total;
+    if (rep)
+    {
+      rep->pois = b_total;
+      rep->jobs = nj;
+      rep->graph = repeat ? 1 : 0;
+      int64_t valid = 0;
+      if (!on_device)
+        for (int j = 0; j < nj; ++j)
+          for (int64_t i = 0; i < jobs[j].count; ++i) valid += jobs[j].pois[i].zncc >= 0.f;
+      rep->valid = on_device ? -1 : valid;
+    }
+  }
+
   void fill_report(dic_frame_report* r, int64_t n, bool use_skip, const dic_poi* host_results)
   {
     if (!r) return;
@@ -798,6 +1174,9 @@ void dic_engine_destroy(dic_engine* e)
   e->slots.release();
   e->counters.release();
   if (e->seq_graph) cudaGraphExecDestroy(e->seq_graph);
+  e->drop_batch_graph();
+  for (auto& ev : e->tune_ev)
+    if (ev) cudaEventDestroy(ev);
   e->tmpl.release();
   e->prev.release();
   e->scratch.release();
@@ -805,6 +1184,11 @@ void dic_engine_destroy(dic_engine* e)
   e->cand.release();
   e->fcount.release();
   e->baseline.release();
+  for (auto& J : e->jobs_mem) J.release();
+  e->bq.release();
+  e->bpoi.release();
+  e->bjobs.release();
+  e->bnext.release();
   for (int p = 0; p < kPhCount; ++p)
     for (int m = 0; m < dic_engine::kMarks; ++m)
       for (int k = 0; k < 2; ++k)
@@ -1129,6 +1513,51 @@ int dic_process_pair_learned(dic_engine* e, dic_poi* pois, int64_t n, dic_frame_
   });
 }
 
+int dic_batch_process(dic_engine* e, const dic_job* jobs, int32_t njobs, int32_t pixels_on_device,
+                      dic_batch_report* report)
+{
+  return guarded(e, [&] {
+    if (njobs <= 0 || !jobs) throw DicError{DIC_ERR_ARGUMENT, "batch: no jobs"};
+    if (report) *report = dic_batch_report{};
+    for (int j = 0; j < njobs; ++j)
+    {
+      const dic_job& J = jobs[j];
+      const int es = dtype_size(J.dtype);
+      if (!J.ref || !J.tar || es == 0 || J.width < 5 || J.height < 5 || J.row_stride_bytes < (int64_t)J.width * es ||
+          J.count < 0 || (J.count > 0 && !J.pois) || J.subset_radius < 1 || 2 * J.subset_radius > kMaxTwiddleN)
+        throw DicError{DIC_ERR_ARGUMENT, "batch job " + std::to_string(j) +
+                                             ": bad image, queue or subset radius (square, 1..32)"};
+    }
+    e->run_batch(jobs, njobs, pixels_on_device != 0, report);
+  });
+}
+
+int dic_set_autotune(dic_engine* e, int32_t enabled)
+{
+  return guarded(e, [&] {
+    e->autotune = enabled != 0;
+    for (auto& row : e->tuned)
+      for (bool& t : row) t = false;
+  });
+}
+
+int dic_get_tuning(dic_engine* e, dic_tuning* out)
+{
+  return guarded(e, [&] {
+    if (!out) throw DicError{DIC_ERR_ARGUMENT, "get_tuning: null output"};
+    for (int pers = 0; pers < 2; ++pers)
+      for (int col = 0; col < 2; ++col)
+      {
+        dic_launch_shape& d = pers ? out->batch[col] : out->icgn[col];
+        const auto& s = e->shape[pers][col];
+        d.warps_per_cta = s.warps;
+        d.ctas_per_sm = pers ? s.ctas_per_sm : 0;
+        d.tuned = e->tuned[pers][col] ? 1 : 0;
+        d.ms = s.ms;
+      }
+  }, false);
+}
+
 int dic_set_graphs(dic_engine* e, int32_t enabled)
 {
   return guarded(e, [&] {
@@ -1137,6 +1566,11 @@ int dic_set_graphs(dic_engine* e, int32_t enabled)
     {
       cudaGraphExecDestroy(e->seq_graph);
       e->seq_graph = nullptr;
+    }
+    if (!e->use_graphs)
+    {
+      e->drop_batch_graph();
+      e->b_key_seen = false;
     }
   });
 }

@@ -521,12 +521,11 @@ __device__ __forceinline__ float sample_bspline(const float4* __restrict__ coef,
   return fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
 }
 
+// One POI (queue index i) on the calling warp; shared by the per-queue launch (k_icgn) and
+// the persistent multi-job launch (k_icgn_batch).
 template <bool kColumn>
-__global__ void __launch_bounds__(128, 7) k_icgn(IcgnParams P)
+__device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int lane)
 {
-  const int lane = threadIdx.x & 31;
-  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (!queue_slot_active(P, i)) return;
   dic_poi* poi = P.pois + i;
   const float px = poi->x, py = poi->y;
   const float u_in = poi->u, ux_in = poi->ux, uy_in = poi->uy;
@@ -714,6 +713,73 @@ __global__ void __launch_bounds__(128, 7) k_icgn(IcgnParams P)
   poi->zncc = zncc;
   poi->iteration = (float)it;
   poi->convergence = conv;
+}
+
+// Launch shape: kWarps POIs per CTA (one warp each); the occupancy hint keeps 28 warps per
+// SM resident for every shape, which leaves 72 registers per thread.
+constexpr int icgn_min_blocks(int warps) { return 28 / warps; }
+
+template <bool kColumn, int kWarps = 4>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn(IcgnParams P)
+{
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (!queue_slot_active(P, i)) return;
+  icgn_solve<kColumn>(P, i, lane);
+}
+
+// --------------------------------------------------------------------------------------
+// Persistent multi-job IC-GN (uneven batches): every warp takes the next POI of the
+// concatenated queue from an atomic counter, looks up its job (image pair, planes, subset
+// radius) and solves it, so pairs of different sizes, radii and iteration counts share one
+// launch and no warp idles on a short job.  Jobs are sorted by first POI; PoiRef records are
+// concatenated in queue order.  Per-POI results do not depend on which warp takes the POI.
+// --------------------------------------------------------------------------------------
+struct BatchJob
+{
+  const float4* coef;
+  const float4* ref_pack;
+  int64_t first;   // first queue index of the job
+  int w, h, rx, ry;
+};
+
+template <bool kColumn, int kWarps = 4>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_batch(const BatchJob* __restrict__ jobs, int njobs, dic_poi* pois,
+                                                       const PoiRef* poi_ref, int64_t begin, int64_t end,
+                                                       unsigned long long* next, float conv, float max_iter,
+                                                       unsigned long long* iter_sum)
+{
+  const int lane = threadIdx.x & 31;
+  for (;;)
+  {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(next, 1ull);
+    const int64_t k = begin + (int64_t)__shfl_sync(kFull, t, 0);
+    if (k >= end) return;
+    int j = 0, hi = njobs - 1;   // last job whose first index is <= k
+    while (j < hi)
+    {
+      const int mid = (j + hi + 1) >> 1;
+      if (jobs[mid].first <= k) j = mid;
+      else hi = mid - 1;
+    }
+    const BatchJob& J = jobs[j];
+    IcgnParams P;
+    P.coef = J.coef;
+    P.ref_pack = J.ref_pack;
+    P.poi_ref = poi_ref;
+    P.slot = nullptr;
+    P.pois = pois;
+    P.n = end;
+    P.w = J.w;
+    P.h = J.h;
+    P.rx = J.rx;
+    P.ry = J.ry;
+    P.conv = conv;
+    P.max_iter = max_iter;
+    P.iter_sum = iter_sum;
+    icgn_solve<kColumn>(P, k, lane);
+  }
 }
 
 // --------------------------------------------------------------------------------------

@@ -207,6 +207,61 @@ class Engine:
         self._call(self._L.dic_process_pair_learned(self._h, q.ctypes.data, len(q), ctypes.byref(rep)))
         return q, {f: getattr(rep, f) for f, _ in rep._fields_}
 
+    def batch_process(self, jobs):
+        """Uneven batch: jobs is a list of (ref, tar, subset_radius, queue) with host images
+        (uint8 / uint16 / float32) and POI queues; queues are updated in place."""
+        arr = (_lib.DicJob * len(jobs))()
+        keep = []
+        for k, (ref, tar, radius, queue) in enumerate(jobs):
+            r, dt = self._image(ref)
+            t, dt2 = self._image(tar)
+            if r.shape != t.shape or dt != dt2 or r.strides != t.strides:
+                raise ValueError("reference and target of a job must have the same size, type and layout")
+            q = _check_queue(queue)
+            keep += [r, t, q]
+            arr[k] = _lib.DicJob(r.ctypes.data, t.ctypes.data, r.shape[1], r.shape[0], r.strides[0], dt, int(radius),
+                                 q.ctypes.data, len(q))
+        return self._batch(arr, len(jobs), 0)
+
+    def batch_process_device(self, jobs):
+        """Uneven batch with device-resident data: jobs is a list of (ref, tar, subset_radius,
+        queue) torch CUDA tensors -- 2-D uint8 / uint16 / float32 images and a uint8 tensor of
+        dic_poi records, updated in place.  Repeating the same jobs replays a CUDA graph."""
+        import torch
+        tdt = {torch.uint8: _lib.DIC_U8, torch.int16: _lib.DIC_U16, torch.float32: _lib.DIC_F32}
+        if hasattr(torch, "uint16"):
+            tdt[torch.uint16] = _lib.DIC_U16
+        arr = (_lib.DicJob * len(jobs))()
+        rec = POI_DTYPE.itemsize
+        for k, (ref, tar, radius, queue) in enumerate(jobs):
+            if ref.shape != tar.shape or ref.dtype != tar.dtype or ref.dim() != 2 or ref.stride(1) != 1 \
+                    or tar.stride() != ref.stride():
+                raise ValueError("reference and target of a job must have the same size, type and layout")
+            if queue.dtype != torch.uint8 or queue.numel() % rec or not queue.is_contiguous():
+                raise ValueError("a device queue is a contiguous uint8 tensor of dic_poi records")
+            arr[k] = _lib.DicJob(ref.data_ptr(), tar.data_ptr(), ref.shape[1], ref.shape[0],
+                                 ref.stride(0) * ref.element_size(), tdt[ref.dtype], int(radius), queue.data_ptr(),
+                                 queue.numel() // rec)
+        torch.cuda.synchronize()
+        return self._batch(arr, len(jobs), 1)
+
+    def _batch(self, arr, n, on_device):
+        rep = _lib.DicBatchReport()
+        self._call(self._L.dic_batch_process(self._h, arr, n, on_device, ctypes.byref(rep)))
+        return {f: getattr(rep, f) for f, _ in rep._fields_}
+
+    def set_autotune(self, enabled: bool) -> None:
+        self._call(self._L.dic_set_autotune(self._h, int(bool(enabled))))
+
+    def tuning(self) -> dict:
+        t = _lib.DicTuning()
+        self._call(self._L.dic_get_tuning(self._h, ctypes.byref(t)))
+
+        def shape(s):
+            return {f: getattr(s, f) for f, _ in s._fields_}
+        return {"icgn_flat": shape(t.icgn[0]), "icgn_column": shape(t.icgn[1]),
+                "batch_flat": shape(t.batch[0]), "batch_column": shape(t.batch[1])}
+
     def set_graphs(self, enabled: bool) -> None:
         self._call(self._L.dic_set_graphs(self._h, int(bool(enabled))))
 

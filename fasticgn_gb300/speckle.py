@@ -16,6 +16,10 @@ Workload shapes (all sizes in px, values in grey levels):
   displacement of wavelength 256 px, noise 8 DN.
 * ``crack_frame``: 1024x1024 12-bit in u16, uniform strain + a displacement jump across a
   line.
+* ``uneven_batch``: pairs with sides log-uniform in 256..4096 u8, each with its own random
+  affine field (|u|, |v| <= 8 px, strains <= 1 %), 20 % of the area replaced by flat
+  low-texture patches, subset radius drawn from {10, 15, 20, 30} and a POI count
+  log-uniform in 1k..600k (as far as the image holds).
 """
 from __future__ import annotations
 
@@ -173,6 +177,76 @@ def pair_bumps(seed: int = 4, width: int = 2048, height: int = 2048, noise: floa
     ref = quantize(render(width, height, sp), rng, noise, 255, np.uint8)
     tar = quantize(render(width, height, sp, field), rng, noise, 255, np.uint8)
     return Pair(ref, tar, field, 255)
+
+
+def flat_patches(rng: np.random.Generator, width: int, height: int, fraction: float = 0.2):
+    """Boolean mask of random rectangles covering about ``fraction`` of the image."""
+    mask = np.zeros((height, width), dtype=bool)
+    target = fraction * width * height
+    while mask.sum() < target:
+        pw = int(rng.uniform(0.05, 0.25) * width) + 8
+        ph = int(rng.uniform(0.05, 0.25) * height) + 8
+        x0 = int(rng.integers(0, max(1, width - pw)))
+        y0 = int(rng.integers(0, max(1, height - ph)))
+        mask[y0:y0 + ph, x0:x0 + pw] = True
+    return mask
+
+
+@dataclasses.dataclass
+class BatchPair:
+    ref: np.ndarray
+    tar: np.ndarray
+    field: object
+    radius: int
+    step: int
+    flat: np.ndarray         # True inside the flat patches
+
+
+def pair_uneven(rng: np.random.Generator, width: int, height: int, radius: int, pois: int,
+                noise: float = 1.0, flat_fraction: float = 0.2) -> BatchPair:
+    """One pair of the uneven batch: random affine field, flat patches (background plus
+    noise only, in both images) and a POI step giving about ``pois`` grid POIs."""
+    xc, yc = (width - 1) / 2.0, (height - 1) / 2.0
+    u0, v0 = rng.uniform(-8.0, 8.0, 2)
+    grads = rng.uniform(-0.01, 0.01, 4)
+    half = max(width, height) / 2.0
+    # keep |u|, |v| <= 8 px over the image: shrink the translation where the strain adds up
+    lim_u = 8.0 - (abs(grads[0]) + abs(grads[1])) * half
+    lim_v = 8.0 - (abs(grads[2]) + abs(grads[3])) * half
+    if lim_u < 0 or lim_v < 0:
+        grads = grads * min(1.0, 6.0 / ((np.abs(grads).max() * 2.0) * half))
+        lim_u = 8.0 - (abs(grads[0]) + abs(grads[1])) * half
+        lim_v = 8.0 - (abs(grads[2]) + abs(grads[3])) * half
+    u0 = float(np.clip(u0, -lim_u, lim_u))
+    v0 = float(np.clip(v0, -lim_v, lim_v))
+    field = affine_field(u0, v0, *grads, xc, yc)
+    sp = make_speckles(rng, width, height, pad=24.0)
+    ref_f = render(width, height, sp)
+    tar_f = render(width, height, sp, field)
+    flat = flat_patches(rng, width, height, flat_fraction)
+    ref_f[flat] = 40.0
+    tar_f[flat] = 40.0
+    ref = quantize(ref_f, rng, noise, 255, np.uint8)
+    tar = quantize(tar_f, rng, noise, 255, np.uint8)
+    margin = radius + 2
+    span = max(1, min(width, height) - 2 * margin)
+    step = max(1, int(math.ceil(math.sqrt((width - 2 * margin) * (height - 2 * margin) / float(pois)))))
+    step = min(step, span)
+    return BatchPair(ref, tar, field, radius, step, flat)
+
+
+def uneven_batch(seed: int = 3, count: int = 16, min_side: int = 256, max_side: int = 4096,
+                 radii=(10, 15, 20, 30), min_pois: int = 1000, max_pois: int = 600_000):
+    """The uneven batch: ``count`` pairs of random size, radius and POI count."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        w = int(round(math.exp(rng.uniform(math.log(min_side), math.log(max_side)))))
+        h = int(round(math.exp(rng.uniform(math.log(min_side), math.log(max_side)))))
+        r = int(rng.choice(radii))
+        n = int(round(math.exp(rng.uniform(math.log(min_pois), math.log(max_pois)))))
+        out.append(pair_uneven(rng, w, h, r, n))
+    return out
 
 
 def stream_frames(seed: int = 2, width: int = 2048, height: int = 2048, frames: int = 200,

@@ -176,6 +176,61 @@ int dic_sequence_frame(dic_engine* engine, const void* pixels, int32_t width, in
                        dic_frame_report* report);
 int dic_set_graphs(dic_engine* engine, int32_t enabled);
 
+/* Uneven batch: several image pairs of different sizes, each with its own subset radius
+ * (square, 1..32) and POI queue, solved together (FFTCC seed + IC-GN).  No single call of
+ * the reference does this; the CLI loops over pairs.  Per pair the prep and FFTCC launches
+ * run back to back on the engine stream; all POIs of all pairs then go through one
+ * persistent IC-GN launch per code path (subsets up to 32 columns wide, and wider) whose
+ * warps take POIs from a shared atomic counter, so pairs with many POIs or slow-converging
+ * POIs do not leave SMs idle.  Results are written back into each job's queue.  The
+ * engine's conv_criterion and max_iteration apply to all jobs. */
+typedef struct dic_job
+{
+  const void* ref;
+  const void* tar;
+  int32_t width, height;
+  int64_t row_stride_bytes;
+  int32_t dtype;
+  int32_t subset_radius;
+  dic_poi* pois;
+  int64_t count;
+} dic_job;
+
+typedef struct dic_batch_report
+{
+  int64_t pois;
+  int64_t valid;       /* POIs with zncc >= 0 (-1 when the queues are in device memory) */
+  int32_t jobs;
+  int32_t graph;       /* 1 when the call replayed a captured CUDA graph */
+} dic_batch_report;
+
+int dic_batch_process(dic_engine* engine, const dic_job* jobs, int32_t njobs, int32_t pixels_on_device,
+                      dic_batch_report* report);
+
+/* Launch-shape autotuner (no reference counterpart).  IC-GN runs one warp per POI; when
+ * enabled, the first IC-GN launch of each kind (per-queue / persistent batch, column walk
+ * for subsets up to 32 columns / flat walk) with at least 2048 POIs times the candidate
+ * shapes -- 2, 4 or 8 POIs (warps) per CTA, and for the persistent kernel full or 3/4
+ * occupancy in CTAs per SM -- on a copy of its seeded queue and keeps the fastest for the
+ * engine's lifetime.  Results do not depend on the shape.  Enabling (again) clears what
+ * was learnt.  Tuning never runs inside a graph capture. */
+typedef struct dic_launch_shape
+{
+  int32_t warps_per_cta;
+  int32_t ctas_per_sm;   /* persistent kernel only (0 otherwise) */
+  int32_t tuned;
+  float ms;              /* best candidate's time, when tuned */
+} dic_launch_shape;
+
+typedef struct dic_tuning
+{
+  dic_launch_shape icgn[2];    /* [0] flat walk, [1] column walk */
+  dic_launch_shape batch[2];
+} dic_tuning;
+
+int dic_set_autotune(dic_engine* engine, int32_t enabled);
+int dic_get_tuning(dic_engine* engine, dic_tuning* out);
+
 /* Device-resident variant: pois points to device memory (count records) and the call only
  * enqueues work on the engine stream (dic_get_stats or a stream sync waits for it).  flags
  * selects the phases, run in this order: DIC_RUN_PREPARE (take this queue's integer (x, y)
