@@ -1138,27 +1138,54 @@ __device__ __forceinline__ float block_sum(float v, float* sbuf)
 }
 
 // out[line][k] = sum_j in[line][j] W^(j k) along rows (by_rows) or columns; conj twiddles
-// when inverse.  in/out are m x s float2 arrays (row stride s).
+// when inverse.  in/out are m x s float2 arrays (row stride s, odd), m even.  A warp takes
+// one bin pair (k, k + m/2) for all lines, lane = line: the twiddle index j k mod m is the
+// same in every lane (one constant-cache broadcast per term), the line reads are
+// conflict-free, and the pair shares its even- and odd-j sums,
+// out[k] = E + O, out[k + m/2] = E - O, since W^(j m/2) = (-1)^j.
 __device__ void dft_lines(const float2* in, float2* out, int m, int s, bool by_rows, bool inverse)
 {
   const float2* tw = c_tw + tw_offset(m);
-  for (int t = threadIdx.x; t < m * m; t += blockDim.x)
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int half = m >> 1;
+  const float sgn = inverse ? -1.f : 1.f;
+  const int step_in = by_rows ? 1 : s;      // along the line
+  const int line_in = by_rows ? s : 1;      // between lines
+  for (int k = warp; k < half; k += nw)
   {
-    const int line = t / m, k = t % m;
-    float re = 0.f, im = 0.f;
-    int e = 0;
-    for (int j = 0; j < m; ++j)
+    for (int line = lane; line < m; line += 32)
     {
-      const float2 a = by_rows ? in[line * s + j] : in[j * s + line];
-      float2 wv = tw[e];
-      if (inverse) wv.y = -wv.y;
-      re += a.x * wv.x - a.y * wv.y;
-      im += a.x * wv.y + a.y * wv.x;
-      e += k;
-      if (e >= m) e -= m;
+      const float2* src = in + line * line_in;
+      float2 E = make_float2(0.f, 0.f), O = make_float2(0.f, 0.f);
+      int e = 0;
+      for (int j = 0; j < m; j += 2)
+      {
+        const float2 a = src[j * step_in];
+        const float2 wa = tw[e];
+        e += k;
+        if (e >= m) e -= m;
+        const float2 b = src[(j + 1) * step_in];
+        const float2 wb = tw[e];
+        e += k;
+        if (e >= m) e -= m;
+        const float wai = sgn * wa.y, wbi = sgn * wb.y;
+        E.x += a.x * wa.x - a.y * wai;
+        E.y += a.x * wai + a.y * wa.x;
+        O.x += b.x * wb.x - b.y * wbi;
+        O.y += b.x * wbi + b.y * wb.x;
+      }
+      const float2 lo = make_float2(E.x + O.x, E.y + O.y), hi = make_float2(E.x - O.x, E.y - O.y);
+      if (by_rows)
+      {
+        out[line * s + k] = lo;
+        out[line * s + k + half] = hi;
+      }
+      else
+      {
+        out[k * s + line] = lo;
+        out[(k + half) * s + line] = hi;
+      }
     }
-    if (by_rows) out[line * s + k] = make_float2(re, im);
-    else out[k * s + line] = make_float2(re, im);
   }
   __syncthreads();
 }

@@ -235,18 +235,34 @@ def pair_uneven(rng: np.random.Generator, width: int, height: int, radius: int, 
     return BatchPair(ref, tar, field, radius, step, flat)
 
 
-def uneven_batch(seed: int = 3, count: int = 16, min_side: int = 256, max_side: int = 4096,
+def uneven_specs(seed: int = 3, count: int = 16, min_side: int = 256, max_side: int = 4096,
                  radii=(10, 15, 20, 30), min_pois: int = 1000, max_pois: int = 600_000):
-    """The uneven batch: ``count`` pairs of random size, radius and POI count."""
+    """Shapes of the uneven batch: (pair seed, width, height, radius, POI count) per pair."""
     rng = np.random.default_rng(seed)
     out = []
-    for _ in range(count):
+    for k in range(count):
         w = int(round(math.exp(rng.uniform(math.log(min_side), math.log(max_side)))))
         h = int(round(math.exp(rng.uniform(math.log(min_side), math.log(max_side)))))
         r = int(rng.choice(radii))
         n = int(round(math.exp(rng.uniform(math.log(min_pois), math.log(max_pois)))))
-        out.append(pair_uneven(rng, w, h, r, n))
+        out.append((seed * 1000 + k, w, h, r, n))
     return out
+
+
+def render_uneven(spec) -> BatchPair:
+    seed, w, h, r, n = spec
+    return pair_uneven(np.random.default_rng(seed), w, h, r, n)
+
+
+def render_uneven_job(spec):
+    """(ref, tar, radius, step) of one uneven-batch pair (picklable, for worker pools)."""
+    p = render_uneven(spec)
+    return p.ref, p.tar, p.radius, p.step
+
+
+def uneven_batch(seed: int = 3, count: int = 16, **kw):
+    """The uneven batch: ``count`` pairs of random size, radius and POI count."""
+    return [render_uneven(s) for s in uneven_specs(seed, count, **kw)]
 
 
 def stream_frames(seed: int = 2, width: int = 2048, height: int = 2048, frames: int = 200,

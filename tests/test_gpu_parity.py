@@ -115,7 +115,7 @@ def test_fftcc_matches_oracle_r15(dic, oracle_mod, affine_pair):
     assert np.median(np.abs(q["u"] - ut)) < 1.0 and np.median(np.abs(q["v"] - vt)) < 1.0
 
 
-@pytest.mark.parametrize("radius", [4, 10, 12, 16, 20, 31])
+@pytest.mark.parametrize("radius", [4, 10, 12, 16, 17, 20, 25, 30, 31, 32])
 def test_fftcc_matches_oracle_radii(dic, oracle_mod, radius):
     """Register FFT (2r <= 32) and the large-radius path against the oracle, shifted speckle."""
     O = oracle_mod
