@@ -48,7 +48,7 @@ class DicFrameReport(ctypes.Structure):
     _fields_ = [("pois", ctypes.c_int64), ("bad_before_repair", ctypes.c_int64),
                 ("bad_after_repair", ctypes.c_int64), ("repaired_candidates", ctypes.c_int64),
                 ("frame_fallback_used", ctypes.c_int32), ("fftcc_used", ctypes.c_int32),
-                ("iteration_mean", ctypes.c_double)]
+                ("iteration_mean", ctypes.c_double), ("repaired_recovered", ctypes.c_int64)]
 
 
 class DicJob(ctypes.Structure):
@@ -85,6 +85,8 @@ _i32, _i64 = ctypes.c_int32, ctypes.c_int64
 SIGNATURES = {
     "dic_version": (ctypes.c_char_p, []),
     "dic_abi_version": (_i32, []),
+    "dic_device_info": (ctypes.c_int, [_i32, ctypes.c_char_p, _i32, ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                                       ctypes.POINTER(_i32), ctypes.POINTER(_i32)]),
     "dic_engine_create": (ctypes.c_int, [ctypes.POINTER(DicConfig), ctypes.POINTER(_vp)]),
     "dic_engine_destroy": (None, [_vp]),
     "dic_last_error": (ctypes.c_char_p, [_vp]),

@@ -1066,6 +1066,7 @@ struct dic_engine
     r->bad_before_repair = (int64_t)c.bad;
     r->bad_after_repair = (int64_t)c.bad_after;
     r->repaired_candidates = use_skip && c.poi_repair ? (int64_t)c.candidates : 0;
+    r->repaired_recovered = use_skip && c.poi_repair ? (int64_t)c.recovered : 0;
     r->frame_fallback_used = use_skip ? c.frame_fallback : 0;
     r->fftcc_used = (!use_skip || c.frame_fallback || c.poi_repair) ? 1 : 0;
     double it = 0.0;
@@ -1155,6 +1156,24 @@ int dic_engine_create(const dic_config* config, dic_engine** out)
     return err.code;
   }
   *out = e;
+  return DIC_OK;
+}
+
+int dic_device_info(int32_t device, char* name, int32_t name_capacity, int32_t* cc_major, int32_t* cc_minor,
+                    int32_t* driver_version, int32_t* runtime_version)
+{
+  cudaDeviceProp prop{};
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return DIC_ERR_CUDA;
+  if (name && name_capacity > 0)
+  {
+    std::strncpy(name, prop.name, (size_t)name_capacity - 1);
+    name[name_capacity - 1] = 0;
+  }
+  if (cc_major) *cc_major = prop.major;
+  if (cc_minor) *cc_minor = prop.minor;
+  int d = 0, r = 0;
+  if (driver_version) *driver_version = cudaDriverGetVersion(&d) == cudaSuccess ? d : 0;
+  if (runtime_version) *runtime_version = cudaRuntimeGetVersion(&r) == cudaSuccess ? r : 0;
   return DIC_OK;
 }
 

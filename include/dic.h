@@ -86,6 +86,7 @@ typedef struct dic_frame_report
   int32_t frame_fallback_used;
   int32_t fftcc_used;
   double iteration_mean;
+  int64_t repaired_recovered;   /* repair candidates replaced and no longer bad (:3004-3020) */
 } dic_frame_report;
 
 /* Device timings (CUDA events on the engine stream) of the most recent call of each
@@ -107,6 +108,10 @@ typedef struct dic_stats
 typedef struct dic_engine dic_engine;
 
 const char* dic_version(void);
+/* Name, compute capability and CUDA driver / runtime versions of a device, for run
+ * metadata (the manifest's engine.cuda block, opencorr_cli_cuda_mvp.cpp:2587-2610). */
+int dic_device_info(int32_t device, char* name, int32_t name_capacity, int32_t* cc_major, int32_t* cc_minor,
+                    int32_t* driver_version, int32_t* runtime_version);
 int32_t dic_abi_version(void);
 
 /* ICGN2D1CudaMvp::ICGN2D1CudaMvp / FFTCC2DCuda::FFTCC2DCuda (src/icgn2d1_cuda_mvp.h:98-100,

@@ -1,0 +1,142 @@
+"""The command line end to end on the GPU: multi-frame raw runs (records + manifest as the
+pipeline reads them), CSV output, single-frame mode, 12-bit input handling, --line and the
+output filters.  Records are checked bit for bit against the engine's own sequence API on
+the same inputs, and the solution against the synthetic truth."""
+import numpy as np
+import pytest
+
+import cli_files as F
+import dic_checks as C
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def cli(dic):
+    from fasticgn_gb300 import _build
+    return _build.build_cli()
+
+
+@pytest.fixture(scope="module")
+def stream12(tmp_path_factory):
+    """Six 12-bit frames of the sine/strain stream, written as 16-bit PGM (maxval 4095)."""
+    from fasticgn_gb300 import speckle
+    d = tmp_path_factory.mktemp("stream12")
+    ref, frames = speckle.stream_frames(width=256, height=224, frames=200, which=[0, 1, 2, 3, 4, 5])
+    F.write_pgm(d / "ref.pgm", ref, maxval=4095)
+    lines = []
+    for k, tar, _ in frames:
+        F.write_pgm(d / f"tar {k:03d}.pgm", tar, maxval=4095)      # a space in the path, as camera exports have
+        lines.append(f"{d / f'tar {k:03d}.pgm'} frame_{k:06d}.csv")
+    (d / "tar_list.txt").write_text("\n".join(lines) + "\n")
+    return d, ref, [f[1] for f in frames], [f[2] for f in frames]
+
+
+def engine_sequence(dic, ref, tars, radius, step, lines=None, skip=True, poi_fallback=True):
+    tmpl = dic.grid_queue(ref.shape[1], ref.shape[0], radius, step, lines=lines)
+    e = dic.Engine(radius)
+    e.set_ref(ref)
+    e.sequence_begin(tmpl, skip_fftcc=skip, poi_fallback=poi_fallback)
+    out = []
+    for tar in tars:
+        res = np.zeros_like(tmpl)
+        rep = e.sequence_frame(tar, res)
+        out.append((res, rep))
+    e.close()
+    return out
+
+
+def test_multi_frame_raw_matches_engine(dic, cli, stream12, tmp_path):
+    d, ref, tars, fields = stream12
+    out = tmp_path / "out"
+    rc, status, err = F.run_cli(cli, ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", d / "tar_list.txt",
+                                      "--output-dir", out, "12", "8", "--input-depth", "12", "--output-format", "raw",
+                                      "--gpu-device", "0"])
+    assert rc == 0, err
+    assert status["status"] == "ok" and status["frames_processed"] == 6 and status["mode"] == "multi-frame"
+    assert status["totals"]["skip_fftcc_frames"] == 5
+    assert "Reference input: source_depth=CV_16U" in err and "effective_depth=12" in err
+    m = F.read_manifest(out / "manifest.opencorr-raw.json")
+    assert m["subset_radius"] == 12 and m["grid_space"] == 8 and m["engine"]["oob_policy"] == "geometric-v1"
+    assert m["engine"]["frame_fallback_policy"] == "per-poi-merge-v1" and m["input_image"]["depth"] == "12"
+    assert [f["file"] for f in m["frames"]] == [f"frame_{k:06d}.bin" for k in range(6)]
+    assert [f["output_name"] for f in m["frames"]] == [f"frame_{k:06d}.csv" for k in range(6)]
+    want = engine_sequence(dic, ref, tars, 12, 8)
+    for k, ((entry, rec), (res, rep)) in enumerate(zip(F.iter_frames(out / "manifest.opencorr-raw.json"), want)):
+        assert np.array_equal(rec["x"], res["x"].astype(np.int32)) and np.array_equal(rec["y"], res["y"].astype(np.int32))
+        for name in ("u", "v", "ux", "uy", "vx", "vy", "zncc"):
+            np.testing.assert_array_equal(rec[name], res[name], err_msg=f"frame {k} {name}")
+        assert entry["skip_fftcc_used"] == (k > 0) and entry["fallback_used"] is False
+        assert entry["valid_ratio"] == pytest.approx(float((res["zncc"] >= 0).mean()), abs=1e-6)
+        assert entry["bad_ratio"] == pytest.approx(rep["bad_after_repair"] / len(res), abs=1e-6)
+        assert (entry["baseline_bad_ratio"] is not None) and entry["fallback_threshold"] == pytest.approx(
+            entry["baseline_bad_ratio"] + 0.03, abs=1e-6)
+        # against the synthetic truth: the reference's subpixel gate kind of check
+        u, v = fields[k](rec["x"].astype(np.float64), rec["y"].astype(np.float64))
+        ok = rec["zncc"] >= 0
+        assert ok.mean() > 0.95
+        assert np.median(np.abs(rec["u"][ok] - u[ok])) < 0.02 and np.median(np.abs(rec["v"][ok] - v[ok])) < 0.02
+
+
+def test_csv_and_filters(dic, cli, stream12, tmp_path):
+    d, ref, tars, _ = stream12
+    out = tmp_path / "csv"
+    rc, status, err = F.run_cli(cli, ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", d / "tar_list.txt",
+                                      "--output-dir", out, "12", "8", "--input-depth", "12", "--quiet", "--no-preload",
+                                      "--output-roi", "40,30,200,150", "--output-step", "2"])
+    assert rc == 0, err
+    assert not (out / "manifest.opencorr-raw.json").exists() and "[2/6]" not in err
+    want = engine_sequence(dic, ref, tars, 12, 8)
+    for k, (res, _) in enumerate(want):
+        got = F.read_csv(out / f"frame_{k:06d}.csv")
+        x, y = res["x"].astype(int), res["y"].astype(int)
+        keep = (x >= 40) & (x <= 200) & (y >= 30) & (y <= 150) & (x % 2 == 0) & (y % 2 == 0)
+        sel = res[keep]
+        assert len(got) == keep.sum() > 0
+        np.testing.assert_array_equal(got["x"], sel["x"])
+        for name in ("u", "v", "zncc", "ux", "uy", "vx", "vy"):
+            # six significant digits, as the reference prints them
+            np.testing.assert_allclose(got[name], sel[name], rtol=1e-5, atol=1e-30)
+
+
+def test_line_mode_and_no_skip(dic, cli, stream12, tmp_path):
+    d, ref, tars, _ = stream12
+    out = tmp_path / "line"
+    lines = [100, 40, 100, 3]       # given order, repeats kept, rows inside the margin only
+    rc, _, err = F.run_cli(cli, ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", d / "tar_list.txt",
+                                 "--output-dir", out, "12", "8", "--input-depth", "12", "--line", "100,40",
+                                 "--line", "100,3", "--no-skip-fftcc", "--output-format", "raw"])
+    assert rc == 0, err
+    want = engine_sequence(dic, ref, tars, 12, 8, lines=lines, skip=False)
+    frames = list(F.iter_frames(out / "manifest.opencorr-raw.json"))
+    assert frames[0][1]["y"].tolist()[:2] == [100, 100]
+    for (entry, rec), (res, _) in zip(frames, want):
+        assert entry["skip_fftcc_used"] is False and entry["baseline_bad_ratio"] is None
+        np.testing.assert_array_equal(rec["u"], res["u"])
+        np.testing.assert_array_equal(rec["zncc"], res["zncc"])
+
+
+def test_single_frame_raw_and_left_aligned_12_bit(dic, cli, tmp_path, oracle_mod):
+    from fasticgn_gb300 import speckle
+    O = oracle_mod
+    pr = speckle.pair_affine(seed=9, width=256, height=256)
+    ref16, tar16 = pr.ref.astype(np.uint16) * 16 * 16, pr.tar.astype(np.uint16) * 16 * 16   # 12-bit left-aligned
+    F.write_tiff(tmp_path / "ref.tif", ref16)
+    F.write_tiff(tmp_path / "tar.tif", tar16, big_endian=True)
+    rc, status, err = F.run_cli(cli, [tmp_path / "ref.tif", tmp_path / "tar.tif", "15", "8", tmp_path / "res" / "pair.csv",
+                                      "--input-depth", "12", "--output-format", "raw", "--diagnostics"])
+    assert rc == 0, err
+    assert status["mode"] == "single-frame" and status["output_path"].endswith("pair.bin")
+    assert "effective_align=left" in err and "scale=0.0625" in err
+    m = F.read_manifest(tmp_path / "res" / "pair.bin.manifest.json")
+    entry, rec = next(F.iter_frames(tmp_path / "res" / "pair.bin.manifest.json"))
+    # left-aligned 12-bit read with scale 1/16 is the 8-bit pair times 16: same solution as the
+    # CPU path on the 12-bit values
+    pois = O.grid_pois(256, 256, 15, 8)
+    O.run_pair((ref16 / 16.0).astype(np.float32), (tar16 / 16.0).astype(np.float32), pois, 15)
+    res = C.compare_frame({"u": pois["p"][:, O.P_U], "v": pois["p"][:, O.P_V], "zncc": pois["r"][:, O.R_ZNCC]},
+                          {"u": rec["u"], "v": rec["v"], "zncc": rec["zncc"]})
+    assert res["pass"], res
+    diag = (tmp_path / "res" / "pair.bin.diagnostics" / "pair.csv").read_text().splitlines()
+    assert diag[0] == "x,y,iteration,convergence,status,zncc" and len(diag) == len(rec) + 1
+    assert m["frames"][0]["rows"] == len(rec)
