@@ -90,6 +90,53 @@ def load_uneven():
     return jobs
 
 
+STREAMS = [
+    # 12-bit 2048x2048 sine/strain stream, skip-FFTCC seeding from the previous frame; 16
+    # consecutive frames from the middle of the 200-frame ramp
+    {"name": "stream2048_12bit_r15_step5", "kind": "stream", "seed": 2, "width": 2048, "height": 2048,
+     "frames": 200, "window": list(range(100, 116)), "radius": 15, "step": 5, "learned": False},
+    # 12-bit 1024x1024 crack stream, learned seed + FFTCC fallback on every frame; the last 48
+    # frames of the 5000-frame ramp (crack jump 1.49-1.5 px)
+    {"name": "crack1024_12bit_r12_step4", "kind": "crack", "seed": 5, "width": 1024, "height": 1024,
+     "frames": 5000, "window": list(range(4952, 5000)), "radius": 12, "step": 4, "learned": True},
+]
+
+
+def load_streams():
+    """Reference + window frames of each stream, rendered on all host cores, cached."""
+    from fasticgn_gb300 import speckle
+    out, todo = {}, []
+    for st in STREAMS:
+        cache = Path(os.environ.get("DIC_BENCH_CACHE", "/tmp")) / f"gb300_dic_{st['name']}_v1.npz"
+        if cache.exists():
+            d = np.load(cache)
+            out[st["name"]] = (d["ref"], [d[f"f{k}"] for k in st["window"]])
+        else:
+            todo.append(st)
+    if todo:
+        t = time.time()
+        specs = [(st["kind"], st["seed"], st["width"], st["height"], st["frames"], k)
+                 for st in todo for k in [-1] + st["window"]]
+        import multiprocessing as mp
+        with mp.get_context("spawn").Pool(min(len(specs), os.cpu_count() or 1)) as pool:
+            imgs = pool.map(speckle.stream_image, specs, chunksize=1)
+        log(f"generated streams in {time.time() - t:.1f} s")
+        pos = 0
+        for st in todo:
+            n = 1 + len(st["window"])
+            ref, frames = imgs[pos], imgs[pos + 1:pos + n]
+            pos += n
+            out[st["name"]] = (ref, frames)
+            try:
+                cache = Path(os.environ.get("DIC_BENCH_CACHE", "/tmp")) / f"gb300_dic_{st['name']}_v1.npz"
+                tmp = cache.with_suffix(f".tmp{os.getpid()}.npz")
+                np.savez(tmp, ref=ref, **{f"f{k}": f for k, f in zip(st["window"], frames)})
+                os.replace(tmp, cache)
+            except OSError:
+                pass
+    return out
+
+
 def grid():
     from fasticgn_gb300 import grid_queue
     return grid_queue(WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["radius"], WORKLOAD["step"])
@@ -335,6 +382,89 @@ def measure_uneven(dic, torch, dev, flush, jobs, steps, warmup):
     return out
 
 
+def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
+    """A fixed-reference stream through dic_sequence_*: e2e = host frames staged on the side
+    stream (dic_stage_frame) and results read back every frame, host clock; device =
+    frames already in HBM, back-to-back frames without host syncs, CUDA events.  Frames 0
+    (first / FFTCC) and 1 (graph capture) of the window are untimed warm-up."""
+    from fasticgn_gb300 import _lib, speckle
+    W, H, R = st["width"], st["height"], st["radius"]
+    tmpl = dic.grid_queue(W, H, R, st["step"])
+    n = len(tmpl)
+    learned = st["learned"] and net is not None
+    eng = dic.Engine(R, R, WORKLOAD["conv"], WORKLOAD["max_iter"], device=dev.index)
+    eng.set_autotune(True)
+    if learned:
+        eng.set_proposal(net)
+    eng.set_ref(ref)
+    stream = torch.cuda.ExternalStream(eng.stream, device=dev)
+    # one pinned result buffer per frame, so that reading results back costs no extra copy
+    res_all = torch.empty((len(tars), n * dic.POI_DTYPE.itemsize), dtype=torch.uint8).pin_memory().numpy()
+    tars_h = [torch.from_numpy(t).pin_memory().numpy() for t in tars]
+
+    # ---- e2e: staged host frames, results every frame
+    eng.sequence_begin(tmpl, learned_seed=learned)
+    reports, results = [], []
+    eng.stage_frame(tars_h[0])
+    t0 = None
+    for k in range(len(tars_h)):
+        if k == 2:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+        if k + 1 < len(tars_h):
+            eng.stage_frame(tars_h[k + 1])
+        res = res_all[k].view(dic.POI_DTYPE)
+        rep = eng.sequence_frame(None, res, staged=True, width=W, height=H, dtype=_lib.DIC_U16)
+        if k >= 2:
+            reports.append(rep)
+            results.append(res)
+    e2e_s = time.perf_counter() - t0
+    timed = len(tars_h) - 2
+    # ---- device-resident frames
+    tars_d = [torch.from_numpy(t).to(dev) for t in tars]
+    eng.sequence_begin(tmpl, learned_seed=learned)
+    for k in range(2):
+        eng.sequence_frame(None, device_ptr=tars_d[k].data_ptr(), width=W, height=H, dtype=_lib.DIC_U16)
+    with torch.cuda.stream(stream):
+        flush.random_(0, 255)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+    l0 = eng.stats()["kernel_launches"]
+    for k in range(2, len(tars_d)):
+        eng.sequence_frame(None, device_ptr=tars_d[k].data_ptr(), width=W, height=H, dtype=_lib.DIC_U16,
+                           report=False)
+    with torch.cuda.stream(stream):
+        e.record(stream)
+    e.synchronize()
+    dev_ms = s.elapsed_time(e)
+    launches = (eng.stats()["kernel_launches"] - l0) / timed
+    allr = np.concatenate(results)
+    out = {"workload": st["name"], "image": f"{W}x{H} 12-bit in u16", "subset_radius": R, "poi_step": st["step"],
+           "pois_per_frame": n, "frames_timed": timed, "seed": "learned proposal + FFTCC fallback" if learned
+           else "previous frame (skip-FFTCC), POI-level repair and whole-frame fallback",
+           "window": [st["window"][0], st["window"][-1]], "ramp_frames": st["frames"],
+           "frames_per_s": timed / e2e_s, "pois_per_s": timed * n / e2e_s,
+           "device_frames_per_s": timed / (dev_ms * 1e-3), "device_pois_per_s": timed * n / (dev_ms * 1e-3),
+           "kernel_launches_per_frame": launches,
+           "valid_ratio": float((allr["zncc"] >= 0).mean()),
+           "icgn_iterations_per_poi": float(allr["iteration"][allr["zncc"] >= 0].mean()),
+           "fallback_rate": float(np.mean([r["repaired_candidates"] for r in reports]) / n),
+           "frame_fallbacks": int(sum(r["frame_fallback_used"] for r in reports)),
+           "tuning": eng.tuning(),
+           "timing": "e2e: host clock over the timed frames, staged uploads + result reads included; "
+                     "device: CUDA events on the engine stream, frames resident, no per-frame host sync"}
+    if st["kind"] == "crack":
+        _, _, p0, direction = speckle.crack_setup(st["seed"], W, H)
+        dist = speckle.crack_distance(tmpl["x"], tmpl["y"], (p0, direction))
+        near = dist <= R + 2
+        fb = np.stack([(q["u0"] == np.round(q["u0"])) & (q["v0"] == np.round(q["v0"])) for q in results])
+        out["fallback_rate_near_crack"] = float(fb[:, near].mean())
+        out["fallback_rate_away_from_crack"] = float(fb[:, ~near].mean())
+        out["near_crack"] = f"POIs within r + 2 = {R + 2} px of the crack line ({int(near.sum())} of {n})"
+    eng.close()
+    return out
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -346,7 +476,8 @@ def run_ours(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    uneven_jobs = load_uneven() if not args.skip_batch else None   # host worker pool before any CUDA use
+    uneven_jobs = load_uneven() if not args.skip_batch else None   # host worker pools before any CUDA use
+    streams = load_streams() if not args.skip_streams else None
     torch.cuda.set_device(local)
     _build.build_lib()
 
@@ -467,6 +598,10 @@ def run_ours(args):
     uneven = None
     if uneven_jobs is not None:
         uneven = measure_uneven(dic, torch, dev, flush, uneven_jobs, max(5, min(args.steps, 20)), args.warmup)
+    stream_lines = None
+    if streams is not None:
+        stream_lines = {st["name"]: measure_stream(dic, torch, dev, st, *streams[st["name"]], net, flush)
+                        for st in STREAMS}
 
     if rank != 0:
         if world > 1:
@@ -520,6 +655,7 @@ def run_ours(args):
         "learned_vs_fftcc": (seed_modes["learned"]["value"] / seed_modes["fftcc"]["value"]) if "learned" in seed_modes else None,
         "parity_vs_cpu": seed_modes[headline]["parity_vs_cpu"],
         "uneven_batch": uneven,
+        "streams": stream_lines,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -533,6 +669,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--skip-batch", action="store_true", help="do not measure the uneven batch")
+    ap.add_argument("--skip-streams", action="store_true", help="do not measure the frame streams")
     ap.add_argument("--seed", choices=["fftcc", "learned"], default="fftcc",
                     help="seed method of the headline value (both are measured when the proposal weights exist)")
     args = ap.parse_args()

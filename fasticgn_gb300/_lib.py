@@ -21,6 +21,7 @@ DIC_ERR_MEMORY = -5
 
 DIC_U8, DIC_U16, DIC_F32 = 1, 2, 3
 DIC_RUN_FFTCC, DIC_RUN_ICGN, DIC_RUN_PREPARE, DIC_RUN_LEARNED = 1, 2, 4, 8
+DIC_PIXELS_STAGED = 2
 DIC_PLANE_REF, DIC_PLANE_REF_PACK, DIC_PLANE_TAR, DIC_PLANE_TAR_COEF = 1, 2, 3, 4
 
 # struct dic_poi (include/dic.h), 56 bytes
@@ -41,7 +42,8 @@ class DicConfig(ctypes.Structure):
 
 class DicFramePolicy(ctypes.Structure):
     _fields_ = [("skip_fftcc", ctypes.c_int32), ("poi_fallback", ctypes.c_int32),
-                ("zncc_threshold", ctypes.c_float), ("frame_fallback_ratio", ctypes.c_float)]
+                ("zncc_threshold", ctypes.c_float), ("frame_fallback_ratio", ctypes.c_float),
+                ("learned_seed", ctypes.c_int32)]
 
 
 class DicFrameReport(ctypes.Structure):
@@ -104,6 +106,7 @@ SIGNATURES = {
                                          ctypes.POINTER(DicFrameReport)]),
     "dic_run_device": (ctypes.c_int, [_vp, _vp, _i64, _i32]),
     "dic_sequence_begin": (ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(DicFramePolicy)]),
+    "dic_stage_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32]),
     "dic_sequence_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32, _i32, _vp,
                                           ctypes.POINTER(DicFrameReport)]),
     "dic_set_graphs": (ctypes.c_int, [_vp, _i32]),

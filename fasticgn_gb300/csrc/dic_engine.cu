@@ -496,12 +496,12 @@ struct dic_engine
   struct IcgnShape
   {
     int warps = 4;
-    int ctas_per_sm = 7;
+    int ctas_per_sm = 7;     // persistent launches: resident CTAs per SM (0: one CTA per kWarps POIs)
     float ms = 0.f;
   };
   static constexpr int64_t kTuneMinPois = 2048;
   bool autotune = false;
-  IcgnShape shape[2][2];
+  IcgnShape shape[2][2] = {{{4, 0, 0.f}, {4, 0, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}}};
   bool tuned[2][2] = {};
   DevBuf<dic_poi> tune_q;
   cudaEvent_t tune_ev[2] = {};
@@ -522,6 +522,20 @@ struct dic_engine
       DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn<C, W>, W * 32, 0));
     return std::max(b, 1);
   }
+  template <bool C, int W>
+  static int max_ctas_single()
+  {
+    int b = 0;
+    DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_persistent<C, W>, W * 32, 0));
+    return std::max(b, 1);
+  }
+  static int occupancy_single(bool column, int warps)
+  {
+    if (column) return warps == 2 ? max_ctas_single<true, 2>() : warps == 8 ? max_ctas_single<true, 8>()
+                                                                             : max_ctas_single<true, 4>();
+    return warps == 2 ? max_ctas_single<false, 2>() : warps == 8 ? max_ctas_single<false, 8>()
+                                                                  : max_ctas_single<false, 4>();
+  }
   static int occupancy(bool persistent, bool column, int warps)
   {
     if (column) return warps == 2 ? max_ctas<true, 2>(persistent) : warps == 8 ? max_ctas<true, 8>(persistent)
@@ -529,8 +543,34 @@ struct dic_engine
     return warps == 2 ? max_ctas<false, 2>(persistent) : warps == 8 ? max_ctas<false, 8>(persistent)
                                                                      : max_ctas<false, 4>(persistent);
   }
-  void launch_icgn(const IcgnParams& p, bool column, int warps)
+  DevBuf<unsigned long long> icgn_next;   // work counter of the persistent single-queue launch
+
+  void launch_icgn(const IcgnParams& p, bool column, const IcgnShape& sh)
   {
+    const int warps = sh.warps;
+    if (sh.ctas_per_sm > 0)
+    {
+      icgn_next.ensure(1);
+      DIC_CUDA(cudaMemsetAsync(icgn_next.ptr, 0, sizeof(unsigned long long), stream));
+      int sms = 0;
+      DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+      const unsigned grid = (unsigned)std::min<int64_t>((int64_t)sms * sh.ctas_per_sm, (p.n + warps - 1) / warps);
+#define DIC_ICGN_PERSIST(C, W) k_icgn_persistent<C, W><<<grid, W * 32, 0, stream>>>(p, icgn_next.ptr)
+      if (column)
+      {
+        if (warps == 2) DIC_ICGN_PERSIST(true, 2);
+        else if (warps == 8) DIC_ICGN_PERSIST(true, 8);
+        else DIC_ICGN_PERSIST(true, 4);
+      }
+      else
+      {
+        if (warps == 2) DIC_ICGN_PERSIST(false, 2);
+        else if (warps == 8) DIC_ICGN_PERSIST(false, 8);
+        else DIC_ICGN_PERSIST(false, 4);
+      }
+#undef DIC_ICGN_PERSIST
+      return;
+    }
     const unsigned blocks = (unsigned)((p.n + warps - 1) / warps);
 #define DIC_ICGN_LAUNCH(C, W) k_icgn<C, W><<<blocks, W * 32, 0, stream>>>(p)
     if (column)
@@ -604,15 +644,17 @@ struct dic_engine
     IcgnShape best;
     best.ms = INFINITY;
     for (int warps : {2, 4, 8})
-    {
-      float t = INFINITY;
-      for (int rep = 0; rep < 2; ++rep)
+      for (int persistent = 0; persistent < 2; ++persistent)
       {
-        DIC_CUDA(cudaMemcpyAsync(tune_q.ptr, p0.pois, sizeof(dic_poi) * p0.n, cudaMemcpyDeviceToDevice, stream));
-        t = std::min(t, time_once([&] { launch_icgn(p, column, warps); }));
+        const IcgnShape sh{warps, persistent ? occupancy_single(column, warps) : 0, 0.f};
+        float t = INFINITY;
+        for (int rep = 0; rep < 2; ++rep)
+        {
+          DIC_CUDA(cudaMemcpyAsync(tune_q.ptr, p0.pois, sizeof(dic_poi) * p0.n, cudaMemcpyDeviceToDevice, stream));
+          t = std::min(t, time_once([&] { launch_icgn(p, column, sh); }));
+        }
+        if (t < best.ms) best = IcgnShape{sh.warps, sh.ctas_per_sm, t};
       }
-      if (t < best.ms) best = IcgnShape{warps, 0, t};
-    }
     shape[0][column] = best;
     tuned[0][column] = true;
   }
@@ -707,7 +749,7 @@ struct dic_engine
     const bool column = 2 * p.rx + 1 <= 32;
     if (autotune && !tuned[0][column] && n >= kTuneMinPois && !capturing()) tune_icgn(p, column);
     mark(kPhIcgn, 0);
-    launch_icgn(p, column, shape[0][column].warps);
+    launch_icgn(p, column, shape[0][column]);
     check_launch("k_icgn");
     mark(kPhIcgn, 1);
     icgn_pois = n;
@@ -798,9 +840,11 @@ struct dic_engine
   static constexpr float kLearnedAccept = 0.9f;  // ZNCC the proposal's result must reach
   static constexpr int64_t kProposalBatch = 32768;
 
-  // Queue `queue` holds the template (x, y); layout is this queue's.  Proposal seeds, IC-GN
-  // capped at kLearnedMaxIter, then FFTCC + IC-GN (full budget) for the POIs that fail.
-  void enqueue_learned(int64_t n)
+  // Proposal seeds, IC-GN capped at kLearnedMaxIter, then FFTCC + IC-GN (full budget) for
+  // the POIs that fail; the layout is the template's.  from_template: the sequence form
+  // (tmpl holds the template, copied into queue); otherwise `queue` holds it (pair form).
+  // `bad_thr` counts the final bad POIs for the frame report.
+  void enqueue_learned(int64_t n, bool from_template = false, float bad_thr = 0.8f)
   {
     if (!proposal) throw DicError{DIC_ERR_STATE, "no proposal network attached (dic_set_proposal)"};
     ensure_ref();
@@ -809,7 +853,10 @@ struct dic_engine
     const unsigned tb = 256, nb = (unsigned)((n + tb - 1) / tb);
     DIC_CUDA(cudaMemsetAsync(fcount.ptr, 0, sizeof(FrameCounters), stream));
     DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
-    DIC_CUDA(cudaMemcpyAsync(tmpl.ptr, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, stream));
+    if (from_template)
+      DIC_CUDA(cudaMemcpyAsync(queue.ptr, tmpl.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, stream));
+    else
+      DIC_CUDA(cudaMemcpyAsync(tmpl.ptr, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, stream));
     mark(kPhProposal, 0);
     {
       // fused inference: one persistent CTA per SM, kT POIs per tile, seeds into the queue
@@ -833,8 +880,99 @@ struct dic_engine
     check_launch("k_gather_candidates");
     run_fftcc(fq.ptr, n, cn, pr);
     run_icgn(fq.ptr, n, cand.ptr, cn, pr, false);
-    k_merge_fallback<<<nb, tb, 0, stream>>>(queue.ptr, fq.ptr, cand.ptr, fcount.ptr, n);
+    k_merge_fallback<<<nb, tb, 0, stream>>>(queue.ptr, fq.ptr, cand.ptr, fcount.ptr, bad_thr, n);
     check_launch("k_merge_fallback");
+    k_count_bad<<<nb, tb, 0, stream>>>(queue.ptr, bad_thr, &fcount.ptr->bad_after, n);
+    check_launch("k_count_bad");
+  }
+
+  // ---------------------------------------------------------------- staged uploads
+  cudaStream_t up_stream = nullptr;
+  unsigned char* stage_host[2] = {nullptr, nullptr};
+  size_t stage_host_cap[2] = {0, 0};
+  DevBuf<unsigned char> stage_dev[2];
+  cudaEvent_t stage_uploaded[2] = {nullptr, nullptr}, stage_consumed[2] = {nullptr, nullptr};
+  int stage_w[2] = {0, 0}, stage_h[2] = {0, 0}, stage_dtype[2] = {0, 0};
+  bool stage_full[2] = {false, false};
+  int stage_next = 0, stage_take = 0;
+
+  void stage_frame(const void* px, int width, int height, int64_t stride, int dtype)
+  {
+    const int es = dtype_size(dtype);
+    if (!px || es == 0 || width < 5 || height < 5 || stride < (int64_t)width * es)
+      throw DicError{DIC_ERR_ARGUMENT, "stage_frame: null pixels, unknown dtype, bad size or stride"};
+    const int s = stage_next;
+    if (stage_full[s]) throw DicError{DIC_ERR_STATE, "stage_frame: two frames are already staged"};
+    if (!up_stream)
+    {
+      DIC_CUDA(cudaStreamCreateWithFlags(&up_stream, cudaStreamNonBlocking));
+      for (int k = 0; k < 2; ++k)
+      {
+        DIC_CUDA(cudaEventCreateWithFlags(&stage_uploaded[k], cudaEventDisableTiming));
+        DIC_CUDA(cudaEventCreateWithFlags(&stage_consumed[k], cudaEventDisableTiming));
+      }
+    }
+    const size_t row = (size_t)width * es, bytes = row * height;
+    DIC_CUDA(cudaEventSynchronize(stage_uploaded[s]));   // the pinned buffer's last copy is done
+    if (stage_host_cap[s] < bytes)
+    {
+      if (stage_host[s]) DIC_CUDA(cudaFreeHost(stage_host[s]));
+      stage_host[s] = nullptr;
+      stage_host_cap[s] = 0;
+      if (cudaMallocHost((void**)&stage_host[s], bytes) != cudaSuccess)
+      {
+        stage_host[s] = nullptr;
+        throw DicError{DIC_ERR_MEMORY, "stage_frame: pinned allocation failed"};
+      }
+      stage_host_cap[s] = bytes;
+    }
+    const unsigned char* src = static_cast<const unsigned char*>(px);
+    if ((size_t)stride == row) std::memcpy(stage_host[s], src, bytes);
+    else
+      for (int y = 0; y < height; ++y) std::memcpy(stage_host[s] + (size_t)y * row, src + (size_t)y * stride, row);
+    if (stage_dev[s].cap < bytes)
+    {
+      DIC_CUDA(cudaEventSynchronize(stage_consumed[s]));
+      stage_dev[s].ensure(bytes);
+    }
+    DIC_CUDA(cudaStreamWaitEvent(up_stream, stage_consumed[s], 0));   // the device copy was taken
+    DIC_CUDA(cudaMemcpyAsync(stage_dev[s].ptr, stage_host[s], bytes, cudaMemcpyHostToDevice, up_stream));
+    DIC_CUDA(cudaEventRecord(stage_uploaded[s], up_stream));
+    stage_w[s] = width;
+    stage_h[s] = height;
+    stage_dtype[s] = dtype;
+    stage_full[s] = true;
+    stage_next ^= 1;
+  }
+
+  // The oldest staged frame becomes the target (engine stream waits for its copy only).
+  void take_staged(int width, int height, int dtype)
+  {
+    const int s = stage_take;
+    if (!stage_full[s]) throw DicError{DIC_ERR_STATE, "no staged frame (dic_stage_frame)"};
+    if (stage_w[s] != width || stage_h[s] != height || stage_dtype[s] != dtype)
+      throw DicError{DIC_ERR_ARGUMENT, "the staged frame's size or type differs from the call's"};
+    DIC_CUDA(cudaStreamWaitEvent(stream, stage_uploaded[s], 0));
+    set_image(false, stage_dev[s].ptr, width, height, (int64_t)width * dtype_size(dtype), dtype, true);
+    DIC_CUDA(cudaEventRecord(stage_consumed[s], stream));
+    stage_full[s] = false;
+    stage_take ^= 1;
+  }
+
+  void release_staging()
+  {
+    if (up_stream) cudaStreamSynchronize(up_stream);
+    for (int k = 0; k < 2; ++k)
+    {
+      if (stage_host[k]) cudaFreeHost(stage_host[k]);
+      stage_host[k] = nullptr;
+      stage_dev[k].release();
+      if (stage_uploaded[k]) cudaEventDestroy(stage_uploaded[k]);
+      if (stage_consumed[k]) cudaEventDestroy(stage_consumed[k]);
+      stage_uploaded[k] = stage_consumed[k] = nullptr;
+    }
+    if (up_stream) cudaStreamDestroy(up_stream);
+    up_stream = nullptr;
   }
 
   // ---------------------------------------------------------------- uneven batches
@@ -1056,12 +1194,30 @@ struct dic_engine
     }
   }
 
-  void fill_report(dic_frame_report* r, int64_t n, bool use_skip, const dic_poi* host_results)
+  void fill_report(dic_frame_report* r, int64_t n, bool use_skip, const dic_poi* host_results, bool learned = false)
   {
     if (!r) return;
     FrameCounters c{};
     DIC_CUDA(cudaMemcpyAsync(&c, fcount.ptr, sizeof(c), cudaMemcpyDeviceToHost, stream));
     DIC_CUDA(cudaStreamSynchronize(stream));
+    if (learned)
+    {
+      // learned seed: "before repair" = POIs the proposal's IC-GN did not bring to ZNCC 0.9
+      r->pois = n;
+      r->bad_before_repair = (int64_t)c.candidates;
+      r->bad_after_repair = (int64_t)c.bad_after;
+      r->repaired_candidates = (int64_t)c.candidates;
+      r->repaired_recovered = (int64_t)c.recovered;
+      r->frame_fallback_used = 0;
+      r->fftcc_used = c.candidates > 0 ? 1 : 0;
+      double it = 0.0;
+      int64_t valid = 0;
+      if (host_results)
+        for (int64_t i = 0; i < n; ++i)
+          if (host_results[i].zncc >= 0.f) { it += host_results[i].iteration; ++valid; }
+      r->iteration_mean = valid ? it / (double)valid : 0.0;
+      return;
+    }
     r->pois = n;
     r->bad_before_repair = (int64_t)c.bad;
     r->bad_after_repair = (int64_t)c.bad_after;
@@ -1208,6 +1364,9 @@ void dic_engine_destroy(dic_engine* e)
   e->bpoi.release();
   e->bjobs.release();
   e->bnext.release();
+  e->icgn_next.release();
+  e->tune_q.release();
+  e->release_staging();
   for (int p = 0; p < kPhCount; ++p)
     for (int m = 0; m < dic_engine::kMarks; ++m)
       for (int k = 0; k < 2; ++k)
@@ -1424,19 +1583,39 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
     const int64_t n = e->seq_n;
     if (e->ref_dirty || !e->layout_ready || e->layout_count != n)
       throw DicError{DIC_ERR_STATE, "the reference or the POI layout changed; call dic_sequence_begin again"};
-    const int64_t launches_before = e->launches;
-    e->set_image(false, px, w, h, stride, dtype, pixels_on_device != 0);
     const dic_frame_policy& pol = e->seq_policy;
-    const bool use_skip = pol.skip_fftcc && e->seq_frame > 0;
+    const bool learned = pol.learned_seed != 0;
+    if (learned && !e->proposal) throw DicError{DIC_ERR_STATE, "learned-seed sequence without a proposal network"};
+    if (pixels_on_device == DIC_PIXELS_STAGED)
+      e->take_staged(w, h, dtype);
+    else
+      e->set_image(false, px, w, h, stride, dtype, pixels_on_device != 0);
+    const bool use_skip = !learned && pol.skip_fftcc && e->seq_frame > 0;
+    // the steady-state frame (learned: every frame after the first; skip-FFTCC: every seeded
+    // frame): target table, seeds, IC-GN, repair paths behind device switches, merge, count,
+    // results -> prev
+    auto steady = [&] {
+      e->ensure_tar();
+      if (learned)
+        e->enqueue_learned(n, true, pol.zncc_threshold);
+      else
+        e->enqueue_frame(n, true, pol, e->baseline.ptr, 0.f);
+      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+    };
     e->mark(kPhFrame, 0);
-    if (!use_skip)
+    if (!use_skip && !(learned && e->seq_frame > 0))
     {
       e->ensure_tar();
-      e->enqueue_frame(n, false, pol, nullptr, INFINITY);
-      if (pol.skip_fftcc && e->seq_frame == 0)
+      if (learned)
+        e->enqueue_learned(n, true, pol.zncc_threshold);
+      else
       {
-        k_set_baseline<<<1, 32, 0, e->stream>>>(e->fcount.ptr, n, pol.frame_fallback_ratio, e->baseline.ptr);
-        e->check_launch("k_set_baseline");
+        e->enqueue_frame(n, false, pol, nullptr, INFINITY);
+        if (pol.skip_fftcc && e->seq_frame == 0)
+        {
+          k_set_baseline<<<1, 32, 0, e->stream>>>(e->fcount.ptr, n, pol.frame_fallback_ratio, e->baseline.ptr);
+          e->check_launch("k_set_baseline");
+        }
       }
       DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
     }
@@ -1444,8 +1623,7 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
     {
       if (!e->seq_graph)
       {
-        // Capture the steady-state frame once: target table, seed, IC-GN, scan, decide,
-        // both repair paths behind device switches, merge, count, results -> prev.
+        // Capture the steady-state frame once (all buffers exist after the first frame).
         const bool timing = e->timing;
         e->timing = false;
         e->tar_dirty = true;
@@ -1454,9 +1632,7 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
         DIC_CUDA(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
         try
         {
-          e->ensure_tar();
-          e->enqueue_frame(n, true, pol, e->baseline.ptr, 0.f);
-          DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+          steady();
         }
         catch (...)
         {
@@ -1482,19 +1658,14 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
       e->tar_dirty = false;
     }
     else
-    {
-      e->ensure_tar();
-      e->enqueue_frame(n, true, pol, e->baseline.ptr, 0.f);
-      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
-    }
+      steady();
     e->mark(kPhFrame, 1);
     e->iter_pending = true;
     e->icgn_pois = n;
-    (void)launches_before;
     if (results)
       DIC_CUDA(cudaMemcpyAsync(results, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, e->stream));
     if (results || report) DIC_CUDA(cudaStreamSynchronize(e->stream));
-    e->fill_report(report, n, use_skip, results);
+    e->fill_report(report, n, use_skip, results, learned);
     ++e->seq_frame;
   });
 }
@@ -1505,7 +1676,18 @@ int dic_set_proposal(dic_engine* e, dic_cnn* net)
     if (net && net->device != e->cfg.device)
       throw DicError{DIC_ERR_ARGUMENT, "the proposal network lives on another device"};
     e->proposal = net;
+    if (e->seq_graph)
+    {
+      cudaGraphExecDestroy(e->seq_graph);   // it holds the previous network's weight pointers
+      e->seq_graph = nullptr;
+    }
   });
+}
+
+int dic_stage_frame(dic_engine* e, const void* pixels, int32_t width, int32_t height, int64_t row_stride_bytes,
+                    int32_t dtype)
+{
+  return guarded(e, [&] { e->stage_frame(pixels, width, height, row_stride_bytes, dtype); });
 }
 
 int dic_process_pair_learned(dic_engine* e, dic_poi* pois, int64_t n, dic_frame_report* report)
@@ -1528,7 +1710,7 @@ int dic_process_pair_learned(dic_engine* e, dic_poi* pois, int64_t n, dic_frame_
     e->iter_pending = true;
     e->icgn_pois = n;
     e->download_queue(pois, n);
-    e->fill_report(report, n, true, pois);
+    e->fill_report(report, n, true, pois, true);
   });
 }
 
@@ -1570,7 +1752,7 @@ int dic_get_tuning(dic_engine* e, dic_tuning* out)
         dic_launch_shape& d = pers ? out->batch[col] : out->icgn[col];
         const auto& s = e->shape[pers][col];
         d.warps_per_cta = s.warps;
-        d.ctas_per_sm = pers ? s.ctas_per_sm : 0;
+        d.ctas_per_sm = s.ctas_per_sm;
         d.tuned = e->tuned[pers][col] ? 1 : 0;
         d.ms = s.ms;
       }

@@ -728,6 +728,25 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn(I
   icgn_solve<kColumn>(P, i, lane);
 }
 
+// Persistent single-queue form: CTAs stay resident and each warp takes the next POI from an
+// atomic counter (reset to 0 before the launch), so POIs that need many iterations do not
+// hold a whole CTA back.  Same solver and guards as k_icgn.
+template <bool kColumn, int kWarps = 4>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_persistent(IcgnParams P,
+                                                                                          unsigned long long* next)
+{
+  const int lane = threadIdx.x & 31;
+  if (P.enable && *P.enable == 0) return;
+  for (;;)
+  {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(next, 1ull);
+    const int64_t i = (int64_t)__shfl_sync(kFull, t, 0);
+    if (!queue_slot_active(P, i)) return;
+    icgn_solve<kColumn>(P, i, lane);
+  }
+}
+
 // --------------------------------------------------------------------------------------
 // Persistent multi-job IC-GN (uneven batches): every warp takes the next POI of the
 // concatenated queue from an atomic counter, looks up its job (image pair, planes, subset
@@ -1454,14 +1473,17 @@ __global__ void k_enable_candidates(FrameCounters* c)
   c->frame_fallback = 0;
 }
 
-// The fallback result replaces the learned attempt for every candidate.
+// The fallback result replaces the learned attempt for every candidate; `recovered` counts
+// the candidates whose fallback result is not bad (zncc >= thr, or -3).
 __global__ void k_merge_fallback(dic_poi* __restrict__ cur, const dic_poi* __restrict__ fq,
-                                 const int64_t* __restrict__ cand, const FrameCounters* c, int64_t n_max)
+                                 const int64_t* __restrict__ cand, FrameCounters* c, float thr, int64_t n_max)
 {
   if (c->poi_repair == 0) return;
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= c->candidate_count || k >= n_max) return;
-  cur[cand[k]] = fq[k];
+  const dic_poi f = fq[k];
+  if (!is_bad_poi(f.zncc, thr)) atomicAdd(&c->recovered, 1ull);
+  cur[cand[k]] = f;
 }
 
 __global__ void k_count_bad(const dic_poi* __restrict__ cur, float thr, unsigned long long* out, int64_t n)

@@ -167,34 +167,50 @@ class Engine:
         return q, {f: getattr(rep, f) for f, _ in rep._fields_}
 
     def sequence_begin(self, template: np.ndarray, skip_fftcc: bool = True, poi_fallback: bool = True,
-                       zncc_threshold: float = 0.8, frame_fallback_margin: float = 0.03) -> None:
+                       zncc_threshold: float = 0.8, frame_fallback_margin: float = 0.03,
+                       learned_seed: bool = False) -> None:
+        """learned_seed: every frame seeded by the attached proposal network (IC-GN capped at
+        6 iterations, FFTCC + IC-GN below ZNCC 0.9) instead of FFTCC / the previous frame."""
         q = _check_queue(template)
         pol = _lib.DicFramePolicy(int(skip_fftcc), int(poi_fallback), float(zncc_threshold),
-                                  float(frame_fallback_margin))
+                                  float(frame_fallback_margin), int(bool(learned_seed)))
         self._call(self._L.dic_sequence_begin(self._h, q.ctypes.data, len(q), ctypes.byref(pol)))
         self._seq_n = len(q)
 
+    def stage_frame(self, img: np.ndarray) -> None:
+        """Start the upload of the next frame on the engine's upload stream (see
+        sequence_frame(staged=True))."""
+        img, dt = self._image(img)
+        self._call(self._L.dic_stage_frame(self._h, img.ctypes.data, img.shape[1], img.shape[0], img.strides[0], dt))
+
     def sequence_frame(self, tar, results: np.ndarray | None = None, device_ptr: int | None = None,
-                       width: int = 0, height: int = 0, dtype: int = _lib.DIC_U8):
+                       width: int = 0, height: int = 0, dtype: int = _lib.DIC_U8, staged: bool = False,
+                       report: bool = True):
         """Solve one target frame of the sequence; ``tar`` is a host image, or None with
-        ``device_ptr`` (dense rows) for a frame already on the device."""
+        ``device_ptr`` (dense rows) for a frame already on the device, or None with
+        ``staged`` for the oldest frame passed to stage_frame."""
         rep = _lib.DicFrameReport()
+        rep_ptr = ctypes.byref(rep) if report else None   # no report and no results: no host sync
         out_ptr = None
         if results is not None:
             results = _check_queue(results)
             if len(results) != self._seq_n:
                 raise ValueError("results must hold one record per template POI")
             out_ptr = results.ctypes.data
-        if tar is not None:
+        if staged:
+            es = {_lib.DIC_U8: 1, _lib.DIC_U16: 2, _lib.DIC_F32: 4}[dtype]
+            rc = self._L.dic_sequence_frame(self._h, None, width, height, width * es, dtype, _lib.DIC_PIXELS_STAGED,
+                                            out_ptr, rep_ptr)
+        elif tar is not None:
             img, dt = self._image(tar)
             rc = self._L.dic_sequence_frame(self._h, img.ctypes.data, img.shape[1], img.shape[0], img.strides[0], dt,
-                                            0, out_ptr, ctypes.byref(rep))
+                                            0, out_ptr, rep_ptr)
         else:
             es = {_lib.DIC_U8: 1, _lib.DIC_U16: 2, _lib.DIC_F32: 4}[dtype]
             rc = self._L.dic_sequence_frame(self._h, device_ptr, width, height, width * es, dtype, 1, out_ptr,
-                                            ctypes.byref(rep))
+                                            rep_ptr)
         self._call(rc)
-        return {f: getattr(rep, f) for f, _ in rep._fields_}
+        return {f: getattr(rep, f) for f, _ in rep._fields_} if report else None
 
     def set_proposal(self, net) -> None:
         """Attach a ProposalNet (or None) for process_pair_learned / DIC_RUN_LEARNED."""

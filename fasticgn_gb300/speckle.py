@@ -14,8 +14,8 @@ Workload shapes (all sizes in px, values in grey levels):
   bumps scaled to |u|, |v| <= 12 px and local strain <= 2 %, noise 2 DN.
 * ``stream_frame``: 2048x2048 12-bit in u16, affine strain ramp + a sinusoidal
   displacement of wavelength 256 px, noise 8 DN.
-* ``crack_frame``: 1024x1024 12-bit in u16, uniform strain + a displacement jump across a
-  line.
+* ``crack_frames``: 1024x1024 12-bit in u16, uniform strain ramping to 3e-3 + a displacement
+  jump across a random line growing to 1.5 px, noise 6 DN.
 * ``uneven_batch``: pairs with sides log-uniform in 256..4096 u8, each with its own random
   affine field (|u|, |v| <= 8 px, strains <= 1 %), 20 % of the area replaced by flat
   low-texture patches, subset radius drawn from {10, 15, 20, 30} and a POI count
@@ -281,6 +281,68 @@ def stream_frames(seed: int = 2, width: int = 2048, height: int = 2048, frames: 
         tar = quantize(render(width, height, sp, field, background=bg), frng, noise, 4095, np.uint16)
         out.append((k, tar, field))
     return ref, out
+
+
+def crack_setup(seed: int = 5, width: int = 1024, height: int = 1024):
+    """Reference and crack geometry of the high-speed crack stream: a random line through
+    the middle half of the image, 12-bit speckle (values scaled to 4095)."""
+    rng = np.random.default_rng(seed)
+    sp = make_speckles(rng, width, height, pad=24.0, peak=(80.0 * 4095 / 255, 200.0 * 4095 / 255))
+    p0 = (rng.uniform(0.35, 0.65) * width, rng.uniform(0.35, 0.65) * height)
+    ang = rng.uniform(0.0, np.pi)
+    direction = (float(np.cos(ang)), float(np.sin(ang)))
+    return rng, sp, p0, direction
+
+
+def crack_frames(seed: int = 5, width: int = 1024, height: int = 1024, frames: int = 5000, which=None,
+                 noise: float = 6.0, max_strain: float = 3e-3, max_jump: float = 1.5):
+    """Reference + requested frames of the crack stream: uniform strain ramping to
+    ``max_strain`` plus a displacement jump across the crack line growing to ``max_jump`` px
+    (normal to the line), noise ``noise`` DN, 12-bit values in u16.  Returns
+    (ref, [(k, tar, field)], crack) with crack = (p0, direction)."""
+    rng, sp, p0, direction = crack_setup(seed, width, height)
+    bg = 40.0 * 4095 / 255
+    ref = quantize(render(width, height, sp, background=bg), rng, noise, 4095, np.uint16)
+    xc, yc = (width - 1) / 2.0, (height - 1) / 2.0
+    out = []
+    for k in (which if which is not None else range(frames)):
+        frac = (k + 1) / frames
+        field = crack_field(max_strain * frac, max_jump * frac, p0, direction, xc, yc)
+        frng = np.random.default_rng(seed * 100003 + k)
+        tar = quantize(render(width, height, sp, field, background=bg), frng, noise, 4095, np.uint16)
+        out.append((k, tar, field))
+    return ref, out, (p0, direction)
+
+
+def crack_distance(x, y, crack):
+    """Distance of (x, y) from the crack line."""
+    (px, py), (dx, dy) = crack
+    return np.abs((np.asarray(x) - px) * (-dy) + (np.asarray(y) - py) * dx)
+
+
+def stream_image(spec):
+    """One image of a stream, picklable for worker pools: spec = (kind, seed, width, height,
+    frames, k) with kind "stream" (stream_frames) or "crack" (crack_frames) and k = -1 for
+    the reference.  Gives the same pixels as those functions."""
+    kind, seed, width, height, frames, k = spec
+    bg = 40.0 * 4095 / 255
+    if kind == "stream":
+        rng = np.random.default_rng(seed)
+        sp = make_speckles(rng, width, height, pad=24.0, peak=(80.0 * 4095 / 255, 200.0 * 4095 / 255))
+        noise = 8.0
+        xc, yc = (width - 1) / 2.0, (height - 1) / 2.0
+        frac = (k + 1) / frames
+        field = sine_field(0.5 * frac, 256.0, 5e-3 * frac, xc, yc) if k >= 0 else None
+    else:
+        rng, sp, p0, direction = crack_setup(seed, width, height)
+        noise = 6.0
+        xc, yc = (width - 1) / 2.0, (height - 1) / 2.0
+        frac = (k + 1) / frames
+        field = crack_field(3e-3 * frac, 1.5 * frac, p0, direction, xc, yc) if k >= 0 else None
+    if k < 0:
+        return quantize(render(width, height, sp, background=bg), rng, noise, 4095, np.uint16)
+    frng = np.random.default_rng(seed * 100003 + k)
+    return quantize(render(width, height, sp, field, background=bg), frng, noise, 4095, np.uint16)
 
 
 def grid_xy(width: int, height: int, radius: int, step: int):

@@ -75,6 +75,10 @@ typedef struct dic_frame_policy
   int32_t poi_fallback;          /* POI-level FFTCC repair of bad POIs */
   float zncc_threshold;          /* bad = zncc < threshold and != -3 (default 0.8) */
   float frame_fallback_ratio;    /* whole-frame FFTCC+IC-GN when bad ratio exceeds this */
+  int32_t learned_seed;          /* sequences only (no reference counterpart): seed every frame
+                                    with the attached proposal network, IC-GN capped at 6
+                                    iterations, FFTCC + IC-GN for POIs below ZNCC 0.9; the
+                                    skip/repair fields above are then unused */
 } dic_frame_policy;
 
 typedef struct dic_frame_report
@@ -181,6 +185,18 @@ int dic_sequence_frame(dic_engine* engine, const void* pixels, int32_t width, in
                        dic_frame_report* report);
 int dic_set_graphs(dic_engine* engine, int32_t enabled);
 
+/* Frame upload on a side stream (no reference counterpart; the reference decodes the next
+ * frame on a thread and uploads it inside the next compute call).  dic_stage_frame copies a
+ * host frame into one of two pinned buffers and starts its host-to-device copy on the
+ * engine's upload stream, then returns; the copy overlaps whatever the engine stream is
+ * running (typically the previous frame's solve).  dic_sequence_frame with
+ * pixels_on_device = DIC_PIXELS_STAGED (pixels NULL) consumes the oldest staged frame: the
+ * engine stream waits for its copy, nothing else does.  At most two frames are staged at a
+ * time. */
+#define DIC_PIXELS_STAGED 2
+int dic_stage_frame(dic_engine* engine, const void* pixels, int32_t width, int32_t height, int64_t row_stride_bytes,
+                    int32_t dtype);
+
 /* Uneven batch: several image pairs of different sizes, each with its own subset radius
  * (square, 1..32) and POI queue, solved together (FFTCC seed + IC-GN).  No single call of
  * the reference does this; the CLI loops over pairs.  Per pair the prep and FFTCC launches
@@ -215,14 +231,16 @@ int dic_batch_process(dic_engine* engine, const dic_job* jobs, int32_t njobs, in
 /* Launch-shape autotuner (no reference counterpart).  IC-GN runs one warp per POI; when
  * enabled, the first IC-GN launch of each kind (per-queue / persistent batch, column walk
  * for subsets up to 32 columns / flat walk) with at least 2048 POIs times the candidate
- * shapes -- 2, 4 or 8 POIs (warps) per CTA, and for the persistent kernel full or 3/4
+ * shapes -- 2, 4 or 8 POIs (warps) per CTA; for a single queue a grid of one CTA per
+ * POI group or a persistent work-queue launch at full occupancy; for a batch full or 3/4
  * occupancy in CTAs per SM -- on a copy of its seeded queue and keeps the fastest for the
  * engine's lifetime.  Results do not depend on the shape.  Enabling (again) clears what
  * was learnt.  Tuning never runs inside a graph capture. */
 typedef struct dic_launch_shape
 {
   int32_t warps_per_cta;
-  int32_t ctas_per_sm;   /* persistent kernel only (0 otherwise) */
+  int32_t ctas_per_sm;   /* > 0: persistent launch with this many resident CTAs per SM drawing POIs
+                            from an atomic counter; 0: one CTA per warps_per_cta POIs */
   int32_t tuned;
   float ms;              /* best candidate's time, when tuned */
 } dic_launch_shape;

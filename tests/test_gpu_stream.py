@@ -1,0 +1,151 @@
+"""GPU tests of the high-speed stream path: learned-seed sequences (proposal CNN seeds every
+frame, IC-GN capped at 6 iterations, FFTCC + IC-GN fallback below ZNCC 0.9), their CUDA
+graph, frame uploads staged on the side stream, and the crack stream's fallback pattern."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def crack():
+    from fasticgn_gb300 import speckle
+    ref, frames, geom = speckle.crack_frames(seed=5, width=384, height=352, frames=5000,
+                                             which=[4990, 4991, 4992, 4993, 4994])
+    return ref, frames, geom
+
+
+@pytest.fixture(scope="module")
+def net(dic):
+    from fasticgn_gb300 import proposal
+    if not proposal.WEIGHTS.exists():
+        pytest.skip("no trained weights")
+    n = proposal.ProposalNet.load()
+    yield n
+    n.close()
+
+
+def is_fallback(q):
+    """POIs whose final IC-GN started from an FFTCC seed (integer u0, v0) rather than from the
+    proposal."""
+    return (q["u0"] == np.round(q["u0"])) & (q["v0"] == np.round(q["v0"]))
+
+
+def learned_sequence(dic, net, ref, tars, radius, step, graphs=True, staged=False):
+    tmpl = dic.grid_queue(ref.shape[1], ref.shape[0], radius, step)
+    e = dic.Engine(radius)
+    e.set_graphs(graphs)
+    e.set_proposal(net)
+    e.set_ref(ref)
+    e.sequence_begin(tmpl, learned_seed=True)
+    out = []
+    if staged:
+        e.stage_frame(tars[0])
+    for k, tar in enumerate(tars):
+        res = np.zeros_like(tmpl)
+        if staged:
+            if k + 1 < len(tars):
+                e.stage_frame(tars[k + 1])     # uploads while frame k is solved
+            rep = e.sequence_frame(None, res, staged=True, width=tar.shape[1], height=tar.shape[0],
+                                   dtype=dic._lib.DIC_U16)
+        else:
+            rep = e.sequence_frame(tar, res)
+        out.append((res, rep))
+    e.close()
+    return out
+
+
+def test_learned_sequence_equals_learned_pairs(dic, net, crack):
+    """Each frame of a learned-seed sequence (graph-replayed after the first) equals the
+    single-pair learned solve of the same pair, bit for bit."""
+    ref, frames, _ = crack
+    tars = [f[1] for f in frames[:3]]
+    seq = learned_sequence(dic, net, ref, tars, 12, 6)
+    for k, (tar, (res, rep)) in enumerate(zip(tars, seq)):
+        e = dic.Engine(12)
+        e.set_proposal(net)
+        e.set_ref(ref)
+        e.set_tar(tar)
+        q = dic.grid_queue(ref.shape[1], ref.shape[0], 12, 6)
+        q, prep = e.process_pair_learned(q)
+        e.close()
+        np.testing.assert_array_equal(res.view(np.uint8), q.view(np.uint8), err_msg=f"frame {k}")
+        assert rep["repaired_candidates"] == prep["repaired_candidates"]
+        assert rep["repaired_candidates"] == int(is_fallback(res).sum())
+        assert rep["bad_after_repair"] == int(((res["zncc"] != -3) & ~(res["zncc"] >= 0.8)).sum())
+    eager = learned_sequence(dic, net, ref, tars, 12, 6, graphs=False)
+    for (a, _), (b, _) in zip(seq, eager):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def test_staged_uploads_equal_direct(dic, net, crack):
+    ref, frames, _ = crack
+    tars = [f[1] for f in frames]
+    direct = learned_sequence(dic, net, ref, tars, 12, 6)
+    staged = learned_sequence(dic, net, ref, tars, 12, 6, staged=True)
+    for (a, ra), (b, rb) in zip(direct, staged):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+        assert ra == rb
+    # the skip-FFTCC sequence through staged uploads, too
+    tmpl = dic.grid_queue(ref.shape[1], ref.shape[0], 12, 6)
+    outs = []
+    for st in (False, True):
+        e = dic.Engine(12)
+        e.set_ref(ref)
+        e.sequence_begin(tmpl)
+        got = []
+        if st:
+            e.stage_frame(tars[0])
+        for k, tar in enumerate(tars):
+            res = np.zeros_like(tmpl)
+            if st:
+                if k + 1 < len(tars):
+                    e.stage_frame(tars[k + 1])
+                e.sequence_frame(None, res, staged=True, width=tar.shape[1], height=tar.shape[0],
+                                 dtype=dic._lib.DIC_U16)
+            else:
+                e.sequence_frame(tar, res)
+            got.append(res)
+        outs.append(got)
+        e.close()
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def test_staging_errors(dic, crack):
+    ref, frames, _ = crack
+    e = dic.Engine(12)
+    e.set_ref(ref)
+    e.sequence_begin(dic.grid_queue(ref.shape[1], ref.shape[0], 12, 6))
+    with pytest.raises(RuntimeError):      # nothing staged
+        e.sequence_frame(None, None, staged=True, width=ref.shape[1], height=ref.shape[0], dtype=dic._lib.DIC_U16)
+    e.stage_frame(frames[0][1])
+    e.stage_frame(frames[1][1])
+    with pytest.raises(RuntimeError):      # a third frame while two are staged
+        e.stage_frame(frames[2][1])
+    with pytest.raises(ValueError):        # size differs from the staged frame's
+        e.sequence_frame(None, None, staged=True, width=ref.shape[1], height=ref.shape[0], dtype=dic._lib.DIC_U8)
+    e.close()
+
+
+def test_crack_stream_fallback_is_at_the_crack(dic, net, crack):
+    """On the crack stream the proposal's misses (FFTCC fallbacks) and the invalid POIs sit at
+    the crack; away from it the learned-seed results match the truth."""
+    from fasticgn_gb300 import speckle
+    ref, frames, geom = crack
+    tars = [f[1] for f in frames]
+    r = 12
+    seq = learned_sequence(dic, net, ref, tars, r, 4)
+    for (res, rep), (_, _, field) in zip(seq, frames):
+        dist = speckle.crack_distance(res["x"], res["y"], geom)
+        near = dist <= r + 2
+        fb = is_fallback(res)
+        assert rep["repaired_candidates"] < 0.2 * len(res), rep
+        # fallback rate near the crack well above the rate away from it (measured on these
+        # frames: about 10 % against 2.6 %)
+        assert fb[near].mean() > 2 * max(fb[~near].mean(), 1e-3), (fb[near].mean(), fb[~near].mean())
+        far = (dist > r + 3) & (res["zncc"] >= 0)
+        assert far.mean() > 0.7
+        u, v = field(res["x"].astype(np.float64), res["y"].astype(np.float64))
+        assert np.median(np.abs(res["u"][far] - u[far])) < 0.02
+        assert np.median(np.abs(res["v"][far] - v[far])) < 0.02
