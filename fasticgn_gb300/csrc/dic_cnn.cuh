@@ -491,11 +491,14 @@ __global__ void k_write_seeds(const float* __restrict__ out, dic_poi* __restrict
 // grid (tiles strided over CTAs).  Same arithmetic as the GEMM path (BF16 operands, FP32
 // accumulation, BF16 ReLU outputs), so both give the same seeds up to accumulation order.
 //
-// Shared memory (bytes): W1 [32][32] 2 KB; W2..W4 [32][296] 57 KB (row padded to 37
+// Shared memory (bytes): W1 [32][40] 2.5 KB (rows padded to 80 B: the B-fragment loads of
+// 8 rows x 4 lanes hit 32 distinct banks); W2..W4 [32][296] 57 KB (row padded to 37
 // 16-byte chunks: conflict-free ldmatrix); x0p [4][33][33][2] 17 KB (zero border);
-// a1p [4][18][18][40] 104 KB and a2p [4][10][10][40] 32 KB (zero border, pixel stride 80 B
-// so the stride-2 im2col rows of an ldmatrix spread over the banks); a3p, a4, a5 overlay
-// x0p once conv1 has consumed it.
+// a1p [4][18][18][40] 104 KB and a2p [4][10][10][40] 32 KB (zero border, pixel stride 80 B).
+// The padded activation rows are stored parity-split: padded column X sits at
+// (X & 1) * (width / 2) + (X >> 1), so the stride-2 im2col rows of an ldmatrix (8 output
+// pixels, input columns 2 ox + kx) are 8 consecutive 80 B pixels, which cover all 32 banks.
+// a3p, a4, a5 overlay x0p once conv1 has consumed it.
 // --------------------------------------------------------------------------------------
 constexpr int kT = 4;
 constexpr int kFusedThreads = 512;
@@ -504,7 +507,8 @@ constexpr int kWRow = 296;                      // padded row of W2..W4 (288 + 8
 constexpr int kSmX0 = kT * 33 * 33 * 2 * 2;     // 17424
 constexpr int kSmA1 = kT * 18 * 18 * kPix * 2;  // 103680
 constexpr int kSmA2 = kT * 10 * 10 * kPix * 2;  // 32000
-constexpr int kSmW1 = 32 * 32 * 2;              // 2048
+constexpr int kW1Row = 40;                      // padded row of W1 (32 + 8)
+constexpr int kSmW1 = 32 * kW1Row * 2;          // 2560
 constexpr int kSmW = 3 * 32 * kWRow * 2;        // 56832
 constexpr int kSmOut = kT * 8 * 4;              // 128
 constexpr int kSmTotal = kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmOut;
@@ -512,6 +516,13 @@ static_assert(kT * 6 * 6 * kPix * 2 + kT * 128 * 2 + kT * 256 * 2 <= kSmX0, "ove
 static_assert(kSmTotal <= 227 * 1024, "shared memory");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// storage column of padded column X in a parity-split row of WIDTH (even) padded columns
+template <int WIDTH>
+__device__ __forceinline__ int pcol(int X)
+{
+  return (X & 1) * (WIDTH / 2) + (X >> 1);
+}
 
 __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], uint32_t addr)
 {
@@ -537,7 +548,8 @@ __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloa
     const int arow = mt * 16 + (q & 1) * 8 + (lane & 7);
     const int rr = arow < M ? arow : M - 1;
     const int p = rr / (SO * SO), oy = (rr % (SO * SO)) / SO, ox = rr % SO;
-    const __nv_bfloat16* abase = in + ((p * SIP + 2 * oy) * SIP + 2 * ox) * kPix + (q >> 1) * 8;
+    // input pixel (2 oy + ky, 2 ox + kx): storage column ox + (kx >> 1) + (kx & 1) * SIP / 2
+    const __nv_bfloat16* abase = in + ((p * SIP + 2 * oy) * SIP + ox) * kPix + (q >> 1) * 8;
     // ldmatrix B addresses: lane -> n row (q >> 1) * 8 + (lane & 7), k offset (q & 1) * 8
     const __nv_bfloat16* bbase = W + (nh * 16 + (q >> 1) * 8 + (lane & 7)) * kWRow + (q & 1) * 8;
     float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
@@ -549,7 +561,7 @@ __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloa
       for (int half = 0; half < 2; ++half)
       {
         uint32_t a[4], b[4];
-        ldsm_x4(a, smem_u32(abase + (ky * SIP + kx) * kPix + half * 16));
+        ldsm_x4(a, smem_u32(abase + (ky * SIP + (kx >> 1) + (kx & 1) * (SIP / 2)) * kPix + half * 16));
         ldsm_x4(b, smem_u32(bbase + kk * 32 + half * 16));
         const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
         mma_bf16_16816(acc[0], a, b0);
@@ -567,7 +579,7 @@ __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloa
         const int row = mt * 16 + g + h2 * 8;
         if (row >= M) continue;
         const int pp = row / (SO * SO), y = (row % (SO * SO)) / SO, x = row % SO;
-        __nv_bfloat16* dst = out + ((pp * SOP + y + 1) * SOP + x + 1) * kPix + co;
+        __nv_bfloat16* dst = out + ((pp * SOP + y + 1) * SOP + pcol<SOP>(x + 1)) * kPix + co;
         *reinterpret_cast<uint32_t*>(dst) =
             pack_bf16(__float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)), __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
       }
@@ -597,7 +609,11 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   using P = ParamLayout;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
   // weights and zero borders, once per CTA
-  for (int i = tid; i < 32 * 32; i += kFusedThreads) W1s[i] = wb[L::c1 + i];
+  for (int i = tid; i < 32 * kW1Row; i += kFusedThreads)
+  {
+    const int r = i / kW1Row, c = i % kW1Row;
+    W1s[i] = c < 32 ? wb[L::c1 + r * 32 + c] : bz();
+  }
   for (int i = tid; i < 3 * 32 * kWRow; i += kFusedThreads)
   {
     const int l = i / (32 * kWRow), r = (i / kWRow) % 32, c = i % kWRow;
@@ -690,7 +706,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
 #pragma unroll
           for (int j = 0; j < 4; ++j)
           {
-            const __nv_bfloat16* wr = W1s + (j * 8 + g) * 32 + ks * 16 + t4 * 2;
+            const __nv_bfloat16* wr = W1s + (j * 8 + g) * kW1Row + ks * 16 + t4 * 2;
             const uint32_t b[2] = {*reinterpret_cast<const uint32_t*>(wr), *reinterpret_cast<const uint32_t*>(wr + 8)};
             mma_bf16_16816(acc[j], a, b);
           }
@@ -705,7 +721,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
           {
             const int row = mt * 16 + g + h2 * 8;
             const int p = row >> 8, y = (row >> 4) & 15, x = row & 15;
-            __nv_bfloat16* dst = a1p + ((p * 18 + y + 1) * 18 + x + 1) * kPix + co;
+            __nv_bfloat16* dst = a1p + ((p * 18 + y + 1) * 18 + pcol<18>(x + 1)) * kPix + co;
             *reinterpret_cast<uint32_t*>(dst) = pack_bf16(__float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)),
                                                           __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
           }
@@ -726,7 +742,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       const int nh = warp, q = lane >> 3;
       const int arow = (q & 1) * 8 + (lane & 7);
       const int p = arow / 4, oy = (arow % 4) / 2, ox = arow % 2;
-      const __nv_bfloat16* abase = a3p + ((p * SIP + 2 * oy) * SIP + 2 * ox) * kPix + (q >> 1) * 8;
+      const __nv_bfloat16* abase = a3p + ((p * SIP + 2 * oy) * SIP + ox) * kPix + (q >> 1) * 8;
       const __nv_bfloat16* bbase = W4s + (nh * 16 + (q >> 1) * 8 + (lane & 7)) * kWRow + (q & 1) * 8;
       float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
@@ -735,7 +751,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         for (int half = 0; half < 2; ++half)
         {
           uint32_t a[4], b[4];
-          ldsm_x4(a, smem_u32(abase + ((kk / 3) * SIP + kk % 3) * kPix + half * 16));
+          ldsm_x4(a, smem_u32(abase + ((kk / 3) * SIP + ((kk % 3) >> 1) + ((kk % 3) & 1) * (SIP / 2)) * kPix +
+                                  half * 16));
           ldsm_x4(b, smem_u32(bbase + kk * 32 + half * 16));
           const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
           mma_bf16_16816(acc[0], a, b0);

@@ -521,6 +521,16 @@ __device__ __forceinline__ float sample_bspline(const float4* __restrict__ coef,
   return fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
 }
 
+// Rows of the column walk unrolled together (their gathers in flight at once), and the
+// warps per SM the IC-GN launch bounds keep resident (which sets the register budget).
+#ifndef DIC_ICGN_ROW_UNROLL
+#define DIC_ICGN_ROW_UNROLL 1
+#endif
+#ifndef DIC_ICGN_RESIDENT_WARPS
+#define DIC_ICGN_RESIDENT_WARPS 28
+#endif
+constexpr int kIcgnRowUnroll = DIC_ICGN_ROW_UNROLL;
+
 // One POI (queue index i) on the calling warp; shared by the per-queue launch (k_icgn) and
 // the persistent multi-job launch (k_icgn_batch).
 template <bool kColumn>
@@ -570,7 +580,7 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
       if (col_active)
       {
         const float ax = fmaf(W[0], flx_col, W[2]), ay = fmaf(W[3], flx_col, W[5]);
-#pragma unroll 1
+#pragma unroll kIcgnRowUnroll
         for (int r = 0; r < 2 * ry + 1; ++r)
         {
           const float fly = (float)(r - ry);
@@ -715,9 +725,9 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
   poi->convergence = conv;
 }
 
-// Launch shape: kWarps POIs per CTA (one warp each); the occupancy hint keeps 28 warps per
-// SM resident for every shape, which leaves 72 registers per thread.
-constexpr int icgn_min_blocks(int warps) { return 28 / warps; }
+// Launch shape: kWarps POIs per CTA (one warp each); the occupancy hint keeps
+// DIC_ICGN_RESIDENT_WARPS (28: 72 registers per thread) warps per SM resident for every shape.
+constexpr int icgn_min_blocks(int warps) { return DIC_ICGN_RESIDENT_WARPS / warps; }
 
 template <bool kColumn, int kWarps = 4>
 __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn(IcgnParams P)
