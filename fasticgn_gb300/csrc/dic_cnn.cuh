@@ -493,7 +493,10 @@ __global__ void k_write_seeds(const float* __restrict__ out, dic_poi* __restrict
 //
 // Shared memory (bytes): W1 [32][40] 2.5 KB (rows padded to 80 B: the B-fragment loads of
 // 8 rows x 4 lanes hit 32 distinct banks); W2..W4 [32][296] 57 KB (row padded to 37
-// 16-byte chunks: conflict-free ldmatrix); x0p [4][33][33][2] 17 KB (zero border);
+// 16-byte chunks: conflict-free ldmatrix); x0p [4][33][48][2] 25 KB (zero border; a
+// 48-pixel row puts tap (ky, kx) at word 16 ky + kx mod 32, and conv1's K slots are
+// grouped so that each A-fragment load reads taps {0, 16, 1, 17} or {2, 18, 1} words
+// apart: 32 distinct banks for the 8 stride-2 rows x 4 taps of a load);
 // a1p [4][18][18][40] 104 KB and a2p [4][10][10][40] 32 KB (zero border, pixel stride 80 B).
 // The padded activation rows are stored parity-split: padded column X sits at
 // (X & 1) * (width / 2) + (X >> 1), so the stride-2 im2col rows of an ldmatrix (8 output
@@ -504,7 +507,8 @@ constexpr int kT = 4;
 constexpr int kFusedThreads = 512;
 constexpr int kPix = 40;                        // padded channel stride (80 B) of a1p/a2p/a3p
 constexpr int kWRow = 296;                      // padded row of W2..W4 (288 + 8)
-constexpr int kSmX0 = kT * 33 * 33 * 2 * 2;     // 17424
+constexpr int kX0Row = 48;                      // x0p row stride in pixels (33 used)
+constexpr int kSmX0 = kT * 33 * kX0Row * 2 * 2; // 25344
 constexpr int kSmA1 = kT * 18 * 18 * kPix * 2;  // 103680
 constexpr int kSmA2 = kT * 10 * 10 * kPix * 2;  // 32000
 constexpr int kW1Row = 40;                      // padded row of W1 (32 + 8)
@@ -512,10 +516,22 @@ constexpr int kSmW1 = 32 * kW1Row * 2;          // 2560
 constexpr int kSmW = 3 * 32 * kWRow * 2;        // 56832
 constexpr int kSmOut = kT * 8 * 4;              // 128
 constexpr int kSmTotal = kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmOut;
-static_assert(kT * 6 * 6 * kPix * 2 + kT * 128 * 2 + kT * 256 * 2 <= kSmX0, "overlay fits");
+static_assert(kT * 6 * 6 * kPix * 2 + kT * (128 + 8) * 2 + kT * (256 + 8) * 2 <= kSmX0, "overlay fits");
+constexpr int kSmScratch = (8 * 16 * 32 + 16 * kT * 8) * 4;   // conv4 + f2 split-K partials in a1p
+static_assert(kSmScratch <= kSmA1, "partials fit in a1p");
 static_assert(kSmTotal <= 227 * 1024, "shared memory");
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// conv1 K slot -> tap (ky * 3 + kx), or -1 for a zero slot; k = 2 slot + channel.  Each
+// group of four slots is read by one A-fragment load (see the x0p row stride).
+__device__ __forceinline__ int conv1_slot_tap(int slot)
+{
+  // {0, 3, 1, 4, 2, 5, 7, -, 6, -, -, -, 8, -, -, -}, four bits per slot, 15 = zero slot
+  constexpr unsigned long long kTaps = 0xFFF8FFF6F7524130ull;
+  const int t = (int)((kTaps >> (4 * slot)) & 15ull);
+  return t == 15 ? -1 : t;
+}
 
 // storage column of padded column X in a parity-split row of WIDTH (even) padded columns
 template <int WIDTH>
@@ -532,60 +548,81 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], uint32_t addr)
 }
 
 // One 3x3 stride-2 conv layer from padded NHWC smem (pixel stride kPix) to the interior of
-// the next padded buffer, K = 288 (ci = 32).  Tasks = (m-tile, pair of n-tiles).
-template <int SIP, int SO, int SOP>
+// the next padded buffer, K = 288 (ci = 32).  Tasks = (MPAIR m-tiles MT/MPAIR apart, pair
+// of n-tiles): with MPAIR = 2 a warp loads each B fragment once for two m-tiles.
+template <int SIP, int SO, int SOP, int MPAIR>
 __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloat16* out, const __nv_bfloat16* W,
-                                             const float* __restrict__ bias, int nt, int warp, int lane)
+                                             const float* __restrict__ bias, int warp, int lane)
 {
   constexpr int M = kT * SO * SO;
   constexpr int MT = (M + 15) / 16;
+  static_assert(MT % MPAIR == 0, "m-tiles split evenly");
+  constexpr int MSTEP = MT / MPAIR;
   const int g = lane >> 2, t4 = lane & 3;
-  for (int task = warp; task < MT * 2; task += kFusedThreads / 32)
+  const int q = lane >> 3;
+  for (int task = warp; task < MSTEP * 2; task += kFusedThreads / 32)
   {
-    const int mt = task >> 1, nh = task & 1;
-    // ldmatrix A addresses: lane -> row (q & 1) * 8 + (lane & 7), k offset (q >> 1) * 8
-    const int q = lane >> 3;
-    const int arow = mt * 16 + (q & 1) * 8 + (lane & 7);
-    const int rr = arow < M ? arow : M - 1;
-    const int p = rr / (SO * SO), oy = (rr % (SO * SO)) / SO, ox = rr % SO;
+    const int mt0 = task >> 1, nh = task & 1;
+    // ldmatrix A addresses: lane -> row (q & 1) * 8 + (lane & 7), k offset (q >> 1) * 8;
     // input pixel (2 oy + ky, 2 ox + kx): storage column ox + (kx >> 1) + (kx & 1) * SIP / 2
-    const __nv_bfloat16* abase = in + ((p * SIP + 2 * oy) * SIP + ox) * kPix + (q >> 1) * 8;
+    const __nv_bfloat16* abase[MPAIR];
+#pragma unroll
+    for (int m = 0; m < MPAIR; ++m)
+    {
+      const int arow = (mt0 + m * MSTEP) * 16 + (q & 1) * 8 + (lane & 7);
+      const int rr = arow < M ? arow : M - 1;
+      const int p = rr / (SO * SO), oy = (rr % (SO * SO)) / SO, ox = rr % SO;
+      abase[m] = in + ((p * SIP + 2 * oy) * SIP + ox) * kPix + (q >> 1) * 8;
+    }
     // ldmatrix B addresses: lane -> n row (q >> 1) * 8 + (lane & 7), k offset (q & 1) * 8
     const __nv_bfloat16* bbase = W + (nh * 16 + (q >> 1) * 8 + (lane & 7)) * kWRow + (q & 1) * 8;
-    float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+    float acc[MPAIR][2][4];
+#pragma unroll
+    for (int m = 0; m < MPAIR; ++m)
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[m][j][e] = 0.f;
 #pragma unroll
     for (int kk = 0; kk < 9; ++kk)
     {
       const int ky = kk / 3, kx = kk % 3;
+      const int aoff = (ky * SIP + (kx >> 1) + (kx & 1) * (SIP / 2)) * kPix;
 #pragma unroll
       for (int half = 0; half < 2; ++half)
       {
-        uint32_t a[4], b[4];
-        ldsm_x4(a, smem_u32(abase + (ky * SIP + (kx >> 1) + (kx & 1) * (SIP / 2)) * kPix + half * 16));
+        uint32_t b[4];
         ldsm_x4(b, smem_u32(bbase + kk * 32 + half * 16));
         const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
-        mma_bf16_16816(acc[0], a, b0);
-        mma_bf16_16816(acc[1], a, b1);
+#pragma unroll
+        for (int m = 0; m < MPAIR; ++m)
+        {
+          uint32_t a[4];
+          ldsm_x4(a, smem_u32(abase[m] + aoff + half * 16));
+          mma_bf16_16816(acc[m][0], a, b0);
+          mma_bf16_16816(acc[m][1], a, b1);
+        }
       }
     }
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
-    {
-      const int co = nh * 16 + j * 8 + t4 * 2;
-      const float bb0 = bias[co], bb1 = bias[co + 1];
+    for (int m = 0; m < MPAIR; ++m)
 #pragma unroll
-      for (int h2 = 0; h2 < 2; ++h2)
+      for (int j = 0; j < 2; ++j)
       {
-        const int row = mt * 16 + g + h2 * 8;
-        if (row >= M) continue;
-        const int pp = row / (SO * SO), y = (row % (SO * SO)) / SO, x = row % SO;
-        __nv_bfloat16* dst = out + ((pp * SOP + y + 1) * SOP + pcol<SOP>(x + 1)) * kPix + co;
-        *reinterpret_cast<uint32_t*>(dst) =
-            pack_bf16(__float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)), __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
+        const int co = nh * 16 + j * 8 + t4 * 2;
+        const float bb0 = bias[co], bb1 = bias[co + 1];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2)
+        {
+          const int row = (mt0 + m * MSTEP) * 16 + g + h2 * 8;
+          if (row >= M) continue;
+          const int pp = row / (SO * SO), y = (row % (SO * SO)) / SO, x = row % SO;
+          __nv_bfloat16* dst = out + ((pp * SOP + y + 1) * SOP + pcol<SOP>(x + 1)) * kPix + co;
+          *reinterpret_cast<uint32_t*>(dst) = pack_bf16(__float2bfloat16(fmaxf(acc[m][j][h2 * 2] + bb0, 0.f)),
+                                                        __float2bfloat16(fmaxf(acc[m][j][h2 * 2 + 1] + bb1, 0.f)));
+        }
       }
-    }
   }
-  (void)nt;
 }
 
 __global__ void __launch_bounds__(kFusedThreads, 1)
@@ -603,8 +640,10 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   __nv_bfloat16* a2p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1);
   float* outs = reinterpret_cast<float*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2);
   __nv_bfloat16* a3p = x0p;                                   // [4][6][6][kPix]
-  __nv_bfloat16* a4 = x0p + kT * 6 * 6 * kPix;                // [4][128]
-  __nv_bfloat16* a5 = a4 + kT * 128;                          // [4][256]
+  // a4 / a5 rows padded by 16 B so that the kT rows of an A fragment hit distinct banks
+  constexpr int kA4Row = 128 + 8, kA5Row = 256 + 8;
+  __nv_bfloat16* a4 = x0p + kT * 6 * 6 * kPix;                // [4][136]
+  __nv_bfloat16* a5 = a4 + kT * kA4Row;                       // [4][264]
   using L = WeightLayout;
   using P = ParamLayout;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
@@ -612,7 +651,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   for (int i = tid; i < 32 * kW1Row; i += kFusedThreads)
   {
     const int r = i / kW1Row, c = i % kW1Row;
-    W1s[i] = c < 32 ? wb[L::c1 + r * 32 + c] : bz();
+    const int tap = c < 32 ? conv1_slot_tap(c >> 1) : -1;
+    W1s[i] = tap >= 0 ? wb[L::c1 + r * 32 + 2 * tap + (c & 1)] : bz();
   }
   for (int i = tid; i < 3 * 32 * kWRow; i += kFusedThreads)
   {
@@ -626,8 +666,10 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
   {
     const int64_t p0 = tile * kT;
-    // a3p/a4/a5 of the previous tile overlay x0p: clear it so its border reads as padding
+    // a3p/a4/a5 of the previous tile overlay x0p, and the split-K partial sums of conv4 and
+    // f2 overlay the start of a1p: clear both so their borders read as padding again
     for (int i = tid; i < kSmX0 / 4; i += kFusedThreads) reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
+    for (int i = tid; i < kSmScratch / 4; i += kFusedThreads) reinterpret_cast<uint32_t*>(a1p)[i] = 0u;
     __syncthreads();
     // ---- input windows: warp 2p + c stages channel c (0 ref, 1 tar) of POI p.  Lane l holds
     // column l of the 31x31 window in registers (coalesced row loads, one pass), the warp
@@ -667,9 +709,9 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         const float inv = q > 0.f ? rsqrtf(q / NPIX) : 1.f;
         if (lane < kWin)
         {
-          __nv_bfloat16* dst = x0p + (p * 33 * 33 + 33 + lane + 1) * 2 + ch;
+          __nv_bfloat16* dst = x0p + ((p * 33 + 1) * kX0Row + lane + 1) * 2 + ch;
 #pragma unroll
-          for (int r = 0; r < kWin; ++r) dst[r * 33 * 2] = __float2bfloat16((v[r] - mean) * inv);
+          for (int r = 0; r < kWin; ++r) dst[r * kX0Row * 2] = __float2bfloat16((v[r] - mean) * inv);
         }
       }
     }
@@ -685,7 +727,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         {
           const int row = mt * 16 + g + h2 * 8;
           const int p = row >> 8, oy = (row >> 4) & 15, ox = row & 15;
-          rbase[h2] = ((p * 33 + 2 * oy) * 33 + 2 * ox) * 2;
+          rbase[h2] = ((p * 33 + 2 * oy) * kX0Row + 2 * ox) * 2;
         }
         float acc[4][4];
 #pragma unroll
@@ -699,9 +741,10 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
 #pragma unroll
           for (int r = 0; r < 4; ++r)
           {
-            const int kk = ks * 8 + (r >> 1) * 4 + t4;   // (ky, kx) index of k = ks*16 + (r>>1)*8 + 2 t4
+            const int tap = conv1_slot_tap(ks * 8 + (r >> 1) * 4 + t4);   // k = ks*16 + (r>>1)*8 + 2 t4
             const int h2 = r & 1;
-            a[r] = kk < 9 ? *reinterpret_cast<const uint32_t*>(x0p + rbase[h2] + ((kk / 3) * 33 + kk % 3) * 2) : 0u;
+            a[r] = tap >= 0 ? *reinterpret_cast<const uint32_t*>(x0p + rbase[h2] + ((tap / 3) * kX0Row + tap % 3) * 2)
+                            : 0u;
           }
 #pragma unroll
           for (int j = 0; j < 4; ++j)
@@ -731,95 +774,120 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     __syncthreads();
     // x0p is free: zero the a3p region (its border must read as zero padding)
     for (int i = tid; i < kT * 6 * 6 * kPix / 2; i += kFusedThreads) reinterpret_cast<uint32_t*>(a3p)[i] = 0u;
-    fused_conv32<18, 8, 10>(a1p, a2p, W2s, params + P::b2, 0, warp, lane);
+    fused_conv32<18, 8, 10, 2>(a1p, a2p, W2s, params + P::b2, warp, lane);
     __syncthreads();
-    fused_conv32<10, 4, 6>(a2p, a3p, W3s, params + P::b3, 0, warp, lane);
+    fused_conv32<10, 4, 6, 1>(a2p, a3p, W3s, params + P::b3, warp, lane);
     __syncthreads();
-    // ---- conv4: 4x4 -> 2x2, M = kT*4 = 16 rows (one m-tile), written unpadded to a4 [p][y][x][c]
-    if (warp < 2)
+    // ---- conv4: 4x4 -> 2x2, M = kT*4 = 16 rows (one m-tile), N = 32, K = 288, split over
+    // all 16 warps: warp = (n-tile pair, one of 8 K slices of the 18 k16 steps).  Partial
+    // sums go to the free a1p region and are added in slice order (deterministic), then
+    // bias + ReLU into a4 [p][y][x][c].
     {
-      constexpr int SIP = 6, SO = 2, M = kT * SO * SO;
-      const int nh = warp, q = lane >> 3;
+      constexpr int SIP = 6;
+      float* part = reinterpret_cast<float*>(a1p);              // [8][16][32]
+      const int nh = warp & 1, slice = warp >> 1, q = lane >> 3;
+      const int s0 = slice * 18 / 8, s1 = (slice + 1) * 18 / 8;
       const int arow = (q & 1) * 8 + (lane & 7);
       const int p = arow / 4, oy = (arow % 4) / 2, ox = arow % 2;
       const __nv_bfloat16* abase = a3p + ((p * SIP + 2 * oy) * SIP + ox) * kPix + (q >> 1) * 8;
       const __nv_bfloat16* bbase = W4s + (nh * 16 + (q >> 1) * 8 + (lane & 7)) * kWRow + (q & 1) * 8;
       float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
-#pragma unroll
-      for (int kk = 0; kk < 9; ++kk)
-#pragma unroll
-        for (int half = 0; half < 2; ++half)
-        {
-          uint32_t a[4], b[4];
-          ldsm_x4(a, smem_u32(abase + ((kk / 3) * SIP + ((kk % 3) >> 1) + ((kk % 3) & 1) * (SIP / 2)) * kPix +
-                                  half * 16));
-          ldsm_x4(b, smem_u32(bbase + kk * 32 + half * 16));
-          const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
-          mma_bf16_16816(acc[0], a, b0);
-          mma_bf16_16816(acc[1], a, b1);
-        }
+      for (int st = s0; st < s1; ++st)
+      {
+        const int kk = st >> 1, half = st & 1;
+        uint32_t a[4], b[4];
+        ldsm_x4(a, smem_u32(abase + ((kk / 3) * SIP + ((kk % 3) >> 1) + ((kk % 3) & 1) * (SIP / 2)) * kPix +
+                                half * 16));
+        ldsm_x4(b, smem_u32(bbase + kk * 32 + half * 16));
+        const uint32_t b0[2] = {b[0], b[1]}, b1[2] = {b[2], b[3]};
+        mma_bf16_16816(acc[0], a, b0);
+        mma_bf16_16816(acc[1], a, b1);
+      }
 #pragma unroll
       for (int j = 0; j < 2; ++j)
       {
         const int co = nh * 16 + j * 8 + t4 * 2;
-        const float bb0 = params[P::b4 + co], bb1 = params[P::b4 + co + 1];
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2)
         {
-          const int row = g + h2 * 8;
-          if (row >= M) continue;
-          *reinterpret_cast<uint32_t*>(a4 + row * 32 + co) = pack_bf16(
-              __float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)), __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
+          float* dst = part + (slice * 16 + g + h2 * 8) * 32 + co;
+          dst[0] = acc[j][h2 * 2];
+          dst[1] = acc[j][h2 * 2 + 1];
         }
+      }
+      __syncthreads();
+      {
+        const int row = tid >> 5, col = tid & 31;    // 512 threads = 16 rows x 32 channels
+        float sum = 0.f;
+#pragma unroll
+        for (int sl = 0; sl < 8; ++sl) sum += part[(sl * 16 + row) * 32 + col];
+        a4[(row >> 2) * kA4Row + (row & 3) * 32 + col] = __float2bfloat16(fmaxf(sum + params[P::b4 + col], 0.f));
       }
     }
     __syncthreads();
-    // ---- f1: [kT x 128] x W5^T -> [kT x 256]; rows >= kT are zero; B fragments from global (L1)
-    for (int nt = warp; nt < kHidden / 8; nt += kFusedThreads / 32)
+    // ---- f1: [kT x 128] x W5^T -> [kT x 256]; rows >= kT are zero; B fragments from global
+    // (L1).  A warp takes n-tiles warp and warp + 16 and loads each A fragment once for both.
     {
-      float acc[4] = {0.f, 0.f, 0.f, 0.f};
+      static_assert(kHidden / 8 == 2 * (kFusedThreads / 32), "two f1 n-tiles per warp");
+      float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
 #pragma unroll
       for (int ks = 0; ks < 8; ++ks)
       {
         const int c = ks * 16 + t4 * 2;
         uint32_t a[4];
-        a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * 128 + c) : 0u;
+        a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * kA4Row + c) : 0u;
         a[1] = 0u;
-        a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * 128 + c + 8) : 0u;
+        a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * kA4Row + c + 8) : 0u;
         a[3] = 0u;
-        const __nv_bfloat16* wr = wb + L::f1 + (nt * 8 + g) * 128 + c;
-        const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)), __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
-        mma_bf16_16816(acc, a, b);
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+        {
+          const int nt = warp + h * (kFusedThreads / 32);
+          const __nv_bfloat16* wr = wb + L::f1 + (nt * 8 + g) * 128 + c;
+          const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)),
+                                 __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
+          mma_bf16_16816(acc[h], a, b);
+        }
       }
-      const int co = nt * 8 + t4 * 2;
-      if (g < kT)
-        *reinterpret_cast<uint32_t*>(a5 + g * 256 + co) =
-            pack_bf16(__float2bfloat16(fmaxf(acc[0] + params[P::b5 + co], 0.f)),
-                      __float2bfloat16(fmaxf(acc[1] + params[P::b5 + co + 1], 0.f)));
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+      {
+        const int co = (warp + h * (kFusedThreads / 32)) * 8 + t4 * 2;
+        if (g < kT)
+          *reinterpret_cast<uint32_t*>(a5 + g * kA5Row + co) =
+              pack_bf16(__float2bfloat16(fmaxf(acc[h][0] + params[P::b5 + co], 0.f)),
+                        __float2bfloat16(fmaxf(acc[h][1] + params[P::b5 + co + 1], 0.f)));
+      }
     }
     __syncthreads();
-    // ---- f2: [kT x 256] x W6^T -> [kT x 6] (n padded to 8), one warp
-    if (warp == 0)
+    // ---- f2: [kT x 256] x W6^T -> [kT x 6] (n padded to 8): warp w takes k16 step w,
+    // partials [16][kT][8] in the free a1p region, summed in step order
     {
+      float* part = reinterpret_cast<float*>(a1p) + 8 * 16 * 32;
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
-#pragma unroll
-      for (int ks = 0; ks < 16; ++ks)
-      {
-        const int c = ks * 16 + t4 * 2;
-        uint32_t a[4];
-        a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * 256 + c) : 0u;
-        a[1] = 0u;
-        a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * 256 + c + 8) : 0u;
-        a[3] = 0u;
-        const __nv_bfloat16* wr = wb + L::f2 + g * 256 + c;
-        const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)), __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
-        mma_bf16_16816(acc, a, b);
-      }
-      const int co = t4 * 2;
+      const int c = warp * 16 + t4 * 2;
+      uint32_t a[4];
+      a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c) : 0u;
+      a[1] = 0u;
+      a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c + 8) : 0u;
+      a[3] = 0u;
+      const __nv_bfloat16* wr = wb + L::f2 + g * 256 + c;
+      const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)),
+                             __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
+      mma_bf16_16816(acc, a, b);
       if (g < kT)
       {
-        outs[g * 8 + co] = acc[0] + (co < kOut ? params[P::b6 + co] : 0.f);
-        outs[g * 8 + co + 1] = acc[1] + (co + 1 < kOut ? params[P::b6 + co + 1] : 0.f);
+        part[(warp * kT + g) * 8 + t4 * 2] = acc[0];
+        part[(warp * kT + g) * 8 + t4 * 2 + 1] = acc[1];
+      }
+      __syncthreads();
+      if (tid < kT * 8)
+      {
+        const int row = tid >> 3, co = tid & 7;
+        float sum = 0.f;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) sum += part[(k * kT + row) * 8 + co];
+        outs[row * 8 + co] = sum + (co < kOut ? params[P::b6 + co] : 0.f);
       }
     }
     __syncthreads();
