@@ -514,10 +514,17 @@ constexpr int kSmA2 = kT * 10 * 10 * kPix * 2;  // 32000
 constexpr int kW1Row = 40;                      // padded row of W1 (32 + 8)
 constexpr int kSmW1 = 32 * kW1Row * 2;          // 2560
 constexpr int kSmW = 3 * 32 * kWRow * 2;        // 56832
-constexpr int kSmOut = kT * 8 * 4;              // 128
-constexpr int kSmTotal = kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmOut;
-static_assert(kT * 6 * 6 * kPix * 2 + kT * (128 + 8) * 2 + kT * (256 + 8) * 2 <= kSmX0, "overlay fits");
-constexpr int kSmScratch = (8 * 16 * 32 + 16 * kT * 8) * 4;   // conv4 + f2 split-K partials in a1p
+// The MLP runs once per kMlpTiles tiles (16 POIs: one full m-tile), so its 64 KB of f1
+// weights stream from L2 once per 16 POIs instead of once per tile.
+constexpr int kMlpTiles = 4;
+constexpr int kMlpRows = kMlpTiles * kT;         // 16
+constexpr int kA4Row = 128 + 8, kA5Row = 256 + 8;   // rows padded by 16 B: distinct banks per fragment
+constexpr int kSmA4 = kMlpRows * kA4Row * 2;     // 4352, persists across the batched tiles
+constexpr int kSmOut = kMlpRows * 8 * 4;         // 512
+constexpr int kSmPoi = kMlpTiles * 8;            // first POI of each batched tile
+constexpr int kSmTotal = kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut + kSmPoi;
+static_assert(kT * 6 * 6 * kPix * 2 + kMlpRows * kA5Row * 2 <= kSmX0, "a3p + a5 overlay x0p");
+constexpr int kSmScratch = (8 * 16 * 32 + 16 * kMlpRows * 8) * 4;   // conv4 + f2 split-K partials in a1p
 static_assert(kSmScratch <= kSmA1, "partials fit in a1p");
 static_assert(kSmTotal <= 227 * 1024, "shared memory");
 
@@ -638,12 +645,11 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   __nv_bfloat16* x0p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW);
   __nv_bfloat16* a1p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0);
   __nv_bfloat16* a2p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1);
-  float* outs = reinterpret_cast<float*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2);
+  __nv_bfloat16* a4 = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2);   // [16][136]
+  float* outs = reinterpret_cast<float*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmA4);          // [16][8]
+  int64_t* tile_p0 = reinterpret_cast<int64_t*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut);
   __nv_bfloat16* a3p = x0p;                                   // [4][6][6][kPix]
-  // a4 / a5 rows padded by 16 B so that the kT rows of an A fragment hit distinct banks
-  constexpr int kA4Row = 128 + 8, kA5Row = 256 + 8;
-  __nv_bfloat16* a4 = x0p + kT * 6 * 6 * kPix;                // [4][136]
-  __nv_bfloat16* a5 = a4 + kT * kA4Row;                       // [4][264]
+  __nv_bfloat16* a5 = x0p + kT * 6 * 6 * kPix;                // [16][264]
   using L = WeightLayout;
   using P = ParamLayout;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
@@ -663,6 +669,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
   __syncthreads();
   const int64_t tiles = (n + kT - 1) / kT;
+  int nsub = 0;   // tiles whose conv4 output waits in a4 (uniform over the CTA)
   for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
   {
     const int64_t p0 = tile * kT;
@@ -821,12 +828,21 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         float sum = 0.f;
 #pragma unroll
         for (int sl = 0; sl < 8; ++sl) sum += part[(sl * 16 + row) * 32 + col];
-        a4[(row >> 2) * kA4Row + (row & 3) * 32 + col] = __float2bfloat16(fmaxf(sum + params[P::b4 + col], 0.f));
+        a4[(nsub * kT + (row >> 2)) * kA4Row + (row & 3) * 32 + col] =
+            __float2bfloat16(fmaxf(sum + params[P::b4 + col], 0.f));
+        if (tid == 0) tile_p0[nsub] = p0;
       }
     }
+    ++nsub;
+    if (nsub < kMlpTiles && tile + gridDim.x < tiles)
+    {
+      __syncthreads();
+      continue;   // the MLP waits for a full m-tile of POIs
+    }
     __syncthreads();
-    // ---- f1: [kT x 128] x W5^T -> [kT x 256]; rows >= kT are zero; B fragments from global
-    // (L1).  A warp takes n-tiles warp and warp + 16 and loads each A fragment once for both.
+    // ---- f1: [16 x 128] x W5^T -> [16 x 256] for the batched tiles (rows past nsub * kT
+    // hold stale values and are never written out); B fragments from global (L2).  A warp
+    // takes n-tiles warp and warp + 16 and loads each A fragment once for both.
     {
       static_assert(kHidden / 8 == 2 * (kFusedThreads / 32), "two f1 n-tiles per warp");
       float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
@@ -835,10 +851,10 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       {
         const int c = ks * 16 + t4 * 2;
         uint32_t a[4];
-        a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * kA4Row + c) : 0u;
-        a[1] = 0u;
-        a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a4 + g * kA4Row + c + 8) : 0u;
-        a[3] = 0u;
+        a[0] = *reinterpret_cast<const uint32_t*>(a4 + g * kA4Row + c);
+        a[1] = *reinterpret_cast<const uint32_t*>(a4 + (g + 8) * kA4Row + c);
+        a[2] = *reinterpret_cast<const uint32_t*>(a4 + g * kA4Row + c + 8);
+        a[3] = *reinterpret_cast<const uint32_t*>(a4 + (g + 8) * kA4Row + c + 8);
 #pragma unroll
         for (int h = 0; h < 2; ++h)
         {
@@ -853,48 +869,51 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       for (int h = 0; h < 2; ++h)
       {
         const int co = (warp + h * (kFusedThreads / 32)) * 8 + t4 * 2;
-        if (g < kT)
-          *reinterpret_cast<uint32_t*>(a5 + g * kA5Row + co) =
-              pack_bf16(__float2bfloat16(fmaxf(acc[h][0] + params[P::b5 + co], 0.f)),
-                        __float2bfloat16(fmaxf(acc[h][1] + params[P::b5 + co + 1], 0.f)));
+        const float bb0 = params[P::b5 + co], bb1 = params[P::b5 + co + 1];
+#pragma unroll
+        for (int h2 = 0; h2 < 2; ++h2)
+          *reinterpret_cast<uint32_t*>(a5 + (g + h2 * 8) * kA5Row + co) =
+              pack_bf16(__float2bfloat16(fmaxf(acc[h][h2 * 2] + bb0, 0.f)),
+                        __float2bfloat16(fmaxf(acc[h][h2 * 2 + 1] + bb1, 0.f)));
       }
     }
     __syncthreads();
-    // ---- f2: [kT x 256] x W6^T -> [kT x 6] (n padded to 8): warp w takes k16 step w,
-    // partials [16][kT][8] in the free a1p region, summed in step order
+    // ---- f2: [16 x 256] x W6^T -> [16 x 6] (n padded to 8): warp w takes k16 step w,
+    // partials [16][16][8] in the free a1p region, summed in step order
     {
       float* part = reinterpret_cast<float*>(a1p) + 8 * 16 * 32;
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
       const int c = warp * 16 + t4 * 2;
       uint32_t a[4];
-      a[0] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c) : 0u;
-      a[1] = 0u;
-      a[2] = g < kT ? *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c + 8) : 0u;
-      a[3] = 0u;
+      a[0] = *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c);
+      a[1] = *reinterpret_cast<const uint32_t*>(a5 + (g + 8) * kA5Row + c);
+      a[2] = *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c + 8);
+      a[3] = *reinterpret_cast<const uint32_t*>(a5 + (g + 8) * kA5Row + c + 8);
       const __nv_bfloat16* wr = wb + L::f2 + g * 256 + c;
       const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)),
                              __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
       mma_bf16_16816(acc, a, b);
-      if (g < kT)
+#pragma unroll
+      for (int h2 = 0; h2 < 2; ++h2)
       {
-        part[(warp * kT + g) * 8 + t4 * 2] = acc[0];
-        part[(warp * kT + g) * 8 + t4 * 2 + 1] = acc[1];
+        part[(warp * kMlpRows + g + h2 * 8) * 8 + t4 * 2] = acc[h2 * 2];
+        part[(warp * kMlpRows + g + h2 * 8) * 8 + t4 * 2 + 1] = acc[h2 * 2 + 1];
       }
       __syncthreads();
-      if (tid < kT * 8)
+      if (tid < kMlpRows * 8)
       {
         const int row = tid >> 3, co = tid & 7;
         float sum = 0.f;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sum += part[(k * kT + row) * 8 + co];
+        for (int k = 0; k < 16; ++k) sum += part[(k * kMlpRows + row) * 8 + co];
         outs[row * 8 + co] = sum + (co < kOut ? params[P::b6 + co] : 0.f);
       }
     }
     __syncthreads();
-    if (tid < kT && p0 + tid < n)
+    if (tid < nsub * kT && tile_p0[tid / kT] + tid % kT < n)
     {
       const float* o = outs + tid * 8;
-      dic_poi* dst = pois + p0 + tid;
+      dic_poi* dst = pois + tile_p0[tid / kT] + tid % kT;
       dst->u = o[0];
       dst->v = o[1];
       dst->ux = o[2] / out_scale(2);
@@ -903,6 +922,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       dst->vy = o[5] / out_scale(5);
       dst->u0 = 0.f; dst->v0 = 0.f; dst->zncc = 0.f; dst->iteration = 0.f; dst->convergence = 0.f; dst->feature = 0.f;
     }
+    nsub = 0;
     __syncthreads();
   }
 }
