@@ -487,6 +487,7 @@ def run_ours(args):
     P = len(tmpl)
     dev = torch.device("cuda", local)
     eng = dic.Engine(R, R, WORKLOAD["conv"], WORKLOAD["max_iter"], device=local)
+    eng.set_autotune(True)          # launch shapes tuned on the first (warm-up) step
     net = None
     modes = ["fftcc"]
     if proposal.WEIGHTS.exists():
@@ -651,6 +652,7 @@ def run_ours(args):
                          "detail": cpu_detail},
         "clocks": clk.summary() if clk else None,
         "gpu_launches": int(round(H0["launches_per_step"] * args.steps)),
+        "icgn_launch_shape": eng.tuning()["icgn_column"],
         "seed_modes": seed_modes,
         "learned_vs_fftcc": (seed_modes["learned"]["value"] / seed_modes["fftcc"]["value"]) if "learned" in seed_modes else None,
         "parity_vs_cpu": seed_modes[headline]["parity_vs_cpu"],
