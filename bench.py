@@ -465,6 +465,51 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
     return out
 
 
+def measure_config1(dic, torch, dev):
+    """The reference's CPU-runnable case: 512x512 u8, translation (2.37, -1.61) + strain 1e-3,
+    noise 1 DN, r 15, step 10.  Host API per pair (upload, FFTCC + IC-GN, download), timed on
+    the host clock; CPU oracle on the whole queue for the same pair."""
+    from fasticgn_gb300 import speckle
+    from oracle import oracle as O
+    pr = speckle.pair_affine(seed=1, width=512, height=512)
+    q0 = dic.grid_queue(512, 512, 15, 10)
+    eng = dic.Engine(15, 15, WORKLOAD["conv"], WORKLOAD["max_iter"], device=dev.index)
+    q = q0.copy()
+    for _ in range(3):
+        q = q0.copy()
+        eng.set_ref(pr.ref)
+        eng.set_tar(pr.tar)
+        eng.process_pair(q)
+    torch.cuda.synchronize()
+    t = []
+    for _ in range(20):
+        q = q0.copy()
+        t0 = time.perf_counter()
+        eng.set_ref(pr.ref)
+        eng.set_tar(pr.tar)
+        eng.process_pair(q)
+        t.append(time.perf_counter() - t0)
+    eng.close()
+    pois = O.grid_pois(512, 512, 15, 10)
+    threads = O.default_threads()
+    c0 = time.perf_counter()
+    O.run_pair(pr.ref.astype(np.float32), pr.tar.astype(np.float32), pois, 15, threads=threads)
+    cpu_s = time.perf_counter() - c0
+    cz, gz = pois["r"][:, O.R_ZNCC], q["zncc"]
+    both = (cz >= 0) & (gz >= 0)
+    du = np.abs(pois["p"][both, O.P_U] - q["u"][both])
+    dv = np.abs(pois["p"][both, O.P_V] - q["v"][both])
+    ms = 1e3 * float(np.median(t))
+    return {"workload": "pair512_affine_r15_step10", "pois": len(q0), "ms_per_pair_e2e": ms,
+            "pois_per_s_e2e": len(q0) / (ms * 1e-3), "cpu_oracle_ms": 1e3 * cpu_s, "cpu_cores": threads,
+            "parity_vs_cpu": {"median_du": float(np.median(du)), "median_dv": float(np.median(dv)),
+                              "p99_du": float(np.quantile(du, .99)), "max_du": float(du.max()),
+                              "max_dv": float(dv.max()),
+                              "flags_agree": float(np.mean((cz >= 0) == (gz >= 0)))},
+            "timing": "host clock, median of 20 pairs: set_ref + set_tar + process_pair (upload, prep, FFTCC, "
+                      "IC-GN, download); the CPU oracle on the whole queue, all host threads"}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -599,6 +644,7 @@ def run_ours(args):
     uneven = None
     if uneven_jobs is not None:
         uneven = measure_uneven(dic, torch, dev, flush, uneven_jobs, max(5, min(args.steps, 20)), args.warmup)
+    config1 = measure_config1(dic, torch, dev) if rank == 0 else None
     stream_lines = None
     if streams is not None:
         stream_lines = {st["name"]: measure_stream(dic, torch, dev, st, *streams[st["name"]], net, flush)
@@ -656,6 +702,7 @@ def run_ours(args):
         "seed_modes": seed_modes,
         "learned_vs_fftcc": (seed_modes["learned"]["value"] / seed_modes["fftcc"]["value"]) if "learned" in seed_modes else None,
         "parity_vs_cpu": seed_modes[headline]["parity_vs_cpu"],
+        "config1_pair512": config1,
         "uneven_batch": uneven,
         "streams": stream_lines,
     }
