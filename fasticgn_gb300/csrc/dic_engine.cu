@@ -701,6 +701,12 @@ struct dic_engine
       DIC_FFTCC_CASE2(18) DIC_FFTCC_CASE2(20) DIC_FFTCC_CASE2(22) DIC_FFTCC_CASE2(24) DIC_FFTCC_CASE2(26)
       DIC_FFTCC_CASE2(28) DIC_FFTCC_CASE2(30) DIC_FFTCC_CASE2(32)
 #undef DIC_FFTCC_CASE2
+#define DIC_FFTCC_BIG(M) \
+  case M: k_fftcc_big<M><<<(unsigned)p.n, 128, (size_t)M * (M + 1) * sizeof(float2), stream>>>(p); break;
+      // 2r = 2 x prime (34, 38, 46, 58, 62) stays on the line-DFT kernel below
+      DIC_FFTCC_BIG(36) DIC_FFTCC_BIG(40) DIC_FFTCC_BIG(42) DIC_FFTCC_BIG(44) DIC_FFTCC_BIG(48)
+      DIC_FFTCC_BIG(50) DIC_FFTCC_BIG(52) DIC_FFTCC_BIG(54) DIC_FFTCC_BIG(56) DIC_FFTCC_BIG(60) DIC_FFTCC_BIG(64)
+#undef DIC_FFTCC_BIG
       default:
         if (r < 1 || 2 * r > kMaxTwiddleN)
           throw DicError{DIC_ERR_ARGUMENT, "FFTCC supports subset radius 1..32 on this engine"};

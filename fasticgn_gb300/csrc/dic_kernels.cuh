@@ -1303,6 +1303,181 @@ __global__ void __launch_bounds__(256) k_fftcc_large(FftccParams P, int m)
 }
 
 // --------------------------------------------------------------------------------------
+// FFTCC for 32 < M <= 64 (subset radius 17..32) as a real FFT: one 128-thread CTA per POI,
+// the packed window z = ref + i tar in shared memory ([M][M + 1] float2), every line
+// transform a four-step FFT M = N1 * N2 done in place by small register FFTs:
+//   forward, natural input -> output X[k1 + N1 k2] stored at N2 k1 + k2 (permuted);
+//   inverse of a permuted input -> natural output, so no transpose pass is needed.
+// Rows, then columns, the cross-power conj(R) T paired with its mirror frequency (in place),
+// inverse columns, inverse rows, argmax with the CPU's tie rule.  Same packing and algebra
+// as k_fftcc.
+// --------------------------------------------------------------------------------------
+__host__ __device__ constexpr int big_n1(int m)
+{
+  int best = 1;
+  for (int d = 2; d * d <= m; ++d)
+    if (m % d == 0) best = d;
+  return best;
+}
+
+template <int M, bool kRows>
+__device__ __forceinline__ int line_at(int line, int j)
+{
+  return kRows ? line * (M + 1) + j : j * (M + 1) + line;
+}
+
+// forward line transforms over all M lines: natural -> permuted
+template <int M, bool kRows>
+__device__ __forceinline__ void big_forward(float2* z)
+{
+  constexpr int N1 = big_n1(M), N2 = M / N1;
+  const float2* tw = c_tw + tw_offset(M);
+  for (int t = threadIdx.x; t < M * N2; t += blockDim.x)
+  {
+    const int line = kRows ? t / N2 : t % M, n2 = kRows ? t % N2 : t / M;
+    float2 a[N1], b[N1];
+#pragma unroll
+    for (int n1 = 0; n1 < N1; ++n1) a[n1] = z[line_at<M, kRows>(line, N2 * n1 + n2)];
+    Fft<N1>::run(a, b);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) z[line_at<M, kRows>(line, N2 * k1 + n2)] = k1 ? cmul(b[k1], tw[n2 * k1]) : b[k1];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < M * N1; t += blockDim.x)
+  {
+    const int line = kRows ? t / N1 : t % M, k1 = kRows ? t % N1 : t / M;
+    float2 a[N2], b[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2) a[n2] = z[line_at<M, kRows>(line, N2 * k1 + n2)];
+    Fft<N2>::run(a, b);
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) z[line_at<M, kRows>(line, N2 * k1 + k2)] = b[k2];
+  }
+  __syncthreads();
+}
+
+// forward-kernel transforms of permuted input over all M lines: permuted -> natural
+template <int M, bool kRows>
+__device__ __forceinline__ void big_from_permuted(float2* z)
+{
+  constexpr int N1 = big_n1(M), N2 = M / N1;
+  const float2* tw = c_tw + tw_offset(M);
+  for (int t = threadIdx.x; t < M * N1; t += blockDim.x)
+  {
+    const int line = kRows ? t / N1 : t % M, k1 = kRows ? t % N1 : t / M;
+    float2 a[N2], b[N2];
+#pragma unroll
+    for (int k2 = 0; k2 < N2; ++k2) a[k2] = z[line_at<M, kRows>(line, N2 * k1 + k2)];
+    Fft<N2>::run(a, b);
+#pragma unroll
+    for (int j = 0; j < N2; ++j) z[line_at<M, kRows>(line, N2 * k1 + j)] = k1 ? cmul(b[j], tw[j * k1]) : b[j];
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < M * N2; t += blockDim.x)
+  {
+    const int line = kRows ? t / N2 : t % M, j = kRows ? t % N2 : t / M;
+    float2 a[N1], b[N1];
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1) a[k1] = z[line_at<M, kRows>(line, N2 * k1 + j)];
+    Fft<N1>::run(a, b);
+#pragma unroll
+    for (int i = 0; i < N1; ++i) z[line_at<M, kRows>(line, N2 * i + j)] = b[i];
+  }
+  __syncthreads();
+}
+
+template <int M>
+__global__ void __launch_bounds__(128) k_fftcc_big(FftccParams P)
+{
+  constexpr int N1 = big_n1(M), N2 = M / N1, S = M + 1, R = M / 2;
+  extern __shared__ float2 zbig[];
+  __shared__ float s_red[32];
+  __shared__ int s_idx[32];
+  const int64_t i = blockIdx.x;
+  if (!queue_slot_active(P, i)) return;
+  dic_poi* poi = P.pois + i;
+  const float px = poi->x, py = poi->y, u_init = poi->u, v_init = poi->v;
+  const int w = P.w, h = P.h;
+  if ((int)px < R || (int)px >= w - R || (int)py < R || (int)py >= h - R ||
+      int(px + u_init) < R || int(px + u_init) >= w - R || int(py + v_init) < R ||
+      int(py + v_init) >= h - R)
+    return;
+  float rsum = 0.f, tsum = 0.f;
+  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
+  {
+    const int r = t / M, c = t % M;
+    const float fxr = __fsub_rn(__fadd_rn(px, (float)c), (float)R);
+    const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
+    const float rv = P.ref[(size_t)(int)fyr * w + (int)fxr];
+    const float tv = P.tar[(size_t)(int)__fadd_rn(fyr, v_init) * w + (int)__fadd_rn(fxr, u_init)];
+    zbig[r * S + c] = make_float2(rv, tv);
+    rsum += rv;
+    tsum += tv;
+  }
+  rsum = block_sum(rsum, s_red);
+  tsum = block_sum(tsum, s_red);
+  const float rmean = rsum / (float)(M * M), tmean = tsum / (float)(M * M);
+  float rn = 0.f, tn = 0.f;
+  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
+  {
+    const int r = t / M, c = t % M;
+    float2 v = zbig[r * S + c];
+    v.x -= rmean;
+    v.y -= tmean;
+    rn += v.x * v.x;
+    tn += v.y * v.y;
+    zbig[r * S + c] = v;
+  }
+  rn = block_sum(rn, s_red);
+  tn = block_sum(tn, s_red);
+  __syncthreads();
+  big_forward<M, true>(zbig);    // rows
+  big_forward<M, false>(zbig);   // columns: Z[kr][kc] at (pos kr, pos kc)
+  // cross-power, conjugated for the inverse (conj(FFT(conj(.))) keeps the real part):
+  // X(k) = conj(R(k)) T(k) with R, T recovered from Z[k] and Z[-k]; X(-k) = conj(X(k)).
+  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
+  {
+    const int pr = t / M, pc = t % M;
+    const int kr = pr / N2 + N1 * (pr % N2), kc = pc / N2 + N1 * (pc % N2);
+    const int mr = (M - kr) % M, mc = (M - kc) % M;
+    const int qr = N2 * (mr % N1) + mr / N1, qc = N2 * (mc % N1) + mc / N1;
+    const int p = pr * M + pc, q = qr * M + qc;
+    if (p > q) continue;
+    const float2 A = zbig[pr * S + pc];
+    const float2 zm = zbig[qr * S + qc];
+    const float2 B = make_float2(zm.x, -zm.y);
+    const float2 Rk = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y + B.y));
+    const float2 D = csub(A, B);
+    const float2 Tk = make_float2(0.5f * D.y, -0.5f * D.x);
+    const float2 X = make_float2(Rk.x * Tk.x + Rk.y * Tk.y, Rk.x * Tk.y - Rk.y * Tk.x);
+    zbig[pr * S + pc] = make_float2(X.x, -X.y);
+    if (q != p) zbig[qr * S + qc] = X;
+  }
+  __syncthreads();
+  big_from_permuted<M, false>(zbig);   // columns back to natural rows
+  big_from_permuted<M, true>(zbig);    // rows back to natural columns: correlation in .x
+  float best = -2.f;
+  int best_idx = 0;
+  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
+  {
+    const float v = zbig[(t / M) * S + t % M].x;
+    if (v > best) { best = v; best_idx = t; }
+  }
+  block_argmax(best, best_idx, s_red, s_idx);
+  if (threadIdx.x == 0)
+  {
+    int lu = best_idx % M, lv = best_idx / M;
+    if (lu > R) lu -= M;
+    if (lv > R) lv -= M;
+    poi->u = (float)lu + u_init;
+    poi->v = (float)lv + v_init;
+    poi->u0 = u_init;
+    poi->v0 = v_init;
+    poi->zncc = best / (sqrtf(rn * tn) * (float)(M * M));
+  }
+}
+
+// --------------------------------------------------------------------------------------
 // Frame policy (processFrame, opencorr_cli_cuda_mvp.cpp:3024-3210) on the device.
 // A frame is one fixed launch sequence: seed from the previous frame, IC-GN, scan for bad
 // POIs, decide, then either the whole-frame FFTCC + IC-GN pass with a per-POI merge or
