@@ -1481,12 +1481,15 @@ int dic_process_pair(dic_engine* e, dic_poi* pois, int64_t n)
       throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D supports positive square radii only"};
     if (n == 0) return;
     e->upload_queue(pois, n);
+    // FFTCC reads only (x, y, u, v) and writes the seed; the per-POI reference data reads
+    // only (x, y).  Launching FFTCC first lets the host's layout check and record (a pass
+    // over the queue) run while the GPU works.
+    e->run_fftcc(e->queue.ptr, n);
     if (!e->layout_matches(pois, n))
     {
       e->record_layout(pois, n);
       e->prepare_layout_device(e->queue.ptr, n);
     }
-    e->run_fftcc(e->queue.ptr, n);
     e->run_icgn(e->queue.ptr, n, nullptr);
     e->download_queue(pois, n);
   });

@@ -204,10 +204,13 @@ __device__ __forceinline__ float warp_sum(float v)
 
 // 6x6 inverse by partial-pivot LU in float (restates Eigen's Matrix6f::inverse, which
 // src/oc_icgn.cpp:234 calls).  Fully unrolled with static indices, so the matrix lives in
-// registers; row swaps are predicated.
-__device__ __forceinline__ void inverse6(float (&a)[6][6], float (&inv)[6][6])
+// registers; row swaps are predicated.  lu6 factorises in place, solve6_column produces one
+// column of the inverse; the column solves are independent, so k_poi_prepare runs them on
+// six lanes at once.
+__device__ __forceinline__ void lu6(float (&a)[6][6], int (&perm)[6])
 {
-  int perm[6] = {0, 1, 2, 3, 4, 5};
+#pragma unroll
+  for (int i = 0; i < 6; ++i) perm[i] = i;
 #pragma unroll
   for (int k = 0; k < 6; ++k)
   {
@@ -239,26 +242,26 @@ __device__ __forceinline__ void inverse6(float (&a)[6][6], float (&inv)[6][6])
       for (int j = k + 1; j < 6; ++j) a[i][j] -= a[i][k] * a[k][j];
     }
   }
+}
+
+__device__ __forceinline__ void solve6_column(const float (&a)[6][6], const int (&perm)[6], int col, float (&x)[6])
+{
+  float y[6];
 #pragma unroll
-  for (int col = 0; col < 6; ++col)
+  for (int i = 0; i < 6; ++i)
   {
-    float y[6];
+    float s = (perm[i] == col) ? 1.f : 0.f;
 #pragma unroll
-    for (int i = 0; i < 6; ++i)
-    {
-      float s = (perm[i] == col) ? 1.f : 0.f;
+    for (int j = 0; j < i; ++j) s -= a[i][j] * y[j];
+    y[i] = s;
+  }
 #pragma unroll
-      for (int j = 0; j < i; ++j) s -= a[i][j] * y[j];
-      y[i] = s;
-    }
+  for (int i = 5; i >= 0; --i)
+  {
+    float s = y[i];
 #pragma unroll
-    for (int i = 5; i >= 0; --i)
-    {
-      float s = y[i];
-#pragma unroll
-      for (int j = i + 1; j < 6; ++j) s -= a[i][j] * inv[j][col];
-      inv[i][col] = s / a[i][i];
-    }
+    for (int j = i + 1; j < 6; ++j) s -= a[i][j] * x[j];
+    x[i] = s / a[i][i];
   }
 }
 
@@ -418,27 +421,39 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
   for (int a = 0; a < 6; ++a) { S[a] = warp_sum(S[a]); G[a] = warp_sum(G[a]); }
 #pragma unroll
   for (int t = 0; t < 21; ++t) H[t] = warp_sum(H[t]);
-  if (lane == 0)
+  // Every lane holds the same sums (butterfly reductions), so the LU runs uniformly and
+  // lane c < 6 solves and writes column c of the inverse and entry c of S and G.
   {
-    float hf[6][6], inv[6][6];
+    float hf[6][6];
     int t = 0;
 #pragma unroll
     for (int a = 0; a < 6; ++a)
 #pragma unroll
       for (int b = 0; b <= a; ++b) { hf[a][b] = H[t]; hf[b][a] = H[t]; ++t; }
-    inverse6(hf, inv);
+    int perm[6];
+    lu6(hf, perm);
     const float m_r = src * (1.f / (float)size);
-    const float rn_sq = fmaf(-src, m_r, nsq);
-    rec->ref_norm = sqrtf(rn_sq);
-    rec->ref_norm_sq = rn_sq;
-    rec->sum_rc = src;
+    if (lane < 6)
+    {
+      float x[6];
+      solve6_column(hf, perm, lane, x);
 #pragma unroll
-    for (int a = 0; a < 6; ++a) { rec->S[a] = S[a]; rec->G[a] = fmaf(-m_r, S[a], G[a]); }
+      for (int a = 0; a < 6; ++a) rec->inv_h[a * 6 + lane] = x[a];
+      float S_l = S[0], G_l = G[0];
 #pragma unroll
-    for (int a = 0; a < 6; ++a)
-#pragma unroll
-      for (int b = 0; b < 6; ++b) rec->inv_h[a * 6 + b] = inv[a][b];
-    rec->valid = 1.f;
+      for (int a = 1; a < 6; ++a)
+        if (lane == a) { S_l = S[a]; G_l = G[a]; }
+      rec->S[lane] = S_l;
+      rec->G[lane] = fmaf(-m_r, S_l, G_l);
+    }
+    if (lane == 0)
+    {
+      const float rn_sq = fmaf(-src, m_r, nsq);
+      rec->ref_norm = sqrtf(rn_sq);
+      rec->ref_norm_sq = rn_sq;
+      rec->sum_rc = src;
+      rec->valid = 1.f;
+    }
   }
 }
 
