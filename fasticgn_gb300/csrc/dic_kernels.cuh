@@ -1319,8 +1319,10 @@ __global__ void __launch_bounds__(256) k_fftcc_large(FftccParams P, int m)
 
 // --------------------------------------------------------------------------------------
 // FFTCC for 32 < M <= 64 (subset radius 17..32) as a real FFT: one 128-thread CTA per POI,
-// the packed window z = ref + i tar in shared memory ([M][M + 1] float2), every line
-// transform a four-step FFT M = N1 * N2 done in place by small register FFTs:
+// the packed window z = ref + i tar in shared memory ([M][M + 1] float2; consecutive lanes
+// take consecutive lines, whose odd float2 stride keeps a warp's accesses conflict-free in
+// both directions), every line transform a four-step FFT M = N1 * N2 done in place by
+// small register FFTs:
 //   forward, natural input -> output X[k1 + N1 k2] stored at N2 k1 + k2 (permuted);
 //   inverse of a permuted input -> natural output, so no transpose pass is needed.
 // Rows, then columns, the cross-power conj(R) T paired with its mirror frequency (in place),
@@ -1349,7 +1351,7 @@ __device__ __forceinline__ void big_forward(float2* z)
   const float2* tw = c_tw + tw_offset(M);
   for (int t = threadIdx.x; t < M * N2; t += blockDim.x)
   {
-    const int line = kRows ? t / N2 : t % M, n2 = kRows ? t % N2 : t / M;
+    const int line = t % M, n2 = t / M;
     float2 a[N1], b[N1];
 #pragma unroll
     for (int n1 = 0; n1 < N1; ++n1) a[n1] = z[line_at<M, kRows>(line, N2 * n1 + n2)];
@@ -1360,7 +1362,7 @@ __device__ __forceinline__ void big_forward(float2* z)
   __syncthreads();
   for (int t = threadIdx.x; t < M * N1; t += blockDim.x)
   {
-    const int line = kRows ? t / N1 : t % M, k1 = kRows ? t % N1 : t / M;
+    const int line = t % M, k1 = t / M;
     float2 a[N2], b[N2];
 #pragma unroll
     for (int n2 = 0; n2 < N2; ++n2) a[n2] = z[line_at<M, kRows>(line, N2 * k1 + n2)];
@@ -1379,7 +1381,7 @@ __device__ __forceinline__ void big_from_permuted(float2* z)
   const float2* tw = c_tw + tw_offset(M);
   for (int t = threadIdx.x; t < M * N1; t += blockDim.x)
   {
-    const int line = kRows ? t / N1 : t % M, k1 = kRows ? t % N1 : t / M;
+    const int line = t % M, k1 = t / M;
     float2 a[N2], b[N2];
 #pragma unroll
     for (int k2 = 0; k2 < N2; ++k2) a[k2] = z[line_at<M, kRows>(line, N2 * k1 + k2)];
@@ -1390,7 +1392,7 @@ __device__ __forceinline__ void big_from_permuted(float2* z)
   __syncthreads();
   for (int t = threadIdx.x; t < M * N2; t += blockDim.x)
   {
-    const int line = kRows ? t / N2 : t % M, j = kRows ? t % N2 : t / M;
+    const int line = t % M, j = t / M;
     float2 a[N1], b[N1];
 #pragma unroll
     for (int k1 = 0; k1 < N1; ++k1) a[k1] = z[line_at<M, kRows>(line, N2 * k1 + j)];
