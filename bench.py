@@ -691,6 +691,26 @@ def run_ours(args):
                 "model": "64 B B-spline texel per warped sample per iteration + 12 B ref/grad per sample "
                          "+ 224 B per-POI record/IO; the gathers are served on chip, see profiles/"}
 
+    # ---- the other hot kernels against their own bounds (SURVEY 8(d) FLOP models)
+    M = 2 * R
+    fftcc_flop = 2 * (2.5 * M * M * np.log2(M * M)) + 6 * M * (M // 2 + 1) + 4 * M * M
+    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12       # nominal FP32: 152 SMs x 128 FMA/clk at 2.07 GHz
+    try:
+        bf16_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"])
+        bf16_src = "measured"
+    except (OSError, KeyError, ValueError):
+        bf16_peak, bf16_src = 1900.0, "fallback"
+    other = {"k_fftcc": {"bound": "fp32", "flop_per_poi": fftcc_flop,
+                         "achieved": fftcc_flop * P / (H0["kernels_ms"]["ms_fftcc"] * 1e-3) / 1e12,
+                         "peak": fp32_peak, "unit": "TFLOP/s", "peak_source": "nominal"}}
+    if "learned" in res:
+        cnn_flop = 2 * (256 * 32 * 18 + 64 * 32 * 288 + 16 * 32 * 288 + 4 * 32 * 288 + 128 * 256 + 256 * 6)
+        other["k_proposal_fused"] = {"bound": "tensor", "flop_per_poi": cnn_flop,
+                                     "achieved": cnn_flop * P / (res["learned"]["kernels_ms"]["ms_proposal"] * 1e-3) / 1e12,
+                                     "peak": bf16_peak, "unit": "TFLOP/s", "peak_source": bf16_src}
+    for v in other.values():
+        v["frac"] = v["achieved"] / v["peak"]
+
     # ---- CPU baseline on a bounded sample, and parity of each GPU mode on that sample
     from oracle import oracle as O
     threads = O.default_threads()
@@ -698,8 +718,14 @@ def run_ours(args):
     seed_modes = {}
     for mode, r in res.items():
         ok = r["result"]["zncc"] >= 0
+        its = r["result"]["iteration"][ok].astype(np.int64)
+        hist = np.bincount(its, minlength=WORKLOAD["max_iter"] + 1)
         seed_modes[mode] = {"value": r["value"], "ms_per_step": r["ms_per_step"], "kernels_ms": r["kernels_ms"],
                             "icgn_iterations_per_poi": r["icgn_iterations"] / P, "valid_ratio": float(ok.mean()),
+                            "iterations_histogram": {str(k): int(c) for k, c in enumerate(hist) if c},
+                            "fftcc_fallback_ratio": (float(np.mean((r["result"]["u0"] == np.round(r["result"]["u0"])) &
+                                                                   (r["result"]["v0"] == np.round(r["result"]["v0"]))))
+                                                     if mode == "learned" else None),
                             "kernel_launches_per_step": r["launches_per_step"],
                             "parity_vs_cpu": parity_vs_cpu(r["result"], cpu_sample)}
     h2d = ref.nbytes + tar.nbytes + tmpl.nbytes
@@ -714,6 +740,7 @@ def run_ours(args):
         "e2e": {"value": whole_job_rate(world, P, e2e_ms), "unit": "POI/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(tmpl.nbytes)},
         "roofline": roofline,
+        "roofline_other_kernels": other,
         "cpu_baseline": {"value": cpu_value, "unit": "POI/s", "cores": threads, "kind": "port",
                          "sample": f"full-image prep + FFTCC/IC-GN on every {CPU_SAMPLE_STRIDE}th POI "
                                    f"({cpu_detail['sample_pois']} POIs), extrapolated; own FFT, not FFTW",
