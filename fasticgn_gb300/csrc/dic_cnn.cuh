@@ -486,47 +486,66 @@ __global__ void k_write_seeds(const float* __restrict__ out, dic_poi* __restrict
 }
 
 // --------------------------------------------------------------------------------------
-// Fused inference: the whole network for kT POIs per tile in one CTA, activations
-// resident in shared memory, writing the seeds straight into the POI queue.  Persistent
-// grid (tiles strided over CTAs).  Same arithmetic as the GEMM path (BF16 operands, FP32
-// accumulation, BF16 ReLU outputs), so both give the same seeds up to accumulation order.
+// Fused inference: the whole network, activations resident in shared memory, seeds written
+// straight into the POI queue.  One 512-thread CTA per SM holds two independent warp groups
+// of 8 warps; each group runs tiles of kT = 2 POIs (tiles strided over groups and CTAs) and
+// syncs on its own named barrier, so one group's serial phases (window staging, conv3/conv4,
+// the MLP) overlap the other's conv1/conv2.  Same arithmetic as the GEMM path (BF16
+// operands, FP32 accumulation, BF16 ReLU outputs), so both give the same seeds up to
+// accumulation order.
 //
-// Shared memory (bytes): W1 [32][40] 2.5 KB (rows padded to 80 B: the B-fragment loads of
-// 8 rows x 4 lanes hit 32 distinct banks); W2..W4 [32][296] 57 KB (row padded to 37
-// 16-byte chunks: conflict-free ldmatrix); x0p [4][33][48][2] 25 KB (zero border; a
-// 48-pixel row puts tap (ky, kx) at word 16 ky + kx mod 32, and conv1's K slots are
-// grouped so that each A-fragment load reads taps {0, 16, 1, 17} or {2, 18, 1} words
-// apart: 32 distinct banks for the 8 stride-2 rows x 4 taps of a load);
-// a1p [4][18][18][40] 104 KB and a2p [4][10][10][40] 32 KB (zero border, pixel stride 80 B).
+// Shared memory (bytes), weights shared by the groups: W1 [32][40] 2.5 KB (rows padded to
+// 80 B: the B-fragment loads of 8 rows x 4 lanes hit 32 distinct banks); W2..W4 [32][296]
+// 57 KB (row padded to 37 16-byte chunks: conflict-free ldmatrix).  Per group: x0p
+// [2][33][48][2] 12.4 KB (zero border; a 48-pixel row puts tap (ky, kx) at word
+// 16 ky + kx mod 32, and conv1's K slots are grouped so that each A-fragment load reads taps
+// {0, 16, 1, 17} or {2, 18, 1} words apart: 32 distinct banks for the 8 stride-2 rows x 4
+// taps of a load); a1p [2][18][18][40] 50.6 KB and a2p [2][10][10][40] 15.6 KB (zero border,
+// pixel stride 80 B); a4 [16][136] (conv4 outputs of 8 tiles, for the batched MLP).
 // The padded activation rows are stored parity-split: padded column X sits at
 // (X & 1) * (width / 2) + (X >> 1), so the stride-2 im2col rows of an ldmatrix (8 output
 // pixels, input columns 2 ox + kx) are 8 consecutive 80 B pixels, which cover all 32 banks.
-// a3p, a4, a5 overlay x0p once conv1 has consumed it.
+// a3p overlays x0p once conv1 has consumed it; the split-K partials and a5 overlay the start
+// of a1p once conv2 has.
 // --------------------------------------------------------------------------------------
-constexpr int kT = 4;
-constexpr int kFusedThreads = 512;
+constexpr int kT = 2;                           // POIs per tile of a warp group
+constexpr int kGroups = 2;                      // independent warp groups per CTA
+constexpr int kGW = 8;                          // warps per group
+constexpr int kGThreads = kGW * 32;             // 256
+constexpr int kFusedThreads = kGroups * kGThreads;
 constexpr int kPix = 40;                        // padded channel stride (80 B) of a1p/a2p/a3p
 constexpr int kWRow = 296;                      // padded row of W2..W4 (288 + 8)
 constexpr int kX0Row = 48;                      // x0p row stride in pixels (33 used)
-constexpr int kSmX0 = kT * 33 * kX0Row * 2 * 2; // 25344
-constexpr int kSmA1 = kT * 18 * 18 * kPix * 2;  // 103680
-constexpr int kSmA2 = kT * 10 * 10 * kPix * 2;  // 32000
+constexpr int kSmX0 = kT * 33 * kX0Row * 2 * 2; // 12672
+constexpr int kSmA1 = kT * 18 * 18 * kPix * 2;  // 51840
+constexpr int kSmA2 = kT * 10 * 10 * kPix * 2;  // 16000
 constexpr int kW1Row = 40;                      // padded row of W1 (32 + 8)
 constexpr int kSmW1 = 32 * kW1Row * 2;          // 2560
 constexpr int kSmW = 3 * 32 * kWRow * 2;        // 56832
 // The MLP runs once per kMlpTiles tiles (16 POIs: one full m-tile), so its 64 KB of f1
 // weights stream from L2 once per 16 POIs instead of once per tile.
-constexpr int kMlpTiles = 4;
+constexpr int kMlpTiles = 8;
 constexpr int kMlpRows = kMlpTiles * kT;         // 16
 constexpr int kA4Row = 128 + 8, kA5Row = 256 + 8;   // rows padded by 16 B: distinct banks per fragment
 constexpr int kSmA4 = kMlpRows * kA4Row * 2;     // 4352, persists across the batched tiles
 constexpr int kSmOut = kMlpRows * 8 * 4;         // 512
 constexpr int kSmPoi = kMlpTiles * 8;            // first POI of each batched tile
-constexpr int kSmTotal = kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut + kSmPoi;
-static_assert(kT * 6 * 6 * kPix * 2 + kMlpRows * kA5Row * 2 <= kSmX0, "a3p + a5 overlay x0p");
-constexpr int kSmScratch = (8 * 16 * 32 + 16 * kMlpRows * 8) * 4;   // conv4 + f2 split-K partials in a1p
-static_assert(kSmScratch <= kSmA1, "partials fit in a1p");
+constexpr int kSmGroup = kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut + kSmPoi;   // 85440
+constexpr int kSmTotal = kSmW1 + kSmW + kGroups * kSmGroup;
+static_assert(kT * 6 * 6 * kPix * 2 <= kSmX0, "a3p overlays x0p");
+// In a1p, free after conv2: conv4 split-K partials [4][16][32], f2 partials [8][16][8], a5
+constexpr int kSmPart4 = 4 * 16 * 32 * 4, kSmPart2 = kGW * 16 * 8 * 4;
+constexpr int kSmA5Off = kSmPart4 + kSmPart2;
+constexpr int kSmScratch = kSmA5Off + kMlpRows * kA5Row * 2;
+static_assert(kSmScratch <= kSmA1 && kSmA5Off % 16 == 0, "partials and a5 fit in a1p");
+static_assert(kSmGroup % 16 == 0, "group regions stay 16-byte aligned");
 static_assert(kSmTotal <= 227 * 1024, "shared memory");
+
+// barrier of one warp group (ids 1.., 0 is __syncthreads)
+__device__ __forceinline__ void group_sync(int grp)
+{
+  asm volatile("bar.sync %0, %1;\n" ::"r"(1 + grp), "r"(kGThreads) : "memory");
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -559,7 +578,7 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], uint32_t addr)
 // of n-tiles): with MPAIR = 2 a warp loads each B fragment once for two m-tiles.
 template <int SIP, int SO, int SOP, int MPAIR>
 __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloat16* out, const __nv_bfloat16* W,
-                                             const float* __restrict__ bias, int warp, int lane)
+                                             const float* __restrict__ bias, int warp, int lane)   // warp: within the group
 {
   constexpr int M = kT * SO * SO;
   constexpr int MT = (M + 15) / 16;
@@ -567,7 +586,7 @@ __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloa
   constexpr int MSTEP = MT / MPAIR;
   const int g = lane >> 2, t4 = lane & 3;
   const int q = lane >> 3;
-  for (int task = warp; task < MSTEP * 2; task += kFusedThreads / 32)
+  for (int task = warp; task < MSTEP * 2; task += kGW)
   {
     const int mt0 = task >> 1, nh = task & 1;
     // ldmatrix A addresses: lane -> row (q & 1) * 8 + (lane & 7), k offset (q >> 1) * 8;
@@ -642,18 +661,22 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   __nv_bfloat16* W2s = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1);
   __nv_bfloat16* W3s = W2s + 32 * kWRow;
   __nv_bfloat16* W4s = W3s + 32 * kWRow;
-  __nv_bfloat16* x0p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW);
-  __nv_bfloat16* a1p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0);
-  __nv_bfloat16* a2p = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1);
-  __nv_bfloat16* a4 = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2);   // [16][136]
-  float* outs = reinterpret_cast<float*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmA4);          // [16][8]
-  int64_t* tile_p0 = reinterpret_cast<int64_t*>(sm + kSmW1 + kSmW + kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut);
-  __nv_bfloat16* a3p = x0p;                                   // [4][6][6][kPix]
-  __nv_bfloat16* a5 = x0p + kT * 6 * 6 * kPix;                // [16][264]
   using L = WeightLayout;
   using P = ParamLayout;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
-  // weights and zero borders, once per CTA
+  const int tid = threadIdx.x, lane = tid & 31, g = lane >> 2, t4 = lane & 3;
+  const int grp = tid / kGThreads, gt = tid % kGThreads, warp = gt >> 5;   // warp within the group
+  unsigned char* gs = sm + kSmW1 + kSmW + grp * kSmGroup;
+  __nv_bfloat16* x0p = reinterpret_cast<__nv_bfloat16*>(gs);
+  __nv_bfloat16* a1p = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0);
+  __nv_bfloat16* a2p = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0 + kSmA1);
+  __nv_bfloat16* a4 = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0 + kSmA1 + kSmA2);           // [16][136]
+  float* outs = reinterpret_cast<float*>(gs + kSmX0 + kSmA1 + kSmA2 + kSmA4);                 // [16][8]
+  int64_t* tile_p0 = reinterpret_cast<int64_t*>(gs + kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut);
+  __nv_bfloat16* a3p = x0p;                                                                  // [2][6][6][kPix]
+  float* part4 = reinterpret_cast<float*>(a1p);                                              // [4][16][32]
+  float* part2 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(a1p) + kSmPart4); // [8][16][8]
+  __nv_bfloat16* a5 = reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<unsigned char*>(a1p) + kSmA5Off);   // [16][264]
+  // weights and zero borders, once per CTA (both groups)
   for (int i = tid; i < 32 * kW1Row; i += kFusedThreads)
   {
     const int r = i / kW1Row, c = i % kW1Row;
@@ -665,19 +688,22 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     const int l = i / (32 * kWRow), r = (i / kWRow) % 32, c = i % kWRow;
     W2s[i] = c < 288 ? wb[L::c2 + l * 32 * 288 + r * 288 + c] : bz();
   }
-  for (int i = tid; i < (kSmX0 + kSmA1 + kSmA2) / 4; i += kFusedThreads)
-    reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
+  for (int i = tid; i < kGroups * kSmGroup / 4; i += kFusedThreads)
+    reinterpret_cast<uint32_t*>(sm + kSmW1 + kSmW)[i] = 0u;
   __syncthreads();
+  // From here on the two groups run independently: group grp takes tiles 2 b + grp, stepping
+  // by 2 * gridDim.x, and meets only its own barrier.
   const int64_t tiles = (n + kT - 1) / kT;
-  int nsub = 0;   // tiles whose conv4 output waits in a4 (uniform over the CTA)
-  for (int64_t tile = blockIdx.x; tile < tiles; tile += gridDim.x)
+  const int64_t tstep = (int64_t)gridDim.x * kGroups;
+  int nsub = 0;   // tiles whose conv4 output waits in a4 (uniform over the group)
+  for (int64_t tile = (int64_t)blockIdx.x * kGroups + grp; tile < tiles; tile += tstep)
   {
     const int64_t p0 = tile * kT;
-    // a3p/a4/a5 of the previous tile overlay x0p, and the split-K partial sums of conv4 and
-    // f2 overlay the start of a1p: clear both so their borders read as padding again
-    for (int i = tid; i < kSmX0 / 4; i += kFusedThreads) reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
-    for (int i = tid; i < kSmScratch / 4; i += kFusedThreads) reinterpret_cast<uint32_t*>(a1p)[i] = 0u;
-    __syncthreads();
+    // a3p of the previous tile overlays x0p, and the split-K partials and a5 overlay the
+    // start of a1p: clear both so their borders read as padding again
+    for (int i = gt; i < kSmX0 / 4; i += kGThreads) reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
+    for (int i = gt; i < kSmScratch / 4; i += kGThreads) reinterpret_cast<uint32_t*>(a1p)[i] = 0u;
+    group_sync(grp);
     // ---- input windows: warp 2p + c stages channel c (0 ref, 1 tar) of POI p.  Lane l holds
     // column l of the 31x31 window in registers (coalesced row loads, one pass), the warp
     // reduces mean and variance, and writes the normalised values into x0p's interior.
@@ -722,11 +748,11 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         }
       }
     }
-    __syncthreads();
+    group_sync(grp);
     // ---- conv1: M = kT * 256 rows, K = 18 (padded 32), A gathered as (ci0, ci1) pairs
     {
       constexpr int M = kT * 256;
-      for (int mt = warp; mt < M / 16; mt += kFusedThreads / 32)
+      for (int mt = warp; mt < M / 16; mt += kGW)
       {
         int rbase[2];
 #pragma unroll
@@ -778,23 +804,22 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         }
       }
     }
-    __syncthreads();
+    group_sync(grp);
     // x0p is free: zero the a3p region (its border must read as zero padding)
-    for (int i = tid; i < kT * 6 * 6 * kPix / 2; i += kFusedThreads) reinterpret_cast<uint32_t*>(a3p)[i] = 0u;
+    for (int i = gt; i < kT * 6 * 6 * kPix / 2; i += kGThreads) reinterpret_cast<uint32_t*>(a3p)[i] = 0u;
     fused_conv32<18, 8, 10, 2>(a1p, a2p, W2s, params + P::b2, warp, lane);
-    __syncthreads();
+    group_sync(grp);
     fused_conv32<10, 4, 6, 1>(a2p, a3p, W3s, params + P::b3, warp, lane);
-    __syncthreads();
-    // ---- conv4: 4x4 -> 2x2, M = kT*4 = 16 rows (one m-tile), N = 32, K = 288, split over
-    // all 16 warps: warp = (n-tile pair, one of 8 K slices of the 18 k16 steps).  Partial
-    // sums go to the free a1p region and are added in slice order (deterministic), then
-    // bias + ReLU into a4 [p][y][x][c].
+    group_sync(grp);
+    // ---- conv4: 4x4 -> 2x2, M = kT*4 = 8 rows (half an m-tile), N = 32, K = 288, split over
+    // the group's 8 warps: warp = (n-tile pair, one of 4 K slices of the 18 k16 steps).
+    // Partial sums go to a1p (free after conv2) and are added in slice order
+    // (deterministic), then bias + ReLU into this tile's rows of a4 [p][y][x][c].
     {
-      constexpr int SIP = 6;
-      float* part = reinterpret_cast<float*>(a1p);              // [8][16][32]
+      constexpr int SIP = 6, M = kT * 4;
       const int nh = warp & 1, slice = warp >> 1, q = lane >> 3;
-      const int s0 = slice * 18 / 8, s1 = (slice + 1) * 18 / 8;
-      const int arow = (q & 1) * 8 + (lane & 7);
+      const int s0 = slice * 18 / 4, s1 = (slice + 1) * 18 / 4;
+      const int arow = min((q & 1) * 8 + (lane & 7), M - 1);
       const int p = arow / 4, oy = (arow % 4) / 2, ox = arow % 2;
       const __nv_bfloat16* abase = a3p + ((p * SIP + 2 * oy) * SIP + ox) * kPix + (q >> 1) * 8;
       const __nv_bfloat16* bbase = W4s + (nh * 16 + (q >> 1) * 8 + (lane & 7)) * kWRow + (q & 1) * 8;
@@ -814,38 +839,39 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       for (int j = 0; j < 2; ++j)
       {
         const int co = nh * 16 + j * 8 + t4 * 2;
-#pragma unroll
-        for (int h2 = 0; h2 < 2; ++h2)
-        {
-          float* dst = part + (slice * 16 + g + h2 * 8) * 32 + co;
-          dst[0] = acc[j][h2 * 2];
-          dst[1] = acc[j][h2 * 2 + 1];
-        }
+        float* dst = part4 + (slice * 16 + g) * 32 + co;   // rows g < 8 = the M rows
+        dst[0] = acc[j][0];
+        dst[1] = acc[j][1];
       }
-      __syncthreads();
+      group_sync(grp);
       {
-        const int row = tid >> 5, col = tid & 31;    // 512 threads = 16 rows x 32 channels
+        const int row = gt >> 5, col = gt & 31;    // 256 threads = 8 rows x 32 channels
         float sum = 0.f;
 #pragma unroll
-        for (int sl = 0; sl < 8; ++sl) sum += part[(sl * 16 + row) * 32 + col];
+        for (int sl = 0; sl < 4; ++sl) sum += part4[(sl * 16 + row) * 32 + col];
         a4[(nsub * kT + (row >> 2)) * kA4Row + (row & 3) * 32 + col] =
             __float2bfloat16(fmaxf(sum + params[P::b4 + col], 0.f));
-        if (tid == 0) tile_p0[nsub] = p0;
+        if (gt == 0) tile_p0[nsub] = p0;
       }
     }
     ++nsub;
-    if (nsub < kMlpTiles && tile + gridDim.x < tiles)
+    if (nsub < kMlpTiles && tile + tstep < tiles)
     {
-      __syncthreads();
+      group_sync(grp);
       continue;   // the MLP waits for a full m-tile of POIs
     }
-    __syncthreads();
+    group_sync(grp);
     // ---- f1: [16 x 128] x W5^T -> [16 x 256] for the batched tiles (rows past nsub * kT
     // hold stale values and are never written out); B fragments from global (L2).  A warp
-    // takes n-tiles warp and warp + 16 and loads each A fragment once for both.
+    // takes n-tiles warp + 8 h, h < 4, and loads each A fragment once for the four.
     {
-      static_assert(kHidden / 8 == 2 * (kFusedThreads / 32), "two f1 n-tiles per warp");
-      float acc[2][4] = {{0.f, 0.f, 0.f, 0.f}, {0.f, 0.f, 0.f, 0.f}};
+      constexpr int NT = kHidden / 8 / kGW;   // 4
+      static_assert(kHidden / 8 == NT * kGW, "f1 n-tiles split evenly over the group");
+      float acc[NT][4];
+#pragma unroll
+      for (int hh = 0; hh < NT; ++hh)
+#pragma unroll
+        for (int e = 0; e < 4; ++e) acc[hh][e] = 0.f;
 #pragma unroll
       for (int ks = 0; ks < 8; ++ks)
       {
@@ -856,64 +882,67 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
         a[2] = *reinterpret_cast<const uint32_t*>(a4 + g * kA4Row + c + 8);
         a[3] = *reinterpret_cast<const uint32_t*>(a4 + (g + 8) * kA4Row + c + 8);
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+        for (int hh = 0; hh < NT; ++hh)
         {
-          const int nt = warp + h * (kFusedThreads / 32);
+          const int nt = warp + hh * kGW;
           const __nv_bfloat16* wr = wb + L::f1 + (nt * 8 + g) * 128 + c;
           const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)),
                                  __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
-          mma_bf16_16816(acc[h], a, b);
+          mma_bf16_16816(acc[hh], a, b);
         }
       }
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
+      for (int hh = 0; hh < NT; ++hh)
       {
-        const int co = (warp + h * (kFusedThreads / 32)) * 8 + t4 * 2;
+        const int co = (warp + hh * kGW) * 8 + t4 * 2;
         const float bb0 = params[P::b5 + co], bb1 = params[P::b5 + co + 1];
 #pragma unroll
         for (int h2 = 0; h2 < 2; ++h2)
           *reinterpret_cast<uint32_t*>(a5 + (g + h2 * 8) * kA5Row + co) =
-              pack_bf16(__float2bfloat16(fmaxf(acc[h][h2 * 2] + bb0, 0.f)),
-                        __float2bfloat16(fmaxf(acc[h][h2 * 2 + 1] + bb1, 0.f)));
+              pack_bf16(__float2bfloat16(fmaxf(acc[hh][h2 * 2] + bb0, 0.f)),
+                        __float2bfloat16(fmaxf(acc[hh][h2 * 2 + 1] + bb1, 0.f)));
       }
     }
-    __syncthreads();
-    // ---- f2: [16 x 256] x W6^T -> [16 x 6] (n padded to 8): warp w takes k16 step w,
-    // partials [16][16][8] in the free a1p region, summed in step order
+    group_sync(grp);
+    // ---- f2: [16 x 256] x W6^T -> [16 x 6] (n padded to 8): warp w takes k16 steps 2w and
+    // 2w + 1, partials [8][16][8] summed in warp order
     {
-      float* part = reinterpret_cast<float*>(a1p) + 8 * 16 * 32;
       float acc[4] = {0.f, 0.f, 0.f, 0.f};
-      const int c = warp * 16 + t4 * 2;
-      uint32_t a[4];
-      a[0] = *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c);
-      a[1] = *reinterpret_cast<const uint32_t*>(a5 + (g + 8) * kA5Row + c);
-      a[2] = *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c + 8);
-      a[3] = *reinterpret_cast<const uint32_t*>(a5 + (g + 8) * kA5Row + c + 8);
-      const __nv_bfloat16* wr = wb + L::f2 + g * 256 + c;
-      const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)),
-                             __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
-      mma_bf16_16816(acc, a, b);
+#pragma unroll
+      for (int kk = 0; kk < 2; ++kk)
+      {
+        const int c = (warp * 2 + kk) * 16 + t4 * 2;
+        uint32_t a[4];
+        a[0] = *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c);
+        a[1] = *reinterpret_cast<const uint32_t*>(a5 + (g + 8) * kA5Row + c);
+        a[2] = *reinterpret_cast<const uint32_t*>(a5 + g * kA5Row + c + 8);
+        a[3] = *reinterpret_cast<const uint32_t*>(a5 + (g + 8) * kA5Row + c + 8);
+        const __nv_bfloat16* wr = wb + L::f2 + g * 256 + c;
+        const uint32_t b[2] = {__ldg(reinterpret_cast<const unsigned int*>(wr)),
+                               __ldg(reinterpret_cast<const unsigned int*>(wr + 8))};
+        mma_bf16_16816(acc, a, b);
+      }
 #pragma unroll
       for (int h2 = 0; h2 < 2; ++h2)
       {
-        part[(warp * kMlpRows + g + h2 * 8) * 8 + t4 * 2] = acc[h2 * 2];
-        part[(warp * kMlpRows + g + h2 * 8) * 8 + t4 * 2 + 1] = acc[h2 * 2 + 1];
+        part2[(warp * kMlpRows + g + h2 * 8) * 8 + t4 * 2] = acc[h2 * 2];
+        part2[(warp * kMlpRows + g + h2 * 8) * 8 + t4 * 2 + 1] = acc[h2 * 2 + 1];
       }
-      __syncthreads();
-      if (tid < kMlpRows * 8)
+      group_sync(grp);
+      if (gt < kMlpRows * 8)
       {
-        const int row = tid >> 3, co = tid & 7;
+        const int row = gt >> 3, co = gt & 7;
         float sum = 0.f;
 #pragma unroll
-        for (int k = 0; k < 16; ++k) sum += part[(k * kMlpRows + row) * 8 + co];
+        for (int k = 0; k < kGW; ++k) sum += part2[(k * kMlpRows + row) * 8 + co];
         outs[row * 8 + co] = sum + (co < kOut ? params[P::b6 + co] : 0.f);
       }
     }
-    __syncthreads();
-    if (tid < nsub * kT && tile_p0[tid / kT] + tid % kT < n)
+    group_sync(grp);
+    if (gt < nsub * kT && tile_p0[gt / kT] + gt % kT < n)
     {
-      const float* o = outs + tid * 8;
-      dic_poi* dst = pois + tile_p0[tid / kT] + tid % kT;
+      const float* o = outs + gt * 8;
+      dic_poi* dst = pois + tile_p0[gt / kT] + gt % kT;
       dst->u = o[0];
       dst->v = o[1];
       dst->ux = o[2] / out_scale(2);
@@ -923,7 +952,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       dst->u0 = 0.f; dst->v0 = 0.f; dst->zncc = 0.f; dst->iteration = 0.f; dst->convergence = 0.f; dst->feature = 0.f;
     }
     nsub = 0;
-    __syncthreads();
+    group_sync(grp);
   }
 }
 

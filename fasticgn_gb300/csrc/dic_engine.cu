@@ -865,11 +865,11 @@ struct dic_engine
       DIC_CUDA(cudaMemcpyAsync(tmpl.ptr, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, stream));
     mark(kPhProposal, 0);
     {
-      // fused inference: one persistent CTA per SM, kT POIs per tile, seeds into the queue
+      // fused inference: one persistent CTA per SM (two warp groups of kT POIs per tile), seeds into the queue
       int sms = 0;
       DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
       const int64_t tiles = (n + cnn::kT - 1) / cnn::kT;
-      const unsigned grid = (unsigned)std::min<int64_t>(tiles, sms);
+      const unsigned grid = (unsigned)std::min<int64_t>((tiles + cnn::kGroups - 1) / cnn::kGroups, sms);
       cnn::k_proposal_fused<<<grid, cnn::kFusedThreads, cnn::kSmTotal, stream>>>(
           ref_f32.ptr, tar_f32.ptr, w, h, queue.ptr, n, proposal->wb.ptr, proposal->params.ptr);
       check_launch("k_proposal_fused");
@@ -1964,7 +1964,8 @@ int dic_cnn_seed(dic_cnn* c, const float* d_ref, const float* d_tar, int32_t w, 
     DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
     DIC_CUDA(cudaFuncSetAttribute(cnn::k_proposal_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cnn::kSmTotal));
     const int64_t tiles = (n + cnn::kT - 1) / cnn::kT;
-    cnn::k_proposal_fused<<<(unsigned)std::min<int64_t>(tiles, sms), cnn::kFusedThreads, cnn::kSmTotal, c->stream>>>(
+    cnn::k_proposal_fused<<<(unsigned)std::min<int64_t>((tiles + cnn::kGroups - 1) / cnn::kGroups, sms),
+                            cnn::kFusedThreads, cnn::kSmTotal, c->stream>>>(
         d_ref, d_tar, w, h, d_pois, n, c->wb.ptr, c->params.ptr);
     c->check("k_proposal_fused");
     DIC_CUDA(cudaStreamSynchronize(c->stream));
