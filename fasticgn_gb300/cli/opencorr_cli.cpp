@@ -20,9 +20,10 @@
 // bookkeeping, not the numeric path), --dual-gpu (one GPU), --kernel legacy, --fftcc cpu
 // and --temporal-extrapolation.  Asking for them is an error with a message saying so.
 //
-// Host threads: a decode thread reads frame k+1 while frame k is solved (--preload, the
-// default), and a writer thread formats and publishes frame k's payload while frame k+1
-// is solved.  Payload bytes do not depend on either.
+// Host threads and streams: a decode thread reads frame k+1 while frame k is solved
+// (--preload, the default), its upload runs on the engine's upload stream (dic_stage_frame)
+// during that solve, and a writer thread formats and publishes frame k's payload while
+// frame k+1 is solved.  Payload bytes do not depend on any of this.
 #include "dic.h"
 #include "image_io.h"
 
@@ -36,6 +37,7 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <exception>
 #include <filesystem>
 #include <fstream>
 #include <functional>
@@ -1227,23 +1229,46 @@ int run_multi(const std::vector<std::string>& args)
   bool baseline_ready = false;
   float baseline = 0.f;
   long long depth_mismatches = 0;
-  for (size_t k = 0; k < entries.size(); ++k)
-  {
-    writer.check();
-    Samples tar = pre.get(k);
-    if (tar.width != ref.width || tar.height != ref.height)
-      throw std::runtime_error("target " + entries[k].tar_path + " is " + std::to_string(tar.width) + "x" +
-                               std::to_string(tar.height) + ", the reference " + std::to_string(ref.width) + "x" +
+  // Frame k + 1 is decoded (preload thread) and staged (its upload started on the engine's
+  // upload stream) before frame k is solved, so decode, upload and solve overlap.
+  auto check_frame = [&](const Samples& t, size_t k) {
+    if (t.width != ref.width || t.height != ref.height)
+      throw std::runtime_error("target " + entries[k].tar_path + " is " + std::to_string(t.width) + "x" +
+                               std::to_string(t.height) + ", the reference " + std::to_string(ref.width) + "x" +
                                std::to_string(ref.height));
-    if (tar.dtype != ref.dtype || tar.scale != ref.scale)
+    if (t.dtype != ref.dtype || t.scale != ref.scale)
     {
       ++depth_mismatches;
       throw std::runtime_error("target " + entries[k].tar_path + " is not on the reference's grey scale");
     }
+  };
+  auto stage = [&](size_t k) {
+    const Samples t = pre.get(k);
+    check_frame(t, k);
+    eng.check(dic_stage_frame(eng.e, t.data(), t.width, t.height, t.row_bytes(), t.dtype), "stage frame");
+  };
+  stage(0);
+  std::exception_ptr next_failed;   // a bad next frame fails the run after this frame is written
+  for (size_t k = 0; k < entries.size(); ++k)
+  {
+    writer.check();
+    if (next_failed) std::rethrow_exception(next_failed);
+    if (k + 1 < entries.size())
+    {
+      try
+      {
+        stage(k + 1);
+      }
+      catch (...)
+      {
+        next_failed = std::current_exception();
+      }
+    }
     std::vector<dic_poi>& res = bufs[k % bufs.size()];
     dic_frame_report rep{};
     const bool attempted_skip = o.skip_fftcc && k > 0;
-    eng.check(dic_sequence_frame(eng.e, tar.data(), tar.width, tar.height, tar.row_bytes(), tar.dtype, 0, res.data(), &rep),
+    eng.check(dic_sequence_frame(eng.e, nullptr, ref.width, ref.height, ref.row_bytes(), ref.dtype, DIC_PIXELS_STAGED,
+                                 res.data(), &rep),
               "frame");
     FrameRecord f;
     f.tar_path = entries[k].tar_path;

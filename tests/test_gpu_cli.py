@@ -140,3 +140,21 @@ def test_single_frame_raw_and_left_aligned_12_bit(dic, cli, tmp_path, oracle_mod
     diag = (tmp_path / "res" / "pair.bin.diagnostics" / "pair.csv").read_text().splitlines()
     assert diag[0] == "x,y,iteration,convergence,status,zncc" and len(diag) == len(rec) + 1
     assert m["frames"][0]["rows"] == len(rec)
+
+
+def test_bad_frame_keeps_earlier_frames(dic, cli, stream12, tmp_path):
+    """A target that cannot be decoded fails the run (exit 1, status line with the error)
+    after the frames before it are written."""
+    d, ref, tars, _ = stream12
+    bad = tmp_path / "bad.pgm"
+    bad.write_bytes(b"P5\n10 10\n255\n" + b"\x00" * 7)     # truncated
+    lines = [f"{d / 'tar 000.pgm'} frame_000000.csv", f"{d / 'tar 001.pgm'} frame_000001.csv",
+             f"{bad} frame_000002.csv", f"{d / 'tar 003.pgm'} frame_000003.csv"]
+    (tmp_path / "list.txt").write_text("\n".join(lines) + "\n")
+    out = tmp_path / "out"
+    rc, status, err = F.run_cli(cli, ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", tmp_path / "list.txt",
+                                      "--output-dir", out, "12", "8", "--input-depth", "12", "--output-format", "raw"])
+    assert rc == 1 and status["status"] == "error" and "truncated PGM" in status["error"], status
+    assert status["frames_processed"] == 2
+    assert (out / "frame_000000.bin").exists() and (out / "frame_000001.bin").exists()
+    assert not (out / "frame_000002.bin").exists() and not (out / "manifest.opencorr-raw.json").exists()
