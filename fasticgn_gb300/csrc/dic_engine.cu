@@ -696,11 +696,12 @@ struct dic_engine
     switch (2 * r)
     {
 #define DIC_FFTCC_CASE2(M) \
-  case M: k_fftcc<M><<<blocks, 128, 0, stream>>>(p); break;
+  case M: k_fftcc2<M><<<(unsigned)((p.n + 3) / 4), 64, 0, stream>>>(p); break;
       DIC_FFTCC_CASE2(8) DIC_FFTCC_CASE2(10) DIC_FFTCC_CASE2(12) DIC_FFTCC_CASE2(14) DIC_FFTCC_CASE2(16)
       DIC_FFTCC_CASE2(18) DIC_FFTCC_CASE2(20) DIC_FFTCC_CASE2(22) DIC_FFTCC_CASE2(24) DIC_FFTCC_CASE2(26)
-      DIC_FFTCC_CASE2(28) DIC_FFTCC_CASE2(30) DIC_FFTCC_CASE2(32)
+      DIC_FFTCC_CASE2(28) DIC_FFTCC_CASE2(30)
 #undef DIC_FFTCC_CASE2
+      case 32: k_fftcc<32><<<blocks, 128, 0, stream>>>(p); break;
 #define DIC_FFTCC_BIG(M) \
   case M: k_fftcc_big<M><<<(unsigned)p.n, 128, (size_t)M * (M + 1) * sizeof(float2), stream>>>(p); break;
       // 2r = 2 x prime (34, 38, 46, 58, 62) stays on the line-DFT kernel below

@@ -1140,6 +1140,199 @@ __global__ void __launch_bounds__(128) k_fftcc(FftccParams P)
 }
 
 // --------------------------------------------------------------------------------------
+// FFTCC for M <= 30 with two POIs per warp and the Hermitian half of the inverse.
+// The correlation is real, so its spectrum X is Hermitian: after the forward transform only
+// the columns 0..M/2 of conj(X) need the inverse column pass (the others are conjugate
+// mirrors), and the inverse row pass pairs rows (ra, rb) into one complex transform whose
+// real and imaginary parts are the two real output rows.  A warp owns two POIs: the
+// forward passes run once per POI (lane = line), the inverse passes once for both (lanes
+// 0-15 POI 0, 16-31 POI 1), i.e. 3 line passes per POI instead of 4.  Same packing,
+// algebra, tie rule and outputs as k_fftcc (the results differ only in float rounding).
+// --------------------------------------------------------------------------------------
+template <int M>
+__global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
+{
+  static_assert(M % 2 == 0 && M / 2 + 1 <= 16, "16 inverse lanes per POI");
+  constexpr int R = M / 2, S = M + 1;
+  constexpr int kWarps = 2;
+  __shared__ float2 smem[kWarps * 2][M * S];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t i0 = ((int64_t)blockIdx.x * kWarps + warp) * 2;
+  const int w = P.w, h = P.h;
+  bool live[2];
+  float rn[2] = {0.f, 0.f}, tn[2] = {0.f, 0.f};
+  float u_in[2], v_in[2];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+  {
+    const int64_t i = i0 + q;
+    live[q] = queue_slot_active(P, i);
+    u_in[q] = 0.f;
+    v_in[q] = 0.f;
+    if (!live[q]) continue;
+    const dic_poi* poi = P.pois + i;
+    const float px = poi->x, py = poi->y;
+    u_in[q] = poi->u;
+    v_in[q] = poi->v;
+    // out-of-range POIs are left untouched, as the CPU leaves them
+    live[q] = !((int)px < R || (int)px >= w - R || (int)py < R || (int)py >= h - R ||
+                int(px + u_in[q]) < R || int(px + u_in[q]) >= w - R || int(py + v_in[q]) < R ||
+                int(py + v_in[q]) >= h - R);
+    if (!live[q]) continue;
+    float2* z = smem[warp * 2 + q];
+    float rv[M], tv[M];
+    float rsum = 0.f, tsum = 0.f;
+    if (lane < M)
+    {
+      const float fxr = __fsub_rn(__fadd_rn(px, (float)lane), (float)R);
+      const int xr = (int)fxr, xt = (int)__fadd_rn(fxr, u_in[q]);
+#pragma unroll
+      for (int r = 0; r < M; ++r)
+      {
+        const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
+        const int yr = (int)fyr, yt = (int)__fadd_rn(fyr, v_in[q]);
+        rv[r] = P.ref[(size_t)yr * w + xr];
+        tv[r] = P.tar[(size_t)yt * w + xt];
+        rsum += rv[r];
+        tsum += tv[r];
+      }
+    }
+    rsum = warp_sum(rsum);
+    tsum = warp_sum(tsum);
+    const float rmean = rsum / (float)(M * M), tmean = tsum / (float)(M * M);
+    float rnl = 0.f, tnl = 0.f;
+    if (lane < M)
+    {
+#pragma unroll
+      for (int r = 0; r < M; ++r)
+      {
+        rv[r] -= rmean;
+        tv[r] -= tmean;
+        rnl += rv[r] * rv[r];
+        tnl += tv[r] * tv[r];
+        z[r * S + lane] = make_float2(rv[r], tv[r]);
+      }
+    }
+    rn[q] = warp_sum(rnl);
+    tn[q] = warp_sum(tnl);
+  }
+  __syncwarp();
+  // forward rows, then forward columns, one POI at a time (lane = line)
+  float2 a[M], b[M];
+#pragma unroll
+  for (int q = 0; q < 2; ++q)
+  {
+    if (!live[q]) continue;
+    float2* z = smem[warp * 2 + q];
+    if (lane < M)
+    {
+#pragma unroll
+      for (int k = 0; k < M; ++k) a[k] = z[lane * S + k];
+      Fft<M>::run(a, b);
+#pragma unroll
+      for (int k = 0; k < M; ++k) z[lane * S + k] = b[k];
+    }
+    __syncwarp();
+    if (lane < M)
+    {
+#pragma unroll
+      for (int k = 0; k < M; ++k) a[k] = z[k * S + lane];
+      Fft<M>::run(a, b);
+#pragma unroll
+      for (int k = 0; k < M; ++k) z[k * S + lane] = b[k];
+    }
+    __syncwarp();
+  }
+  // inverse columns c = 0..R of conj(X), X = conj(R) T, both POIs at once: lane -> (POI, c)
+  const int q = lane >> 4, c = lane & 15;
+  float2* zq = smem[warp * 2 + q];
+  // selects, not indexing: a lane-dependent index would put the per-POI arrays on the stack
+  const bool live_q = q ? live[1] : live[0];
+  const bool col_live = live_q && c <= R;
+  if (col_live)
+  {
+    const int cm = (M - c) % M;
+#pragma unroll
+    for (int k = 0; k < M; ++k)
+    {
+      const float2 A = zq[k * S + c];
+      const float2 zm = zq[((M - k) % M) * S + cm];
+      const float2 B = make_float2(zm.x, -zm.y);
+      const float2 Rk = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y + B.y));
+      const float2 D = csub(A, B);
+      const float2 Tk = make_float2(0.5f * D.y, -0.5f * D.x);  // D / (2i)
+      const float2 X = make_float2(Rk.x * Tk.x + Rk.y * Tk.y, Rk.x * Tk.y - Rk.y * Tk.x);
+      a[k] = make_float2(X.x, -X.y);
+    }
+    Fft<M>::run(a, b);
+  }
+  __syncwarp();   // every partner column is read before any column is overwritten
+  if (col_live)
+  {
+#pragma unroll
+    for (int k = 0; k < M; ++k) zq[k * S + c] = b[k];
+  }
+  __syncwarp();
+  // inverse rows, rows 2j and 2j + 1 of POI q in one transform; columns past R are the
+  // conjugate mirrors of 1..R-1
+  const int j = c;
+  const bool row_live = live_q && j < R;
+  float best = -2.f;
+  int best_idx = 0;
+  if (row_live)
+  {
+    const int ra = 2 * j, rb = 2 * j + 1;
+#pragma unroll
+    for (int col = 0; col < M; ++col)
+    {
+      float2 va, vb;
+      if (col <= R)
+      {
+        va = zq[ra * S + col];
+        vb = zq[rb * S + col];
+      }
+      else
+      {
+        const float2 ma = zq[ra * S + (M - col)], mb = zq[rb * S + (M - col)];
+        va = make_float2(ma.x, -ma.y);
+        vb = make_float2(mb.x, -mb.y);
+      }
+      a[col] = make_float2(va.x - vb.y, va.y + vb.x);   // va + i vb
+    }
+    Fft<M>::run(a, b);
+    // real part: row ra, imaginary part: row rb (ra first: lower row-major indices)
+#pragma unroll
+    for (int k = 0; k < M; ++k)
+      if (b[k].x > best) { best = b[k].x; best_idx = ra * M + k; }
+#pragma unroll
+    for (int k = 0; k < M; ++k)
+      if (b[k].y > best) { best = b[k].y; best_idx = rb * M + k; }
+  }
+  // argmax over the 16 lanes of each POI (largest value, then lowest index)
+#pragma unroll
+  for (int o = 8; o > 0; o >>= 1)
+  {
+    const float ov = __shfl_xor_sync(kFull, best, o);
+    const int oi = __shfl_xor_sync(kFull, best_idx, o);
+    if (ov > best || (ov == best && oi < best_idx)) { best = ov; best_idx = oi; }
+  }
+  if (c == 0 && live_q)
+  {
+    const float uq = q ? u_in[1] : u_in[0], vq = q ? v_in[1] : v_in[0];
+    const float nq = q ? rn[1] * tn[1] : rn[0] * tn[0];
+    dic_poi* poi = P.pois + i0 + q;
+    int lu = best_idx % M, lv = best_idx / M;
+    if (lu > R) lu -= M;
+    if (lv > R) lv -= M;
+    poi->u = (float)lu + uq;
+    poi->v = (float)lv + vq;
+    poi->u0 = uq;
+    poi->v0 = vq;
+    poi->zncc = best / (sqrtf(nq) * (float)(M * M));
+  }
+}
+
+// --------------------------------------------------------------------------------------
 // FFTCC for 32 < M <= 64 (subset radius 17..32): one 256-thread CTA per POI.  Same packing
 // and cross-power algebra as k_fftcc; each 1-D transform is a direct DFT over one line,
 // with (line, bin) outputs spread over the CTA and twiddles from the constant table.
