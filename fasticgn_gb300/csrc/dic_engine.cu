@@ -478,11 +478,10 @@ struct dic_engine
     if (n > 0)
     {
       mark(kPhPoi, 0);
-      const int wpb = 4;
-      const unsigned blocks = (unsigned)((n + wpb - 1) / wpb);
-      k_poi_prepare<<<blocks, wpb * 32, 0, stream>>>(ref_pack.ptr, w, h, src, n, cfg.subset_radius_x,
-                                                     cfg.subset_radius_y, poi_ref.ptr);
-      check_launch("k_poi_prepare");
+      const unsigned blocks = (unsigned)((n + kPrepPois - 1) / kPrepPois);
+      k_poi_prepare32<<<blocks, kPrepWarps * 32, 0, stream>>>(ref_pack.ptr, w, h, src, n, cfg.subset_radius_x,
+                                                              cfg.subset_radius_y, poi_ref.ptr);
+      check_launch("k_poi_prepare32");
       mark(kPhPoi, 1);
     }
     layout_ready = true;
@@ -1088,9 +1087,9 @@ struct dic_engine
       const int r = J.subset_radius;
       dic_poi* q = bq.ptr + b_first[k];
       DIC_CUDA(cudaMemcpyAsync(q, J.pois, sizeof(dic_poi) * J.count, in_kind, stream));
-      k_poi_prepare<<<(unsigned)((J.count + 3) / 4), 128, 0, stream>>>(M.ref_pack.ptr, J.width, J.height, q,
-                                                                      J.count, r, r, bpoi.ptr + b_first[k]);
-      check_launch("k_poi_prepare");
+      k_poi_prepare32<<<(unsigned)((J.count + kPrepPois - 1) / kPrepPois), kPrepWarps * 32, 0, stream>>>(
+          M.ref_pack.ptr, J.width, J.height, q, J.count, r, r, bpoi.ptr + b_first[k]);
+      check_launch("k_poi_prepare32");
       FftccParams fp{M.ref_f32.ptr, M.tar_f32.ptr, q, J.count, J.width, J.height};
       fftcc_launch(fp, r);
     }

@@ -311,20 +311,22 @@ __device__ __forceinline__ void solve6_column(const float (&a)[6][6], const int 
 // 21 Hessian entries from them once; S and G likewise (S_1 = lx * sum gx, ...).  The
 // target-side sums of k_icgn use the same forms, which keeps the exact self-match.
 // --------------------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ ref_pack, int w, int h,
-                                                     const dic_poi* __restrict__ pois, int64_t n,
-                                                     int rx, int ry, PoiRef* __restrict__ out)
+// Sums of one POI's reference subset, butterfly-reduced so every lane holds them.
+struct PoiSums
 {
-  const int lane = threadIdx.x & 31;
-  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
-  if (i >= n) return;
-  const float px = pois[i].x, py = pois[i].y;
-  PoiRef* rec = out + i;
+  float nsq, src, S[6], G[6], H[21];
+};
+
+// Entry test, mean (written to rec->t0), and the warp-reduced sums of one POI.  Returns false
+// (after writing valid = 0) when the reference subset leaves the image.
+__device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, int w, int h, float px, float py,
+                                         int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums)
+{
   // Entry-test geometry of src/oc_icgn.cpp:184-185.
   if (!(py - ry >= 0 && px - rx >= 0 && py + ry <= h - 1 && px + rx <= w - 1))
   {
     if (lane == 0) rec->valid = 0.f;
-    return;
+    return false;
   }
   const int sw = 2 * rx + 1, size = sw * (2 * ry + 1);
   const int cx = (int)px, cy = (int)py;
@@ -421,39 +423,138 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
   for (int a = 0; a < 6; ++a) { S[a] = warp_sum(S[a]); G[a] = warp_sum(G[a]); }
 #pragma unroll
   for (int t = 0; t < 21; ++t) H[t] = warp_sum(H[t]);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) { out_sums.S[a] = S[a]; out_sums.G[a] = G[a]; }
+#pragma unroll
+  for (int t = 0; t < 21; ++t) out_sums.H[t] = H[t];
+  out_sums.nsq = nsq;
+  out_sums.src = src;
+  return true;
+}
+
+// S and G (lane c < 6 writes entry c, G centred), the norms and valid (lane 0).
+__device__ __forceinline__ void poi_write_sums(const PoiSums& q, int size, int lane, PoiRef* __restrict__ rec)
+{
+  const float m_r = q.src * (1.f / (float)size);
+  if (lane < 6)
+  {
+    float S_l = q.S[0], G_l = q.G[0];
+#pragma unroll
+    for (int a = 1; a < 6; ++a)
+      if (lane == a) { S_l = q.S[a]; G_l = q.G[a]; }
+    rec->S[lane] = S_l;
+    rec->G[lane] = fmaf(-m_r, S_l, G_l);
+  }
+  if (lane == 0)
+  {
+    const float rn_sq = fmaf(-q.src, m_r, q.nsq);
+    rec->ref_norm = sqrtf(rn_sq);
+    rec->ref_norm_sq = rn_sq;
+    rec->sum_rc = q.src;
+    rec->valid = 1.f;
+  }
+}
+
+__global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ ref_pack, int w, int h,
+                                                     const dic_poi* __restrict__ pois, int64_t n,
+                                                     int rx, int ry, PoiRef* __restrict__ out)
+{
+  const int lane = threadIdx.x & 31;
+  const int64_t i = (int64_t)blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (i >= n) return;
+  PoiRef* rec = out + i;
+  PoiSums q;
+  if (!poi_sums(ref_pack, w, h, pois[i].x, pois[i].y, rx, ry, lane, rec, q)) return;
   // Every lane holds the same sums (butterfly reductions), so the LU runs uniformly and
-  // lane c < 6 solves and writes column c of the inverse and entry c of S and G.
+  // lane c < 6 solves and writes column c of the inverse.
+  float hf[6][6];
+  int t = 0;
+#pragma unroll
+  for (int a = 0; a < 6; ++a)
+#pragma unroll
+    for (int b = 0; b <= a; ++b) { hf[a][b] = q.H[t]; hf[b][a] = q.H[t]; ++t; }
+  int perm[6];
+  lu6(hf, perm);
+  if (lane < 6)
+  {
+    float x[6];
+    solve6_column(hf, perm, lane, x);
+#pragma unroll
+    for (int a = 0; a < 6; ++a) rec->inv_h[a * 6 + lane] = x[a];
+  }
+  poi_write_sums(q, (2 * rx + 1) * (2 * ry + 1), lane, rec);
+}
+
+// --------------------------------------------------------------------------------------
+// The same record for 32 POIs per CTA with the inverse batched: four warps form the sums
+// of eight POIs each (poi_sums, as above), the 21 Hessian entries go to shared memory, and
+// warp 0 factorises and inverts all 32 Hessians at once, one POI per lane (the same lu6 /
+// solve6_column code), instead of every warp running one uniform LU per POI.  The inverse
+// leaves through shared memory as one 144 B run per POI.
+// --------------------------------------------------------------------------------------
+constexpr int kPrepPois = 32, kPrepWarps = 4;
+__global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4* __restrict__ ref_pack, int w,
+                                                                  int h, const dic_poi* __restrict__ pois,
+                                                                  int64_t n, int rx, int ry,
+                                                                  PoiRef* __restrict__ out)
+{
+  __shared__ float sh_h[kPrepPois * 21];       // odd stride: lane p reads row p conflict-free
+  __shared__ float sh_inv[kPrepPois * 37];
+  __shared__ int sh_live[kPrepPois];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * kPrepPois;
+  const int size = (2 * rx + 1) * (2 * ry + 1);
+  for (int k = 0; k < kPrepPois / kPrepWarps; ++k)
+  {
+    const int p = warp + kPrepWarps * k;
+    const int64_t i = base + p;
+    bool live = false;
+    if (i < n)
+    {
+      PoiSums q;
+      live = poi_sums(ref_pack, w, h, pois[i].x, pois[i].y, rx, ry, lane, out + i, q);
+      if (live)
+      {
+        poi_write_sums(q, size, lane, out + i);
+        if (lane == 0)
+        {
+#pragma unroll
+          for (int t = 0; t < 21; ++t) sh_h[p * 21 + t] = q.H[t];
+        }
+      }
+    }
+    if (lane == 0) sh_live[p] = live ? 1 : 0;
+  }
+  __syncthreads();
+  if (warp == 0 && sh_live[lane])
   {
     float hf[6][6];
     int t = 0;
 #pragma unroll
     for (int a = 0; a < 6; ++a)
 #pragma unroll
-      for (int b = 0; b <= a; ++b) { hf[a][b] = H[t]; hf[b][a] = H[t]; ++t; }
+      for (int b = 0; b <= a; ++b)
+      {
+        const float v = sh_h[lane * 21 + t];
+        hf[a][b] = v;
+        hf[b][a] = v;
+        ++t;
+      }
     int perm[6];
     lu6(hf, perm);
-    const float m_r = src * (1.f / (float)size);
-    if (lane < 6)
+    for (int c = 0; c < 6; ++c)
     {
       float x[6];
-      solve6_column(hf, perm, lane, x);
+      solve6_column(hf, perm, c, x);
 #pragma unroll
-      for (int a = 0; a < 6; ++a) rec->inv_h[a * 6 + lane] = x[a];
-      float S_l = S[0], G_l = G[0];
-#pragma unroll
-      for (int a = 1; a < 6; ++a)
-        if (lane == a) { S_l = S[a]; G_l = G[a]; }
-      rec->S[lane] = S_l;
-      rec->G[lane] = fmaf(-m_r, S_l, G_l);
+      for (int a = 0; a < 6; ++a) sh_inv[lane * 37 + a * 6 + c] = x[a];
     }
-    if (lane == 0)
-    {
-      const float rn_sq = fmaf(-src, m_r, nsq);
-      rec->ref_norm = sqrtf(rn_sq);
-      rec->ref_norm_sq = rn_sq;
-      rec->sum_rc = src;
-      rec->valid = 1.f;
-    }
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < kPrepPois * 36; idx += kPrepWarps * 32)
+  {
+    const int p = idx / 36, e = idx - p * 36;
+    if (sh_live[p]) out[base + p].inv_h[e] = sh_inv[p * 37 + e];
   }
 }
 
@@ -1145,9 +1246,11 @@ __global__ void __launch_bounds__(128) k_fftcc(FftccParams P)
 // the columns 0..M/2 of conj(X) need the inverse column pass (the others are conjugate
 // mirrors), and the inverse row pass pairs rows (ra, rb) into one complex transform whose
 // real and imaginary parts are the two real output rows.  A warp owns two POIs: the
-// forward passes run once per POI (lane = line), the inverse passes once for both (lanes
-// 0-15 POI 0, 16-31 POI 1), i.e. 3 line passes per POI instead of 4.  Same packing,
-// algebra, tie rule and outputs as k_fftcc (the results differ only in float rounding).
+// forward passes run once per POI (lane = line; the column transform straight from the
+// loaded registers, so the raw subset never goes through shared memory), the inverse
+// passes once for both (lanes 0-15 POI 0, 16-31 POI 1), i.e. 3 line passes per POI instead
+// of 4.  Same packing, algebra, tie rule and outputs as k_fftcc (the results differ only in
+// float rounding: columns are transformed before rows).
 // --------------------------------------------------------------------------------------
 template <int M>
 __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
@@ -1162,6 +1265,9 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
   bool live[2];
   float rn[2] = {0.f, 0.f}, tn[2] = {0.f, 0.f};
   float u_in[2], v_in[2];
+  float2 a[M], b[M];
+  // per POI: load (lane = subset column), zero-mean, forward column transform from the
+  // registers, store; then the forward row transform (lane = row) in place
 #pragma unroll
   for (int q = 0; q < 2; ++q)
   {
@@ -1210,20 +1316,15 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
         tv[r] -= tmean;
         rnl += rv[r] * rv[r];
         tnl += tv[r] * tv[r];
-        z[r * S + lane] = make_float2(rv[r], tv[r]);
+        a[r] = make_float2(rv[r], tv[r]);
       }
+      Fft<M>::run(a, b);
+#pragma unroll
+      for (int k = 0; k < M; ++k) z[k * S + lane] = b[k];
     }
     rn[q] = warp_sum(rnl);
     tn[q] = warp_sum(tnl);
-  }
-  __syncwarp();
-  // forward rows, then forward columns, one POI at a time (lane = line)
-  float2 a[M], b[M];
-#pragma unroll
-  for (int q = 0; q < 2; ++q)
-  {
-    if (!live[q]) continue;
-    float2* z = smem[warp * 2 + q];
+    __syncwarp();
     if (lane < M)
     {
 #pragma unroll
@@ -1231,15 +1332,6 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
       Fft<M>::run(a, b);
 #pragma unroll
       for (int k = 0; k < M; ++k) z[lane * S + k] = b[k];
-    }
-    __syncwarp();
-    if (lane < M)
-    {
-#pragma unroll
-      for (int k = 0; k < M; ++k) a[k] = z[k * S + lane];
-      Fft<M>::run(a, b);
-#pragma unroll
-      for (int k = 0; k < M; ++k) z[k * S + lane] = b[k];
     }
     __syncwarp();
   }
@@ -1273,15 +1365,15 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
     for (int k = 0; k < M; ++k) zq[k * S + c] = b[k];
   }
   __syncwarp();
-  // inverse rows, rows 2j and 2j + 1 of POI q in one transform; columns past R are the
-  // conjugate mirrors of 1..R-1
+  // inverse rows, rows j and j + R of POI q in one transform (with the odd stride S the 16
+  // lanes' rows fall in distinct banks); columns past R are the conjugate mirrors of 1..R-1
   const int j = c;
   const bool row_live = live_q && j < R;
   float best = -2.f;
   int best_idx = 0;
   if (row_live)
   {
-    const int ra = 2 * j, rb = 2 * j + 1;
+    const int ra = j, rb = j + R;
 #pragma unroll
     for (int col = 0; col < M; ++col)
     {

@@ -84,11 +84,13 @@ def check_fftcc(O, ref, tar, radius, gq, oq):
     mism = np.flatnonzero((gq["u"] != ou) | (gq["v"] != ov))
     m = 2 * radius
     for i in mism:
-        cmap = O.fftcc2d_map(ref, tar, radius, float(gq["x"][i]), float(gq["y"][i]))
+        # the map of the window at the initial guess, indexed by the peak offset u - u0
+        u0, v0 = float(gq["u0"][i]), float(gq["v0"][i])
+        cmap = O.fftcc2d_map(ref, tar, radius, float(gq["x"][i]), float(gq["y"][i]), u0, v0)
         assert cmap is not None, f"POI {i}: GPU computed a POI the oracle leaves untouched"
         def val(u, v):
-            lu = int(u) % m
-            lv = int(v) % m
+            lu = int(round(float(u) - u0)) % m
+            lv = int(round(float(v) - v0)) % m
             return cmap[lv, lu]
         peak = cmap.max()
         assert abs(val(gq["u"][i], gq["v"][i]) - val(ou[i], ov[i])) <= 1e-5 * abs(peak), \
