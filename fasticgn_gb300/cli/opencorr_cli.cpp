@@ -13,12 +13,15 @@
 // policy of runMultiFrame / processFrame (:3834-4516, :3024-3210; here run on the device
 // through dic_sequence_*), the 36-byte opencorr-gpu-raw-v1 records (:2498-2536), the CSV
 // rows (:1091-1160), the raw manifest with its engine block and per-frame QA
-// (:2544-2731, :654-723), temp-file + rename publishing, and one JSON status line
-// (schema fasticgn.run-status/1) on stdout at the end of every computing run.
+// (:2544-2731, :654-723), the diagnostics CSV and its manifest (:2734-2800), one JSON status
+// line (schema fasticgn.run-status/1) on stdout at the end of every computing run, and the
+// output ledger (ledger.h): multi-frame runs publish through .opencorr-state/, a rerun of
+// the same command verifies or resumes (replay from frame 1), --repair quarantines damaged
+// files, --durability picks rename or fsync, and --verify-only <dir> audits a directory
+// without computing (:3785-4060, :4613-4760).
 //
-// Not provided: the resume ledger and --verify-only / --repair (output integrity is host
-// bookkeeping, not the numeric path), --dual-gpu (one GPU), --kernel legacy, --fftcc cpu
-// and --temporal-extrapolation.  Asking for them is an error with a message saying so.
+// Not provided: --dual-gpu (one GPU), --kernel legacy, --fftcc cpu and
+// --temporal-extrapolation.  Asking for them is an error with a message saying so.
 //
 // Host threads and streams: a decode thread reads frame k+1 while frame k is solved
 // (--preload, the default), its upload runs on the engine's upload stream (dic_stage_frame)
@@ -26,6 +29,8 @@
 // frame k+1 is solved.  Payload bytes do not depend on any of this.
 #include "dic.h"
 #include "image_io.h"
+#include "json.h"
+#include "ledger.h"
 
 #include <algorithm>
 #include <atomic>
@@ -43,9 +48,12 @@
 #include <functional>
 #include <iostream>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <optional>
+#include <set>
 #include <sstream>
+#include <system_error>
 #include <stdexcept>
 #include <string>
 #include <thread>
@@ -86,6 +94,7 @@ struct Report
   std::vector<std::string> warnings;
   long long skip_fftcc_frames = 0, fallback_frames = 0, poi_fallback_frames = 0, poi_fallback_pois = 0,
             poi_fallback_recovered = 0;
+  long long frames_skipped = 0, resumed_files = 0;
   bool multi = false;
 };
 Report g_report;
@@ -149,7 +158,7 @@ void print_status(int exit_code, double elapsed)
     << ",\"exit_code\":" << exit_code << ",\"error\":" << (g_report.error.empty() ? "null" : jstr(g_report.error))
     << ",\"mode\":" << (g_report.mode.empty() ? "null" : jstr(g_report.mode))
     << ",\"frames_total\":" << g_report.frames_total << ",\"frames_processed\":" << g_report.frames_processed
-    << ",\"frames_skipped\":0";
+    << ",\"frames_skipped\":" << g_report.frames_skipped;
   if (g_report.multi) o << ",\"output_dir\":" << jstr(g_report.output_dir);
   else o << ",\"output_path\":" << jstr(g_report.output_path);
   o << ",\"output_format\":" << jstr(g_report.output_format) << ",\"elapsed_sec\":" << std::round(elapsed * 1000.0) / 1000.0
@@ -162,7 +171,8 @@ void print_status(int exit_code, double elapsed)
       << ",\"poi_fallback_frames\":" << g_report.poi_fallback_frames
       << ",\"poi_fallback_pois\":" << g_report.poi_fallback_pois
       << ",\"poi_fallback_recovered\":" << g_report.poi_fallback_recovered
-      << ",\"temporal_seed_frames\":0,\"temporal_seed_pois\":0,\"resumed_from_existing_files\":0}";
+      << ",\"temporal_seed_frames\":0,\"temporal_seed_pois\":0,\"resumed_from_existing_files\":" << g_report.resumed_files
+      << "}";
   o << ",\"warning_count\":" << g_report.warnings.size() << ",\"warnings\":[";
   for (size_t i = 0; i < g_report.warnings.size() && i < 20; ++i) o << (i ? "," : "") << jstr(g_report.warnings[i]);
   o << "]}";
@@ -186,6 +196,7 @@ struct Options
   std::string diagnostics_dir;
   InputOptions input;
   bool fsync = false;
+  bool repair = false;
   bool quiet = false;
   bool skip_fftcc = true, poi_fallback = true, preload = true;
   int decode_threads = 1;
@@ -344,8 +355,9 @@ bool parse_common(const std::vector<std::string>& a, size_t& i, Options& o, std:
     o.fsync = *v == "fsync";
     return true;
   }
-  if (arg == "--repair") return unsupported("--repair (the resume ledger)");
-  if (arg == "--no-repair" || arg == "--no-temporal-extrapolation") return true;
+  if (arg == "--repair") return o.repair = true, true;
+  if (arg == "--no-repair") return o.repair = false, true;
+  if (arg == "--no-temporal-extrapolation") return true;
   if (arg == "--quiet") return o.quiet = true, true;
   if (arg == "--dual-gpu") return unsupported("--dual-gpu");
   if (arg == "--skip-fftcc") return o.skip_fftcc = true, true;
@@ -487,18 +499,23 @@ void print_usage(std::ostream& out, bool full)
       << "       [--output-roi x1,y1,x2,y2] [--output-step N] [--durability rename|fsync] [--quiet]\n"
       << "   or: " << kTool << " --multi-frame --ref <ref_image> --tar-list <tar_list.txt> --output-dir <output_dir>\n"
       << "       <subset_radius> <grid_space> [the options above] [--skip-fftcc|--no-skip-fftcc]\n"
-      << "       [--poi-fallback|--no-poi-fallback] [--preload|--no-preload] [--decode-threads N]\n"
+      << "       [--poi-fallback|--no-poi-fallback] [--preload|--no-preload] [--decode-threads N] [--repair]\n"
+      << "   or: " << kTool << " --verify-only <output_dir>\n"
       << "   or: " << kTool << " --version\n"
       << "   or: " << kTool << " --help\n"
       << "<subset_radius> is the subset RADIUS in pixels; --subset-size N gives the odd full SIZE instead.\n"
       << "Images: PGM (P5/P2, 8 or 16 bit) and uncompressed grey TIFF.\n"
-      << "stdout: one JSON status line (schema fasticgn.run-status/1) at the end of every computing run.\n";
+      << "stdout: one JSON status line (schema fasticgn.run-status/1) at the end of every computing run;\n"
+      << "  --verify-only prints its own verdict (schema fasticgn.verify-only/1) instead.\n"
+      << "Multi-frame output carries a .opencorr-state/ ledger: rerunning the same command verifies a complete\n"
+      << "  directory without computing, or replays from frame 1 and publishes what is missing; --repair moves\n"
+      << "  damaged files to .opencorr-state/quarantine/ and regenerates them; --verify-only audits a directory.\n";
   if (full)
     out << "Defaults: --max-iter 10, --conv-threshold 0.001, --gpu-device 0, --output-format csv, --input-depth 8,\n"
         << "  --input-normalize none, --skip-fftcc on, --poi-fallback on, --preload on, --durability rename.\n"
-        << "Not available here: --dual-gpu, --kernel legacy, --fftcc cpu, --temporal-extrapolation, --repair,\n"
-        << "  --verify-only (one GPU; the output ledger is not built).\n"
-        << "Exit status: 0 success; 1 any usage, input, compute or output error.\n";
+        << "Not available here: --dual-gpu, --kernel legacy, --fftcc cpu, --temporal-extrapolation (one GPU).\n"
+        << "Exit status: 0 success (--verify-only: the directory is complete and verified); 1 any usage, input,\n"
+        << "  compute or output error (--verify-only: the directory is not complete, or could not be read).\n";
 }
 
 void print_version()
@@ -611,47 +628,11 @@ std::string format_diagnostics(const std::vector<dic_poi>& q)
   return o.str();
 }
 
-// temp file in the destination directory + rename; with fsync also the file and directory
+// a uniquely named temporary in the destination directory, then rename (replaces);
+// with fsync also the file and the directory
 void publish(const fs::path& dst, const char* data, size_t n, bool do_fsync)
 {
-  const fs::path dir = dst.parent_path().empty() ? fs::path(".") : dst.parent_path();
-  const fs::path tmp = dir / (".opencorr-tmp-" + dst.filename().string() + "." + std::to_string(::getpid()));
-  const int fd = ::open(tmp.c_str(), O_WRONLY | O_CREAT | O_TRUNC, 0644);
-  if (fd < 0) throw std::runtime_error("cannot create " + tmp.string());
-  size_t off = 0;
-  while (off < n)
-  {
-    const ssize_t w = ::write(fd, data + off, n - off);
-    if (w < 0)
-    {
-      if (errno == EINTR) continue;
-      ::close(fd);
-      ::unlink(tmp.c_str());
-      throw std::runtime_error("write failed for " + dst.string());
-    }
-    off += (size_t)w;
-  }
-  if (do_fsync && ::fsync(fd) != 0)
-  {
-    ::close(fd);
-    ::unlink(tmp.c_str());
-    throw std::runtime_error("fsync failed for " + dst.string());
-  }
-  if (::close(fd) != 0) throw std::runtime_error("close failed for " + dst.string());
-  if (std::rename(tmp.c_str(), dst.c_str()) != 0)
-  {
-    ::unlink(tmp.c_str());
-    throw std::runtime_error("cannot publish " + dst.string());
-  }
-  if (do_fsync)
-  {
-    const int dfd = ::open(dir.c_str(), O_RDONLY);
-    if (dfd >= 0)
-    {
-      ::fsync(dfd);
-      ::close(dfd);
-    }
-  }
+  publish_file(dst, data, n, true, do_fsync);
 }
 
 // per-frame QA of computeFrameQa (:654-723)
@@ -802,6 +783,41 @@ std::string manifest_json(const std::string& ref_path, const std::string& tar_li
       << ",\"poi_fallback_recovered\":" << q.poi_fallback_recovered
       << ",\"temporal_seed_used\":false,\"temporal_seed_count\":0}" << (i + 1 < frames.size() ? "," : "") << "\n";
   }
+  s << "  ]\n}\n";
+  return s.str();
+}
+
+// diagnosticsPathForFrame (:2802-2807): <output stem>.diagnostics.csv
+fs::path diagnostics_file(const fs::path& dir, const std::string& output_file)
+{
+  return dir / (fs::path(output_file).stem().string() + ".diagnostics.csv");
+}
+
+struct DiagRecord
+{
+  std::string tar_path, output_name, file;
+  size_t rows = 0;
+};
+
+// writeDiagnosticsManifest (:2758-2792)
+std::string diagnostics_manifest_json(const std::string& ref_path, const std::string& tar_list, const Options& o,
+                                      const std::vector<DiagRecord>& frames)
+{
+  std::ostringstream s;
+  s << "{\n"
+    << "  \"format\": \"opencorr-gpu-diagnostics-csv-v1\",\n"
+    << "  \"ref_path\": " << jstr(ref_path) << ",\n"
+    << "  \"tar_list_path\": " << jstr(tar_list) << ",\n"
+    << "  \"status_semantics\": \"1 means zncc>=0 success; negative values mirror failure/status codes carried by "
+       "zncc; non-finite zncc maps to -5\",\n"
+    << "  \"durability\": " << (o.fsync ? "\"fsync\"" : "\"rename\"") << ",\n"
+    << engine_block(o, o.device)
+    << "  \"columns\": [\"x\",\"y\",\"iteration\",\"convergence\",\"status\",\"zncc\"],\n"
+    << "  \"frames\": [\n";
+  for (size_t i = 0; i < frames.size(); ++i)
+    s << "    {\"tar_path\":" << jstr(frames[i].tar_path) << ",\"output_name\":" << jstr(frames[i].output_name)
+      << ",\"file\":" << jstr(frames[i].file) << ",\"rows\":" << frames[i].rows << "}" << (i + 1 < frames.size() ? "," : "")
+      << "\n";
   s << "  ]\n}\n";
   return s.str();
 }
@@ -1089,10 +1105,18 @@ int run_single(const std::vector<std::string>& args)
   }
   if (o.diagnostics)
   {
-    const fs::path d = o.diagnostics_dir.empty() ? fs::path(out_path.string() + ".diagnostics") : fs::path(o.diagnostics_dir);
+    // defaultDiagnosticsDirForSingleFrame (:2794-2800): <output stem>.diagnostics beside the output
+    const fs::path parent = out_path.parent_path();
+    const fs::path dflt = parent.empty() ? fs::path(out_path.stem().string() + ".diagnostics")
+                                         : parent / (out_path.stem().string() + ".diagnostics");
+    const fs::path d = o.diagnostics_dir.empty() ? dflt : fs::path(o.diagnostics_dir);
     fs::create_directories(d);
     const std::string text = format_diagnostics(q);
-    publish(d / (out_path.stem().string() + ".csv"), text.data(), text.size(), o.fsync);
+    const fs::path file = diagnostics_file(d, out_path.filename().string());
+    publish(file, text.data(), text.size(), o.fsync);
+    const std::string m = diagnostics_manifest_json(
+        ref_path, "", o, {DiagRecord{tar_path, out_path.filename().string(), file.filename().string(), q.size()}});
+    publish(d / "manifest.opencorr-diagnostics.json", m.data(), m.size(), o.fsync);
   }
   g_report.frames_processed = 1;
   return 0;
@@ -1129,6 +1153,144 @@ std::vector<ListEntry> load_tar_list(const std::string& path)
     out.push_back(e);
   }
   return out;
+}
+
+void require_utf8(const std::string& what, const std::string& text)
+{
+  if (!valid_utf8(text)) throw std::runtime_error("non-UTF-8 " + what + ": " + text);
+}
+
+// inputIdentity (:3777-3782): canonical path and content fingerprint
+Json input_identity(const std::string& path)
+{
+  const std::string c = fs::canonical(path).string();
+  require_utf8("input path", c);
+  Json j = Json::object();
+  j["path"] = c;
+  j["content"] = file_fingerprint(c);
+  return j;
+}
+
+// validateOutputName (:3784-3792): a unique plain file name, not in the reserved namespace
+void check_output_name(const std::string& name)
+{
+  const fs::path p(name);
+  if (name.empty() || p.filename() != p || name == "." || name == ".." || name.rfind(".opencorr-", 0) == 0 ||
+      std::any_of(name.begin(), name.end(), [](unsigned char c) { return c < 32 || c == 127; }))
+    throw std::runtime_error("output names must be unique plain filenames: " + name);
+  require_utf8("output name", name);
+}
+
+std::string diagnostics_dir_text(const Options& o)
+{
+  return o.diagnostics_dir.empty() ? std::string("default") : fs::weakly_canonical(fs::absolute(o.diagnostics_dir)).string();
+}
+
+// runContract (:3794-3833): everything that decides the output bytes.  Scheduling options
+// (--gpu-device, --threads, --preload, --decode-threads), --durability, --repair and
+// --quiet are not part of it.
+Json run_contract(const std::string& ref_path, const std::vector<ListEntry>& entries, const Positionals& g,
+                  const Options& o, std::vector<std::string>& files)
+{
+  Json c = Json::object();
+  c["schema_version"] = 1;
+  c["git_hash"] = DIC_CLI_GIT_HASH;
+  c["build_date"] = DIC_CLI_BUILD_DATE;
+  c["binary"] = file_fingerprint("/proc/self/exe");
+  c["reference"] = input_identity(ref_path);
+  Json op = Json::object();
+  op["radius"] = g.radius;
+  op["step"] = g.grid;
+  op["dual_gpu"] = false;
+  op["kernel"] = "warp";
+  op["fftcc"] = "gpu";
+  op["max_iteration"] = o.max_iter;
+  op["convergence"] = (double)o.conv;
+  op["skip_fftcc"] = o.skip_fftcc;
+  op["poi_fallback"] = o.poi_fallback;
+  op["temporal_extrapolation"] = false;
+  op["format"] = o.raw ? "raw" : "csv";
+  Json lines = Json::array();
+  for (int y : o.lines) lines.push(y);
+  op["line_ys"] = lines;
+  op["input_depth"] = depth_name(o.input.depth);
+  op["input_align"] = align_name(o.input.align);
+  op["input_normalize"] = normalize_name(o.input.normalize);
+  op["output_roi_enabled"] = o.roi;
+  Json roi = Json::array();
+  for (int v : {o.roi_x1, o.roi_y1, o.roi_x2, o.roi_y2}) roi.push(v);
+  op["output_roi"] = roi;
+  op["output_step"] = o.out_step;
+  op["diagnostics"] = o.diagnostics;
+  op["diagnostics_dir"] = diagnostics_dir_text(o);
+  c["options"] = op;
+  Json targets = Json::array();
+  std::map<std::string, Json> seen;
+  std::set<std::string> names;
+  files.clear();
+  for (const auto& e : entries)
+  {
+    check_output_name(e.output_name);
+    const std::string file = o.raw ? raw_name(e.output_name) : e.output_name;
+    if (!names.insert(file).second) throw std::runtime_error("duplicate output filename: " + file);
+    const std::string path = fs::canonical(e.tar_path).string();
+    auto it = seen.find(path);
+    if (it == seen.end()) it = seen.emplace(path, input_identity(path)).first;
+    Json t = Json::object();
+    t["input"] = it->second;
+    t["output_name"] = e.output_name;
+    t["file"] = file;
+    targets.push(t);
+    files.push_back(file);
+  }
+  c["targets"] = targets;
+  return c;
+}
+
+// An existing manifest must describe a prefix of the requested frames (:4000-4030): a
+// reader takes the frame list from it.
+void check_existing_manifests(const fs::path& root, const fs::path& diag_dir, const std::vector<ListEntry>& entries,
+                              const std::vector<std::string>& files, uint64_t rows, uint64_t diag_rows, const Options& o)
+{
+  const auto same_input = [](const std::string& a, const std::string& b) {
+    std::error_code e1, e2;
+    const fs::path x = fs::weakly_canonical(a, e1), y = fs::weakly_canonical(b, e2);
+    return !e1 && !e2 && x == y;
+  };
+  const fs::path raw_m = root / "manifest.opencorr-raw.json";
+  if (o.raw && fs::exists(raw_m))
+  {
+    const Json m = read_json_file(raw_m);
+    if (!m.is_object() || m.str_or("format", "") != "opencorr-gpu-raw-v1" || !m.has("frames") || !m.at("frames").is_array())
+      throw std::runtime_error("invalid existing raw manifest: unexpected layout");
+    const Json& fr = m.at("frames");
+    if (fr.size() > entries.size()) throw std::runtime_error("existing manifest is not a prefix of this run");
+    for (size_t i = 0; i < fr.size(); ++i)
+    {
+      const Json& f = fr.at(i);
+      if (!f.is_object() || f.str_or("output_name", "") != entries[i].output_name || f.str_or("file", "") != files[i] ||
+          !same_input(f.str_or("tar_path", ""), entries[i].tar_path) || f.u64_or("rows", ~0ull) != rows)
+        throw std::runtime_error("existing raw manifest does not describe the requested frames");
+    }
+  }
+  const fs::path diag_m = diag_dir / "manifest.opencorr-diagnostics.json";
+  if (o.diagnostics && fs::exists(diag_m))
+  {
+    const Json m = read_json_file(diag_m);
+    Json cols = Json::array();
+    for (const char* c : {"x", "y", "iteration", "convergence", "status", "zncc"}) cols.push(c);
+    if (!m.is_object() || m.str_or("format", "") != "opencorr-gpu-diagnostics-csv-v1" || !m.has("columns") ||
+        m.at("columns") != cols || !m.has("frames") || !m.at("frames").is_array() || m.at("frames").size() > entries.size())
+      throw std::runtime_error("invalid diagnostics manifest schema");
+    for (size_t i = 0; i < m.at("frames").size(); ++i)
+    {
+      const Json& f = m.at("frames").at(i);
+      if (!f.is_object() || f.str_or("output_name", "") != entries[i].output_name ||
+          f.str_or("file", "") != diagnostics_file(diag_dir, files[i]).filename().string() ||
+          f.u64_or("rows", ~0ull) != diag_rows)
+        throw std::runtime_error("diagnostics manifest does not describe the requested frames");
+    }
+  }
 }
 
 int run_multi(const std::vector<std::string>& args)
@@ -1194,6 +1356,15 @@ int run_multi(const std::vector<std::string>& args)
   const std::vector<ListEntry> entries = load_tar_list(list_path);
   if (entries.empty()) throw std::runtime_error("tar list is empty");
   g_report.frames_total = (long long)entries.size();
+  // the ledger is JSON: paths and names must be UTF-8, refused before any file exists
+  require_utf8("reference path", ref_path);
+  require_utf8("output directory", fs::absolute(out_dir).string());
+  if (!o.diagnostics_dir.empty()) require_utf8("diagnostics directory", fs::absolute(o.diagnostics_dir).string());
+  for (const auto& e : entries)
+  {
+    require_utf8("target path", e.tar_path);
+    require_utf8("output name", e.output_name);
+  }
   fs::create_directories(out_dir);
 
   Samples ref = configure(read_image(ref_path), o.input, ref_path);
@@ -1203,6 +1374,54 @@ int run_multi(const std::vector<std::string>& args)
   std::vector<dic_poi> tmpl = build_queue(ref.width, ref.height, g.radius, g.grid, o.lines);
   if (tmpl.empty()) throw std::runtime_error("no POIs generated");
   const int64_t n = (int64_t)tmpl.size();
+  uint64_t out_rows = 0;   // rows of every frame payload after --output-roi / --output-step
+  for (const auto& poi : tmpl) out_rows += o.keep((int)poi.x, (int)poi.y) ? 1 : 0;
+
+  // the run record: a rerun of the same command verifies or resumes, anything else is refused
+  const fs::path root(out_dir);
+  const fs::path diag_dir = o.diagnostics ? (o.diagnostics_dir.empty() ? root / "diagnostics" : fs::path(o.diagnostics_dir))
+                                          : fs::path();
+  std::vector<std::string> files;
+  Json contract = run_contract(ref_path, entries, g, o, files);
+  std::vector<LedgerOutput> outs;
+  for (size_t k = 0; k < entries.size(); ++k)
+  {
+    outs.push_back(LedgerOutput{"frame/" + files[k], root / files[k], out_rows, o.raw ? (uint64_t)kRecordBytes : 0});
+    if (o.diagnostics)
+    {
+      const fs::path d = diagnostics_file(diag_dir, files[k]);
+      outs.push_back(LedgerOutput{"diagnostics/" + d.filename().string(), d, (uint64_t)n, 0});
+    }
+  }
+  std::vector<fs::path> manifests;
+  if (o.raw) manifests.push_back(root / "manifest.opencorr-raw.json");
+  if (o.diagnostics) manifests.push_back(diag_dir / "manifest.opencorr-diagnostics.json");
+  RunLedger ledger(root, std::move(contract), std::move(outs), manifests, list_path,
+                   o.fsync ? Durability::Fsync : Durability::Rename, o.repair);
+  if (ledger.quarantined())
+    std::cerr << "Repair: quarantined " << ledger.quarantined() << " damaged file(s) in " << ledger.quarantine_dir().string()
+              << "; they are regenerated by replay" << std::endl;
+  check_existing_manifests(root, diag_dir, entries, files, out_rows, (uint64_t)n, o);
+  ledger.archive_residue();
+  if (ledger.complete())
+  {
+    std::ostringstream mib;
+    mib.setf(std::ios::fixed);
+    mib.precision(1);
+    mib << (double)ledger.verified_bytes() / (1024.0 * 1024.0);
+    std::cerr << "Verified complete run; no computation or output rewrite required (" << ledger.verified_files()
+              << " output files re-read and checked, " << mib.str() << " MiB, plus a full fingerprint of every input)"
+              << std::endl;
+    std::cerr << "Processed frames: 0, skipped: " << entries.size() << std::endl;
+    g_report.frames_skipped = (long long)entries.size();
+    return 0;
+  }
+  ledger.begin();
+  g_report.resumed_files = (long long)ledger.existing_files();
+  if (ledger.existing_files())
+    std::cerr << "Resume: " << ledger.existing_files()
+              << " verified files; replay from frame 1 to restore temporal state (no overwrite)" << std::endl;
+  std::cerr << "Durability: " << (o.fsync ? "fsync" : "rename") << (o.repair ? ", repair: enabled" : "") << std::endl;
   if (!o.quiet)
     std::cerr << "Multi-frame: " << entries.size() << " targets, image " << ref.width << "x" << ref.height << ", radius "
               << g.radius << ", grid " << g.grid << ", " << n << " POIs, skip_fftcc=" << (o.skip_fftcc ? "on" : "off")
@@ -1211,7 +1430,7 @@ int run_multi(const std::vector<std::string>& args)
   Engine eng(g.radius, o, ref.scale);
   eng.check(dic_set_ref(eng.e, ref.data(), ref.width, ref.height, ref.row_bytes(), ref.dtype), "set reference");
   const dic_frame_policy pol{o.skip_fftcc ? 1 : 0, o.poi_fallback ? 1 : 0, kSkipFftccZnccThreshold,
-                             kSkipFftccBadRatioMargin};
+                             kSkipFftccBadRatioMargin, /*learned_seed=*/0};
   eng.check(dic_sequence_begin(eng.e, tmpl.data(), n, &pol), "sequence begin");
 
   std::vector<std::string> paths;
@@ -1221,8 +1440,6 @@ int run_multi(const std::vector<std::string>& args)
   std::vector<FrameRecord> frames(entries.size());
   std::mutex frames_m;
   std::vector<std::vector<dic_poi>> bufs(3, std::vector<dic_poi>((size_t)n));
-  const fs::path diag_dir = o.diagnostics ? (o.diagnostics_dir.empty() ? fs::path(out_dir) / "diagnostics" : fs::path(o.diagnostics_dir))
-                                          : fs::path();
   if (o.diagnostics) fs::create_directories(diag_dir);
   Preloader pre(paths, o.input, o.preload);
   Writer writer;
@@ -1319,7 +1536,7 @@ int run_multi(const std::vector<std::string>& args)
       const double t0 = now_sec();
       Payload p = o.raw ? format_raw(*resp, o) : format_csv(*resp, o);
       const double t1 = now_sec();
-      publish(fs::path(out_dir) / f.file, p.bytes.data(), p.bytes.size(), o.fsync);
+      ledger.publish(root / f.file, p.bytes.data(), p.bytes.size());
       f.rows = p.rows;
       f.bytes = p.bytes.size();
       f.format_sec = t1 - t0;
@@ -1327,7 +1544,7 @@ int run_multi(const std::vector<std::string>& args)
       if (o.diagnostics)
       {
         const std::string text = format_diagnostics(*resp);
-        publish(diag_dir / (fs::path(f.output_name).stem().string() + ".csv"), text.data(), text.size(), o.fsync);
+        ledger.publish(diagnostics_file(diag_dir, f.file), text.data(), text.size());
       }
       std::lock_guard<std::mutex> l(frames_m);
       frames[idx] = f;
@@ -1353,7 +1570,25 @@ int run_multi(const std::vector<std::string>& args)
   if (o.raw)
   {
     const std::string m = manifest_json(ref_path, list_path, out_dir, g.radius, g.grid, o, ref, frames, depth_mismatches);
-    publish(fs::path(out_dir) / "manifest.opencorr-raw.json", m.data(), m.size(), o.fsync);
+    publish(root / "manifest.opencorr-raw.json", m.data(), m.size(), o.fsync);
+  }
+  if (o.diagnostics)
+  {
+    std::vector<DiagRecord> dr;
+    for (size_t k = 0; k < entries.size(); ++k)
+      dr.push_back(DiagRecord{entries[k].tar_path, entries[k].output_name,
+                              diagnostics_file(diag_dir, files[k]).filename().string(), (size_t)n});
+    const std::string m = diagnostics_manifest_json(ref_path, list_path, o, dr);
+    publish(diag_dir / "manifest.opencorr-diagnostics.json", m.data(), m.size(), o.fsync);
+  }
+  ledger.finish();
+  try
+  {
+    ledger.archive_residue();   // after the completion record: a failure here is only a warning
+  }
+  catch (const std::exception& ex)
+  {
+    warning_line(std::string("post-run housekeeping: ") + ex.what());
   }
   if (!o.quiet)
     std::cerr << "Done: " << entries.size() << " frames, skip-FFTCC frames " << g_report.skip_fftcc_frames
@@ -1362,12 +1597,166 @@ int run_multi(const std::vector<std::string>& args)
   return 0;
 }
 
+// ------------------------------------------------------------------ --verify-only
+// auditLayoutFromContract (:4571-4611): the files a contract promises, by the run's naming
+AuditLayout layout_from_contract(const Json& contract, const fs::path& root)
+{
+  AuditLayout l;
+  const Json& op = contract.at("options");
+  const std::string format = op.at("format").as_string();
+  if (format != "csv" && format != "raw") throw std::runtime_error("unknown output format in contract: " + format);
+  const bool raw = format == "raw";
+  const bool diag = op.has("diagnostics") && op.at("diagnostics").is_bool() && op.at("diagnostics").as_bool();
+  fs::path dd;
+  if (diag)
+  {
+    const std::string rec = op.str_or("diagnostics_dir", "default");
+    dd = rec == "default" ? root / "diagnostics" : fs::path(rec);
+  }
+  for (const auto& t : contract.at("targets").items())
+  {
+    const std::string file = t.at("file").as_string();
+    check_output_name(file);
+    l.outputs.push_back(AuditOutput{"frame/" + file, root / file, raw ? (uint64_t)kRecordBytes : 0, true});
+    if (diag)
+    {
+      const fs::path d = diagnostics_file(dd, file);
+      l.outputs.push_back(AuditOutput{"diagnostics/" + d.filename().string(), d, 0, false});
+    }
+  }
+  if (raw) l.manifests.push_back(root / "manifest.opencorr-raw.json");
+  if (diag) l.manifests.push_back(dd / "manifest.opencorr-diagnostics.json");
+  return l;
+}
+
+// runVerifyOnly (:4613-4760): one JSON verdict on stdout, a summary on stderr; computes,
+// creates and moves nothing and opens no GPU.  Exit 0 only for "complete".
+int run_verify(const std::vector<std::string>& args)
+{
+  Json report = Json::object();
+  Json contract;
+  if (args.size() != 2 || args[1].empty())
+  {
+    const std::string msg = "--verify-only takes exactly one argument, the multi-frame output directory (got " +
+                            std::to_string(args.size() - 1) + (args.size() == 2 ? ", empty)" : ")");
+    std::cerr << "Error: " << msg << std::endl;
+    report["status"] = "error";
+    report["complete"] = false;
+    report["output_dir"] = nullptr;
+    report["problems"] = Json::array();
+    report["problems"].push(msg);
+  }
+  else
+    try
+    {
+      report = audit_run_directory(args[1], [&](const Json& found, const fs::path& root) {
+        if (contract.is_null()) contract = found;   // the recorded contract comes first
+        return layout_from_contract(found, root);
+      });
+      // a reader takes the frame list from the raw manifest: it must list exactly the
+      // contract's frames, with the sizes on disk
+      const std::string status = report.at("status").as_string();
+      if ((status == "complete" || status == "inputs_changed") && contract.at("options").at("format").as_string() == "raw")
+      {
+        const fs::path root(report.at("output_dir").as_string());
+        std::string problem;
+        try
+        {
+          const Json m = read_json_file(root / "manifest.opencorr-raw.json");
+          const Json& fr = m.at("frames");
+          const Json& tg = contract.at("targets");
+          if (!fr.is_array())
+            problem = "raw manifest layout is invalid: frames is not an array";
+          else if (fr.size() != tg.size())
+            problem = "raw manifest lists " + std::to_string(fr.size()) + " frames, the contract " + std::to_string(tg.size());
+          else
+            for (size_t i = 0; i < fr.size() && problem.empty(); ++i)
+            {
+              const std::string file = tg.at(i).at("file").as_string();
+              std::error_code ec;
+              const auto size = fs::file_size(root / fr.at(i).str_or("file", ""), ec);
+              if (fr.at(i).str_or("file", "") != file || fr.at(i).str_or("output_name", "") != tg.at(i).at("output_name").as_string() ||
+                  ec || size != fr.at(i).u64_or("bytes", ~0ull))
+                problem = "raw manifest entry " + std::to_string(i + 1) + " does not describe frame file " + file;
+            }
+        }
+        catch (const std::system_error&)
+        {
+          throw;
+        }
+        catch (const std::exception& ex)
+        {
+          problem = std::string("raw manifest layout is invalid: ") + ex.what();
+        }
+        if (!problem.empty())
+        {
+          report["problems"].push(problem);
+          report["status"] = "damaged";
+          report["complete"] = false;
+        }
+      }
+    }
+    catch (const std::system_error& ex)
+    {
+      report["status"] = "error";
+      report["complete"] = false;
+      report["problems"] = Json::array();
+      report["problems"].push(std::string(ex.what()) + " (errno=" + std::to_string(ex.code().value()) + ")");
+    }
+    catch (const std::exception& ex)
+    {
+      report["status"] = "error";
+      report["complete"] = false;
+      report["problems"] = Json::array();
+      report["problems"].push(std::string(ex.what()));
+    }
+  const bool complete = report.has("complete") && report.at("complete").is_bool() && report.at("complete").as_bool();
+  if (!report.has("output_dir")) report["output_dir"] = args.size() > 1 ? Json(args[1]) : Json();
+  // the verdict first, then the counts, then the detail
+  std::string line = "{\"schema\":\"fasticgn.verify-only/1\"";
+  std::set<std::string> done;
+  const auto put = [&](const std::string& k, const Json& v) {
+    line += "," + json_quote(k) + ":" + v.dump();
+    done.insert(k);
+  };
+  for (const char* k : {"status", "complete"})
+    if (report.has(k)) put(k, report.at(k));
+  put("exit_code", Json(complete ? 0 : 1));
+  for (const char* k : {"output_dir", "frames_expected", "frames_verified", "files_expected", "files_verified",
+                        "bytes_verified", "rows_per_frame", "problems", "warnings", "completion", "manifests", "inputs",
+                        "contract"})
+    if (report.has(k)) put(k, report.at(k));
+  for (const auto& m : report.members())
+    if (!done.count(m.first)) put(m.first, m.second);
+  // the binary that checked; the one that wrote the directory is under "contract"
+  put("tool", Json(kTool));
+  put("version", Json(kVersion));
+  put("git_hash", Json(DIC_CLI_GIT_HASH));
+  line += "}";
+  std::cerr << "Verify-only: " << report.str_or("status", "error");
+  if (report.has("frames_expected"))
+    std::cerr << ", " << report.u64_or("frames_verified", 0) << "/" << report.u64_or("frames_expected", 0)
+              << " frames match the ledger";
+  std::cerr << "; nothing was computed or written" << std::endl;
+  if (report.has("problems"))
+    for (const auto& pr : report.at("problems").items()) std::cerr << "  problem: " << pr.as_string() << std::endl;
+  if (report.has("warnings"))
+    for (const auto& w : report.at("warnings").items()) std::cerr << "  note: " << w.as_string() << std::endl;
+  std::cout << line << std::endl;
+  return complete ? 0 : 1;
+}
+
+void collect_warning(const std::string& text) { g_report.warnings.push_back(text); }
+
 }  // namespace
 
 int main(int argc, char** argv)
 {
   const double start = now_sec();
   std::vector<std::string> args(argv + 1, argv + argc);
+  // its one argument may be any directory name (even -h)
+  if (!args.empty() && args[0] == "--verify-only") return run_verify(args);
+  set_warning_sink(collect_warning);
   for (const auto& a : args)
     if (a == "--help" || a == "-h")
     {
@@ -1382,9 +1771,7 @@ int main(int argc, char** argv)
   int rc = 1;
   try
   {
-    if (!args.empty() && args[0] == "--verify-only")
-      error_line("--verify-only is not available in this build (the output ledger is not built)");
-    else if (std::find(args.begin(), args.end(), "--multi-frame") != args.end())
+    if (std::find(args.begin(), args.end(), "--multi-frame") != args.end())
       rc = run_multi(args);
     else if (args.empty())
     {

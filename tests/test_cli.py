@@ -49,7 +49,6 @@ def test_version_and_help(cli):
      "not available"),
     (["--multi-frame", "--ref", "r.pgm", "--tar-list", "l.txt", "--output-dir", "o", "0", "2"], "subset_radius out of range"),
     (["a.pgm", "b.pgm", "7", "2"], "positional"),
-    (["--verify-only", "o"], "--verify-only"),
 ])
 def test_rejected_command_lines(cli, tmp_path, args, needle):
     rc, status, err = F.run_cli(cli, args, cwd=tmp_path)
@@ -57,6 +56,52 @@ def test_rejected_command_lines(cli, tmp_path, args, needle):
     assert status["status"] == "error" and status["exit_code"] == 1 and needle in status["error"], status
     assert any(ln.startswith("Error:") for ln in err.splitlines())
     assert status["schema"] == "fasticgn.run-status/1" and status["tool"] == "opencorr_cli_gb300"
+
+
+def verify_only(cli, *args):
+    p = subprocess.run([str(cli), "--verify-only", *map(str, args)], capture_output=True, text=True)
+    lines = p.stdout.strip().splitlines()
+    assert len(lines) == 1, p.stdout
+    return p.returncode, json.loads(lines[0]), p.stderr
+
+
+def test_verify_only_without_a_run(cli, tmp_path):
+    """--verify-only answers with one JSON verdict (schema fasticgn.verify-only/1) for every
+    invocation and exits 0 only for a complete run."""
+    rc, v, err = verify_only(cli, tmp_path / "nope")
+    assert rc == 1 and v["schema"] == "fasticgn.verify-only/1" and v["status"] == "not_found" and v["exit_code"] == 1
+    rc, v, _ = verify_only(cli, tmp_path)
+    assert rc == 1 and v["status"] == "not_a_run" and v["complete"] is False
+    rc, v, err = verify_only(cli)
+    assert rc == 1 and v["status"] == "error" and v["output_dir"] is None and "exactly one argument" in v["problems"][0]
+    assert err.startswith("Error:")
+    rc, v, _ = verify_only(cli, tmp_path, tmp_path)
+    assert rc == 1 and v["status"] == "error"
+    (tmp_path / "d" / ".opencorr-state").mkdir(parents=True)
+    (tmp_path / "d" / ".opencorr-state" / "contract.json").write_text('{"targets": []')
+    rc, v, _ = verify_only(cli, tmp_path / "d")
+    assert rc == 1 and v["status"] == "damaged" and "not a usable run contract" in v["problems"][0]
+    assert v["tool"] == "opencorr_cli_gb300"
+
+
+def test_multi_frame_ledger_refusals_before_the_gpu(cli, tmp_path):
+    """A dedicated output directory: a stray output file or an unknown entry stops a new run
+    before the engine is created (checked on the CPU; the GPU tests cover runs)."""
+    ref = (np.arange(64 * 48) % 251).astype(np.uint8).reshape(48, 64)
+    F.write_pgm(tmp_path / "ref.pgm", ref)
+    F.write_pgm(tmp_path / "t0.pgm", ref)
+    (tmp_path / "list.txt").write_text(f"{tmp_path / 't0.pgm'} frame_000000.csv\n")
+    out = tmp_path / "out"
+    out.mkdir()
+    (out / "frame_000000.csv").write_text("x,y\n")
+    base = ["--multi-frame", "--ref", tmp_path / "ref.pgm", "--tar-list", tmp_path / "list.txt", "--output-dir", out, "7", "4"]
+    rc, status, err = F.run_cli(cli, base)
+    assert rc == 1 and "existing output has no verified run record" in status["error"], status
+    (out / "frame_000000.csv").unlink()
+    (out / "notes.txt").write_text("n")
+    rc, status, err = F.run_cli(cli, base)
+    assert rc == 1 and "untracked entry in output directory" in status["error"], status
+    assert not (out / ".opencorr-state").exists()        # a refused run records nothing
 
 
 def test_tar_list_errors(cli, tmp_path):

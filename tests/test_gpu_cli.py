@@ -2,6 +2,9 @@
 pipeline reads them), CSV output, single-frame mode, 12-bit input handling, --line and the
 output filters.  Records are checked bit for bit against the engine's own sequence API on
 the same inputs, and the solution against the synthetic truth."""
+import json
+import subprocess
+
 import numpy as np
 import pytest
 
@@ -137,8 +140,13 @@ def test_single_frame_raw_and_left_aligned_12_bit(dic, cli, tmp_path, oracle_mod
     res = C.compare_frame({"u": pois["p"][:, O.P_U], "v": pois["p"][:, O.P_V], "zncc": pois["r"][:, O.R_ZNCC]},
                           {"u": rec["u"], "v": rec["v"], "zncc": rec["zncc"]})
     assert res["pass"], res
-    diag = (tmp_path / "res" / "pair.bin.diagnostics" / "pair.csv").read_text().splitlines()
+    # diagnostics beside the output: <stem>.diagnostics/<stem>.diagnostics.csv plus its manifest
+    ddir = tmp_path / "res" / "pair.diagnostics"
+    diag = (ddir / "pair.diagnostics.csv").read_text().splitlines()
     assert diag[0] == "x,y,iteration,convergence,status,zncc" and len(diag) == len(rec) + 1
+    dm = json.loads((ddir / "manifest.opencorr-diagnostics.json").read_text())
+    assert dm["format"] == "opencorr-gpu-diagnostics-csv-v1" and dm["frames"][0]["file"] == "pair.diagnostics.csv"
+    assert dm["frames"][0]["rows"] == len(rec) and dm["columns"][-1] == "zncc"
     assert m["frames"][0]["rows"] == len(rec)
 
 
@@ -158,3 +166,97 @@ def test_bad_frame_keeps_earlier_frames(dic, cli, stream12, tmp_path):
     assert status["frames_processed"] == 2
     assert (out / "frame_000000.bin").exists() and (out / "frame_000001.bin").exists()
     assert not (out / "frame_000002.bin").exists() and not (out / "manifest.opencorr-raw.json").exists()
+    rc, v, _ = verify(cli, out)
+    assert rc == 1 and v["status"] == "incomplete" and v["frames_verified"] == 2 and v["missing_count"] == 2
+    assert v["manifests"][0]["state"] == "missing" and v["completion"]["state"] == "missing"
+
+
+def verify(cli, d):
+    p = subprocess.run([str(cli), "--verify-only", str(d)], capture_output=True, text=True)
+    return p.returncode, json.loads(p.stdout.strip().splitlines()[-1]), p.stderr
+
+
+def multi_args(d, out, *extra, tar_list=None):
+    return ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", tar_list or d / "tar_list.txt", "--output-dir", out,
+            "12", "8", "--input-depth", "12", "--output-format", "raw", *extra]
+
+
+def snapshot(out):
+    return {p.name: (p.read_bytes(), p.stat().st_ino, p.stat().st_mtime_ns) for p in sorted(out.glob("frame_*.bin"))}
+
+
+def test_ledger_rerun_resume_and_repair(cli, stream12, tmp_path):
+    """The same command again verifies without computing; a deleted frame is replayed bit for
+    bit from frame 1; a corrupt one is refused until --repair quarantines and regenerates it."""
+    d, _, _, _ = stream12
+    out = tmp_path / "out"
+    rc, status, err = F.run_cli(cli, multi_args(d, out))
+    assert rc == 0, err
+    first = snapshot(out)
+    rc, v, _ = verify(cli, out)
+    assert rc == 0 and v["status"] == "complete" and v["frames_verified"] == 6 and v["manifests"][0]["state"] == "ok"
+    assert v["inputs"]["status"] == "match" and v["inputs"]["checked"] == 7
+    # rerun: nothing computed or rewritten
+    rc, status, err = F.run_cli(cli, multi_args(d, out))
+    assert rc == 0 and "Verified complete run" in err, err
+    assert status["frames_processed"] == 0 and status["frames_skipped"] == 6
+    assert snapshot(out) == first
+    # a deleted frame: replay from frame 1, the others keep their inodes
+    (out / "frame_000003.bin").unlink()
+    rc, status, err = F.run_cli(cli, multi_args(d, out))
+    assert rc == 0 and "Resume: 5 verified files" in err, err
+    assert status["totals"]["resumed_from_existing_files"] == 5
+    assert snapshot(out)["frame_000003.bin"][0] == first["frame_000003.bin"][0]
+    assert {k: v[1:] for k, v in snapshot(out).items() if k != "frame_000003.bin"} == \
+           {k: v[1:] for k, v in first.items() if k != "frame_000003.bin"}
+    # a corrupt frame: refused, then repaired
+    b = bytearray((out / "frame_000001.bin").read_bytes())
+    b[40] ^= 0x01
+    (out / "frame_000001.bin").write_bytes(bytes(b))
+    rc, status, err = F.run_cli(cli, multi_args(d, out))
+    assert rc == 1 and "corrupt/truncated output" in status["error"] and "--repair" in status["error"]
+    rc, v, _ = verify(cli, out)
+    assert v["status"] == "damaged" and v["mismatched"] == ["frame_000001.bin"]
+    rc, status, err = F.run_cli(cli, multi_args(d, out, "--repair"))
+    assert rc == 0 and "Repair: quarantined 1" in err, err
+    assert (out / "frame_000001.bin").read_bytes() == first["frame_000001.bin"][0]
+    assert verify(cli, out)[1]["status"] == "complete"
+    # an option that decides the output bytes
+    rc, status, err = F.run_cli(cli, multi_args(d, out, "--max-iter", "11"))
+    assert rc == 1 and "options.max_iteration: 10 -> 11" in status["error"], status
+    # scheduling options and the durability policy are not part of the contract
+    rc, status, err = F.run_cli(cli, multi_args(d, out, "--no-preload", "--durability", "fsync", "--threads", "3"))
+    assert rc == 0 and status["frames_skipped"] == 6, err
+
+
+def test_ledger_append_equals_one_run(cli, stream12, tmp_path):
+    """A target list extended by appending continues the run; its frames equal the frames of
+    one uninterrupted run over the whole list (the replay restores the temporal state)."""
+    d, _, _, _ = stream12
+    whole = tmp_path / "whole"
+    assert F.run_cli(cli, multi_args(d, whole))[0] == 0
+    lines = (d / "tar_list.txt").read_text().splitlines()
+    part = tmp_path / "part"
+    short = tmp_path / "short.txt"
+    short.write_text("\n".join(lines[:4]) + "\n")
+    assert F.run_cli(cli, multi_args(d, part, tar_list=short))[0] == 0
+    rc, status, err = F.run_cli(cli, multi_args(d, part))
+    assert rc == 0 and "Resume: 4 verified files" in err, err
+    assert {k: v[0] for k, v in snapshot(part).items()} == {k: v[0] for k, v in snapshot(whole).items()}
+    assert verify(cli, part)[1]["status"] == "complete"
+    rc, status, _ = F.run_cli(cli, multi_args(d, part, tar_list=short))
+    assert rc == 1 and "a shorter list is not a resume" in status["error"]
+
+
+def test_ledger_diagnostics_csv_run(cli, stream12, tmp_path):
+    d, _, _, _ = stream12
+    out = tmp_path / "csv"
+    args = ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", d / "tar_list.txt", "--output-dir", out, "12", "8",
+            "--input-depth", "12", "--diagnostics", "--quiet"]
+    rc, status, err = F.run_cli(cli, args)
+    assert rc == 0, err
+    files = sorted(p.name for p in (out / "diagnostics").iterdir())
+    assert files == sorted([f"frame_{k:06d}.diagnostics.csv" for k in range(6)] + ["manifest.opencorr-diagnostics.json"])
+    rc, v, _ = verify(cli, out)
+    assert rc == 0 and v["status"] == "complete" and v["files_expected"] == 13   # 6 CSV, 6 diagnostics, 1 manifest
+    assert F.run_cli(cli, args)[2].count("Verified complete run") == 1
