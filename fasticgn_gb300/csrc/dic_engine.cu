@@ -500,7 +500,11 @@ struct dic_engine
   };
   static constexpr int64_t kTuneMinPois = 2048;
   bool autotune = false;
-  IcgnShape shape[2][2] = {{{4, 0, 0.f}, {4, 0, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}}};
+  // Untuned default: the persistent form for single queues too.  The grid form of the
+  // column walk (k_icgn<1, 4>) spills a register inside its row loop under the 7-CTA
+  // register cap (a local store and load per row: 14 % of its L1 wavefronts on the 2048²
+  // pair, 3.73 ms against 3.59 ms persistent); the autotuner still times both forms.
+  IcgnShape shape[2][2] = {{{4, 7, 0.f}, {4, 7, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}}};
   bool tuned[2][2] = {};
   DevBuf<dic_poi> tune_q;
   cudaEvent_t tune_ev[2] = {};

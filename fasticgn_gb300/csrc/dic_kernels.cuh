@@ -1262,41 +1262,45 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t i0 = ((int64_t)blockIdx.x * kWarps + warp) * 2;
   const int w = P.w, h = P.h;
-  bool live[2];
-  float rn[2] = {0.f, 0.f}, tn[2] = {0.f, 0.f};
-  float u_in[2], v_in[2];
+  // per-POI scalars of the two POIs, kept as named registers (the POI loop is not unrolled,
+  // which keeps one copy of the forward transforms in the instruction stream)
+  bool live0 = false, live1 = false;
+  float rn0 = 0.f, rn1 = 0.f, tn0 = 0.f, tn1 = 0.f, uq0 = 0.f, uq1 = 0.f, vq0 = 0.f, vq1 = 0.f;
   float2 a[M], b[M];
   // per POI: load (lane = subset column), zero-mean, forward column transform from the
   // registers, store; then the forward row transform (lane = row) in place
-#pragma unroll
+#pragma unroll 1
   for (int q = 0; q < 2; ++q)
   {
     const int64_t i = i0 + q;
-    live[q] = queue_slot_active(P, i);
-    u_in[q] = 0.f;
-    v_in[q] = 0.f;
-    if (!live[q]) continue;
-    const dic_poi* poi = P.pois + i;
-    const float px = poi->x, py = poi->y;
-    u_in[q] = poi->u;
-    v_in[q] = poi->v;
-    // out-of-range POIs are left untouched, as the CPU leaves them
-    live[q] = !((int)px < R || (int)px >= w - R || (int)py < R || (int)py >= h - R ||
-                int(px + u_in[q]) < R || int(px + u_in[q]) >= w - R || int(py + v_in[q]) < R ||
-                int(py + v_in[q]) >= h - R);
-    if (!live[q]) continue;
+    bool lv = queue_slot_active(P, i);
+    float ui = 0.f, vi = 0.f, px = 0.f, py = 0.f;
+    if (lv)
+    {
+      const dic_poi* poi = P.pois + i;
+      px = poi->x;
+      py = poi->y;
+      ui = poi->u;
+      vi = poi->v;
+      // out-of-range POIs are left untouched, as the CPU leaves them
+      lv = !((int)px < R || (int)px >= w - R || (int)py < R || (int)py >= h - R || int(px + ui) < R ||
+             int(px + ui) >= w - R || int(py + vi) < R || int(py + vi) >= h - R);
+    }
+    if (q == 0) { live0 = lv; uq0 = ui; vq0 = vi; }
+    else { live1 = lv; uq1 = ui; vq1 = vi; }
+    if (!lv) continue;
     float2* z = smem[warp * 2 + q];
     float rv[M], tv[M];
     float rsum = 0.f, tsum = 0.f;
     if (lane < M)
     {
       const float fxr = __fsub_rn(__fadd_rn(px, (float)lane), (float)R);
-      const int xr = (int)fxr, xt = (int)__fadd_rn(fxr, u_in[q]);
+      const int xr = (int)fxr, xt = (int)__fadd_rn(fxr, ui);
 #pragma unroll
       for (int r = 0; r < M; ++r)
       {
         const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
-        const int yr = (int)fyr, yt = (int)__fadd_rn(fyr, v_in[q]);
+        const int yr = (int)fyr, yt = (int)__fadd_rn(fyr, vi);
         rv[r] = P.ref[(size_t)yr * w + xr];
         tv[r] = P.tar[(size_t)yt * w + xt];
         rsum += rv[r];
@@ -1322,8 +1326,9 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
 #pragma unroll
       for (int k = 0; k < M; ++k) z[k * S + lane] = b[k];
     }
-    rn[q] = warp_sum(rnl);
-    tn[q] = warp_sum(tnl);
+    const float rnq = warp_sum(rnl), tnq = warp_sum(tnl);
+    if (q == 0) { rn0 = rnq; tn0 = tnq; }
+    else { rn1 = rnq; tn1 = tnq; }
     __syncwarp();
     if (lane < M)
     {
@@ -1338,8 +1343,7 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
   // inverse columns c = 0..R of conj(X), X = conj(R) T, both POIs at once: lane -> (POI, c)
   const int q = lane >> 4, c = lane & 15;
   float2* zq = smem[warp * 2 + q];
-  // selects, not indexing: a lane-dependent index would put the per-POI arrays on the stack
-  const bool live_q = q ? live[1] : live[0];
+  const bool live_q = q ? live1 : live0;
   const bool col_live = live_q && c <= R;
   if (col_live)
   {
@@ -1410,8 +1414,8 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
   }
   if (c == 0 && live_q)
   {
-    const float uq = q ? u_in[1] : u_in[0], vq = q ? v_in[1] : v_in[0];
-    const float nq = q ? rn[1] * tn[1] : rn[0] * tn[0];
+    const float uq = q ? uq1 : uq0, vq = q ? vq1 : vq0;
+    const float nq = q ? rn1 * tn1 : rn0 * tn0;
     dic_poi* poi = P.pois + i0 + q;
     int lu = best_idx % M, lv = best_idx / M;
     if (lu > R) lu -= M;
