@@ -66,7 +66,7 @@ class DicBatchReport(ctypes.Structure):
 
 class DicLaunchShape(ctypes.Structure):
     _fields_ = [("warps_per_cta", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("tuned", ctypes.c_int32),
-                ("ms", ctypes.c_float)]
+                ("ms", ctypes.c_float), ("tile", ctypes.c_int32)]
 
 
 class DicTuning(ctypes.Structure):
@@ -113,6 +113,7 @@ SIGNATURES = {
     "dic_batch_process": (ctypes.c_int, [_vp, ctypes.POINTER(DicJob), _i32, _i32, ctypes.POINTER(DicBatchReport)]),
     "dic_set_autotune": (ctypes.c_int, [_vp, _i32]),
     "dic_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(DicTuning)]),
+    "dic_set_launch_shape": (ctypes.c_int, [_vp, _i32, ctypes.POINTER(DicLaunchShape)]),
     "dic_read_plane": (ctypes.c_int, [_vp, _i32, _vp, _i64]),
     "dic_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(DicStats)]),
     "dic_set_timing": (ctypes.c_int, [_vp, _i32]),

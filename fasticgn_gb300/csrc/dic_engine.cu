@@ -349,6 +349,7 @@ struct dic_engine
       DIC_CUDA(cudaMemcpyAsync(&iter_sum, counters.ptr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
       DIC_CUDA(cudaStreamSynchronize(stream));
       iter_pending = false;
+      check_tile_error();
     }
   }
 
@@ -452,6 +453,7 @@ struct dic_engine
   {
     DIC_CUDA(cudaMemcpyAsync(pois, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, stream));
     DIC_CUDA(cudaStreamSynchronize(stream));
+    check_tile_error();
   }
   bool layout_matches(const dic_poi* pois, int64_t n) const
   {
@@ -497,7 +499,83 @@ struct dic_engine
     int warps = 4;
     int ctas_per_sm = 7;     // persistent launches: resident CTAs per SM (0: one CTA per kWarps POIs)
     float ms = 0.f;
+    int tile = 0;            // column walk: 0 gathers from the table; 1, 2: k_icgn_tile (kTileKinds)
   };
+  // TMA-staged tile forms: POIs (warps) per CTA, block width and height in texels, CTAs per SM
+  // (shared memory: 4 planes x 16 B per texel, 110.7 KB and 163.9 KB)
+  struct TileKind
+  {
+    int warps, bx, by, ctas;
+  };
+  static constexpr TileKind kTileKinds[3] = {{0, 0, 0, 0}, {4, 48, 36, 2}, {8, 64, 40, 1}};
+  // cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
+  using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                     const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                     CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static EncodeTiledFn encode_tiled()
+  {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+      void* f = nullptr;
+      cudaDriverEntryPointQueryResult q{};
+      if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+          q == cudaDriverEntryPointSuccess)
+        fn = reinterpret_cast<EncodeTiledFn>(f);
+      else
+        cudaGetLastError();
+    });
+    return fn;
+  }
+  struct TileMap
+  {
+    alignas(128) CUtensorMap map;
+    const void* base = nullptr;
+    int w = 0, h = 0;
+  };
+  TileMap tile_maps[3];
+  DevBuf<int> tile_err;        // set by a k_icgn_tile CTA whose copy did not arrive in time
+  bool tile_pending = false;   // a tile launch since the last check
+  // the 4-D map {component, x, y, plane} of a coefficient table, box {4, bx, by, 4}
+  const CUtensorMap& coef_map(int kind, const float4* table, int tw, int th)
+  {
+    TileMap& m = tile_maps[kind];
+    if (m.base == table && m.w == tw && m.h == th) return m.map;
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) throw DicError{DIC_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver"};
+    const TileKind& k = kTileKinds[kind];
+    const cuuint64_t dims[4] = {4, (cuuint64_t)tw, (cuuint64_t)th, 4};
+    const cuuint64_t strides[3] = {sizeof(float4), sizeof(float4) * (cuuint64_t)tw,
+                                   sizeof(float4) * (cuuint64_t)tw * (cuuint64_t)th};
+    const cuuint32_t box[4] = {4, (cuuint32_t)k.bx, (cuuint32_t)k.by, 4};
+    const cuuint32_t estr[4] = {1, 1, 1, 1};
+    const CUresult r = fn(&m.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float4*>(table), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+    {
+      m.base = nullptr;
+      throw DicError{DIC_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")"};
+    }
+    m.base = table;
+    m.w = tw;
+    m.h = th;
+    return m.map;
+  }
+  // after a synchronisation: a tile launch whose copy timed out makes its results invalid
+  void check_tile_error()
+  {
+    if (!tile_pending) return;
+    tile_pending = false;
+    int flag = 0;
+    DIC_CUDA(cudaMemcpyAsync(&flag, tile_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    DIC_CUDA(cudaStreamSynchronize(stream));
+    if (flag)
+    {
+      DIC_CUDA(cudaMemsetAsync(tile_err.ptr, 0, sizeof(int), stream));
+      throw DicError{DIC_ERR_CUDA, "k_icgn_tile: a TMA tile copy did not complete in time; results are invalid"};
+    }
+  }
   static constexpr int64_t kTuneMinPois = 2048;
   bool autotune = false;
   // Untuned default: the persistent form for single queues too.  The grid form of the
@@ -548,9 +626,38 @@ struct dic_engine
   }
   DevBuf<unsigned long long> icgn_next;   // work counter of the persistent single-queue launch
 
+  template <int W, int BX, int BY>
+  void launch_tile(const IcgnParams& p, int kind, int sms)
+  {
+    static std::once_flag attr;
+    std::call_once(attr, [] {
+      DIC_CUDA(cudaFuncSetAttribute(k_icgn_tile<W, BX, BY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)tile_smem_bytes<BX, BY>()));
+    });
+    const CUtensorMap& m = coef_map(kind, p.coef, p.w, p.h);
+    const unsigned grid =
+        (unsigned)std::min<int64_t>((int64_t)sms * kTileKinds[kind].ctas, (p.n + W - 1) / W);
+    k_icgn_tile<W, BX, BY><<<grid, W * 32, tile_smem_bytes<BX, BY>(), stream>>>(p, m, icgn_next.ptr, tile_err.ptr);
+  }
   void launch_icgn(const IcgnParams& p, bool column, const IcgnShape& sh)
   {
     const int warps = sh.warps;
+    if (sh.tile && column)
+    {
+      icgn_next.ensure(1);
+      if (!tile_err.ptr)
+      {
+        tile_err.ensure(1);
+        DIC_CUDA(cudaMemsetAsync(tile_err.ptr, 0, sizeof(int), stream));
+      }
+      DIC_CUDA(cudaMemsetAsync(icgn_next.ptr, 0, sizeof(unsigned long long), stream));
+      int sms = 0;
+      DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+      if (sh.tile == 1) launch_tile<4, 48, 36>(p, 1, sms);
+      else launch_tile<8, 64, 40>(p, 2, sms);
+      tile_pending = true;
+      return;
+    }
     if (sh.ctas_per_sm > 0)
     {
       icgn_next.ensure(1);
@@ -646,18 +753,25 @@ struct dic_engine
     p.iter_sum = nullptr;
     IcgnShape best;
     best.ms = INFINITY;
+    std::vector<IcgnShape> cand;
     for (int warps : {2, 4, 8})
       for (int persistent = 0; persistent < 2; ++persistent)
+        cand.push_back(IcgnShape{warps, persistent ? occupancy_single(column, warps) : 0, 0.f, 0});
+    // the TMA-staged tile forms (column walk, where the driver provides tensor maps)
+    if (column && encode_tiled())
+      for (int kind = 1; kind <= 2; ++kind)
+        cand.push_back(IcgnShape{kTileKinds[kind].warps, kTileKinds[kind].ctas, 0.f, kind});
+    for (const IcgnShape& sh : cand)
+    {
+      float t = INFINITY;
+      for (int rep = 0; rep < 2; ++rep)
       {
-        const IcgnShape sh{warps, persistent ? occupancy_single(column, warps) : 0, 0.f};
-        float t = INFINITY;
-        for (int rep = 0; rep < 2; ++rep)
-        {
-          DIC_CUDA(cudaMemcpyAsync(tune_q.ptr, p0.pois, sizeof(dic_poi) * p0.n, cudaMemcpyDeviceToDevice, stream));
-          t = std::min(t, time_once([&] { launch_icgn(p, column, sh); }));
-        }
-        if (t < best.ms) best = IcgnShape{sh.warps, sh.ctas_per_sm, t};
+        DIC_CUDA(cudaMemcpyAsync(tune_q.ptr, p0.pois, sizeof(dic_poi) * p0.n, cudaMemcpyDeviceToDevice, stream));
+        t = std::min(t, time_once([&] { launch_icgn(p, column, sh); }));
       }
+      if (t < best.ms) best = IcgnShape{sh.warps, sh.ctas_per_sm, t, sh.tile};
+    }
+    check_tile_error();
     shape[0][column] = best;
     tuned[0][column] = true;
   }
@@ -1210,6 +1324,7 @@ struct dic_engine
     FrameCounters c{};
     DIC_CUDA(cudaMemcpyAsync(&c, fcount.ptr, sizeof(c), cudaMemcpyDeviceToHost, stream));
     DIC_CUDA(cudaStreamSynchronize(stream));
+    check_tile_error();
     if (learned)
     {
       // learned seed: "before repair" = POIs the proposal's IC-GN did not bring to ZNCC 0.9
@@ -1677,7 +1792,11 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
     e->icgn_pois = n;
     if (results)
       DIC_CUDA(cudaMemcpyAsync(results, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, e->stream));
-    if (results || report) DIC_CUDA(cudaStreamSynchronize(e->stream));
+    if (results || report)
+    {
+      DIC_CUDA(cudaStreamSynchronize(e->stream));
+      e->check_tile_error();
+    }
     e->fill_report(report, n, use_skip, results, learned);
     ++e->seq_frame;
   });
@@ -1768,8 +1887,40 @@ int dic_get_tuning(dic_engine* e, dic_tuning* out)
         d.ctas_per_sm = s.ctas_per_sm;
         d.tuned = e->tuned[pers][col] ? 1 : 0;
         d.ms = s.ms;
+        d.tile = s.tile;
       }
   }, false);
+}
+
+int dic_set_launch_shape(dic_engine* e, int32_t column_walk, const dic_launch_shape* shape)
+{
+  return guarded(e, [&] {
+    if (!shape) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: null shape"};
+    const int col = column_walk ? 1 : 0;
+    dic_engine::IcgnShape sh;
+    if (shape->tile != 0)
+    {
+      if (shape->tile < 0 || shape->tile > 2 || !col)
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0, or 1 or 2 with the column walk"};
+      const auto& k = dic_engine::kTileKinds[shape->tile];
+      sh = dic_engine::IcgnShape{k.warps, k.ctas, 0.f, shape->tile};
+    }
+    else
+    {
+      if (shape->warps_per_cta != 2 && shape->warps_per_cta != 4 && shape->warps_per_cta != 8)
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: warps_per_cta must be 2, 4 or 8"};
+      if (shape->ctas_per_sm < 0) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: ctas_per_sm must be >= 0"};
+      sh = dic_engine::IcgnShape{shape->warps_per_cta, shape->ctas_per_sm, 0.f, 0};
+    }
+    e->shape[0][col] = sh;
+    e->tuned[0][col] = false;
+    if (e->seq_graph)
+    {
+      // a captured sequence frame holds the previous launch
+      cudaGraphExecDestroy(e->seq_graph);
+      e->seq_graph = nullptr;
+    }
+  });
 }
 
 int dic_set_graphs(dic_engine* e, int32_t enabled)

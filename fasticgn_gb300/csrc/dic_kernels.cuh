@@ -9,7 +9,9 @@
 //   queue              dic_poi records (56 B)
 #pragma once
 
+#include <climits>
 #include <cstdint>
+#include <cuda.h>            // CUtensorMap (the type only; maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include "../../include/dic.h"
@@ -637,6 +639,49 @@ __device__ __forceinline__ float sample_bspline(const float4* __restrict__ coef,
   return fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
 }
 
+// A block of the coefficient table staged in shared memory (k_icgn_tile): texels
+// [ox, ox + bx) x [oy, oy + by) of all four coefficient-row planes, plane-major, rows of bx
+// float4.  Samples whose texel lies outside it are read from the global table; either way
+// the same 16 values enter the same polynomial, so results are bit-identical to
+// sample_bspline.
+struct CoefTile
+{
+  const float4* s = nullptr;
+  int ox = 0, oy = 0, bx = 0, by = 0;
+};
+
+__device__ __forceinline__ float sample_bspline_tile(const CoefTile& T, const float4* __restrict__ coef, size_t plane,
+                                                     int w, float gxp, float gyp)
+{
+  const float fx = floorf(gxp), fy = floorf(gyp);
+  const int ix = (int)fx, iy = (int)fy;
+  const float dx = gxp - fx, dy = gyp - fy;
+  const int tx = ix - T.ox, ty = iy - T.oy;
+  float4 c0, c1, c2, c3;
+  if ((unsigned)tx < (unsigned)T.bx && (unsigned)ty < (unsigned)T.by)
+  {
+    const int pl = T.bx * T.by;
+    const float4* t = T.s + ty * T.bx + tx;
+    c0 = t[0];
+    c1 = t[pl];
+    c2 = t[2 * pl];
+    c3 = t[3 * pl];
+  }
+  else
+  {
+    const float4* c = coef + ((size_t)(iy * w + ix));
+    c0 = __ldg(c);
+    c1 = __ldg(c + plane);
+    c2 = __ldg(c + 2 * plane);
+    c3 = __ldg(c + 3 * plane);
+  }
+  const float r0 = fmaf(fmaf(fmaf(c0.w, dx, c0.z), dx, c0.y), dx, c0.x);
+  const float r1 = fmaf(fmaf(fmaf(c1.w, dx, c1.z), dx, c1.y), dx, c1.x);
+  const float r2 = fmaf(fmaf(fmaf(c2.w, dx, c2.z), dx, c2.y), dx, c2.x);
+  const float r3 = fmaf(fmaf(fmaf(c3.w, dx, c3.z), dx, c3.y), dx, c3.x);
+  return fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
+}
+
 // Rows of the column walk unrolled together (their gathers in flight at once), and the
 // warps per SM the IC-GN launch bounds keep resident (which sets the register budget).
 #ifndef DIC_ICGN_ROW_UNROLL
@@ -649,8 +694,8 @@ constexpr int kIcgnRowUnroll = DIC_ICGN_ROW_UNROLL;
 
 // One POI (queue index i) on the calling warp; shared by the per-queue launch (k_icgn) and
 // the persistent multi-job launch (k_icgn_batch).
-template <bool kColumn>
-__device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int lane)
+template <bool kColumn, bool kTile = false>
+__device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int lane, const CoefTile& T = CoefTile{})
 {
   dic_poi* poi = P.pois + i;
   const float px = poi->x, py = poi->y;
@@ -707,7 +752,11 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
             bad = true;
             continue;
           }
-          const float t = sample_bspline(coef, plane, w, gxp, gyp);
+          float t;
+          if constexpr (kTile)
+            t = sample_bspline_tile(T, coef, plane, w, gxp, gyp);
+          else
+            t = sample_bspline(coef, plane, w, gxp, gyp);
           const float4 rv = __ldg(ref_col + (size_t)r * w);
           const float tau = t - t0;
           const float rc = rv.x - t0;
@@ -870,6 +919,169 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_p
     const int64_t i = (int64_t)__shfl_sync(kFull, t, 0);
     if (!queue_slot_active(P, i)) return;
     icgn_solve<kColumn>(P, i, lane);
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// mbarrier and TMA (cp.async.bulk.tensor) in inline PTX, sm_90 and later.
+// --------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity)
+{
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(done)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// a bounded wait: false when the phase did not complete within `limit` polls
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint32_t limit)
+{
+  for (uint32_t k = 0; k < limit; ++k)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// generic-proxy reads of shared memory ordered before a following async-proxy (TMA) write
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
+      : "memory");
+}
+
+// --------------------------------------------------------------------------------------
+// IC-GN with the target coefficient tile staged in shared memory by TMA (column walk).
+// Persistent CTAs of kWarps warps take chunks of kWarps consecutive queue POIs (for a grid
+// queue: neighbours along a row, whose warped subsets overlap by most of their width).  Per
+// chunk, every warp bounds its POI's warped subset at the incoming warp (corners, plus
+// kTileMargin texels for the updates to come), the CTA takes the union, and one thread
+// loads that BX x BY texel block of all four coefficient planes with one
+// cp.async.bulk.tensor (4-D map {component, x, y, plane}; the innermost coordinate is always
+// 0, other coordinates may be negative: out-of-range texels read as zero and are never
+// sampled, the range test rejects them first).  Warps then solve their POIs reading texels
+// from shared memory (global table outside the block, or for the whole chunk when the union
+// does not fit).  The mbarrier wait is bounded; a timeout is decided for the whole CTA,
+// flagged in `err`, and the CTA waits (bounded) for its copy before it leaves.
+// --------------------------------------------------------------------------------------
+constexpr int kTileMargin = 2;
+constexpr uint32_t kTileWaitPolls = 1u << 22;
+
+// dynamic shared memory of one k_icgn_tile CTA: the block plus room to align it to 128 B
+template <int BX, int BY>
+constexpr size_t tile_smem_bytes() { return (size_t)4 * BX * BY * sizeof(float4) + 128; }
+
+template <int kWarps, int BX, int BY>
+__global__ void __launch_bounds__(kWarps * 32) k_icgn_tile(IcgnParams P, const __grid_constant__ CUtensorMap map,
+                                                           unsigned long long* next, int* err)
+{
+  extern __shared__ unsigned char tile_raw[];
+  // the TMA destination on a 128 B boundary
+  unsigned char* tile_smem = tile_raw + ((128u - (smem_addr(tile_raw) & 127u)) & 127u);
+  __shared__ __align__(8) unsigned long long bar;
+  __shared__ int box[kWarps][4];
+  __shared__ int org[3];
+  __shared__ unsigned long long chunk;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (P.enable && *P.enable == 0) return;
+  const uint32_t bar_a = smem_addr(&bar);
+  if (threadIdx.x == 0) mbar_init(bar_a, 1);
+  __syncthreads();
+  uint32_t parity = 0;
+  const int rx = P.rx, ry = P.ry;
+  for (;;)
+  {
+    if (threadIdx.x == 0) chunk = atomicAdd(next, 1ull);
+    __syncthreads();
+    const int64_t first = (int64_t)chunk * kWarps;
+    if (!queue_slot_active(P, first)) break;   // uniform: every thread read the same chunk
+    const int64_t i = first + warp;
+    const bool active = queue_slot_active(P, i);
+    if (lane == 0)
+    {
+      int b[4] = {INT_MAX, INT_MAX, INT_MIN, INT_MIN};
+      if (active)
+      {
+        const dic_poi* poi = P.pois + i;
+        const float px = poi->x, py = poi->y, u = poi->u, v = poi->v;
+        const float W0 = 1.f + poi->ux, W1 = poi->uy, W3 = poi->vx, W4 = 1.f + poi->vy;
+        // only POIs the solver will sample (its entry test passes a non-negative incoming zncc)
+        if (poi->zncc >= 0.f && isfinite(u) && isfinite(v) && isfinite(W0) && isfinite(W1) && isfinite(W3) &&
+            isfinite(W4) && fabsf(u) < P.w && fabsf(v) < P.h)
+        {
+          float x0 = 3.4e38f, x1 = -3.4e38f, y0 = 3.4e38f, y1 = -3.4e38f;
+#pragma unroll
+          for (int k = 0; k < 4; ++k)
+          {
+            const float lx = (k & 1) ? (float)rx : (float)-rx, ly = (k & 2) ? (float)ry : (float)-ry;
+            const float gx = px + (W0 * lx + W1 * ly + u), gy = py + (W3 * lx + W4 * ly + v);
+            x0 = fminf(x0, gx); x1 = fmaxf(x1, gx);
+            y0 = fminf(y0, gy); y1 = fmaxf(y1, gy);
+          }
+          b[0] = (int)floorf(x0) - kTileMargin;
+          b[1] = (int)floorf(y0) - kTileMargin;
+          b[2] = (int)floorf(x1) + kTileMargin;
+          b[3] = (int)floorf(y1) + kTileMargin;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 4; ++k) box[warp][k] = b[k];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      int u0 = INT_MAX, v0 = INT_MAX, u1 = INT_MIN, v1 = INT_MIN;
+      for (int k = 0; k < kWarps; ++k)
+      {
+        u0 = min(u0, box[k][0]); v0 = min(v0, box[k][1]);
+        u1 = max(u1, box[k][2]); v1 = max(v1, box[k][3]);
+      }
+      const bool fits = u0 <= u1 && (int64_t)u1 - u0 < BX && (int64_t)v1 - v0 < BY;
+      org[0] = fits ? u0 : 0;
+      org[1] = fits ? v0 : 0;
+      org[2] = fits ? 1 : 0;
+      if (fits)
+      {
+        fence_proxy_async_smem();   // the previous chunk's shared-memory reads come first
+        mbar_arrive_expect_tx(bar_a, (uint32_t)(4 * BX * BY * sizeof(float4)));
+        tma_load_4d(smem_addr(tile_smem), &map, 0, u0, v0, 0, bar_a);
+      }
+    }
+    __syncthreads();
+    CoefTile T;
+    T.s = reinterpret_cast<const float4*>(tile_smem);
+    T.bx = BX;
+    T.by = BY;
+    T.ox = org[0];
+    T.oy = org[1];
+    if (org[2])
+    {
+      const bool done = mbar_wait_bounded(bar_a, parity, kTileWaitPolls);
+      parity ^= 1u;
+      if (!__syncthreads_and(done))
+      {
+        if (threadIdx.x == 0) atomicOr(err, 1);
+        mbar_wait_bounded(bar_a, parity ^ 1u, kTileWaitPolls);   // the copy in flight, once more
+        return;
+      }
+    }
+    else
+      T.bx = 0;   // nothing staged: every texel from the global table
+    if (active) icgn_solve<true, true>(P, i, lane, T);
+    __syncthreads();   // every read of this block before the next copy overwrites it
   }
 }
 

@@ -278,6 +278,12 @@ class Engine:
         return {"icgn_flat": shape(t.icgn[0]), "icgn_column": shape(t.icgn[1]),
                 "batch_flat": shape(t.batch[0]), "batch_column": shape(t.batch[1])}
 
+    def set_launch_shape(self, column_walk: bool, warps_per_cta: int = 4, ctas_per_sm: int = 0, tile: int = 0) -> None:
+        """Fixes the single-queue IC-GN launch of one subset walk (dic_set_launch_shape):
+        ``tile`` 1 or 2 selects the TMA-staged coefficient tile forms (column walk only)."""
+        s = _lib.DicLaunchShape(warps_per_cta, ctas_per_sm, 0, 0.0, tile)
+        self._call(self._L.dic_set_launch_shape(self._h, int(bool(column_walk)), ctypes.byref(s)))
+
     def set_graphs(self, enabled: bool) -> None:
         self._call(self._L.dic_set_graphs(self._h, int(bool(enabled))))
 

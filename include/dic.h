@@ -243,6 +243,10 @@ typedef struct dic_launch_shape
                             from an atomic counter; 0: one CTA per warps_per_cta POIs */
   int32_t tuned;
   float ms;              /* best candidate's time, when tuned */
+  int32_t tile;          /* column-walk IC-GN only: 0 gathers texels from the coefficient table;
+                            1 (4 warps, 48x36 texels, 2 CTAs/SM) or 2 (8 warps, 64x40, 1 CTA/SM)
+                            stage the block a chunk of consecutive POIs warps onto in shared memory
+                            by TMA; warps_per_cta and ctas_per_sm then follow the tile kind */
 } dic_launch_shape;
 
 typedef struct dic_tuning
@@ -253,6 +257,12 @@ typedef struct dic_tuning
 
 int dic_set_autotune(dic_engine* engine, int32_t enabled);
 int dic_get_tuning(dic_engine* engine, dic_tuning* out);
+/* No reference counterpart: fixes the single-queue IC-GN launch shape of one subset walk
+ * (column_walk 1: subsets at most 32 wide, 0: wider), e.g. to compare the gather and the
+ * TMA-staged tile forms.  warps_per_cta in {2, 4, 8}, ctas_per_sm >= 0, tile in {0, 1, 2}
+ * (tile > 0 only with column_walk 1); tuned and ms are ignored.  Results do not depend on
+ * the shape.  An enabled autotuner may replace it on the next large queue. */
+int dic_set_launch_shape(dic_engine* engine, int32_t column_walk, const dic_launch_shape* shape);
 
 /* Device-resident variant: pois points to device memory (count records) and the call only
  * enqueues work on the engine stream (dic_get_stats or a stream sync waits for it).  flags

@@ -47,17 +47,19 @@ def test_struct_layouts_match_header(tmp_path):
     from fasticgn_gb300 import _lib
     src = tmp_path / "sizes.c"
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "dic.h"\n'
-                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dic_poi),'
+                   'int main(void){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(dic_poi),'
                    ' sizeof(dic_config), sizeof(dic_stats), sizeof(dic_frame_policy), sizeof(dic_frame_report),'
                    ' offsetof(dic_poi, zncc), offsetof(dic_stats, icgn_iterations), sizeof(dic_job),'
-                   ' offsetof(dic_job, pois), sizeof(dic_batch_report)); return 0;}\n')
+                   ' offsetof(dic_job, pois), sizeof(dic_batch_report), sizeof(dic_launch_shape),'
+                   ' offsetof(dic_launch_shape, tile), sizeof(dic_tuning)); return 0;}\n')
     exe = tmp_path / "sizes"
     subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
     got = list(map(int, subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()))
     want = [_lib.POI_DTYPE.itemsize, ctypes.sizeof(_lib.DicConfig), ctypes.sizeof(_lib.DicStats),
             ctypes.sizeof(_lib.DicFramePolicy), ctypes.sizeof(_lib.DicFrameReport),
             _lib.POI_DTYPE.fields["zncc"][1], _lib.DicStats.icgn_iterations.offset, ctypes.sizeof(_lib.DicJob),
-            _lib.DicJob.pois.offset, ctypes.sizeof(_lib.DicBatchReport)]
+            _lib.DicJob.pois.offset, ctypes.sizeof(_lib.DicBatchReport), ctypes.sizeof(_lib.DicLaunchShape),
+            _lib.DicLaunchShape.tile.offset, ctypes.sizeof(_lib.DicTuning)]
     assert got == want
 
 

@@ -1,0 +1,82 @@
+"""GPU tests of the TMA-staged IC-GN (k_icgn_tile): each POI's result, iteration count and
+flags are bit-identical to the gather form's, whether its chunk's block fits the tile (texels
+from shared memory), partly fits (texels outside it from the global table) or does not fit at
+all (the whole chunk from the global table), also inside a graph-captured sequence frame and
+under the autotuner."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def solve(dic, pr, radius, step, tile=None, autotune=False):
+    q = dic.grid_queue(pr.ref.shape[1], pr.ref.shape[0], radius, step)
+    e = dic.Engine(radius)
+    if tile is not None:
+        e.set_launch_shape(True, tile=tile)
+    e.set_autotune(autotune)
+    e.set_ref(pr.ref)
+    e.set_tar(pr.tar)
+    e.process_pair(q)
+    st = e.stats()
+    tun = e.tuning()
+    e.close()
+    return q, st, tun
+
+
+@pytest.mark.parametrize("radius,step", [(15, 4), (10, 3), (7, 2), (15, 9), (12, 16)])
+def test_tile_forms_equal_gather(dic, radius, step):
+    from fasticgn_gb300 import speckle
+    pr = speckle.pair_bumps(seed=70 + radius, width=384, height=320, max_disp=8.0, max_strain=0.02)
+    want, st0, _ = solve(dic, pr, radius, step)
+    for tile in (1, 2):
+        got, st, tun = solve(dic, pr, radius, step, tile=tile)
+        assert tun["icgn_column"]["tile"] == tile
+        np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8), err_msg=f"tile {tile}")
+        assert st["icgn_iterations"] == st0["icgn_iterations"]
+    if radius >= 10:   # a 14 px FFTCC window (r 7) misses many of the 8 px displacements
+        assert (want["zncc"] >= 0).mean() > 0.9
+
+
+def test_tile_form_in_sequence_graph(dic):
+    from fasticgn_gb300 import speckle
+    ref, frames = speckle.stream_frames(width=320, height=288, frames=200, which=[0, 1, 2, 3])
+    tmpl = dic.grid_queue(320, 288, 15, 5)
+    outs = []
+    for tile in (None, 1):
+        e = dic.Engine(15)
+        e.set_graphs(True)
+        if tile:
+            e.set_launch_shape(True, tile=tile)
+        e.set_ref(ref)
+        e.sequence_begin(tmpl)
+        got = []
+        for _, tar, _ in frames:
+            res = np.zeros_like(tmpl)
+            e.sequence_frame(tar, res)
+            got.append(res)
+        e.close()
+        outs.append(got)
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def test_autotuner_times_tile_forms(dic):
+    from fasticgn_gb300 import speckle
+    pr = speckle.pair_bumps(seed=5, width=512, height=512, max_disp=6.0, max_strain=0.01)
+    want, _, _ = solve(dic, pr, 15, 4)
+    got, _, tun = solve(dic, pr, 15, 4, autotune=True)
+    np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8))
+    t = tun["icgn_column"]
+    assert t["tuned"] == 1 and t["tile"] in (0, 1, 2) and t["ms"] > 0, t
+
+
+def test_launch_shape_arguments(dic):
+    e = dic.Engine(15)
+    for kw in (dict(column_walk=True, tile=3), dict(column_walk=False, tile=1),
+               dict(column_walk=True, warps_per_cta=3), dict(column_walk=True, ctas_per_sm=-1)):
+        with pytest.raises((ValueError, RuntimeError)):
+            e.set_launch_shape(**kw)
+    e.set_launch_shape(True, warps_per_cta=2, ctas_per_sm=0)
+    assert e.tuning()["icgn_column"]["warps_per_cta"] == 2 and e.tuning()["icgn_column"]["tile"] == 0
+    e.close()
