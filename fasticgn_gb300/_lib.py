@@ -43,14 +43,15 @@ class DicConfig(ctypes.Structure):
 class DicFramePolicy(ctypes.Structure):
     _fields_ = [("skip_fftcc", ctypes.c_int32), ("poi_fallback", ctypes.c_int32),
                 ("zncc_threshold", ctypes.c_float), ("frame_fallback_ratio", ctypes.c_float),
-                ("learned_seed", ctypes.c_int32)]
+                ("learned_seed", ctypes.c_int32), ("temporal_extrapolation", ctypes.c_int32)]
 
 
 class DicFrameReport(ctypes.Structure):
     _fields_ = [("pois", ctypes.c_int64), ("bad_before_repair", ctypes.c_int64),
                 ("bad_after_repair", ctypes.c_int64), ("repaired_candidates", ctypes.c_int64),
                 ("frame_fallback_used", ctypes.c_int32), ("fftcc_used", ctypes.c_int32),
-                ("iteration_mean", ctypes.c_double), ("repaired_recovered", ctypes.c_int64)]
+                ("iteration_mean", ctypes.c_double), ("repaired_recovered", ctypes.c_int64),
+                ("temporal_seed_count", ctypes.c_int64)]
 
 
 class DicJob(ctypes.Structure):
@@ -104,6 +105,8 @@ SIGNATURES = {
     "dic_process_pair": (ctypes.c_int, [_vp, _vp, _i64]),
     "dic_process_frame": (ctypes.c_int, [_vp, _vp, _i64, _vp, ctypes.POINTER(DicFramePolicy),
                                          ctypes.POINTER(DicFrameReport)]),
+    "dic_process_frame_history": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, ctypes.POINTER(DicFramePolicy),
+                                                 ctypes.POINTER(DicFrameReport)]),
     "dic_run_device": (ctypes.c_int, [_vp, _vp, _i64, _i32]),
     "dic_sequence_begin": (ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(DicFramePolicy)]),
     "dic_stage_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32]),

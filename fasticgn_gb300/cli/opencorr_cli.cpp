@@ -20,8 +20,8 @@
 // files, --durability picks rename or fsync, and --verify-only <dir> audits a directory
 // without computing (:3785-4060, :4613-4760).
 //
-// Not provided: --dual-gpu (one GPU), --kernel legacy, --fftcc cpu and
-// --temporal-extrapolation.  Asking for them is an error with a message saying so.
+// Not provided: --dual-gpu (one GPU), --kernel legacy and --fftcc cpu.  Asking for them is an
+// error with a message saying so.
 //
 // Host threads and streams: a decode thread reads frame k+1 while frame k is solved
 // (--preload, the default), its upload runs on the engine's upload stream (dic_stage_frame)
@@ -95,6 +95,7 @@ struct Report
   long long skip_fftcc_frames = 0, fallback_frames = 0, poi_fallback_frames = 0, poi_fallback_pois = 0,
             poi_fallback_recovered = 0;
   long long frames_skipped = 0, resumed_files = 0;
+  long long temporal_seed_frames = 0, temporal_seed_pois = 0;
   bool multi = false;
 };
 Report g_report;
@@ -171,7 +172,9 @@ void print_status(int exit_code, double elapsed)
       << ",\"poi_fallback_frames\":" << g_report.poi_fallback_frames
       << ",\"poi_fallback_pois\":" << g_report.poi_fallback_pois
       << ",\"poi_fallback_recovered\":" << g_report.poi_fallback_recovered
-      << ",\"temporal_seed_frames\":0,\"temporal_seed_pois\":0,\"resumed_from_existing_files\":" << g_report.resumed_files
+      << ",\"temporal_seed_frames\":" << g_report.temporal_seed_frames
+      << ",\"temporal_seed_pois\":" << g_report.temporal_seed_pois
+      << ",\"resumed_from_existing_files\":" << g_report.resumed_files
       << "}";
   o << ",\"warning_count\":" << g_report.warnings.size() << ",\"warnings\":[";
   for (size_t i = 0; i < g_report.warnings.size() && i < 20; ++i) o << (i ? "," : "") << jstr(g_report.warnings[i]);
@@ -199,6 +202,7 @@ struct Options
   bool repair = false;
   bool quiet = false;
   bool skip_fftcc = true, poi_fallback = true, preload = true;
+  bool temporal = false;   // --temporal-extrapolation
   int decode_threads = 1;
   bool keep(int x, int y) const
   {
@@ -357,14 +361,14 @@ bool parse_common(const std::vector<std::string>& a, size_t& i, Options& o, std:
   }
   if (arg == "--repair") return o.repair = true, true;
   if (arg == "--no-repair") return o.repair = false, true;
-  if (arg == "--no-temporal-extrapolation") return true;
+  if (arg == "--temporal-extrapolation") return o.temporal = true, true;
+  if (arg == "--no-temporal-extrapolation") return o.temporal = false, true;
   if (arg == "--quiet") return o.quiet = true, true;
   if (arg == "--dual-gpu") return unsupported("--dual-gpu");
   if (arg == "--skip-fftcc") return o.skip_fftcc = true, true;
   if (arg == "--no-skip-fftcc") return o.skip_fftcc = false, true;
   if (arg == "--poi-fallback") return o.poi_fallback = true, true;
   if (arg == "--no-poi-fallback") return o.poi_fallback = false, true;
-  if (arg == "--temporal-extrapolation") return unsupported("--temporal-extrapolation");
   if (arg == "--output-format")
   {
     auto v = value("--output-format");
@@ -499,7 +503,8 @@ void print_usage(std::ostream& out, bool full)
       << "       [--output-roi x1,y1,x2,y2] [--output-step N] [--durability rename|fsync] [--quiet]\n"
       << "   or: " << kTool << " --multi-frame --ref <ref_image> --tar-list <tar_list.txt> --output-dir <output_dir>\n"
       << "       <subset_radius> <grid_space> [the options above] [--skip-fftcc|--no-skip-fftcc]\n"
-      << "       [--poi-fallback|--no-poi-fallback] [--preload|--no-preload] [--decode-threads N] [--repair]\n"
+      << "       [--poi-fallback|--no-poi-fallback] [--temporal-extrapolation] [--preload|--no-preload]\n"
+      << "       [--decode-threads N] [--repair]\n"
       << "   or: " << kTool << " --verify-only <output_dir>\n"
       << "   or: " << kTool << " --version\n"
       << "   or: " << kTool << " --help\n"
@@ -512,8 +517,9 @@ void print_usage(std::ostream& out, bool full)
       << "  damaged files to .opencorr-state/quarantine/ and regenerates them; --verify-only audits a directory.\n";
   if (full)
     out << "Defaults: --max-iter 10, --conv-threshold 0.001, --gpu-device 0, --output-format csv, --input-depth 8,\n"
-        << "  --input-normalize none, --skip-fftcc on, --poi-fallback on, --preload on, --durability rename.\n"
-        << "Not available here: --dual-gpu, --kernel legacy, --fftcc cpu, --temporal-extrapolation (one GPU).\n"
+        << "  --input-normalize none, --skip-fftcc on, --poi-fallback on, --temporal-extrapolation off, --preload on,\n"
+        << "  --durability rename.\n"
+        << "Not available here: --dual-gpu, --kernel legacy, --fftcc cpu (one GPU).\n"
         << "Exit status: 0 success (--verify-only: the directory is complete and verified); 1 any usage, input,\n"
         << "  compute or output error (--verify-only: the directory is not complete, or could not be read).\n";
 }
@@ -647,6 +653,7 @@ struct FrameQa
   float valid_ratio = 0.f, iteration_mean = 0.f;
   int iteration_max = 0;
   long long poi_fallback_count = 0, poi_fallback_recovered = 0;
+  long long temporal_seed_count = 0;
 };
 
 void fill_qa_stats(const std::vector<dic_poi>& q, FrameQa& qa)
@@ -696,7 +703,7 @@ std::string engine_block(const Options& o, int device)
     << "    \"fftcc_backend\": \"gpu\",\n"
     << "    \"skip_fftcc\": " << (o.skip_fftcc ? "true" : "false") << ",\n"
     << "    \"poi_fallback\": " << (o.poi_fallback ? "true" : "false") << ",\n"
-    << "    \"temporal_extrapolation\": false,\n"
+    << "    \"temporal_extrapolation\": " << (o.temporal ? "true" : "false") << ",\n"
     << "    \"frame_fallback_policy\": \"per-poi-merge-v1\",\n"
     << "    \"preload\": " << (o.preload ? "true" : "false") << ",\n"
     << "    \"durability\": " << (o.fsync ? "\"fsync\"" : "\"rename\"") << ",\n"
@@ -781,7 +788,8 @@ std::string manifest_json(const std::string& ref_path, const std::string& tar_li
       << ",\"valid_ratio\":" << json_float(q.valid_ratio) << ",\"iteration_mean\":" << json_float(q.iteration_mean)
       << ",\"iteration_max\":" << q.iteration_max << ",\"poi_fallback_count\":" << q.poi_fallback_count
       << ",\"poi_fallback_recovered\":" << q.poi_fallback_recovered
-      << ",\"temporal_seed_used\":false,\"temporal_seed_count\":0}" << (i + 1 < frames.size() ? "," : "") << "\n";
+      << ",\"temporal_seed_used\":" << (q.temporal_seed_count > 0 ? "true" : "false")
+      << ",\"temporal_seed_count\":" << q.temporal_seed_count << "}" << (i + 1 < frames.size() ? "," : "") << "\n";
   }
   s << "  ]\n}\n";
   return s.str();
@@ -1208,7 +1216,7 @@ Json run_contract(const std::string& ref_path, const std::vector<ListEntry>& ent
   op["convergence"] = (double)o.conv;
   op["skip_fftcc"] = o.skip_fftcc;
   op["poi_fallback"] = o.poi_fallback;
-  op["temporal_extrapolation"] = false;
+  op["temporal_extrapolation"] = o.temporal;
   op["format"] = o.raw ? "raw" : "csv";
   Json lines = Json::array();
   for (int y : o.lines) lines.push(y);
@@ -1430,7 +1438,7 @@ int run_multi(const std::vector<std::string>& args)
   Engine eng(g.radius, o, ref.scale);
   eng.check(dic_set_ref(eng.e, ref.data(), ref.width, ref.height, ref.row_bytes(), ref.dtype), "set reference");
   const dic_frame_policy pol{o.skip_fftcc ? 1 : 0, o.poi_fallback ? 1 : 0, kSkipFftccZnccThreshold,
-                             kSkipFftccBadRatioMargin, /*learned_seed=*/0};
+                             kSkipFftccBadRatioMargin, /*learned_seed=*/0, o.temporal ? 1 : 0};
   eng.check(dic_sequence_begin(eng.e, tmpl.data(), n, &pol), "sequence begin");
 
   std::vector<std::string> paths;
@@ -1510,6 +1518,12 @@ int run_multi(const std::vector<std::string>& args)
     qa.skip_fftcc_used = attempted_skip;
     qa.poi_fallback_count = rep.repaired_candidates;
     qa.poi_fallback_recovered = rep.repaired_recovered;
+    qa.temporal_seed_count = rep.temporal_seed_count;
+    if (rep.temporal_seed_count > 0)
+    {
+      ++g_report.temporal_seed_frames;
+      g_report.temporal_seed_pois += rep.temporal_seed_count;
+    }
     if (attempted_skip) ++g_report.skip_fftcc_frames;
     if (qa.fallback_used)
     {

@@ -884,6 +884,8 @@ struct dic_engine
   // Device queues of the frame policy: tmpl (layout template), prev (previous frame's
   // results), queue (current frame), scratch (whole-frame pass), fq (repair candidates).
   DevBuf<dic_poi> tmpl, prev, scratch, fq;
+  DevBuf<dic_poi> prev2;          // the frame before prev (temporal extrapolation)
+  DevBuf<int> hist;               // sequence: frames of history in prev / prev2 (0, 1, 2)
   DevBuf<int64_t> cand;
   DevBuf<FrameCounters> fcount;
   DevBuf<float> baseline;         // sequence: first frame's bad ratio + margin
@@ -898,6 +900,8 @@ struct dic_engine
   {
     tmpl.ensure((size_t)n);
     prev.ensure((size_t)n);
+    prev2.ensure((size_t)n);
+    hist.ensure(1);
     scratch.ensure((size_t)n);
     fq.ensure((size_t)n);
     cand.ensure((size_t)n);
@@ -910,7 +914,7 @@ struct dic_engine
   // tmpl's.  use_skip: seed from prev and run the policy; otherwise FFTCC + IC-GN from the
   // template.  frame_threshold: device pointer (sequence) or host value.
   void enqueue_frame(int64_t n, bool use_skip, const dic_frame_policy& pol, const float* threshold_dev,
-                     float threshold_host)
+                     float threshold_host, const dic_poi* prev2_dev = nullptr, const int* hist_dev = nullptr)
   {
     const unsigned tb = 256, nb = (unsigned)((n + tb - 1) / tb);
     const float thr = pol.zncc_threshold;
@@ -927,7 +931,8 @@ struct dic_engine
       check_launch("k_count_bad");
       return;
     }
-    k_seed_from_previous<<<nb, tb, 0, stream>>>(tmpl.ptr, prev.ptr, queue.ptr, n);
+    k_seed_from_previous<<<nb, tb, 0, stream>>>(tmpl.ptr, prev.ptr, pol.temporal_extrapolation ? prev2_dev : nullptr,
+                                                hist_dev, thr, (float)cfg.subset_radius_x, queue.ptr, n, fcount.ptr);
     check_launch("k_seed_from_previous");
     run_icgn(queue.ptr, n, nullptr, nullptr, nullptr, false);
     k_scan_bad<<<nb, tb, 0, stream>>>(queue.ptr, prev.ptr, thr, pol.poi_fallback, fcount.ptr, cand.ptr, n);
@@ -1348,6 +1353,7 @@ struct dic_engine
     r->bad_after_repair = (int64_t)c.bad_after;
     r->repaired_candidates = use_skip && c.poi_repair ? (int64_t)c.candidates : 0;
     r->repaired_recovered = use_skip && c.poi_repair ? (int64_t)c.recovered : 0;
+    r->temporal_seed_count = use_skip ? (int64_t)c.temporal : 0;
     r->frame_fallback_used = use_skip ? c.frame_fallback : 0;
     r->fftcc_used = (!use_skip || c.frame_fallback || c.poi_repair) ? 1 : 0;
     double it = 0.0;
@@ -1648,6 +1654,12 @@ int dic_run_device(dic_engine* e, dic_poi* d_pois, int64_t n, int32_t flags)
 int dic_process_frame(dic_engine* e, dic_poi* pois, int64_t n, const dic_poi* prev,
                       const dic_frame_policy* policy, dic_frame_report* report)
 {
+  return dic_process_frame_history(e, pois, n, prev, nullptr, policy, report);
+}
+
+int dic_process_frame_history(dic_engine* e, dic_poi* pois, int64_t n, const dic_poi* prev, const dic_poi* prev_prev,
+                              const dic_frame_policy* policy, dic_frame_report* report)
+{
   return guarded(e, [&] {
     if (n < 0 || (n > 0 && !pois) || !policy) throw DicError{DIC_ERR_ARGUMENT, "process_frame: bad arguments"};
     if (!e->ref_set || !e->tar_set) throw DicError{DIC_ERR_STATE, "images must be set before compute"};
@@ -1661,12 +1673,16 @@ int dic_process_frame(dic_engine* e, dic_poi* pois, int64_t n, const dic_poi* pr
     const bool use_skip = policy->skip_fftcc && prev != nullptr;
     if (use_skip)
       DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, prev, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, e->stream));
+    const bool with_prev2 = use_skip && prev_prev != nullptr && policy->temporal_extrapolation;
+    if (with_prev2)
+      DIC_CUDA(cudaMemcpyAsync(e->prev2.ptr, prev_prev, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, e->stream));
     if (!e->layout_matches(pois, n))
     {
       e->record_layout(pois, n);
       e->prepare_layout_device(e->tmpl.ptr, n);
     }
-    e->enqueue_frame(n, use_skip, *policy, nullptr, policy->frame_fallback_ratio);
+    e->enqueue_frame(n, use_skip, *policy, nullptr, policy->frame_fallback_ratio, with_prev2 ? e->prev2.ptr : nullptr,
+                     nullptr);
     e->iter_pending = true;
     e->download_queue(pois, n);
     e->fill_report(report, n, use_skip, pois);
@@ -1694,6 +1710,7 @@ int dic_sequence_begin(dic_engine* e, const dic_poi* pois, int64_t n, const dic_
     e->prepare_layout_device(e->tmpl.ptr, n);
     const float inf = INFINITY;
     DIC_CUDA(cudaMemcpyAsync(e->baseline.ptr, &inf, sizeof(float), cudaMemcpyHostToDevice, e->stream));
+    DIC_CUDA(cudaMemsetAsync(e->hist.ptr, 0, sizeof(int), e->stream));
     DIC_CUDA(cudaStreamSynchronize(e->stream));
     e->seq_policy = *policy;
     e->seq_n = n;
@@ -1722,13 +1739,26 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
     // the steady-state frame (learned: every frame after the first; skip-FFTCC: every seeded
     // frame): target table, seeds, IC-GN, repair paths behind device switches, merge, count,
     // results -> prev
+    const bool temporal = !learned && pol.temporal_extrapolation != 0;
+    // results -> prev (and, for temporal extrapolation, prev -> prev2 first and one more frame
+    // of history; the seed kernel reads the depth on the device, so a captured frame stays valid)
+    auto shift_history = [&] {
+      if (temporal)
+        DIC_CUDA(cudaMemcpyAsync(e->prev2.ptr, e->prev.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+      if (temporal)
+      {
+        k_bump_history<<<1, 32, 0, e->stream>>>(e->hist.ptr);
+        e->check_launch("k_bump_history");
+      }
+    };
     auto steady = [&] {
       e->ensure_tar();
       if (learned)
         e->enqueue_learned(n, true, pol.zncc_threshold);
       else
-        e->enqueue_frame(n, true, pol, e->baseline.ptr, 0.f);
-      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+        e->enqueue_frame(n, true, pol, e->baseline.ptr, 0.f, e->prev2.ptr, e->hist.ptr);
+      shift_history();
     };
     e->mark(kPhFrame, 0);
     if (!use_skip && !(learned && e->seq_frame > 0))
@@ -1745,7 +1775,7 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
           e->check_launch("k_set_baseline");
         }
       }
-      DIC_CUDA(cudaMemcpyAsync(e->prev.ptr, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, e->stream));
+      shift_history();
     }
     else if (e->use_graphs)
     {

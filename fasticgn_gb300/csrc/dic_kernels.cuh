@@ -2015,6 +2015,7 @@ struct FrameCounters
   int64_t candidate_count;        // = candidates, as a queue length for the repair launches
   int frame_fallback;             // 1: whole-frame pass runs
   int poi_repair;                 // 1: POI-level repair runs
+  unsigned long long temporal;    // POIs seeded by temporal extrapolation
 };
 
 __device__ __forceinline__ bool is_bad_poi(float z, float thr) { return z != -3.f && (!isfinite(z) || z < thr); }
@@ -2026,11 +2027,22 @@ __device__ __forceinline__ bool replace_with_fallback(float cur_z, float fb_z)
   return fb_z >= cur_z;
 }
 
-// seedPoiQueueFromPrevious (:560-624) without temporal extrapolation: the template record,
-// with the previous frame's six first-order parameters where that result is valid and
-// its result fields cleared.
+// isEligibleTemporalSeedHistory (:499-504)
+__device__ __forceinline__ bool temporal_history_ok(const dic_poi& p, float thr)
+{
+  return isfinite(p.u) && isfinite(p.v) && isfinite(p.zncc) && p.zncc >= thr;
+}
+
+// seedPoiQueueFromPrevious (:560-624): the template record, with the previous frame's six
+// first-order parameters where that result is valid and its result fields cleared.  With
+// `prev2` (the frame before; for sequences only once *hist_frames >= 2) and both results
+// eligible at the same location, u and v become prev + (prev - prev2) when that step is at
+// least 0.05 px and neither component's step exceeds max_delta (the subset radius); float
+// arithmetic with separate roundings, as the CPU's expressions read.
 __global__ void k_seed_from_previous(const dic_poi* __restrict__ tmpl, const dic_poi* __restrict__ prev,
-                                     dic_poi* __restrict__ cur, int64_t n)
+                                     const dic_poi* __restrict__ prev2, const int* __restrict__ hist_frames,
+                                     float thr, float max_delta, dic_poi* __restrict__ cur, int64_t n,
+                                     FrameCounters* __restrict__ counters)
 {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -2041,8 +2053,33 @@ __global__ void k_seed_from_previous(const dic_poi* __restrict__ tmpl, const dic
     q.u = p.u; q.ux = p.ux; q.uy = p.uy;
     q.v = p.v; q.vx = p.vx; q.vy = p.vy;
     q.u0 = 0.f; q.v0 = 0.f; q.zncc = 0.f; q.iteration = 0.f; q.convergence = 0.f; q.feature = 0.f;
+    if (prev2 && (!hist_frames || *hist_frames >= 2))
+    {
+      const dic_poi pp = prev2[i];
+      if (p.x == pp.x && p.y == pp.y && p.x == q.x && p.y == q.y && temporal_history_ok(p, thr) &&
+          temporal_history_ok(pp, thr))
+      {
+        constexpr float kMinStep = 0.05f;   // kTemporalSeedMinStepPx (:481)
+        const float du = __fsub_rn(p.u, pp.u), dv = __fsub_rn(p.v, pp.v);
+        const float pu = __fadd_rn(p.u, du), pv = __fadd_rn(p.v, dv);
+        const float step_sq = __fadd_rn(__fmul_rn(du, du), __fmul_rn(dv, dv));
+        if (isfinite(pu) && isfinite(pv) && step_sq >= __fmul_rn(kMinStep, kMinStep) && fabsf(du) <= max_delta &&
+            fabsf(dv) <= max_delta)
+        {
+          q.u = pu;
+          q.v = pv;
+          atomicAdd(&counters->temporal, 1ull);
+        }
+      }
+    }
   }
   cur[i] = q;
+}
+
+// the sequence's history depth (frames whose results are in prev / prev2), saturating at 2
+__global__ void k_bump_history(int* hist_frames)
+{
+  if (threadIdx.x == 0 && *hist_frames < 2) ++*hist_frames;
 }
 
 __global__ void k_scan_bad(const dic_poi* __restrict__ cur, const dic_poi* __restrict__ prev, float thr,

@@ -151,29 +151,37 @@ class Engine:
 
     def process_frame(self, queue: np.ndarray, prev: np.ndarray | None, skip_fftcc: bool = True,
                       poi_fallback: bool = True, zncc_threshold: float = 0.8,
-                      frame_fallback_ratio: float = float("inf")):
+                      frame_fallback_ratio: float = float("inf"), prev_prev: np.ndarray | None = None,
+                      temporal_extrapolation: bool = False):
+        """processFrame: ``prev_prev`` (the frame before ``prev``) feeds the temporal
+        extrapolation seed when ``temporal_extrapolation`` is set."""
         q = _check_queue(queue)
-        prev_ptr = None
-        if prev is not None:
-            prev = _check_queue(prev)
-            if len(prev) != len(q):
+        ptrs = []
+        for h in (prev, prev_prev):
+            if h is None:
+                ptrs.append(None)
+                continue
+            h = _check_queue(h)
+            if len(h) != len(q):
                 raise ValueError("previous results must have one record per POI")
-            prev_ptr = prev.ctypes.data
+            ptrs.append(h.ctypes.data)
         pol = _lib.DicFramePolicy(int(skip_fftcc), int(poi_fallback), float(zncc_threshold),
-                                  float(frame_fallback_ratio))
+                                  float(frame_fallback_ratio), 0, int(bool(temporal_extrapolation)))
         rep = _lib.DicFrameReport()
-        self._call(self._L.dic_process_frame(self._h, q.ctypes.data, len(q), prev_ptr, ctypes.byref(pol),
-                                             ctypes.byref(rep)))
+        self._call(self._L.dic_process_frame_history(self._h, q.ctypes.data, len(q), ptrs[0], ptrs[1],
+                                                     ctypes.byref(pol), ctypes.byref(rep)))
         return q, {f: getattr(rep, f) for f, _ in rep._fields_}
 
     def sequence_begin(self, template: np.ndarray, skip_fftcc: bool = True, poi_fallback: bool = True,
                        zncc_threshold: float = 0.8, frame_fallback_margin: float = 0.03,
-                       learned_seed: bool = False) -> None:
+                       learned_seed: bool = False, temporal_extrapolation: bool = False) -> None:
         """learned_seed: every frame seeded by the attached proposal network (IC-GN capped at
-        6 iterations, FFTCC + IC-GN below ZNCC 0.9) instead of FFTCC / the previous frame."""
+        6 iterations, FFTCC + IC-GN below ZNCC 0.9) instead of FFTCC / the previous frame.
+        temporal_extrapolation: skip-FFTCC frames seed u, v from the previous two results."""
         q = _check_queue(template)
         pol = _lib.DicFramePolicy(int(skip_fftcc), int(poi_fallback), float(zncc_threshold),
-                                  float(frame_fallback_margin), int(bool(learned_seed)))
+                                  float(frame_fallback_margin), int(bool(learned_seed)),
+                                  int(bool(temporal_extrapolation)))
         self._call(self._L.dic_sequence_begin(self._h, q.ctypes.data, len(q), ctypes.byref(pol)))
         self._seq_n = len(q)
 

@@ -79,6 +79,10 @@ typedef struct dic_frame_policy
                                     with the attached proposal network, IC-GN capped at 6
                                     iterations, FFTCC + IC-GN for POIs below ZNCC 0.9; the
                                     skip/repair fields above are then unused */
+  int32_t temporal_extrapolation; /* skip-FFTCC frames with two previous results: seed u, v with
+                                    prev + (prev - prev_prev) where both results are finite with
+                                    zncc >= zncc_threshold, the step is >= 0.05 px and each
+                                    component's step <= the subset radius (:594-616) */
 } dic_frame_policy;
 
 typedef struct dic_frame_report
@@ -91,6 +95,7 @@ typedef struct dic_frame_report
   int32_t fftcc_used;
   double iteration_mean;
   int64_t repaired_recovered;   /* repair candidates replaced and no longer bad (:3004-3020) */
+  int64_t temporal_seed_count;  /* POIs seeded by temporal extrapolation (:3067) */
 } dic_frame_report;
 
 /* Device timings (CUDA events on the engine stream) of the most recent call of each
@@ -166,6 +171,11 @@ int dic_process_pair(dic_engine* engine, dic_poi* pois, int64_t count);
  * IC-GN.  pois holds the POI template on entry and the results on return. */
 int dic_process_frame(dic_engine* engine, dic_poi* pois, int64_t count, const dic_poi* prev_results,
                       const dic_frame_policy* policy, dic_frame_report* report);
+/* processFrame with both histories (:3024-3070): prev_prev_results (count records, the
+ * frame before prev_results) feeds the policy's temporal extrapolation; NULL: none. */
+int dic_process_frame_history(dic_engine* engine, dic_poi* pois, int64_t count, const dic_poi* prev_results,
+                              const dic_poi* prev_prev_results, const dic_frame_policy* policy,
+                              dic_frame_report* report);
 
 /* Fixed-reference sequence (runMultiFrame, opencorr_cli_cuda_mvp.cpp:3834-4516).
  * dic_sequence_begin takes the POI template (buildPoiQueue order) and the policy, builds the

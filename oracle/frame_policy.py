@@ -1,7 +1,7 @@
 """TEST INFRASTRUCTURE: processFrame's seeding and fallback policy restated over the oracle.
 
 Follows opencorr_cli_cuda_mvp.cpp:3024-3210 (processFrame), :560-624 (seedPoiQueueFromPrevious,
-without temporal extrapolation), :490-558 (isBadPoiForFallback, shouldReplacePoiWithFallback,
+with its temporal extrapolation and :481-504 for its thresholds), :490-558 (isBadPoiForFallback, shouldReplacePoiWithFallback,
 shouldTakeFrameFallbackResult, isPoiLevelFallbackCandidate), :2955-3022 (runPoiLevelFallback)
 and the sequence loop's baseline rule :4244-4279.  POIs are oracle POI2D records.
 """
@@ -15,6 +15,7 @@ from . import oracle as O
 
 SKIP_ZNCC = 0.8
 MARGIN = 0.03
+TEMPORAL_MIN_STEP = np.float32(0.05)   # kTemporalSeedMinStepPx (:481)
 
 
 def is_bad(z, thr=SKIP_ZNCC):
@@ -67,28 +68,54 @@ class Solver:
         O.icgn2d1(self.ref, self.gx, self.gy, self.coef, q, self.r, self.conv, self.max_iter, self.threads)
 
 
-def seed_from_previous(template, prev):
+def eligible_history(p, thr=SKIP_ZNCC):
+    """isEligibleTemporalSeedHistory (:499-504)."""
+    u, v, z = float(p["p"][O.P_U]), float(p["p"][O.P_V]), float(p["r"][O.R_ZNCC])
+    return math.isfinite(u) and math.isfinite(v) and math.isfinite(z) and z >= thr
+
+
+def seed_from_previous(template, prev, prev2=None, temporal=False, max_delta=math.inf, thr=SKIP_ZNCC):
+    """seedPoiQueueFromPrevious: returns (queue, POIs seeded by temporal extrapolation).  The
+    extrapolation is the CPU's float arithmetic, one rounding per operation."""
     q = template.copy()
-    for i in range(len(q)):
-        z = float(prev["r"][i, O.R_ZNCC])
-        if not math.isfinite(z) or z < 0.0:
-            continue
-        q["p"][i] = prev["p"][i]
-        q["r"][i] = 0.0
-        q["e"][i] = 0.0
-    return q
+    count = 0
+    f32 = np.float32
+    with np.errstate(over="ignore", invalid="ignore"):
+        for i in range(len(q)):
+            z = float(prev["r"][i, O.R_ZNCC])
+            if not math.isfinite(z) or z < 0.0:
+                continue
+            q["p"][i] = prev["p"][i]
+            if (temporal and prev2 is not None and prev[i]["x"] == prev2[i]["x"] and prev[i]["y"] == prev2[i]["y"]
+                    and prev[i]["x"] == template[i]["x"] and prev[i]["y"] == template[i]["y"]
+                    and eligible_history(prev[i], thr) and eligible_history(prev2[i], thr)):
+                pu, pv = f32(prev["p"][i, O.P_U]), f32(prev["p"][i, O.P_V])
+                du = f32(pu - f32(prev2["p"][i, O.P_U]))
+                dv = f32(pv - f32(prev2["p"][i, O.P_V]))
+                nu, nv = f32(pu + du), f32(pv + dv)
+                step_sq = f32(f32(du * du) + f32(dv * dv))
+                if (math.isfinite(float(nu)) and math.isfinite(float(nv))
+                        and step_sq >= f32(TEMPORAL_MIN_STEP * TEMPORAL_MIN_STEP)
+                        and abs(float(du)) <= max_delta and abs(float(dv)) <= max_delta):
+                    q["p"][i, O.P_U] = nu
+                    q["p"][i, O.P_V] = nv
+                    count += 1
+            q["r"][i] = 0.0
+            q["e"][i] = 0.0
+    return q, count
 
 
-def process_frame(solver, template, prev, skip, poi_fallback=True, threshold=math.inf, thr=SKIP_ZNCC):
+def process_frame(solver, template, prev, skip, poi_fallback=True, threshold=math.inf, thr=SKIP_ZNCC,
+                  prev2=None, temporal=False):
     """Returns (queue, info) as processFrame leaves them."""
-    info = {"frame_fallback": False, "candidates": 0, "bad": 0, "recovered": 0}
+    info = {"frame_fallback": False, "candidates": 0, "bad": 0, "recovered": 0, "temporal": 0}
     if not skip or prev is None:
         q = template.copy()
         solver.fftcc(q)
         solver.icgn(q)
         info["bad"] = sum(is_bad(float(z), thr) for z in q["r"][:, O.R_ZNCC])
         return q, info
-    q = seed_from_previous(template, prev)
+    q, info["temporal"] = seed_from_previous(template, prev, prev2, temporal, float(solver.r), thr)
     solver.icgn(q)
     bad_count = 0
     cands = []
@@ -119,19 +146,21 @@ def process_frame(solver, template, prev, skip, poi_fallback=True, threshold=mat
     return q, info
 
 
-def run_sequence(ref, targets, template, radius, skip=True, poi_fallback=True, threads=None):
+def run_sequence(ref, targets, template, radius, skip=True, poi_fallback=True, threads=None, temporal=False):
     """The multi-frame loop: frame 0 from scratch sets the baseline bad ratio; later frames are
-    seeded from the previous results with threshold = baseline + 0.03."""
+    seeded from the previous results with threshold = baseline + 0.03 (and, with temporal,
+    from the two previous results); the history shifts after every frame (:4376-4377)."""
     solver = Solver(ref, radius, threads=threads)
-    prev = None
+    prev = prev2 = None
     threshold = math.inf
     out = []
     for k, tar in enumerate(targets):
         solver.set_tar(tar)
         use_skip = skip and k > 0
-        q, info = process_frame(solver, template, prev if use_skip else None, use_skip, poi_fallback, threshold)
+        q, info = process_frame(solver, template, prev if use_skip else None, use_skip, poi_fallback, threshold,
+                                prev2=prev2 if use_skip else None, temporal=temporal)
         if skip and k == 0:
             threshold = float(np.float32(np.float32(info["bad"]) / np.float32(len(q))) + np.float32(MARGIN))
         out.append((q, info))
-        prev = q
+        prev2, prev = prev, q
     return out

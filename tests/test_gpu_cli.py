@@ -260,3 +260,42 @@ def test_ledger_diagnostics_csv_run(cli, stream12, tmp_path):
     rc, v, _ = verify(cli, out)
     assert rc == 0 and v["status"] == "complete" and v["files_expected"] == 13   # 6 CSV, 6 diagnostics, 1 manifest
     assert F.run_cli(cli, args)[2].count("Verified complete run") == 1
+
+
+def test_temporal_extrapolation_run(dic, cli, tmp_path):
+    """--temporal-extrapolation: records equal the engine's temporal sequence; the manifest's
+    per-frame QA and the status totals count the extrapolated seeds."""
+    from fasticgn_gb300 import speckle
+    d = tmp_path / "in"
+    d.mkdir()
+    ref, frames = speckle.stream_frames(width=256, height=224, frames=4, which=[0, 1, 2, 3, 4])
+    F.write_pgm(d / "ref.pgm", ref, maxval=4095)
+    lines = []
+    for k, tar, _ in frames:
+        F.write_pgm(d / f"t{k}.pgm", tar, maxval=4095)
+        lines.append(f"{d / f't{k}.pgm'} frame_{k:06d}.csv")
+    (d / "list.txt").write_text("\n".join(lines) + "\n")
+    out = tmp_path / "out"
+    rc, status, err = F.run_cli(cli, ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", d / "list.txt",
+                                      "--output-dir", out, "12", "8", "--input-depth", "12", "--output-format", "raw",
+                                      "--temporal-extrapolation"])
+    assert rc == 0, err
+    m = F.read_manifest(out / "manifest.opencorr-raw.json")
+    assert m["engine"]["temporal_extrapolation"] is True
+    counts = [f["temporal_seed_count"] for f in m["frames"]]
+    assert counts[:2] == [0, 0] and all(c > 0 for c in counts[2:]), counts
+    assert [f["temporal_seed_used"] for f in m["frames"]] == [c > 0 for c in counts]
+    assert status["totals"]["temporal_seed_frames"] == 3 and status["totals"]["temporal_seed_pois"] == sum(counts)
+    tmpl = dic.grid_queue(256, 224, 12, 8)
+    e = dic.Engine(12)
+    e.set_ref(ref)
+    e.sequence_begin(tmpl, temporal_extrapolation=True)
+    for (entry, rec), (_, tar, _) in zip(F.iter_frames(out / "manifest.opencorr-raw.json"), frames):
+        res = np.zeros_like(tmpl)
+        rep = e.sequence_frame(tar, res)
+        np.testing.assert_array_equal(rec["u"], res["u"])
+        np.testing.assert_array_equal(rec["zncc"], res["zncc"])
+        assert entry["temporal_seed_count"] == rep["temporal_seed_count"]
+    e.close()
+    c = json.loads((out / ".opencorr-state" / "contract.json").read_text())
+    assert c["options"]["temporal_extrapolation"] is True

@@ -146,3 +146,88 @@ def test_poi_level_repair(dic, oracle_mod, affine_pair_small):
 def affine_pair_small():
     from fasticgn_gb300 import speckle
     return speckle.pair_affine(seed=3, width=384, height=320)
+
+
+def temporal_stream():
+    from fasticgn_gb300 import speckle
+    # 4 frames to full amplitude: the displacement grows ~0.125 px per frame, so most POIs
+    # take the extrapolated seed from frame 2 on
+    ref, frames = speckle.stream_frames(width=256, height=256, frames=4, which=[0, 1, 2, 3, 4, 5])
+    return ref, [f[1] for f in frames]
+
+
+def test_temporal_sequence_matches_policy_oracle(dic, oracle_mod):
+    """Skip-FFTCC frames seeded by temporal extrapolation from the two previous results
+    (seedPoiQueueFromPrevious, :594-616), against the restated policy frame by frame."""
+    O = oracle_mod
+    from oracle import frame_policy as FP
+    ref, tars = temporal_stream()
+    radius, step = 12, 8
+    tmpl = dic.grid_queue(256, 256, radius, step)
+    e = dic.Engine(radius)
+    e.set_ref(ref)
+    e.sequence_begin(tmpl, temporal_extrapolation=True)
+    got = []
+    for tar in tars:
+        res = np.zeros_like(tmpl)
+        rep = e.sequence_frame(tar, res)
+        got.append((res, rep))
+    e.close()
+    want = FP.run_sequence(ref, tars, to_oracle(O, tmpl), radius, temporal=True)
+    for k, ((g, rep), (w, info)) in enumerate(zip(got, want)):
+        r = C.compare_frame(oracle_fields(O, w), {"u": g["u"], "v": g["v"], "zncc": g["zncc"]})
+        assert r["pass"], (k, r)
+        # the counts depend on results equal to ~1e-6 px: equal up to a POI or two at the thresholds
+        assert abs(rep["temporal_seed_count"] - info["temporal"]) <= 2, (k, rep, info)
+    counts = [rep["temporal_seed_count"] for _, rep in got]
+    assert counts[0] == 0 and counts[1] == 0 and min(counts[2:]) > 0.3 * len(tmpl), counts
+
+
+def test_temporal_graph_equals_eager_and_off_differs(dic):
+    ref, tars = temporal_stream()
+    tmpl = dic.grid_queue(256, 256, 12, 8)
+    outs = {}
+    for graphs, temporal in ((True, True), (False, True), (True, False)):
+        e = dic.Engine(12)
+        e.set_graphs(graphs)
+        e.set_ref(ref)
+        e.sequence_begin(tmpl, temporal_extrapolation=temporal)
+        seq = []
+        for tar in tars:
+            res = np.zeros_like(tmpl)
+            e.sequence_frame(tar, res)
+            seq.append(res.copy())
+        e.close()
+        outs[(graphs, temporal)] = seq
+    for a, b in zip(outs[(True, True)], outs[(False, True)]):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+    # the seed changes where IC-GN starts: frames 0-1 equal, later frames not bit-identical
+    for k in (0, 1):
+        np.testing.assert_array_equal(outs[(True, True)][k].view(np.uint8), outs[(True, False)][k].view(np.uint8))
+    assert not np.array_equal(outs[(True, True)][3].view(np.uint8), outs[(True, False)][3].view(np.uint8))
+
+
+def test_process_frame_history_matches_oracle(dic, oracle_mod):
+    O = oracle_mod
+    from oracle import frame_policy as FP
+    ref, tars = temporal_stream()
+    radius, step = 12, 8
+    tmpl = dic.grid_queue(256, 256, radius, step)
+    e = dic.Engine(radius)
+    e.set_ref(ref)
+    hist = []
+    for tar in tars[:2]:
+        e.set_tar(tar)
+        q = tmpl.copy()
+        e.process_pair(q)
+        hist.append(q)
+    e.set_tar(tars[2])
+    q, rep = e.process_frame(tmpl.copy(), hist[1], prev_prev=hist[0], temporal_extrapolation=True)
+    e.close()
+    solver = FP.Solver(ref, radius)
+    solver.set_tar(tars[2])
+    oq, info = FP.process_frame(solver, to_oracle(O, tmpl), to_oracle(O, hist[1]), True, True,
+                                prev2=to_oracle(O, hist[0]), temporal=True)
+    assert rep["temporal_seed_count"] > 0 and abs(rep["temporal_seed_count"] - info["temporal"]) <= 2
+    r = C.compare_frame(oracle_fields(O, oq), {"u": q["u"], "v": q["v"], "zncc": q["zncc"]})
+    assert r["pass"], r

@@ -145,3 +145,42 @@ def test_oracle_bspline_integer_nodes(oracle_mod):
             assert O.bspline_value(coef, float(x), float(y)) == img[y, x]
     assert O.bspline_value(coef, 0.5, 5.0) == -1.0      # x < 1
     assert O.bspline_value(coef, 5.0, 18.0) == -1.0     # y >= h - 2
+
+
+def test_policy_temporal_seed_rules(oracle_mod):
+    """seedPoiQueueFromPrevious's temporal extrapolation (:594-616) in the restated policy:
+    prev + (prev - prev_prev) for u and v only where both results are eligible (finite, zncc
+    >= 0.8) at the template's location, the step is >= 0.05 px and each component's step is
+    within the subset radius."""
+    O = oracle_mod
+    from oracle import frame_policy as FP
+    n = 8
+    tmpl = np.zeros(n, dtype=O.POI2D_DTYPE)
+    tmpl["x"] = np.arange(n) * 10.0 + 20.0
+    tmpl["y"] = 30.0
+    prev, prev2 = tmpl.copy(), tmpl.copy()
+    prev["r"][:, O.R_ZNCC] = 0.95
+    prev2["r"][:, O.R_ZNCC] = 0.95
+    prev["p"][:, O.P_U] = 1.0
+    prev["p"][:, O.P_V] = -0.5
+    prev["p"][:, O.P_UX] = 0.001
+    prev2["p"][:, O.P_U] = 0.8          # step (0.2, 0.1): extrapolated to (1.2, -0.4)
+    prev2["p"][:, O.P_V] = -0.6
+    prev2["p"][1, O.P_U] = 0.99         # step 0.01 px: below 0.05, not extrapolated
+    prev2["p"][1, O.P_V] = -0.5
+    prev2["p"][2, O.P_U] = -20.0        # |du| = 21 > radius 15
+    prev2["r"][3, O.R_ZNCC] = 0.7       # history below 0.8
+    prev["r"][4, O.R_ZNCC] = np.nan     # invalid previous result: template seed, nothing copied
+    prev2["x"][5] += 1.0                # another location
+    prev["p"][6, O.P_V] = np.inf        # non-finite previous v
+    q, count = FP.seed_from_previous(tmpl, prev, prev2, temporal=True, max_delta=15.0)
+    assert count == 2                   # POIs 0 and 7
+    for i in (0, 7):
+        assert q["p"][i, O.P_U] == np.float32(np.float32(1.0) + np.float32(np.float32(1.0) - np.float32(0.8)))
+        assert q["p"][i, O.P_V] == np.float32(np.float32(-0.5) + np.float32(np.float32(-0.5) - np.float32(-0.6)))
+        assert q["p"][i, O.P_UX] == np.float32(0.001)   # the other parameters are copied as they were
+    for i in (1, 2, 3, 5, 6):
+        assert q["p"][i, O.P_U] == np.float32(1.0)
+    assert q["p"][4, O.P_U] == 0.0 and np.all(q["r"][:, O.R_ZNCC] == 0.0)
+    q0, c0 = FP.seed_from_previous(tmpl, prev, prev2, temporal=False)
+    assert c0 == 0 and q0["p"][0, O.P_U] == np.float32(1.0)
