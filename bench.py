@@ -384,7 +384,8 @@ def measure_uneven(dic, torch, dev, flush, jobs, steps, warmup):
 
 def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
     """A fixed-reference stream through dic_sequence_*: e2e = host frames staged on the side
-    stream (dic_stage_frame) and results read back every frame, host clock; device =
+    stream (dic_stage_frame) and every frame's results read back one frame behind the solve
+    (dic_sequence_fetch), host clock, including the read of warm-up frame 1; device =
     frames already in HBM, back-to-back frames without host syncs, CUDA events.  Frames 0
     (first / FFTCC) and 1 (graph capture) of the window are untimed warm-up."""
     from fasticgn_gb300 import _lib, speckle
@@ -405,16 +406,24 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
     # ---- e2e: staged host frames, results every frame
     eng.sequence_begin(tmpl, learned_seed=learned)
     reports, results = [], []
-    eng.stage_frame(tars_h[0])
+    def enqueue(k):
+        eng.stage_frame(tars_h[k])
+        eng.sequence_frame(None, None, staged=True, width=W, height=H, dtype=_lib.DIC_U16, report=False)
+
     t0 = None
+    enqueue(0)
     for k in range(len(tars_h)):
-        if k == 2:
+        if k == 1:   # frames 0 and 1 solved; the clock covers staging, solving and reading 2..
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-        if k + 1 < len(tars_h):
-            eng.stage_frame(tars_h[k + 1])
+        # frame k is running: stage frame k + 1 (upload on the side stream, straight from the
+        # page-locked frame) and enqueue it behind frame k, then read frame k's results one
+        # frame back while frame k + 1 runs, so the device never waits for the host
+        ahead = k + 1 < len(tars_h)
+        if ahead:
+            enqueue(k + 1)
         res = res_all[k].view(dic.POI_DTYPE)
-        rep = eng.sequence_frame(None, res, staged=True, width=W, height=H, dtype=_lib.DIC_U16)
+        rep = eng.sequence_fetch(res, frames_back=1 if ahead else 0)
         if k >= 2:
             reports.append(rep)
             results.append(res)
@@ -451,7 +460,9 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
            "fallback_rate": float(np.mean([r["repaired_candidates"] for r in reports]) / n),
            "frame_fallbacks": int(sum(r["frame_fallback_used"] for r in reports)),
            "tuning": eng.tuning(),
-           "timing": "e2e: host clock over the timed frames, staged uploads + result reads included; "
+           "timing": "e2e: host clock over the timed frames, the next frame uploaded and enqueued while each "
+                     "frame runs, every frame's results read one frame behind (uploads and result reads "
+                     "included); "
                      "device: CUDA events on the engine stream, frames resident, no per-frame host sync"}
     if st["kind"] == "crack":
         _, _, p0, direction = speckle.crack_setup(st["seed"], W, H)

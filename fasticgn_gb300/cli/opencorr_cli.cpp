@@ -23,10 +23,11 @@
 // Not provided: --dual-gpu (one GPU), --kernel legacy and --fftcc cpu.  Asking for them is an
 // error with a message saying so.
 //
-// Host threads and streams: a decode thread reads frame k+1 while frame k is solved
-// (--preload, the default), its upload runs on the engine's upload stream (dic_stage_frame)
-// during that solve, and a writer thread formats and publishes frame k's payload while
-// frame k+1 is solved.  Payload bytes do not depend on any of this.
+// Host threads and streams: a decode thread reads ahead (--preload, the default); while frame
+// k is solved, frame k+1 is staged (copied to pinned memory, uploaded on the engine's upload
+// stream, dic_stage_frame) and enqueued behind it, then frame k's results are read one frame
+// back (dic_sequence_fetch) while frame k+1 runs; a writer thread formats and publishes frame
+// k's payload.  Payload bytes do not depend on any of this.
 #include "dic.h"
 #include "image_io.h"
 #include "json.h"
@@ -1472,17 +1473,28 @@ int run_multi(const std::vector<std::string>& args)
     check_frame(t, k);
     eng.check(dic_stage_frame(eng.e, t.data(), t.width, t.height, t.row_bytes(), t.dtype), "stage frame");
   };
+  auto enqueue = [&] {
+    eng.check(dic_sequence_frame(eng.e, nullptr, ref.width, ref.height, ref.row_bytes(), ref.dtype, DIC_PIXELS_STAGED,
+                                 nullptr, nullptr),
+              "frame");
+  };
   stage(0);
+  enqueue();
   std::exception_ptr next_failed;   // a bad next frame fails the run after this frame is written
   for (size_t k = 0; k < entries.size(); ++k)
   {
     writer.check();
     if (next_failed) std::rethrow_exception(next_failed);
+    // frame k is running: decode-wait and stage frame k + 1, enqueue it behind frame k, then
+    // read frame k's results (one frame back) while frame k + 1 runs
+    bool next_enqueued = false;
     if (k + 1 < entries.size())
     {
       try
       {
         stage(k + 1);
+        enqueue();
+        next_enqueued = true;
       }
       catch (...)
       {
@@ -1492,9 +1504,7 @@ int run_multi(const std::vector<std::string>& args)
     std::vector<dic_poi>& res = bufs[k % bufs.size()];
     dic_frame_report rep{};
     const bool attempted_skip = o.skip_fftcc && k > 0;
-    eng.check(dic_sequence_frame(eng.e, nullptr, ref.width, ref.height, ref.row_bytes(), ref.dtype, DIC_PIXELS_STAGED,
-                                 res.data(), &rep),
-              "frame");
+    eng.check(dic_sequence_fetch(eng.e, next_enqueued ? 1 : 0, res.data(), &rep), "frame results");
     FrameRecord f;
     f.tar_path = entries[k].tar_path;
     f.output_name = entries[k].output_name;

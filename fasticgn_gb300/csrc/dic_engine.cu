@@ -892,6 +892,44 @@ struct dic_engine
   dic_frame_policy seq_policy{};
   int64_t seq_n = 0;
   long long seq_frame = 0;
+  bool seq_last_skip = false;     // the most recent frame's kind
+  // The last two frames' results and counters (slot = frame & 1), for dic_sequence_fetch: a
+  // frame's slot is read on down_stream while the next frame already runs on the engine stream.
+  DevBuf<dic_poi> seq_out[2];
+  DevBuf<FrameCounters> seq_cnt[2];
+  long long seq_out_frame[2] = {-1, -1};
+  bool seq_out_skip[2] = {false, false};
+  cudaEvent_t seq_done[2] = {};
+  cudaStream_t down_stream = nullptr;
+  void save_frame_output(int64_t n, bool use_skip)
+  {
+    const int slot = (int)(seq_frame & 1);
+    if (!down_stream)
+    {
+      DIC_CUDA(cudaStreamCreateWithFlags(&down_stream, cudaStreamNonBlocking));
+      for (auto& ev : seq_done) DIC_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    seq_out[slot].ensure((size_t)n);
+    seq_cnt[slot].ensure(1);
+    DIC_CUDA(cudaMemcpyAsync(seq_out[slot].ptr, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToDevice, stream));
+    DIC_CUDA(cudaMemcpyAsync(seq_cnt[slot].ptr, fcount.ptr, sizeof(FrameCounters), cudaMemcpyDeviceToDevice, stream));
+    DIC_CUDA(cudaEventRecord(seq_done[slot], stream));
+    seq_out_frame[slot] = seq_frame;
+    seq_out_skip[slot] = use_skip;
+  }
+  void release_frame_outputs()
+  {
+    if (down_stream) cudaStreamSynchronize(down_stream);
+    for (int k = 0; k < 2; ++k)
+    {
+      seq_out[k].release();
+      seq_cnt[k].release();
+      if (seq_done[k]) cudaEventDestroy(seq_done[k]);
+      seq_done[k] = nullptr;
+    }
+    if (down_stream) cudaStreamDestroy(down_stream);
+    down_stream = nullptr;
+  }
   bool use_graphs = true;
   cudaGraphExec_t seq_graph = nullptr;
   int seq_graph_kernels = 0;
@@ -1042,6 +1080,31 @@ struct dic_engine
       }
     }
     const size_t row = (size_t)width * es, bytes = row * height;
+    // A page-locked source is uploaded straight from the caller's buffer, and the call waits
+    // for that copy (~40 us for 8 MB) so that the buffer is free on return; a pageable one
+    // goes through a host copy into the pinned double buffer and uploads asynchronously.
+    cudaPointerAttributes attr{};
+    const bool pinned = cudaPointerGetAttributes(&attr, px) == cudaSuccess && attr.type == cudaMemoryTypeHost;
+    if (!pinned) cudaGetLastError();
+    if (pinned)
+    {
+      if (stage_dev[s].cap < bytes)
+      {
+        DIC_CUDA(cudaEventSynchronize(stage_consumed[s]));
+        stage_dev[s].ensure(bytes);
+      }
+      DIC_CUDA(cudaStreamWaitEvent(up_stream, stage_consumed[s], 0));   // the device copy was taken
+      DIC_CUDA(cudaMemcpy2DAsync(stage_dev[s].ptr, row, px, (size_t)stride, row, height, cudaMemcpyHostToDevice,
+                                 up_stream));
+      DIC_CUDA(cudaEventRecord(stage_uploaded[s], up_stream));
+      DIC_CUDA(cudaEventSynchronize(stage_uploaded[s]));
+      stage_w[s] = width;
+      stage_h[s] = height;
+      stage_dtype[s] = dtype;
+      stage_full[s] = true;
+      stage_next ^= 1;
+      return;
+    }
     DIC_CUDA(cudaEventSynchronize(stage_uploaded[s]));   // the pinned buffer's last copy is done
     if (stage_host_cap[s] < bytes)
     {
@@ -1330,6 +1393,12 @@ struct dic_engine
     DIC_CUDA(cudaMemcpyAsync(&c, fcount.ptr, sizeof(c), cudaMemcpyDeviceToHost, stream));
     DIC_CUDA(cudaStreamSynchronize(stream));
     check_tile_error();
+    report_from(r, c, n, use_skip, host_results, learned);
+  }
+  void report_from(dic_frame_report* r, const FrameCounters& c, int64_t n, bool use_skip, const dic_poi* host_results,
+                   bool learned)
+  {
+    if (!r) return;
     if (learned)
     {
       // learned seed: "before repair" = POIs the proposal's IC-GN did not bring to ZNCC 0.9
@@ -1498,6 +1567,7 @@ void dic_engine_destroy(dic_engine* e)
   e->icgn_next.release();
   e->tune_q.release();
   e->release_staging();
+  e->release_frame_outputs();
   for (int p = 0; p < kPhCount; ++p)
     for (int m = 0; m < dic_engine::kMarks; ++m)
       for (int k = 0; k < 2; ++k)
@@ -1715,6 +1785,7 @@ int dic_sequence_begin(dic_engine* e, const dic_poi* pois, int64_t n, const dic_
     e->seq_policy = *policy;
     e->seq_n = n;
     e->seq_frame = 0;
+    e->seq_out_frame[0] = e->seq_out_frame[1] = -1;
   });
 }
 
@@ -1820,6 +1891,7 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
     e->mark(kPhFrame, 1);
     e->iter_pending = true;
     e->icgn_pois = n;
+    e->save_frame_output(n, use_skip);
     if (results)
       DIC_CUDA(cudaMemcpyAsync(results, e->queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, e->stream));
     if (results || report)
@@ -1828,7 +1900,35 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
       e->check_tile_error();
     }
     e->fill_report(report, n, use_skip, results, learned);
+    e->seq_last_skip = use_skip;
     ++e->seq_frame;
+  });
+}
+
+int dic_sequence_fetch(dic_engine* e, int32_t frames_back, dic_poi* results, dic_frame_report* report)
+{
+  return guarded(e, [&] {
+    if (frames_back != 0 && frames_back != 1) throw DicError{DIC_ERR_ARGUMENT, "sequence_fetch: frames_back must be 0 or 1"};
+    const long long frame = e->seq_frame - 1 - frames_back;
+    const int slot = (int)(frame & 1);
+    if (frame < 0 || e->seq_out_frame[slot] != frame)
+      throw DicError{DIC_ERR_STATE, "sequence_fetch: that frame of this sequence has not been solved"};
+    const int64_t n = e->seq_n;
+    if (report) *report = dic_frame_report{};
+    // on the download stream: the engine stream may already be solving the next frame
+    FrameCounters c{};
+    DIC_CUDA(cudaStreamWaitEvent(e->down_stream, e->seq_done[slot], 0));
+    if (results)
+      DIC_CUDA(cudaMemcpyAsync(results, e->seq_out[slot].ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost,
+                               e->down_stream));
+    DIC_CUDA(cudaMemcpyAsync(&c, e->seq_cnt[slot].ptr, sizeof(c), cudaMemcpyDeviceToHost, e->down_stream));
+    int tile_flag = 0;   // a TMA-staged IC-GN of this frame whose copy timed out
+    if (e->tile_err.ptr)
+      DIC_CUDA(cudaMemcpyAsync(&tile_flag, e->tile_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, e->down_stream));
+    DIC_CUDA(cudaStreamSynchronize(e->down_stream));
+    if (tile_flag)
+      throw DicError{DIC_ERR_CUDA, "k_icgn_tile: a TMA tile copy did not complete in time; results are invalid"};
+    e->report_from(report, c, n, e->seq_out_skip[slot], results, e->seq_policy.learned_seed != 0);
   });
 }
 

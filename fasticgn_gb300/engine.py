@@ -220,6 +220,21 @@ class Engine:
         self._call(rc)
         return {f: getattr(rep, f) for f, _ in rep._fields_} if report else None
 
+    def sequence_fetch(self, results: np.ndarray | None = None, report: bool = True, frames_back: int = 0):
+        """Results (and report) of an enqueued frame (frames_back 0: the most recent
+        sequence_frame, 1: the one before), waiting only for that frame: a loop enqueues
+        frame k + 1 with sequence_frame(..., report=False), stages frame k + 2, then fetches
+        frame k with frames_back=1 while frame k + 1 runs."""
+        rep = _lib.DicFrameReport()
+        out_ptr = None
+        if results is not None:
+            results = _check_queue(results)
+            if len(results) != self._seq_n:
+                raise ValueError("results must hold one record per template POI")
+            out_ptr = results.ctypes.data
+        self._call(self._L.dic_sequence_fetch(self._h, int(frames_back), out_ptr, ctypes.byref(rep) if report else None))
+        return {f: getattr(rep, f) for f, _ in rep._fields_} if report else None
+
     def set_proposal(self, net) -> None:
         """Attach a ProposalNet (or None) for process_pair_learned / DIC_RUN_LEARNED."""
         self._proposal = net

@@ -193,13 +193,25 @@ int dic_sequence_begin(dic_engine* engine, const dic_poi* pois, int64_t count, c
 int dic_sequence_frame(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
                        int64_t row_stride_bytes, int32_t dtype, int32_t pixels_on_device, dic_poi* results,
                        dic_frame_report* report);
+/* No reference counterpart: the results and report of a frame already enqueued, read
+ * after the fact: frames_back 0 = the most recent dic_sequence_frame, 1 = the one before
+ * (each frame keeps a copy of its results for this until two more frames are enqueued).
+ * dic_sequence_frame with results and report NULL only enqueues the frame and returns, so a
+ * loop can keep the GPU busy: while frame k runs, stage and enqueue frame k + 1, then fetch
+ * frame k (frames_back 1), which reads it on a download stream while frame k + 1 runs.  The
+ * fetch waits only for the frame it reads.  DIC_ERR_ARGUMENT for frames_back other than 0
+ * or 1; DIC_ERR_STATE for a frame that no successful dic_sequence_frame of the current
+ * sequence enqueued. */
+int dic_sequence_fetch(dic_engine* engine, int32_t frames_back, dic_poi* results, dic_frame_report* report);
 int dic_set_graphs(dic_engine* engine, int32_t enabled);
 
 /* Frame upload on a side stream (no reference counterpart; the reference decodes the next
  * frame on a thread and uploads it inside the next compute call).  dic_stage_frame copies a
  * host frame into one of two pinned buffers and starts its host-to-device copy on the
  * engine's upload stream, then returns; the copy overlaps whatever the engine stream is
- * running (typically the previous frame's solve).  dic_sequence_frame with
+ * running (typically the current frame's solve).  A page-locked frame (cudaMallocHost,
+ * cudaHostRegister, pinned torch tensors) skips the host copy: it is uploaded directly and
+ * the call returns when that copy is done, so the caller may reuse the buffer at once.  dic_sequence_frame with
  * pixels_on_device = DIC_PIXELS_STAGED (pixels NULL) consumes the oldest staged frame: the
  * engine stream waits for its copy, nothing else does.  At most two frames are staged at a
  * time. */

@@ -149,3 +149,97 @@ def test_crack_stream_fallback_is_at_the_crack(dic, net, crack):
         u, v = field(res["x"].astype(np.float64), res["y"].astype(np.float64))
         assert np.median(np.abs(res["u"][far] - u[far])) < 0.02
         assert np.median(np.abs(res["v"][far] - v[far])) < 0.02
+
+
+def test_async_frames_with_fetch_equal_synchronous(dic, crack):
+    """sequence_frame without results (enqueue only) with sequence_fetch, both right after the
+    frame (frames_back 0) and one frame behind while the next frame runs (frames_back 1): the
+    same results and reports as the synchronous call.  A fetch may be repeated; a fetch of a
+    frame that was not enqueued in this sequence, or further back than one frame, is refused."""
+    ref, frames, _ = crack
+    tars = [f[1] for f in frames]
+    H, W = tars[0].shape
+    tmpl = dic.grid_queue(W, H, 12, 6)
+    outs = []
+    for mode in ("sync", "fetch", "pipelined"):
+        e = dic.Engine(12)
+        e.set_ref(ref)
+        e.sequence_begin(tmpl)
+
+        def enqueue(k):
+            e.stage_frame(tars[k])
+            assert e.sequence_frame(None, None, staged=True, width=W, height=H, dtype=dic._lib.DIC_U16,
+                                    report=False) is None
+
+        got = []
+        if mode == "sync":
+            for k in range(len(tars)):
+                res = np.zeros_like(tmpl)
+                e.stage_frame(tars[k])
+                rep = e.sequence_frame(None, res, staged=True, width=W, height=H, dtype=dic._lib.DIC_U16)
+                got.append((res, rep))
+        elif mode == "fetch":
+            for fb in (0, 1):
+                with pytest.raises(RuntimeError):
+                    e.sequence_fetch(np.zeros_like(tmpl), frames_back=fb)
+            for k in range(len(tars)):
+                enqueue(k)
+                res = np.zeros_like(tmpl)
+                rep = e.sequence_fetch(res)
+                again = np.zeros_like(tmpl)
+                assert e.sequence_fetch(again) == rep      # fetch may be repeated
+                np.testing.assert_array_equal(again.view(np.uint8), res.view(np.uint8))
+                got.append((res, rep))
+            with pytest.raises(ValueError):
+                e.sequence_fetch(None, frames_back=2)
+        else:
+            enqueue(0)
+            with pytest.raises(RuntimeError):
+                e.sequence_fetch(None, frames_back=1)      # no frame before frame 0
+            for k in range(len(tars)):
+                ahead = k + 1 < len(tars)
+                if ahead:
+                    enqueue(k + 1)
+                res = np.zeros_like(tmpl)
+                rep = e.sequence_fetch(res, frames_back=1 if ahead else 0)
+                got.append((res, rep))
+            e.sequence_begin(tmpl)                         # a new sequence forgets the old frames
+            with pytest.raises(RuntimeError):
+                e.sequence_fetch(None)
+        e.close()
+        outs.append(got)
+    for other in outs[1:]:
+        for (a, ra), (b, rb) in zip(outs[0], other):
+            np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+            assert ra == rb
+
+
+def test_pinned_frames_staged_directly(dic, crack):
+    """Page-locked frames are uploaded straight from the caller's buffer (no host copy) and
+    the buffer is free when dic_stage_frame returns: one pinned buffer refilled per frame gives
+    the same results as pageable frames."""
+    torch = pytest.importorskip("torch")
+    ref, frames, _ = crack
+    tars = [f[1] for f in frames]
+    tmpl = dic.grid_queue(ref.shape[1], ref.shape[0], 12, 6)
+    outs = []
+    for pinned in (False, True):
+        e = dic.Engine(12)
+        e.set_ref(ref)
+        e.sequence_begin(tmpl)
+        buf = torch.empty(tars[0].shape, dtype=torch.int16).pin_memory().numpy().view(np.uint16) if pinned else None
+        got = []
+        for k, tar in enumerate(tars):
+            if pinned:
+                buf[:] = tar                     # the same pinned buffer for every frame
+                e.stage_frame(buf)
+                buf[:] = 0                       # free again once stage_frame has returned
+            else:
+                e.stage_frame(tar)
+            res = np.zeros_like(tmpl)
+            e.sequence_frame(None, res, staged=True, width=tar.shape[1], height=tar.shape[0], dtype=dic._lib.DIC_U16)
+            got.append(res)
+        e.close()
+        outs.append(got)
+    for a, b in zip(*outs):
+        np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
