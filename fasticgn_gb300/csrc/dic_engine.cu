@@ -502,7 +502,7 @@ struct dic_engine
     int tile = 0;            // column walk: 0 gathers from the table; 1, 2: k_icgn_tile (kTileKinds)
   };
   // TMA-staged tile forms: POIs (warps) per CTA, block width and height in texels, CTAs per SM
-  // (shared memory: 4 planes x 16 B per texel, 110.7 KB and 163.9 KB)
+  // (shared memory: 2 planes x 32 B per texel, 110.7 KB and 163.9 KB)
   struct TileKind
   {
     int warps, bx, by, ctas;
@@ -536,7 +536,8 @@ struct dic_engine
   TileMap tile_maps[3];
   DevBuf<int> tile_err;        // set by a k_icgn_tile CTA whose copy did not arrive in time
   bool tile_pending = false;   // a tile launch since the last check
-  // the 4-D map {component, x, y, plane} of a coefficient table, box {4, bx, by, 4}
+  // the 4-D map {component, x, y, plane} of a coefficient table (8 floats per texel and
+  // plane, 2 planes), box {8, bx, by, 2}
   const CUtensorMap& coef_map(int kind, const float4* table, int tw, int th)
   {
     TileMap& m = tile_maps[kind];
@@ -544,10 +545,10 @@ struct dic_engine
     EncodeTiledFn fn = encode_tiled();
     if (!fn) throw DicError{DIC_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver"};
     const TileKind& k = kTileKinds[kind];
-    const cuuint64_t dims[4] = {4, (cuuint64_t)tw, (cuuint64_t)th, 4};
-    const cuuint64_t strides[3] = {sizeof(float4), sizeof(float4) * (cuuint64_t)tw,
-                                   sizeof(float4) * (cuuint64_t)tw * (cuuint64_t)th};
-    const cuuint32_t box[4] = {4, (cuuint32_t)k.bx, (cuuint32_t)k.by, 4};
+    constexpr cuuint64_t texel = 2 * sizeof(float4);
+    const cuuint64_t dims[4] = {8, (cuuint64_t)tw, (cuuint64_t)th, 2};
+    const cuuint64_t strides[3] = {texel, texel * (cuuint64_t)tw, texel * (cuuint64_t)tw * (cuuint64_t)th};
+    const cuuint32_t box[4] = {8, (cuuint32_t)k.bx, (cuuint32_t)k.by, 2};
     const cuuint32_t estr[4] = {1, 1, 1, 1};
     const CUresult r = fn(&m.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float4*>(table), dims, strides, box, estr,
                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

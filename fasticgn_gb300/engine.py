@@ -314,10 +314,14 @@ class Engine:
         self._call(self._L.dic_run_device(self._h, device_pois, count, flags))
 
     def read_plane(self, plane: int, width: int, height: int) -> np.ndarray:
+        """A resident plane; the coefficient table comes back as [row k][y][x][4] (its device
+        layout is two planes of rows 0-1 and 2-3 per texel)."""
         shape = {_lib.DIC_PLANE_REF: (height, width), _lib.DIC_PLANE_TAR: (height, width),
-                 _lib.DIC_PLANE_REF_PACK: (height, width, 4), _lib.DIC_PLANE_TAR_COEF: (4, height, width, 4)}[plane]
+                 _lib.DIC_PLANE_REF_PACK: (height, width, 4), _lib.DIC_PLANE_TAR_COEF: (2, height, width, 2, 4)}[plane]
         out = np.empty(shape, dtype=np.float32)
         self._call(self._L.dic_read_plane(self._h, plane, out.ctypes.data, out.nbytes))
+        if plane == _lib.DIC_PLANE_TAR_COEF:
+            out = np.ascontiguousarray(out.transpose(0, 3, 1, 2, 4).reshape(4, height, width, 4))
         return out
 
     def set_timing(self, enabled: bool) -> None:

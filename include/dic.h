@@ -301,8 +301,9 @@ int dic_run_device(dic_engine* engine, dic_poi* device_pois, int64_t count, int3
  * DIC_PLANE_REF       W*H float reference grey levels
  * DIC_PLANE_REF_PACK  W*H float4 {ref, gx, gy, 0} (Gradient2D4 planes, src/oc_gradient.cpp)
  * DIC_PLANE_TAR       W*H float target grey levels
- * DIC_PLANE_TAR_COEF  BicubicBspline table (src/oc_cubic_bspline.cpp:84-132) as 4 planes of
- *                     W*H float4; plane k holds coefficient row k, c[k][0..3], of every texel
+ * DIC_PLANE_TAR_COEF  BicubicBspline table (src/oc_cubic_bspline.cpp:84-132) as 2 planes of
+ *                     W*H texels x 8 floats; plane j holds coefficient rows 2j and 2j+1,
+ *                     c[2j][0..3] then c[2j+1][0..3], of every texel
  * Prepares the plane first if its image changed.  For inspection and tests. */
 #define DIC_PLANE_REF 1
 #define DIC_PLANE_REF_PACK 2
