@@ -1309,6 +1309,67 @@ struct Fft<N, N>
   __device__ __forceinline__ static void run(const float2 (&in)[N], float2 (&out)[N]) { Dft<N>::run(in, out); }
 };
 
+// Prime-factor (Good-Thomas) transform: N = N1 * N2 with gcd(N1, N2) = 1, N1 the full power
+// of N's smallest prime.  Input n = (N2 n1 + N1 n2) mod N and output k with k = k1 (mod N1),
+// k = k2 (mod N2) make W_N^(nk) = W_N1^(n1 k1) W_N2^(n2 k2), so the N-point DFT is an
+// N1 x N2 two-dimensional DFT with no twiddle multiplications between the stages (30 =
+// 2 x 3 x 5: none at all, against 30 complex products for the Cooley-Tukey split).
+// Prime powers fall back to Fft (Cooley-Tukey).
+__host__ __device__ constexpr int prime_power_part(int n)
+{
+  const int p = first_factor(n) == 4 ? 2 : first_factor(n);
+  int q = 1;
+  while (n % p == 0)
+  {
+    n /= p;
+    q *= p;
+  }
+  return q;
+}
+__host__ __device__ constexpr int inverse_mod(int a, int m)
+{
+  for (int x = 1; x < m; ++x)
+    if ((a * x) % m == 1) return x;
+  return 1;
+}
+
+template <int N, int N1 = prime_power_part(N)>
+struct FftPfa
+{
+  static constexpr int N2 = N / N1;
+  static constexpr int E1 = N2 * inverse_mod(N2 % N1, N1);   // = 1 mod N1, 0 mod N2
+  static constexpr int E2 = N1 * inverse_mod(N1 % N2, N2);   // = 0 mod N1, 1 mod N2
+  __device__ __forceinline__ static void run(const float2 (&in)[N], float2 (&out)[N])
+  {
+    float2 y[N];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; ++n2)
+    {
+      float2 a[N1], b[N1];
+#pragma unroll
+      for (int n1 = 0; n1 < N1; ++n1) a[n1] = in[(N2 * n1 + N1 * n2) % N];
+      Fft<N1>::run(a, b);
+#pragma unroll
+      for (int k1 = 0; k1 < N1; ++k1) y[k1 * N2 + n2] = b[k1];
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < N1; ++k1)
+    {
+      float2 a[N2], b[N2];
+#pragma unroll
+      for (int n2 = 0; n2 < N2; ++n2) a[n2] = y[k1 * N2 + n2];
+      FftPfa<N2>::run(a, b);
+#pragma unroll
+      for (int k2 = 0; k2 < N2; ++k2) out[(k1 * E1 + k2 * E2) % N] = b[k2];
+    }
+  }
+};
+template <int N>
+struct FftPfa<N, N>
+{
+  __device__ __forceinline__ static void run(const float2 (&in)[N], float2 (&out)[N]) { Fft<N>::run(in, out); }
+};
+
 // --------------------------------------------------------------------------------------
 // FFTCC (src/oc_fftcc.cpp:396-496), one warp per POI, M = 2r <= 32.
 // The zero-mean reference and target subsets are packed as z = ref + i*tar and
@@ -1476,8 +1537,9 @@ __global__ void __launch_bounds__(128) k_fftcc(FftccParams P)
 // forward passes run once per POI (lane = line; the column transform straight from the
 // loaded registers, so the raw subset never goes through shared memory), the inverse
 // passes once for both (lanes 0-15 POI 0, 16-31 POI 1), i.e. 3 line passes per POI instead
-// of 4.  Same packing, algebra, tie rule and outputs as k_fftcc (the results differ only in
-// float rounding: columns are transformed before rows).
+// of 4; each line transform is the prime-factor form (FftPfa).  Same packing, algebra, tie
+// rule and outputs as k_fftcc (the results differ only in float rounding: columns are
+// transformed before rows, and without twiddles between coprime stages).
 // --------------------------------------------------------------------------------------
 template <int M>
 __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
@@ -1549,7 +1611,7 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
         tnl += tv[r] * tv[r];
         a[r] = make_float2(rv[r], tv[r]);
       }
-      Fft<M>::run(a, b);
+      FftPfa<M>::run(a, b);
 #pragma unroll
       for (int k = 0; k < M; ++k) z[k * S + lane] = b[k];
     }
@@ -1561,7 +1623,7 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
     {
 #pragma unroll
       for (int k = 0; k < M; ++k) a[k] = z[lane * S + k];
-      Fft<M>::run(a, b);
+      FftPfa<M>::run(a, b);
 #pragma unroll
       for (int k = 0; k < M; ++k) z[lane * S + k] = b[k];
     }
@@ -1587,7 +1649,7 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
       const float2 X = make_float2(Rk.x * Tk.x + Rk.y * Tk.y, Rk.x * Tk.y - Rk.y * Tk.x);
       a[k] = make_float2(X.x, -X.y);
     }
-    Fft<M>::run(a, b);
+    FftPfa<M>::run(a, b);
   }
   __syncwarp();   // every partner column is read before any column is overwritten
   if (col_live)
@@ -1622,7 +1684,7 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
       }
       a[col] = make_float2(va.x - vb.y, va.y + vb.x);   // va + i vb
     }
-    Fft<M>::run(a, b);
+    FftPfa<M>::run(a, b);
     // real part: row ra, imaginary part: row rb (ra first: lower row-major indices)
 #pragma unroll
     for (int k = 0; k < M; ++k)
