@@ -699,8 +699,11 @@ __device__ __forceinline__ float sample_bspline_tile(const CoefTile& T, const fl
 
 // Rows of the column walk unrolled together (their gathers in flight at once), and the
 // warps per SM the IC-GN launch bounds keep resident (which sets the register budget).
+// The 256-bit coefficient gathers are served from L2, so two rows in flight hide more of
+// their latency (3.48 -> 3.44 ms on the 2048x2048 pair; 3 or 4 rows, or 24 resident warps
+// with more registers, were slower).
 #ifndef DIC_ICGN_ROW_UNROLL
-#define DIC_ICGN_ROW_UNROLL 1
+#define DIC_ICGN_ROW_UNROLL 2
 #endif
 #ifndef DIC_ICGN_RESIDENT_WARPS
 #define DIC_ICGN_RESIDENT_WARPS 28
