@@ -11,14 +11,17 @@
 //   f2  256 -> 6: (u, v, 100 ux, 100 uy, 100 vx, 100 vy)
 //
 // Activations are BF16 in NHWC order (channels fastest), weights are kept in FP32 (master)
-// with BF16 working copies, and every product runs on the tensor cores through
-// mma.sync.m16n8k16 bf16 with FP32 accumulation.  One GEMM kernel serves all layers and
-// all passes; an operand functor gathers its A and B tiles (implicit im2col for the
-// convolutions) and an epilogue functor stores the result.
+// with BF16 working copies, and every product runs on the tensor cores with FP32
+// accumulation.  Training: one GEMM kernel (mma.sync.m16n8k16 bf16) serves all layers and
+// passes; an operand functor gathers its A and B tiles (implicit im2col for the
+// convolutions) and an epilogue functor stores the result.  Inference (k_proposal_fused)
+// runs conv2, its largest layer, as tcgen05.mma from shared-memory descriptors into TMEM.
 #pragma once
 
 #include <cuda_bf16.h>
 #include <cstdint>
+
+#include "dic_kernels.cuh"   // mbarrier helpers
 
 namespace dic
 {
@@ -487,7 +490,11 @@ __global__ void k_write_seeds(const float* __restrict__ out, dic_poi* __restrict
 
 // --------------------------------------------------------------------------------------
 // Fused inference: the whole network, activations resident in shared memory, seeds written
-// straight into the POI queue.  One 512-thread CTA per SM holds two independent warp groups
+// straight into the POI queue.  conv2 (62 % of the network's products) runs on tcgen05: a
+// tile's two POIs are one M = 128 (2 POIs x 8 x 8 output pixels), N = 32, K = 288 product,
+// 18 tcgen05.mma.kind::f16 issued by one thread from shared-memory descriptors, accumulated
+// in 32 TMEM columns per warp group and read back with tcgen05.ld for the epilogue; the
+// other layers use mma.sync.  One 512-thread CTA per SM holds two independent warp groups
 // of 8 warps; each group runs tiles of kT = 2 POIs (tiles strided over groups and CTAs) and
 // syncs on its own named barrier, so one group's serial phases (window staging, conv3/conv4,
 // the MLP) overlap the other's conv1/conv2.  Same arithmetic as the GEMM path (BF16
@@ -502,11 +509,20 @@ __global__ void k_write_seeds(const float* __restrict__ out, dic_poi* __restrict
 // {0, 16, 1, 17} or {2, 18, 1} words apart: 32 distinct banks for the 8 stride-2 rows x 4
 // taps of a load); a1p [2][18][18][40] 50.6 KB and a2p [2][10][10][40] 15.6 KB (zero border,
 // pixel stride 80 B); a4 [16][136] (conv4 outputs of 8 tiles, for the batched MLP).
+// conv1's output a1c is conv2's A operand in the canonical no-swizzle K-major layout
+// (core matrices of 8 rows x 16 B): four planes of 8 channels; in a plane, the padded rows
+// of the two POIs interleaved as slots (row Y of POI p in slot (Y >> 1) * 2 + p, the even
+// rows 0..16 first, then the odd rows 1..15), each slot 18 parity-split padded columns of
+// 16 B.  For tap (ky, kx) and M row m = (2 oy + p) * 8 + ox the pixel (2 oy + ky, 2 ox + kx)
+// then sits at a fixed base + (m >> 3) * 288 B + (m & 7) * 16 B: one descriptor per
+// (tap, channel half) with SBO = 288 B (row slot) and LBO = one plane (next 8 channels).
+// W2 is stored as B core matrices too: 8 output channels x 8 k per 128 B, LBO 512 B.
 // The padded activation rows are stored parity-split: padded column X sits at
 // (X & 1) * (width / 2) + (X >> 1), so the stride-2 im2col rows of an ldmatrix (8 output
 // pixels, input columns 2 ox + kx) are 8 consecutive 80 B pixels, which cover all 32 banks.
-// a3p overlays x0p once conv1 has consumed it; the split-K partials and a5 overlay the start
-// of a1p once conv2 has.
+// a3p [2][6][6][40] has its own region, so x0p takes the next tile's windows while conv2's
+// products run; the split-K partials and a5 overlay the start of a1c once those products
+// have completed.
 // --------------------------------------------------------------------------------------
 constexpr int kT = 2;                           // POIs per tile of a warp group
 constexpr int kGroups = 2;                      // independent warp groups per CTA
@@ -517,7 +533,11 @@ constexpr int kPix = 40;                        // padded channel stride (80 B) 
 constexpr int kWRow = 296;                      // padded row of W2..W4 (288 + 8)
 constexpr int kX0Row = 48;                      // x0p row stride in pixels (33 used)
 constexpr int kSmX0 = kT * 33 * kX0Row * 2 * 2; // 12672
-constexpr int kSmA1 = kT * 18 * 18 * kPix * 2;  // 51840
+constexpr int kA1Slot = 18 * 16;                 // one padded row of one POI, 8 channels
+constexpr int kA1Even = 9 * kT * kA1Slot;        // padded rows 0, 2, .., 16 of the tile's POIs
+constexpr int kA1Plane = kA1Even + 8 * kT * kA1Slot;   // + rows 1, 3, .., 15: 9792 B
+constexpr int kSmA1 = 4 * kA1Plane;              // 39168
+static_assert(kT == 2, "conv2's M = 128 rows are the two POIs of a tile");
 constexpr int kSmA2 = kT * 10 * 10 * kPix * 2;  // 16000
 constexpr int kW1Row = 40;                      // padded row of W1 (32 + 8)
 constexpr int kSmW1 = 32 * kW1Row * 2;          // 2560
@@ -530,14 +550,14 @@ constexpr int kA4Row = 128 + 8, kA5Row = 256 + 8;   // rows padded by 16 B: dist
 constexpr int kSmA4 = kMlpRows * kA4Row * 2;     // 4352, persists across the batched tiles
 constexpr int kSmOut = kMlpRows * 8 * 4;         // 512
 constexpr int kSmPoi = kMlpTiles * 8;            // first POI of each batched tile
-constexpr int kSmGroup = kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut + kSmPoi;   // 85440
+constexpr int kSmA3 = kT * 6 * 6 * kPix * 2;    // 5760
+constexpr int kSmGroup = kSmX0 + kSmA1 + kSmA2 + kSmA3 + kSmA4 + kSmOut + kSmPoi;   // 78528
 constexpr int kSmTotal = kSmW1 + kSmW + kGroups * kSmGroup;
-static_assert(kT * 6 * 6 * kPix * 2 <= kSmX0, "a3p overlays x0p");
 // In a1p, free after conv2: conv4 split-K partials [4][16][32], f2 partials [8][16][8], a5
 constexpr int kSmPart4 = 4 * 16 * 32 * 4, kSmPart2 = kGW * 16 * 8 * 4;
 constexpr int kSmA5Off = kSmPart4 + kSmPart2;
 constexpr int kSmScratch = kSmA5Off + kMlpRows * kA5Row * 2;
-static_assert(kSmScratch <= kSmA1 && kSmA5Off % 16 == 0, "partials and a5 fit in a1p");
+static_assert(kSmScratch <= kSmA1 && kSmA5Off % 16 == 0, "partials and a5 fit in a1c");
 static_assert(kSmGroup % 16 == 0, "group regions stay 16-byte aligned");
 static_assert(kSmTotal <= 227 * 1024, "shared memory");
 
@@ -571,6 +591,109 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], uint32_t addr)
   asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
                : "r"(addr));
+}
+
+// byte offset of channel co of padded pixel (Y, X) of POI p in a1c
+__device__ __forceinline__ int a1c_offset(int p, int Y, int X, int co)
+{
+  return (co >> 3) * kA1Plane + (Y & 1) * kA1Even + ((Y >> 1) * kT + p) * kA1Slot + pcol<18>(X) * 16 + (co & 7) * 2;
+}
+
+// tcgen05 shared-memory matrix descriptor, no swizzle: start, LBO (next core matrix along
+// K), SBO (next 8 rows along M or N), descriptor version 1
+__device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo)
+{
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo & 0x3FFFFu) >> 4) << 16) |
+         ((uint64_t)((sbo & 0x3FFFFu) >> 4) << 32) | (1ull << 46);
+}
+// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, N = 32, M = 128
+constexpr uint32_t kConv2Idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((32u >> 3) << 17) | ((128u >> 4) << 24);
+
+__device__ __forceinline__ void umma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, bool accumulate)
+{
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"((uint32_t)accumulate));
+}
+// the mbarrier arrives when every tcgen05.mma this thread issued has completed
+__device__ __forceinline__ void umma_commit(uint32_t bar)
+{
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+// 32 TMEM lanes (the warp's quarter) x 16 columns of 32 bits
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16])
+{
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+// true on every thread of the warp group when v holds on all of them
+__device__ __forceinline__ bool group_all(int grp, bool v)
+{
+  uint32_t r;
+  asm volatile(
+      "{\n .reg .pred p, q;\n setp.ne.u32 p, %1, 0;\n bar.red.and.pred q, %2, %3, p;\n selp.u32 %0, 1, 0, q;\n}\n"
+      : "=r"(r)
+      : "r"((uint32_t)v), "r"(1 + grp), "r"(kGThreads)
+      : "memory");
+  return r != 0;
+}
+constexpr uint32_t kMmaWaitPolls = 1u << 22;
+constexpr int kProposalTmemCols = 32 * kGroups;   // one 128 x 32 f32 accumulator per warp group
+
+// Input windows of the tile starting at POI p0 into x0p's interior: warp 2p + c of the group
+// stages channel c (0 ref, 1 tar) of POI p.  Lane l holds column l of the 31x31 window in
+// registers (coalesced row loads, one pass), the warp reduces mean and variance, and writes
+// the normalised values.  POIs past n leave x0p as it was (their rows are never written out).
+__device__ __forceinline__ void stage_windows(__nv_bfloat16* x0p, const float* __restrict__ ref,
+                                              const float* __restrict__ tar, int w, int h,
+                                              const dic_poi* __restrict__ pois, int64_t n, int64_t p0, int warp,
+                                              int lane)
+{
+  if (warp >= 2 * kT) return;
+  const int p = warp >> 1, ch = warp & 1;
+  const int64_t i = p0 + p;
+  if (i >= n) return;
+  const float* img = ch ? tar : ref;
+  const int cx = (int)pois[i].x, cy = (int)pois[i].y;
+  constexpr int R = kWin / 2, NPIX = kWin * kWin;
+  const int x = min(max(cx + lane - R, 0), w - 1);
+  float v[kWin];
+  float s = 0.f;
+  if (lane < kWin)
+  {
+#pragma unroll
+    for (int r = 0; r < kWin; ++r)
+    {
+      const int y = min(max(cy + r - R, 0), h - 1);
+      v[r] = __ldg(img + (size_t)y * w + x);
+    }
+#pragma unroll
+    for (int r = 0; r < kWin; ++r) s += v[r];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  const float mean = s / NPIX;
+  float q = 0.f;
+  if (lane < kWin)
+  {
+#pragma unroll
+    for (int r = 0; r < kWin; ++r) q += (v[r] - mean) * (v[r] - mean);
+  }
+  for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
+  const float inv = q > 0.f ? rsqrtf(q / NPIX) : 1.f;
+  if (lane < kWin)
+  {
+    __nv_bfloat16* dst = x0p + ((p * 33 + 1) * kX0Row + lane + 1) * 2 + ch;
+#pragma unroll
+    for (int r = 0; r < kWin; ++r) dst[r * kX0Row * 2] = __float2bfloat16((v[r] - mean) * inv);
+  }
 }
 
 // One 3x3 stride-2 conv layer from padded NHWC smem (pixel stride kPix) to the interior of
@@ -654,9 +777,11 @@ __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloa
 __global__ void __launch_bounds__(kFusedThreads, 1)
     k_proposal_fused(const float* __restrict__ ref, const float* __restrict__ tar, int w, int h,
                      dic_poi* __restrict__ pois, int64_t n, const __nv_bfloat16* __restrict__ wb,
-                     const float* __restrict__ params)
+                     const float* __restrict__ params, int* __restrict__ err)
 {
   extern __shared__ __align__(16) unsigned char sm[];
+  __shared__ __align__(8) unsigned long long mma_bar[kGroups];
+  __shared__ uint32_t tmem_base;
   __nv_bfloat16* W1s = reinterpret_cast<__nv_bfloat16*>(sm);
   __nv_bfloat16* W2s = reinterpret_cast<__nv_bfloat16*>(sm + kSmW1);
   __nv_bfloat16* W3s = W2s + 32 * kWRow;
@@ -667,12 +792,13 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   const int grp = tid / kGThreads, gt = tid % kGThreads, warp = gt >> 5;   // warp within the group
   unsigned char* gs = sm + kSmW1 + kSmW + grp * kSmGroup;
   __nv_bfloat16* x0p = reinterpret_cast<__nv_bfloat16*>(gs);
-  __nv_bfloat16* a1p = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0);
+  unsigned char* a1c = gs + kSmX0;
+  __nv_bfloat16* a1p = reinterpret_cast<__nv_bfloat16*>(a1c);   // its start, for the overlays
   __nv_bfloat16* a2p = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0 + kSmA1);
-  __nv_bfloat16* a4 = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0 + kSmA1 + kSmA2);           // [16][136]
-  float* outs = reinterpret_cast<float*>(gs + kSmX0 + kSmA1 + kSmA2 + kSmA4);                 // [16][8]
-  int64_t* tile_p0 = reinterpret_cast<int64_t*>(gs + kSmX0 + kSmA1 + kSmA2 + kSmA4 + kSmOut);
-  __nv_bfloat16* a3p = x0p;                                                                  // [2][6][6][kPix]
+  __nv_bfloat16* a3p = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0 + kSmA1 + kSmA2);          // [2][6][6][kPix]
+  __nv_bfloat16* a4 = reinterpret_cast<__nv_bfloat16*>(gs + kSmX0 + kSmA1 + kSmA2 + kSmA3);   // [16][136]
+  float* outs = reinterpret_cast<float*>(gs + kSmX0 + kSmA1 + kSmA2 + kSmA3 + kSmA4);         // [16][8]
+  int64_t* tile_p0 = reinterpret_cast<int64_t*>(gs + kSmX0 + kSmA1 + kSmA2 + kSmA3 + kSmA4 + kSmOut);
   float* part4 = reinterpret_cast<float*>(a1p);                                              // [4][16][32]
   float* part2 = reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(a1p) + kSmPart4); // [8][16][8]
   __nv_bfloat16* a5 = reinterpret_cast<__nv_bfloat16*>(reinterpret_cast<unsigned char*>(a1p) + kSmA5Off);   // [16][264]
@@ -683,71 +809,51 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     const int tap = c < 32 ? conv1_slot_tap(c >> 1) : -1;
     W1s[i] = tap >= 0 ? wb[L::c1 + r * 32 + 2 * tap + (c & 1)] : bz();
   }
-  for (int i = tid; i < 3 * 32 * kWRow; i += kFusedThreads)
+  // W2 as B core matrices for tcgen05: (k >> 3, co >> 3) at 512 B x 128 B, rows of 16 B
+  for (int i = tid; i < 32 * 288; i += kFusedThreads)
   {
-    const int l = i / (32 * kWRow), r = (i / kWRow) % 32, c = i % kWRow;
-    W2s[i] = c < 288 ? wb[L::c2 + l * 32 * 288 + r * 288 + c] : bz();
+    const int co = i / 288, k = i % 288;
+    W2s[(k >> 3) * 256 + (co >> 3) * 64 + (co & 7) * 8 + (k & 7)] = wb[L::c2 + i];
+  }
+  for (int i = tid; i < 2 * 32 * kWRow; i += kFusedThreads)
+  {
+    const int l = 1 + i / (32 * kWRow), r = (i / kWRow) % 32, c = i % kWRow;
+    W3s[i] = c < 288 ? wb[L::c2 + l * 32 * 288 + r * 288 + c] : bz();
   }
   for (int i = tid; i < kGroups * kSmGroup / 4; i += kFusedThreads)
     reinterpret_cast<uint32_t*>(sm + kSmW1 + kSmW)[i] = 0u;
+  if (tid == 0)
+    for (int g2 = 0; g2 < kGroups; ++g2) mbar_init(smem_addr(&mma_bar[g2]), 1);
+  if (tid < 32)
+  {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                 "n"(kProposalTmemCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  fence_proxy_async_smem();   // W2 (generic writes) before the tensor core reads it
+  tc_fence_before();
   __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_d = tmem_base + 32u * (uint32_t)grp;   // lanes 0..127, this group's 32 columns
+  const uint32_t bar = smem_addr(&mma_bar[grp]);
+  uint32_t mma_phase = 0;
   // From here on the two groups run independently: group grp takes tiles 2 b + grp, stepping
   // by 2 * gridDim.x, and meets only its own barrier.
   const int64_t tiles = (n + kT - 1) / kT;
   const int64_t tstep = (int64_t)gridDim.x * kGroups;
   int nsub = 0;   // tiles whose conv4 output waits in a4 (uniform over the group)
+  // Borders of x0p, a1c, a2p and a3p stay zero: their interiors are all that is written,
+  // except for the overlays at the start of a1c, which each tile clears.  A tile's windows
+  // are staged while the previous tile's conv2 products run (the first tile's here).
+  if ((int64_t)blockIdx.x * kGroups + grp < tiles)
+    stage_windows(x0p, ref, tar, w, h, pois, n, ((int64_t)blockIdx.x * kGroups + grp) * kT, warp, lane);
   for (int64_t tile = (int64_t)blockIdx.x * kGroups + grp; tile < tiles; tile += tstep)
   {
     const int64_t p0 = tile * kT;
-    // a3p of the previous tile overlays x0p, and the split-K partials and a5 overlay the
-    // start of a1p: clear both so their borders read as padding again
-    for (int i = gt; i < kSmX0 / 4; i += kGThreads) reinterpret_cast<uint32_t*>(x0p)[i] = 0u;
+    // the split-K partials and a5 of the previous tile overlay the start of a1c: clear them
+    // so a1c's borders read as padding again
     for (int i = gt; i < kSmScratch / 4; i += kGThreads) reinterpret_cast<uint32_t*>(a1p)[i] = 0u;
-    group_sync(grp);
-    // ---- input windows: warp 2p + c stages channel c (0 ref, 1 tar) of POI p.  Lane l holds
-    // column l of the 31x31 window in registers (coalesced row loads, one pass), the warp
-    // reduces mean and variance, and writes the normalised values into x0p's interior.
-    if (warp < 2 * kT)
-    {
-      const int p = warp >> 1, ch = warp & 1;
-      const int64_t i = p0 + p;
-      if (i < n)
-      {
-        const float* img = ch ? tar : ref;
-        const int cx = (int)pois[i].x, cy = (int)pois[i].y;
-        constexpr int R = kWin / 2, NPIX = kWin * kWin;
-        const int x = min(max(cx + lane - R, 0), w - 1);
-        float v[kWin];
-        float s = 0.f;
-        if (lane < kWin)
-        {
-#pragma unroll
-          for (int r = 0; r < kWin; ++r)
-          {
-            const int y = min(max(cy + r - R, 0), h - 1);
-            v[r] = __ldg(img + (size_t)y * w + x);
-          }
-#pragma unroll
-          for (int r = 0; r < kWin; ++r) s += v[r];
-        }
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        const float mean = s / NPIX;
-        float q = 0.f;
-        if (lane < kWin)
-        {
-#pragma unroll
-          for (int r = 0; r < kWin; ++r) q += (v[r] - mean) * (v[r] - mean);
-        }
-        for (int o = 16; o > 0; o >>= 1) q += __shfl_xor_sync(0xffffffffu, q, o);
-        const float inv = q > 0.f ? rsqrtf(q / NPIX) : 1.f;
-        if (lane < kWin)
-        {
-          __nv_bfloat16* dst = x0p + ((p * 33 + 1) * kX0Row + lane + 1) * 2 + ch;
-#pragma unroll
-          for (int r = 0; r < kWin; ++r) dst[r * kX0Row * 2] = __float2bfloat16((v[r] - mean) * inv);
-        }
-      }
-    }
     group_sync(grp);
     // ---- conv1: M = kT * 256 rows, K = 18 (padded 32), A gathered as (ci0, ci1) pairs
     {
@@ -797,17 +903,60 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
           {
             const int row = mt * 16 + g + h2 * 8;
             const int p = row >> 8, y = (row >> 4) & 15, x = row & 15;
-            __nv_bfloat16* dst = a1p + ((p * 18 + y + 1) * 18 + pcol<18>(x + 1)) * kPix + co;
-            *reinterpret_cast<uint32_t*>(dst) = pack_bf16(__float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)),
-                                                          __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
+            *reinterpret_cast<uint32_t*>(a1c + a1c_offset(p, y + 1, x + 1, co)) =
+                pack_bf16(__float2bfloat16(fmaxf(acc[j][h2 * 2] + bb0, 0.f)),
+                          __float2bfloat16(fmaxf(acc[j][h2 * 2 + 1] + bb1, 0.f)));
           }
         }
       }
     }
+    fence_proxy_async_smem();   // this thread's a1c writes before the tensor core reads them
     group_sync(grp);
-    // x0p is free: zero the a3p region (its border must read as zero padding)
-    for (int i = gt; i < kT * 6 * 6 * kPix / 2; i += kGThreads) reinterpret_cast<uint32_t*>(a3p)[i] = 0u;
-    fused_conv32<18, 8, 10, 2>(a1p, a2p, W2s, params + P::b2, warp, lane);
+    // ---- conv2 on tcgen05: step s = (tap, channel half) reads a1c through one descriptor
+    if (gt == 0)
+    {
+      tc_fence_after();
+      const uint32_t a0 = smem_addr(a1c), b0 = smem_addr(W2s);
+#pragma unroll
+      for (int st = 0; st < 18; ++st)
+      {
+        const int tap = st >> 1, half = st & 1, ky = tap / 3, kx = tap % 3;
+        const uint32_t aoff = 2 * half * kA1Plane + (ky & 1) * kA1Even + (ky >> 1) * kT * kA1Slot +
+                              ((kx & 1) * 9 + (kx >> 1)) * 16;
+        umma_bf16(tmem_d, umma_desc(a0 + aoff, kA1Plane, kA1Slot), umma_desc(b0 + 2 * st * 512, 512, 128), kConv2Idesc,
+                  st > 0);
+      }
+      umma_commit(bar);
+    }
+    // conv1 has consumed x0p: stage the next tile's windows while the products run
+    if (tile + tstep < tiles) stage_windows(x0p, ref, tar, w, h, pois, n, (tile + tstep) * kT, warp, lane);
+    if (!group_all(grp, mbar_wait_bounded(bar, mma_phase, kMmaWaitPolls)))
+    {
+      // the products did not complete in time: flag it, give them one more bounded wait
+      // (TMEM and a1c stay in use until they finish) and leave the tile loop
+      if (gt == 0) atomicOr(err, 2);
+      mbar_wait_bounded(bar, mma_phase, kMmaWaitPolls);
+      break;
+    }
+    mma_phase ^= 1u;
+    tc_fence_after();
+    {
+      // warp w reads TMEM lanes 32 (w & 3) .. + 31 (rows m), columns 16 (w >> 2) .. + 15
+      const int quarter = warp & 3, chalf = warp >> 2;
+      uint32_t r[16];
+      tmem_ld16(tmem_d + ((uint32_t)(32 * quarter) << 16) + 16u * (uint32_t)chalf, r);
+      const int m = 32 * quarter + lane, g2 = m >> 3, ox = m & 7, oy = g2 >> 1, p = g2 & 1;
+      const int co0 = 16 * chalf;
+      uint32_t packed[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        packed[k] = pack_bf16(__float2bfloat16(fmaxf(__uint_as_float(r[2 * k]) + params[P::b2 + co0 + 2 * k], 0.f)),
+                              __float2bfloat16(fmaxf(__uint_as_float(r[2 * k + 1]) + params[P::b2 + co0 + 2 * k + 1], 0.f)));
+      uint4* dst = reinterpret_cast<uint4*>(a2p + ((p * 10 + oy + 1) * 10 + pcol<10>(ox + 1)) * kPix + co0);
+      dst[0] = make_uint4(packed[0], packed[1], packed[2], packed[3]);
+      dst[1] = make_uint4(packed[4], packed[5], packed[6], packed[7]);
+    }
+    tc_fence_before();
     group_sync(grp);
     fused_conv32<10, 4, 6, 1>(a2p, a3p, W3s, params + P::b3, warp, lane);
     group_sync(grp);
@@ -953,6 +1102,14 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     }
     nsub = 0;
     group_sync(grp);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (tid < 32)
+  {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem_base), "n"(kProposalTmemCols)
+                 : "memory");
   }
 }
 

@@ -115,6 +115,7 @@ struct dic_cnn
   std::string last_error;
   DevBuf<float> params, grads, adam_m, adam_v, out, part, row_loss;
   DevBuf<__nv_bfloat16> wb, x0, a1, a2, a3, a4, a5, d1, d2, d3, d4, d5, dout;
+  DevBuf<int> wait_err;   // k_proposal_fused's bounded tensor-core wait (bit 1)
   int64_t cap = 0;
   long long adam_t = 0;
   long long launches = 0;
@@ -349,7 +350,7 @@ struct dic_engine
       DIC_CUDA(cudaMemcpyAsync(&iter_sum, counters.ptr, sizeof(unsigned long long), cudaMemcpyDeviceToHost, stream));
       DIC_CUDA(cudaStreamSynchronize(stream));
       iter_pending = false;
-      check_tile_error();
+      check_wait_error();
     }
   }
 
@@ -453,7 +454,7 @@ struct dic_engine
   {
     DIC_CUDA(cudaMemcpyAsync(pois, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, stream));
     DIC_CUDA(cudaStreamSynchronize(stream));
-    check_tile_error();
+    check_wait_error();
   }
   bool layout_matches(const dic_poi* pois, int64_t n) const
   {
@@ -534,8 +535,21 @@ struct dic_engine
     int w = 0, h = 0;
   };
   TileMap tile_maps[3];
-  DevBuf<int> tile_err;        // set by a k_icgn_tile CTA whose copy did not arrive in time
-  bool tile_pending = false;   // a tile launch since the last check
+  // Bounded waits inside kernels report here instead of hanging: bit 0, a k_icgn_tile CTA
+  // whose TMA copy did not arrive in time; bit 1, a k_proposal_fused warp group whose
+  // tensor-core products did not complete in time.
+  DevBuf<int> wait_err;
+  bool wait_pending = false;   // a launch that can set wait_err since the last check
+  int* wait_flag()
+  {
+    if (!wait_err.ptr)
+    {
+      wait_err.ensure(1);
+      DIC_CUDA(cudaMemsetAsync(wait_err.ptr, 0, sizeof(int), stream));
+    }
+    wait_pending = true;
+    return wait_err.ptr;
+  }
   // the 4-D map {component, x, y, plane} of a coefficient table (8 floats per texel and
   // plane, 2 planes), box {8, bx, by, 2}
   const CUtensorMap& coef_map(int kind, const float4* table, int tw, int th)
@@ -563,18 +577,24 @@ struct dic_engine
     m.h = th;
     return m.map;
   }
-  // after a synchronisation: a tile launch whose copy timed out makes its results invalid
-  void check_tile_error()
+  static std::string wait_error_text(int flag)
   {
-    if (!tile_pending) return;
-    tile_pending = false;
+    std::string t = (flag & 1) ? "k_icgn_tile: a TMA tile copy did not complete in time" : "";
+    if (flag & 2) t += std::string(t.empty() ? "" : "; ") + "k_proposal_fused: a tensor-core product did not complete in time";
+    return t + "; results are invalid";
+  }
+  // after a synchronisation: a launch whose bounded wait ran out makes its results invalid
+  void check_wait_error()
+  {
+    if (!wait_pending) return;
+    wait_pending = false;
     int flag = 0;
-    DIC_CUDA(cudaMemcpyAsync(&flag, tile_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    DIC_CUDA(cudaMemcpyAsync(&flag, wait_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, stream));
     DIC_CUDA(cudaStreamSynchronize(stream));
     if (flag)
     {
-      DIC_CUDA(cudaMemsetAsync(tile_err.ptr, 0, sizeof(int), stream));
-      throw DicError{DIC_ERR_CUDA, "k_icgn_tile: a TMA tile copy did not complete in time; results are invalid"};
+      DIC_CUDA(cudaMemsetAsync(wait_err.ptr, 0, sizeof(int), stream));
+      throw DicError{DIC_ERR_CUDA, wait_error_text(flag)};
     }
   }
   static constexpr int64_t kTuneMinPois = 2048;
@@ -638,7 +658,7 @@ struct dic_engine
     const CUtensorMap& m = coef_map(kind, p.coef, p.w, p.h);
     const unsigned grid =
         (unsigned)std::min<int64_t>((int64_t)sms * kTileKinds[kind].ctas, (p.n + W - 1) / W);
-    k_icgn_tile<W, BX, BY><<<grid, W * 32, tile_smem_bytes<BX, BY>(), stream>>>(p, m, icgn_next.ptr, tile_err.ptr);
+    k_icgn_tile<W, BX, BY><<<grid, W * 32, tile_smem_bytes<BX, BY>(), stream>>>(p, m, icgn_next.ptr, wait_flag());
   }
   void launch_icgn(const IcgnParams& p, bool column, const IcgnShape& sh)
   {
@@ -646,17 +666,11 @@ struct dic_engine
     if (sh.tile && column)
     {
       icgn_next.ensure(1);
-      if (!tile_err.ptr)
-      {
-        tile_err.ensure(1);
-        DIC_CUDA(cudaMemsetAsync(tile_err.ptr, 0, sizeof(int), stream));
-      }
       DIC_CUDA(cudaMemsetAsync(icgn_next.ptr, 0, sizeof(unsigned long long), stream));
       int sms = 0;
       DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
       if (sh.tile == 1) launch_tile<4, 48, 36>(p, 1, sms);
       else launch_tile<8, 64, 40>(p, 2, sms);
-      tile_pending = true;
       return;
     }
     if (sh.ctas_per_sm > 0)
@@ -772,7 +786,7 @@ struct dic_engine
       }
       if (t < best.ms) best = IcgnShape{sh.warps, sh.ctas_per_sm, t, sh.tile};
     }
-    check_tile_error();
+    check_wait_error();
     shape[0][column] = best;
     tuned[0][column] = true;
   }
@@ -1033,7 +1047,7 @@ struct dic_engine
       const int64_t tiles = (n + cnn::kT - 1) / cnn::kT;
       const unsigned grid = (unsigned)std::min<int64_t>((tiles + cnn::kGroups - 1) / cnn::kGroups, sms);
       cnn::k_proposal_fused<<<grid, cnn::kFusedThreads, cnn::kSmTotal, stream>>>(
-          ref_f32.ptr, tar_f32.ptr, w, h, queue.ptr, n, proposal->wb.ptr, proposal->params.ptr);
+          ref_f32.ptr, tar_f32.ptr, w, h, queue.ptr, n, proposal->wb.ptr, proposal->params.ptr, wait_flag());
       check_launch("k_proposal_fused");
     }
     mark(kPhProposal, 1);
@@ -1393,7 +1407,7 @@ struct dic_engine
     FrameCounters c{};
     DIC_CUDA(cudaMemcpyAsync(&c, fcount.ptr, sizeof(c), cudaMemcpyDeviceToHost, stream));
     DIC_CUDA(cudaStreamSynchronize(stream));
-    check_tile_error();
+    check_wait_error();
     report_from(r, c, n, use_skip, host_results, learned);
   }
   void report_from(dic_frame_report* r, const FrameCounters& c, int64_t n, bool use_skip, const dic_poi* host_results,
@@ -1566,6 +1580,7 @@ void dic_engine_destroy(dic_engine* e)
   e->bjobs.release();
   e->bnext.release();
   e->icgn_next.release();
+  e->wait_err.release();
   e->tune_q.release();
   e->release_staging();
   e->release_frame_outputs();
@@ -1898,7 +1913,7 @@ int dic_sequence_frame(dic_engine* e, const void* px, int32_t w, int32_t h, int6
     if (results || report)
     {
       DIC_CUDA(cudaStreamSynchronize(e->stream));
-      e->check_tile_error();
+      e->check_wait_error();
     }
     e->fill_report(report, n, use_skip, results, learned);
     e->seq_last_skip = use_skip;
@@ -1923,12 +1938,11 @@ int dic_sequence_fetch(dic_engine* e, int32_t frames_back, dic_poi* results, dic
       DIC_CUDA(cudaMemcpyAsync(results, e->seq_out[slot].ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost,
                                e->down_stream));
     DIC_CUDA(cudaMemcpyAsync(&c, e->seq_cnt[slot].ptr, sizeof(c), cudaMemcpyDeviceToHost, e->down_stream));
-    int tile_flag = 0;   // a TMA-staged IC-GN of this frame whose copy timed out
-    if (e->tile_err.ptr)
-      DIC_CUDA(cudaMemcpyAsync(&tile_flag, e->tile_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, e->down_stream));
+    int wait_flag = 0;   // a bounded wait of this frame's kernels that ran out
+    if (e->wait_err.ptr)
+      DIC_CUDA(cudaMemcpyAsync(&wait_flag, e->wait_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, e->down_stream));
     DIC_CUDA(cudaStreamSynchronize(e->down_stream));
-    if (tile_flag)
-      throw DicError{DIC_ERR_CUDA, "k_icgn_tile: a TMA tile copy did not complete in time; results are invalid"};
+    if (wait_flag) throw DicError{DIC_ERR_CUDA, dic_engine::wait_error_text(wait_flag)};
     e->report_from(report, c, n, e->seq_out_skip[slot], results, e->seq_policy.learned_seed != 0);
   });
 }
@@ -2199,6 +2213,7 @@ void dic_cnn_destroy(dic_cnn* c)
   for (auto* b : {&c->wb, &c->x0, &c->a1, &c->a2, &c->a3, &c->a4, &c->a5, &c->d1, &c->d2, &c->d3, &c->d4, &c->d5,
                   &c->dout})
     b->release();
+  c->wait_err.release();
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -2250,11 +2265,16 @@ int dic_cnn_seed(dic_cnn* c, const float* d_ref, const float* d_tar, int32_t w, 
     DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
     DIC_CUDA(cudaFuncSetAttribute(cnn::k_proposal_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cnn::kSmTotal));
     const int64_t tiles = (n + cnn::kT - 1) / cnn::kT;
+    c->wait_err.ensure(1);
+    DIC_CUDA(cudaMemsetAsync(c->wait_err.ptr, 0, sizeof(int), c->stream));
     cnn::k_proposal_fused<<<(unsigned)std::min<int64_t>((tiles + cnn::kGroups - 1) / cnn::kGroups, sms),
                             cnn::kFusedThreads, cnn::kSmTotal, c->stream>>>(
-        d_ref, d_tar, w, h, d_pois, n, c->wb.ptr, c->params.ptr);
+        d_ref, d_tar, w, h, d_pois, n, c->wb.ptr, c->params.ptr, c->wait_err.ptr);
     c->check("k_proposal_fused");
+    int flag = 0;
+    DIC_CUDA(cudaMemcpyAsync(&flag, c->wait_err.ptr, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     DIC_CUDA(cudaStreamSynchronize(c->stream));
+    if (flag) throw DicError{DIC_ERR_CUDA, "k_proposal_fused: a tensor-core product did not complete in time"};
   });
 }
 

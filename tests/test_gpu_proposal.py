@@ -80,12 +80,15 @@ def test_learned_seed_parity_and_gain(dic, oracle_mod, torch_mod):
     assert it_learned < it_fftcc, (it_learned, it_fftcc)
 
 
-def test_fused_inference_matches_layerwise(dic, torch_mod):
-    """The fused per-tile kernel (dic_cnn_seed) gives the layer-by-layer GEMM path's outputs."""
+@pytest.mark.parametrize("drop", [0, 3])
+def test_fused_inference_matches_layerwise(dic, torch_mod, drop):
+    """The fused per-tile kernel (dic_cnn_seed; conv2 on tcgen05) gives the layer-by-layer
+    GEMM path's outputs, also for an odd queue (a tile with one live POI, a partial MLP batch)."""
     torch = torch_mod
     from fasticgn_gb300 import proposal, speckle
     pr = speckle.pair_bumps(seed=31, width=320, height=320)
     q = dic.grid_queue(320, 320, 15, 9)
+    q = q[:len(q) - drop].copy()
     n = len(q)
     net = proposal.ProposalNet(0, proposal.init_params(4))
     rf = torch.from_numpy(pr.ref.astype(np.float32)).cuda()
