@@ -711,8 +711,9 @@ __device__ __forceinline__ float sample_bspline_tile(const CoefTile& T, const fl
 constexpr int kIcgnRowUnroll = DIC_ICGN_ROW_UNROLL;
 
 // One POI (queue index i) on the calling warp; shared by the per-queue launch (k_icgn) and
-// the persistent multi-job launch (k_icgn_batch).
-template <bool kColumn, bool kTile = false>
+// the persistent multi-job launch (k_icgn_batch, which keeps one row in flight: its job
+// lookup leaves no registers for two without spilling).
+template <bool kColumn, bool kTile = false, int kRowUnroll = kIcgnRowUnroll>
 __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int lane, const CoefTile& T = CoefTile{})
 {
   dic_poi* poi = P.pois + i;
@@ -759,7 +760,7 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
       if (col_active)
       {
         const float ax = fmaf(W[0], flx_col, W[2]), ay = fmaf(W[3], flx_col, W[5]);
-#pragma unroll kIcgnRowUnroll
+#pragma unroll kRowUnroll
         for (int r = 0; r < 2 * ry + 1; ++r)
         {
           const float fly = (float)(r - ry);
@@ -1153,7 +1154,7 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_b
     P.conv = conv;
     P.max_iter = max_iter;
     P.iter_sum = iter_sum;
-    icgn_solve<kColumn>(P, k, lane);
+    icgn_solve<kColumn, false, 1>(P, k, lane);
   }
 }
 
