@@ -688,7 +688,7 @@ def run_ours(args):
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel (IC-GN; gather model of SURVEY section 8d)
+    # ---- roofline of the dominant kernel (IC-GN; gather model: 64 B texel + 12 B reference per sample and iteration, 224 B per POI)
     N = (2 * R + 1) ** 2
     H0 = res[headline]
     icgn_ms = H0["kernels_ms"]["ms_icgn"]
@@ -702,7 +702,7 @@ def run_ours(args):
                 "model": "64 B B-spline texel per warped sample per iteration + 12 B ref/grad per sample "
                          "+ 224 B per-POI record/IO; the gathers are served on chip, see profiles/"}
 
-    # ---- the other hot kernels against their own bounds (SURVEY 8(d) FLOP models)
+    # ---- the other hot kernels against their own bounds (FLOP models per POI)
     M = 2 * R
     fftcc_flop = 2 * (2.5 * M * M * np.log2(M * M)) + 6 * M * (M // 2 + 1) + 4 * M * M
     fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12       # nominal FP32: 152 SMs x 128 FMA/clk at 2.07 GHz

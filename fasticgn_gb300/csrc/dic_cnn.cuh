@@ -645,7 +645,6 @@ __device__ __forceinline__ bool group_all(int grp, bool v)
       : "memory");
   return r != 0;
 }
-constexpr uint32_t kMmaWaitPolls = 1u << 22;
 constexpr int kProposalTmemCols = 32 * kGroups;   // one 128 x 32 f32 accumulator per warp group
 
 // Input windows of the tile starting at POI p0 into x0p's interior: warp 2p + c of the group
@@ -777,7 +776,8 @@ __device__ __forceinline__ void fused_conv32(const __nv_bfloat16* in, __nv_bfloa
 __global__ void __launch_bounds__(kFusedThreads, 1)
     k_proposal_fused(const float* __restrict__ ref, const float* __restrict__ tar, int w, int h,
                      dic_poi* __restrict__ pois, int64_t n, const __nv_bfloat16* __restrict__ wb,
-                     const float* __restrict__ params, int* __restrict__ err)
+                     const float* __restrict__ params, int* __restrict__ err, uint32_t wait_polls = kWaitPolls,
+                     int wait_test = 0)   // wait_test: never issue conv2's products (timeout-path test)
 {
   extern __shared__ __align__(16) unsigned char sm[];
   __shared__ __align__(8) unsigned long long mma_bar[kGroups];
@@ -913,7 +913,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     fence_proxy_async_smem();   // this thread's a1c writes before the tensor core reads them
     group_sync(grp);
     // ---- conv2 on tcgen05: step s = (tap, channel half) reads a1c through one descriptor
-    if (gt == 0)
+    if (gt == 0 && !wait_test)
     {
       tc_fence_after();
       const uint32_t a0 = smem_addr(a1c), b0 = smem_addr(W2s);
@@ -930,12 +930,12 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     }
     // conv1 has consumed x0p: stage the next tile's windows while the products run
     if (tile + tstep < tiles) stage_windows(x0p, ref, tar, w, h, pois, n, (tile + tstep) * kT, warp, lane);
-    if (!group_all(grp, mbar_wait_bounded(bar, mma_phase, kMmaWaitPolls)))
+    if (!group_all(grp, mbar_wait_bounded(bar, mma_phase, wait_polls)))
     {
       // the products did not complete in time: flag it, give them one more bounded wait
       // (TMEM and a1c stay in use until they finish) and leave the tile loop
       if (gt == 0) atomicOr(err, 2);
-      mbar_wait_bounded(bar, mma_phase, kMmaWaitPolls);
+      mbar_wait_bounded(bar, mma_phase, wait_polls);
       break;
     }
     mma_phase ^= 1u;

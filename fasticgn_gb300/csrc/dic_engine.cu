@@ -5,6 +5,7 @@
 // point of view except dic_run_device, which only enqueues work on the engine stream.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <functional>
 #include <mutex>
@@ -540,6 +541,14 @@ struct dic_engine
   // tensor-core products did not complete in time.
   DevBuf<int> wait_err;
   bool wait_pending = false;   // a launch that can set wait_err since the last check
+  // Timeout-path test hook, read once at engine creation from DIC_TEST_WAIT_FAULT: bit 0,
+  // k_icgn_tile arms its copy wait but never issues the copy; bit 1, k_proposal_fused never
+  // issues conv2's products.  Either wait then runs out after kTestWaitPolls polls, the
+  // kernel reports through wait_err, and the call fails with DIC_ERR_CUDA.  Nothing faults:
+  // no copy or product is left in flight.
+  static constexpr uint32_t kTestWaitPolls = 1u << 12;
+  int wait_test = 0;
+  uint32_t wait_polls = kWaitPolls;
   int* wait_flag()
   {
     if (!wait_err.ptr)
@@ -656,9 +665,12 @@ struct dic_engine
                                     (int)tile_smem_bytes<BX, BY>()));
     });
     const CUtensorMap& m = coef_map(kind, p.coef, p.w, p.h);
+    IcgnParams q = p;
+    q.wait_polls = wait_polls;
+    q.wait_test = wait_test & 1;
     const unsigned grid =
         (unsigned)std::min<int64_t>((int64_t)sms * kTileKinds[kind].ctas, (p.n + W - 1) / W);
-    k_icgn_tile<W, BX, BY><<<grid, W * 32, tile_smem_bytes<BX, BY>(), stream>>>(p, m, icgn_next.ptr, wait_flag());
+    k_icgn_tile<W, BX, BY><<<grid, W * 32, tile_smem_bytes<BX, BY>(), stream>>>(q, m, icgn_next.ptr, wait_flag());
   }
   void launch_icgn(const IcgnParams& p, bool column, const IcgnShape& sh)
   {
@@ -1047,7 +1059,8 @@ struct dic_engine
       const int64_t tiles = (n + cnn::kT - 1) / cnn::kT;
       const unsigned grid = (unsigned)std::min<int64_t>((tiles + cnn::kGroups - 1) / cnn::kGroups, sms);
       cnn::k_proposal_fused<<<grid, cnn::kFusedThreads, cnn::kSmTotal, stream>>>(
-          ref_f32.ptr, tar_f32.ptr, w, h, queue.ptr, n, proposal->wb.ptr, proposal->params.ptr, wait_flag());
+          ref_f32.ptr, tar_f32.ptr, w, h, queue.ptr, n, proposal->wb.ptr, proposal->params.ptr, wait_flag(), wait_polls,
+          (wait_test >> 1) & 1);
       check_launch("k_proposal_fused");
     }
     mark(kPhProposal, 1);
@@ -1513,6 +1526,11 @@ int dic_engine_create(const dic_config* config, dic_engine** out)
     DIC_CUDA(cudaSetDevice(config->device));
     init_constants(config->device);
     DIC_CUDA(cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking));
+    if (const char* t = std::getenv("DIC_TEST_WAIT_FAULT"))
+    {
+      e->wait_test = std::atoi(t) & 3;
+      if (e->wait_test) e->wait_polls = dic_engine::kTestWaitPolls;
+    }
     DIC_CUDA(cudaFuncSetAttribute(k_fftcc_large, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)(2 * kMaxTwiddleN * (kMaxTwiddleN + 1) * sizeof(float2))));
     DIC_CUDA(cudaFuncSetAttribute(cnn::k_proposal_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, cnn::kSmTotal));

@@ -578,6 +578,9 @@ __global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4*
 // when some sample fails does the warp re-walk the subset to apply the CPU's order, out of
 // range (-3) before NaN (-5).
 // --------------------------------------------------------------------------------------
+// Polls of a bounded mbarrier wait before a kernel gives up and reports (a few ms at most).
+constexpr uint32_t kWaitPolls = 1u << 22;
+
 struct IcgnParams
 {
   const float4* coef;      // tar B-spline table: 2 planes of W*H texels x 2 float4
@@ -592,6 +595,8 @@ struct IcgnParams
   unsigned long long* iter_sum;  // sum of iterations (nullable)
   const int64_t* n_dev = nullptr;   // device-side queue length (overrides n when set)
   const int* enable = nullptr;      // device-side switch: the launch does nothing when 0
+  uint32_t wait_polls = kWaitPolls; // k_icgn_tile: bound of its copy wait
+  int wait_test = 0;                // k_icgn_tile: 1 = arm the wait but never issue the copy (timeout-path test)
 };
 
 // Queue-slot guard shared by the solver kernels: launches sized for the largest possible
@@ -997,7 +1002,6 @@ __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* map
 // flagged in `err`, and the CTA waits (bounded) for its copy before it leaves.
 // --------------------------------------------------------------------------------------
 constexpr int kTileMargin = 2;
-constexpr uint32_t kTileWaitPolls = 1u << 22;
 
 // dynamic shared memory of one k_icgn_tile CTA: the block plus room to align it to 128 B
 template <int BX, int BY>
@@ -1076,7 +1080,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_icgn_tile(IcgnParams P, const _
       {
         fence_proxy_async_smem();   // the previous chunk's shared-memory reads come first
         mbar_arrive_expect_tx(bar_a, (uint32_t)(4 * BX * BY * sizeof(float4)));
-        tma_load_4d(smem_addr(tile_smem), &map, 0, u0, v0, 0, bar_a);
+        if (!P.wait_test) tma_load_4d(smem_addr(tile_smem), &map, 0, u0, v0, 0, bar_a);
       }
     }
     __syncthreads();
@@ -1088,12 +1092,12 @@ __global__ void __launch_bounds__(kWarps * 32) k_icgn_tile(IcgnParams P, const _
     T.oy = org[1];
     if (org[2])
     {
-      const bool done = mbar_wait_bounded(bar_a, parity, kTileWaitPolls);
+      const bool done = mbar_wait_bounded(bar_a, parity, P.wait_polls);
       parity ^= 1u;
       if (!__syncthreads_and(done))
       {
         if (threadIdx.x == 0) atomicOr(err, 1);
-        mbar_wait_bounded(bar_a, parity ^ 1u, kTileWaitPolls);   // the copy in flight, once more
+        mbar_wait_bounded(bar_a, parity ^ 1u, P.wait_polls);   // the copy in flight, once more
         return;
       }
     }

@@ -101,3 +101,34 @@ def test_fused_inference_matches_layerwise(dic, torch_mod, drop):
     scale = np.abs(out[:, :6]).max()
     assert np.max(np.abs(got - out[:, :6])) <= 2e-2 * scale, np.max(np.abs(got - out[:, :6]))
     assert np.median(np.abs(got - out[:, :6])) <= 2e-3 * scale
+
+
+def test_proposal_product_timeout_is_reported(dic, monkeypatch):
+    """conv2's tensor-core products never issued (the DIC_TEST_WAIT_FAULT hook) end in the
+    kernel's bounded mbarrier wait: the learned pair fails with DIC_ERR_CUDA naming the
+    products, TMEM is released, and a fresh engine on the same context solves normally."""
+    from fasticgn_gb300 import proposal, speckle, _lib
+    pr = speckle.pair_bumps(seed=41, width=320, height=320)
+    net = proposal.ProposalNet(0, proposal.init_params(2))
+    q = dic.grid_queue(320, 320, 15, 8)
+
+    def run(fault):
+        if fault:
+            monkeypatch.setenv("DIC_TEST_WAIT_FAULT", "2")
+        e = dic.Engine(15)
+        monkeypatch.delenv("DIC_TEST_WAIT_FAULT", raising=False)
+        e.set_proposal(net)
+        e.set_ref(pr.ref)
+        e.set_tar(pr.tar)
+        try:
+            return e.process_pair_learned(q.copy())
+        finally:
+            e.close()
+
+    want, _ = run(False)
+    with pytest.raises(_lib.DicError) as info:
+        run(True)
+    assert info.value.code == _lib.DIC_ERR_CUDA and "tensor-core product" in str(info.value)
+    got, _ = run(False)
+    np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8))
+    net.close()

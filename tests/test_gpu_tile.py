@@ -80,3 +80,26 @@ def test_launch_shape_arguments(dic):
     e.set_launch_shape(True, warps_per_cta=2, ctas_per_sm=0)
     assert e.tuning()["icgn_column"]["warps_per_cta"] == 2 and e.tuning()["icgn_column"]["tile"] == 0
     e.close()
+
+
+def test_tile_copy_timeout_is_reported(dic, monkeypatch):
+    """A TMA copy that never arrives (the DIC_TEST_WAIT_FAULT hook arms the wait and skips the
+    copy) ends in the kernel's bounded wait: the call fails with DIC_ERR_CUDA naming the tile
+    copy, nothing faults, and the same context then solves the pair normally."""
+    from fasticgn_gb300 import speckle, _lib
+    pr = speckle.pair_bumps(seed=9, width=320, height=288, max_disp=4.0, max_strain=0.01)
+    want, _, _ = solve(dic, pr, 15, 4, tile=1)
+    monkeypatch.setenv("DIC_TEST_WAIT_FAULT", "1")
+    e = dic.Engine(15)
+    monkeypatch.delenv("DIC_TEST_WAIT_FAULT")
+    e.set_launch_shape(True, tile=1)
+    e.set_autotune(False)
+    e.set_ref(pr.ref)
+    e.set_tar(pr.tar)
+    q = dic.grid_queue(320, 288, 15, 4)
+    with pytest.raises(_lib.DicError) as info:
+        e.process_pair(q)
+    assert info.value.code == _lib.DIC_ERR_CUDA and "TMA tile copy" in str(info.value)
+    e.close()
+    got, _, _ = solve(dic, pr, 15, 4, tile=1)
+    np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8))
