@@ -656,14 +656,16 @@ struct dic_engine
   }
   DevBuf<unsigned long long> icgn_next;   // work counter of the persistent single-queue launch
 
+  bool tile_attr_set[3] = {};   // per engine, so per device: the shared-memory opt-in of each tile form
   template <int W, int BX, int BY>
   void launch_tile(const IcgnParams& p, int kind, int sms)
   {
-    static std::once_flag attr;
-    std::call_once(attr, [] {
+    if (!tile_attr_set[kind])
+    {
       DIC_CUDA(cudaFuncSetAttribute(k_icgn_tile<W, BX, BY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)tile_smem_bytes<BX, BY>()));
-    });
+      tile_attr_set[kind] = true;
+    }
     const CUtensorMap& m = coef_map(kind, p.coef, p.w, p.h);
     IcgnParams q = p;
     q.wait_polls = wait_polls;
