@@ -16,6 +16,7 @@ e2e    = the same through the C ABI with host buffers (dic_set_ref / dic_set_tar
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -411,6 +412,7 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
         eng.sequence_frame(None, None, staged=True, width=W, height=H, dtype=_lib.DIC_U16, report=False)
 
     t0 = None
+    gc.disable()   # no collector pause inside a ~30 ms host-clocked window
     enqueue(0)
     for k in range(len(tars_h)):
         if k == 1:   # frames 0 and 1 solved; the clock covers staging, solving and reading 2..
@@ -428,6 +430,7 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
             reports.append(rep)
             results.append(res)
     e2e_s = time.perf_counter() - t0
+    gc.enable()
     timed = len(tars_h) - 2
     # ---- device-resident frames
     tars_d = [torch.from_numpy(t).to(dev) for t in tars]
@@ -660,6 +663,7 @@ def run_ours(args):
         q_h.numpy()[:] = tmpl_bytes
         e2e_step()
     e2e_times = []
+    gc.disable()   # no collector pause inside a timed step
     for _ in range(args.steps):
         q_h.numpy()[:] = tmpl_bytes          # the caller's fresh POI queue (untimed)
         with torch.cuda.stream(stream):
@@ -671,6 +675,7 @@ def run_ours(args):
         e.record(stream)
         e.synchronize()
         e2e_times.append(s.elapsed_time(e))
+    gc.enable()
     e2e_ms = rank_max(float(np.mean(e2e_times)))
     assert q_np.tobytes() == res[headline]["result"].tobytes(), "host and device entry points disagree"
 

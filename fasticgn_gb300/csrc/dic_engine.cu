@@ -356,12 +356,20 @@ struct dic_engine
   }
 
   // ---------------------------------------------------------------- images
+  // The solvers index texels with 32-bit products (y * w + x): images stay below 2^31 pixels
+  // (the B-spline table alone would then be 128 GiB).
+  static void check_pixel_count(int width, int height)
+  {
+    if ((int64_t)width * height >= ((int64_t)1 << 31))
+      throw DicError{DIC_ERR_ARGUMENT, "image: 2^31 pixels or more (texel indices are 32-bit)"};
+  }
   void set_image(bool is_ref, const void* px, int width, int height, int64_t stride, int dtype, bool device)
   {
     const int es = dtype_size(dtype);
     if (!px || es == 0 || width < 5 || height < 5)
       throw DicError{DIC_ERR_ARGUMENT, "image: null pixels, unknown dtype or size below 5x5"};
     if (stride < (int64_t)width * es) throw DicError{DIC_ERR_ARGUMENT, "image: row stride smaller than a row"};
+    check_pixel_count(width, height);
     const bool other_set = is_ref ? tar_set : ref_set;
     if (other_set && (width != w || height != h))
     {
@@ -2025,6 +2033,7 @@ int dic_batch_process(dic_engine* e, const dic_job* jobs, int32_t njobs, int32_t
           J.count < 0 || (J.count > 0 && !J.pois) || J.subset_radius < 1 || 2 * J.subset_radius > kMaxTwiddleN)
         throw DicError{DIC_ERR_ARGUMENT, "batch job " + std::to_string(j) +
                                              ": bad image, queue or subset radius (square, 1..32)"};
+      dic_engine::check_pixel_count(J.width, J.height);
     }
     e->run_batch(jobs, njobs, pixels_on_device != 0, report);
   });

@@ -657,7 +657,7 @@ __device__ __forceinline__ float sample_bspline(const float4* __restrict__ coef,
   const float fx = floorf(gxp), fy = floorf(gyp);
   const float dx = gxp - fx, dy = gyp - fy;
   float4 c0, c1, c2, c3;
-  load_texel(coef, plane, (size_t)(int)fy * w + (int)fx, c0, c1, c2, c3);
+  load_texel(coef, plane, (size_t)((int)fy * w + (int)fx), c0, c1, c2, c3);   // images < 2^31 pixels
   const float r0 = fmaf(fmaf(fmaf(c0.w, dx, c0.z), dx, c0.y), dx, c0.x);
   const float r1 = fmaf(fmaf(fmaf(c1.w, dx, c1.z), dx, c1.y), dx, c1.x);
   const float r2 = fmaf(fmaf(fmaf(c2.w, dx, c2.z), dx, c2.y), dx, c2.x);
@@ -694,7 +694,7 @@ __device__ __forceinline__ float sample_bspline_tile(const CoefTile& T, const fl
     c3 = t[2 * pl + 1];
   }
   else
-    load_texel(coef, plane, (size_t)iy * w + ix, c0, c1, c2, c3);
+    load_texel(coef, plane, (size_t)(iy * w + ix), c0, c1, c2, c3);
   const float r0 = fmaf(fmaf(fmaf(c0.w, dx, c0.z), dx, c0.y), dx, c0.x);
   const float r1 = fmaf(fmaf(fmaf(c1.w, dx, c1.z), dx, c1.y), dx, c1.x);
   const float r2 = fmaf(fmaf(fmaf(c2.w, dx, c2.z), dx, c2.y), dx, c2.x);

@@ -385,3 +385,17 @@ def test_state_errors(dic):
         e.set_tar(np.zeros((64, 65), np.uint8))
     with pytest.raises(ValueError):
         e.set_ref(np.zeros((64, 64, 3), np.uint8))
+
+
+def test_oversize_image_rejected(dic):
+    """Texel indices are 32-bit: an image of 2^31 pixels or more is refused before any byte
+    of it is read (the declared size is what is checked; the buffer here is one row)."""
+    from fasticgn_gb300 import _lib
+    e = dic.Engine(7)
+    row = np.zeros(65536, np.uint8)
+    L = _lib.load()
+    rc = L.dic_set_ref(e._h, row.ctypes.data, 65536, 32768, 65536, _lib.DIC_U8)
+    assert rc == _lib.DIC_ERR_ARGUMENT
+    assert b"2^31" in L.dic_last_error(e._h)
+    e.set_ref(np.zeros((64, 64), np.uint8))   # the engine is still usable
+    e.close()
