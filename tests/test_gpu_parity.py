@@ -117,9 +117,12 @@ def test_fftcc_matches_oracle_r15(dic, oracle_mod, affine_pair):
     assert np.median(np.abs(q["u"] - ut)) < 1.0 and np.median(np.abs(q["v"] - vt)) < 1.0
 
 
-@pytest.mark.parametrize("radius", [4, 10, 12, 16, 17, 20, 25, 30, 31, 32])
+@pytest.mark.parametrize("radius", [3, 4, 5, 6, 7, 9, 10, 11, 12, 13, 14, 16, 17, 20, 25, 30, 31, 32])
 def test_fftcc_matches_oracle_radii(dic, oracle_mod, radius):
-    """Register FFT (2r <= 32) and the large-radius path against the oracle, shifted speckle."""
+    """Register FFT (2r <= 32) and the large-radius path against the oracle, shifted speckle.
+    Every prime-factor split of k_fftcc2 is covered: 2r = 6, 10, 14, 18, 22, 26 (2 x odd),
+    12, 20, 28 (4 x odd), 24 (8 x 3), 30 (2 x 3 x 5, the headline test); 8 and 16 are powers
+    of two (Cooley-Tukey)."""
     O = oracle_mod
     from fasticgn_gb300 import speckle
     pr = speckle.pair_affine(seed=radius, width=256, height=224)
