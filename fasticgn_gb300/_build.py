@@ -73,7 +73,7 @@ def build_cli(force: bool = False, verbose: bool = False) -> Path:
     if not cxx:
         raise RuntimeError("a C++17 compiler (g++) is needed for the command line")
     tmp = CLI.with_name(f"{CLI.name}.tmp{os.getpid()}")
-    cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-I", str(INCLUDE),
+    cmd = [cxx, "-O3", "-std=c++17", "-Wall", "-I", str(INCLUDE),
            f'-DDIC_CLI_GIT_HASH="{head or "unknown"}"', f'-DDIC_CLI_BUILD_DATE="{date}"',
            f'-DDIC_CLI_GIT_DIRTY="{dirty}"',
            *[str(p) for p in sorted(CLI_DIR.glob("*.cpp"))], "-o", str(tmp),

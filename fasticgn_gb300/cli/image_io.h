@@ -29,6 +29,10 @@ struct Image
 
 // Throws std::runtime_error with the file name on any decode error.
 Image read_image(const std::string& path);
+// The same, reading the file into `file_buf` and decoding into the vectors of `reuse` (a
+// previous frame's, returned by the caller): a frame loop then allocates nothing.
+Image read_image(const std::string& path, std::vector<uint8_t>& file_buf, Image&& reuse);
+Image read_image(const std::string& path, std::vector<uint8_t>&& file_buf, Image&& reuse);
 
 enum class Depth { k8, k12, k16, kAuto };
 enum class Align { kRight, kLeft, kAuto };

@@ -570,9 +570,10 @@ struct Payload
   size_t rows = 0;
 };
 
-Payload format_raw(const std::vector<dic_poi>& q, const Options& o)
+// into `p`, whose buffer keeps its capacity across frames
+void format_raw_into(const std::vector<dic_poi>& q, const Options& o, Payload& p)
 {
-  Payload p;
+  p.rows = 0;
   p.bytes.resize(q.size() * kRecordBytes);
   char* c = p.bytes.data();
   for (const auto& poi : q)
@@ -587,6 +588,12 @@ Payload format_raw(const std::vector<dic_poi>& q, const Options& o)
     ++p.rows;
   }
   p.bytes.resize((size_t)(c - p.bytes.data()));
+}
+
+Payload format_raw(const std::vector<dic_poi>& q, const Options& o)
+{
+  Payload p;
+  format_raw_into(q, o, p);
   return p;
 }
 
@@ -869,14 +876,20 @@ struct Engine
 };
 
 // ------------------------------------------------------------------ background workers
-// Decodes the targets in list order, at most `ahead` frames ahead of the consumer.
+// Decodes the targets with `workers` threads (--decode-threads; worker w takes frames
+// w, w + workers, ...), at most workers + 1 frames ahead of the consumer, and hands them
+// out in list order, so results do not depend on the count.  Each worker reads files into
+// its own buffer, and decodes into the sample vectors the consumer returns (recycle), so
+// a steady frame loop allocates and first-touches no memory.
 class Preloader
 {
  public:
-  Preloader(std::vector<std::string> paths, InputOptions opt, bool enabled)
-      : paths_(std::move(paths)), opt_(opt), enabled_(enabled)
+  Preloader(std::vector<std::string> paths, InputOptions opt, bool enabled, int workers)
+      : paths_(std::move(paths)), opt_(opt), enabled_(enabled),
+        workers_(std::max(1, std::min<int>(workers, (int)std::max<size_t>(paths_.size(), 1))))
   {
-    if (enabled_) worker_ = std::thread([this] { run(); });
+    if (enabled_)
+      for (int w = 0; w < workers_; ++w) threads_.emplace_back([this, w] { run(w); });
   }
   ~Preloader()
   {
@@ -885,20 +898,31 @@ class Preloader
       stop_ = true;
     }
     cv_.notify_all();
-    if (worker_.joinable()) worker_.join();
+    for (auto& t : threads_)
+      if (t.joinable()) t.join();
   }
   // frame k, in order; rethrows a decode error of that frame
   Samples get(size_t k)
   {
-    if (!enabled_) return configure(read_image(paths_[k]), opt_, paths_[k]);
+    if (!enabled_) return configure(read_image(paths_[k], inline_buf_, take_spare()), opt_, paths_[k]);
     std::unique_lock<std::mutex> l(m_);
-    cv_.wait(l, [&] { return !ready_.empty() || stop_; });
-    Item it = std::move(ready_.front());
-    ready_.pop_front();
+    cv_.wait(l, [&] { return ready_.count(k) != 0 || stop_; });
+    Item it = std::move(ready_[k]);
+    ready_.erase(k);
+    next_ = k + 1;
     cv_.notify_all();
     l.unlock();
     if (!it.error.empty()) throw std::runtime_error(it.error);
     return std::move(it.s);
+  }
+  // a consumed frame's sample vectors, for a later decode
+  void recycle(Samples&& s)
+  {
+    Image spare;
+    spare.u8 = std::move(s.u8);
+    spare.u16 = std::move(s.u16);
+    std::lock_guard<std::mutex> l(m_);
+    if (spares_.size() < (size_t)workers_ + 2) spares_.push_back(std::move(spare));
   }
 
  private:
@@ -907,33 +931,50 @@ class Preloader
     Samples s;
     std::string error;
   };
-  void run()
+  Image take_spare()
   {
-    for (size_t k = 0; k < paths_.size(); ++k)
+    std::lock_guard<std::mutex> l(m_);
+    if (spares_.empty()) return Image{};
+    Image im = std::move(spares_.back());
+    spares_.pop_back();
+    return im;
+  }
+  void run(int w)
+  {
+    std::vector<uint8_t> buf;
+    for (size_t k = (size_t)w; k < paths_.size(); k += (size_t)workers_)
     {
+      {
+        std::unique_lock<std::mutex> l(m_);
+        cv_.wait(l, [&] { return k < next_ + (size_t)workers_ + 1 || stop_; });
+        if (stop_) return;
+      }
       Item it;
       try
       {
-        it.s = configure(read_image(paths_[k]), opt_, paths_[k]);
+        it.s = configure(read_image(paths_[k], buf, take_spare()), opt_, paths_[k]);
       }
       catch (const std::exception& ex)
       {
         it.error = ex.what();
       }
-      std::unique_lock<std::mutex> l(m_);
-      cv_.wait(l, [&] { return ready_.size() < 2 || stop_; });
+      std::lock_guard<std::mutex> l(m_);
       if (stop_) return;
-      ready_.push_back(std::move(it));
+      ready_[k] = std::move(it);
       cv_.notify_all();
     }
   }
   std::vector<std::string> paths_;
   InputOptions opt_;
   bool enabled_;
-  std::thread worker_;
+  int workers_;
+  std::vector<std::thread> threads_;
   std::mutex m_;
   std::condition_variable cv_;
-  std::deque<Item> ready_;
+  std::map<size_t, Item> ready_;
+  std::vector<Image> spares_;
+  std::vector<uint8_t> inline_buf_;   // the file buffer without preloading
+  size_t next_ = 0;                   // the next frame the consumer takes
   bool stop_ = false;
 };
 
@@ -1450,7 +1491,8 @@ int run_multi(const std::vector<std::string>& args)
   std::mutex frames_m;
   std::vector<std::vector<dic_poi>> bufs(3, std::vector<dic_poi>((size_t)n));
   if (o.diagnostics) fs::create_directories(diag_dir);
-  Preloader pre(paths, o.input, o.preload);
+  Preloader pre(paths, o.input, o.preload, o.decode_threads);
+  Payload payload;   // the writer thread's output buffer; declared first, so it outlives the writer
   Writer writer;
   bool baseline_ready = false;
   float baseline = 0.f;
@@ -1469,9 +1511,10 @@ int run_multi(const std::vector<std::string>& args)
     }
   };
   auto stage = [&](size_t k) {
-    const Samples t = pre.get(k);
+    Samples t = pre.get(k);
     check_frame(t, k);
     eng.check(dic_stage_frame(eng.e, t.data(), t.width, t.height, t.row_bytes(), t.dtype), "stage frame");
+    pre.recycle(std::move(t));   // dic_stage_frame has copied it
   };
   auto enqueue = [&] {
     eng.check(dic_sequence_frame(eng.e, nullptr, ref.width, ref.height, ref.row_bytes(), ref.dtype, DIC_PIXELS_STAGED,
@@ -1558,7 +1601,9 @@ int run_multi(const std::vector<std::string>& args)
     writer.submit([&, idx, resp, f]() mutable {
       fill_qa_stats(*resp, f.qa);
       const double t0 = now_sec();
-      Payload p = o.raw ? format_raw(*resp, o) : format_csv(*resp, o);
+      Payload& p = payload;   // the writer runs one job at a time: one buffer for every frame
+      if (o.raw) format_raw_into(*resp, o, p);
+      else p = format_csv(*resp, o);
       const double t1 = now_sec();
       ledger.publish(root / f.file, p.bytes.data(), p.bytes.size());
       f.rows = p.rows;

@@ -299,3 +299,22 @@ def test_temporal_extrapolation_run(dic, cli, tmp_path):
     e.close()
     c = json.loads((out / ".opencorr-state" / "contract.json").read_text())
     assert c["options"]["temporal_extrapolation"] is True
+
+
+@pytest.mark.parametrize("extra", [["--decode-threads", "3"], ["--decode-threads", "2", "--no-preload"]])
+def test_decode_threads_do_not_change_outputs(cli, stream12, tmp_path, extra):
+    """--decode-threads only schedules the decode (frames are handed out in list order), so
+    every payload byte equals the one-worker run's."""
+    d, _, _, _ = stream12
+    outs = []
+    for name, flags in (("one", []), ("many", extra)):
+        out = tmp_path / name
+        rc, status, err = F.run_cli(cli, ["--multi-frame", "--ref", d / "ref.pgm", "--tar-list", d / "tar_list.txt",
+                                          "--output-dir", out, "12", "8", "--input-depth", "12", "--output-format",
+                                          "raw", "--quiet", *flags])
+        assert rc == 0 and status["frames_processed"] == 6, err
+        outs.append(out)
+    files = [[f["file"] for f in F.read_manifest(o / "manifest.opencorr-raw.json")["frames"]] for o in outs]
+    assert len(files[0]) == 6 and files[0] == files[1]
+    for n in files[0]:
+        assert (outs[0] / n).read_bytes() == (outs[1] / n).read_bytes(), n
