@@ -113,6 +113,8 @@ SIGNATURES = {
     "dic_sequence_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32, _i32, _vp,
                                           ctypes.POINTER(DicFrameReport)]),
     "dic_sequence_fetch": (ctypes.c_int, [_vp, _i32, _vp, ctypes.POINTER(DicFrameReport)]),
+    "dic_host_alloc": (ctypes.c_int, [ctypes.c_size_t, ctypes.POINTER(_vp)]),
+    "dic_host_free": (None, [_vp]),
     "dic_set_graphs": (ctypes.c_int, [_vp, _i32]),
     "dic_batch_process": (ctypes.c_int, [_vp, ctypes.POINTER(DicJob), _i32, _i32, ctypes.POINTER(DicBatchReport)]),
     "dic_set_autotune": (ctypes.c_int, [_vp, _i32]),

@@ -564,6 +564,44 @@ std::vector<dic_poi> build_queue(int w, int h, int r, int step, const std::vecto
   return q;
 }
 
+// A read-only view of POI records: a std::vector or a page-locked result buffer.
+struct PoiSpan
+{
+  const dic_poi* p = nullptr;
+  size_t n = 0;
+  PoiSpan(const dic_poi* ptr, size_t count) : p(ptr), n(count) {}
+  PoiSpan(const std::vector<dic_poi>& v) : p(v.data()), n(v.size()) {}
+  const dic_poi* begin() const { return p; }
+  const dic_poi* end() const { return p + n; }
+  size_t size() const { return n; }
+  bool empty() const { return n == 0; }
+  const dic_poi& operator[](size_t i) const { return p[i]; }
+};
+
+// Page-locked POI records (dic_host_alloc): frame results are read into these by DMA.
+class PinnedPois
+{
+ public:
+  explicit PinnedPois(size_t count) : n_(count)
+  {
+    void* ptr = nullptr;
+    if (dic_host_alloc(sizeof(dic_poi) * std::max<size_t>(count, 1), &ptr) != DIC_OK)
+      throw std::runtime_error("cannot allocate page-locked result buffers");
+    p_ = static_cast<dic_poi*>(ptr);
+  }
+  PinnedPois(PinnedPois&& o) noexcept : p_(o.p_), n_(o.n_) { o.p_ = nullptr; }
+  PinnedPois(const PinnedPois&) = delete;
+  PinnedPois& operator=(const PinnedPois&) = delete;
+  ~PinnedPois() { dic_host_free(p_); }
+  dic_poi* data() { return p_; }
+  size_t size() const { return n_; }
+  operator PoiSpan() const { return PoiSpan(p_, n_); }
+
+ private:
+  dic_poi* p_ = nullptr;
+  size_t n_ = 0;
+};
+
 struct Payload
 {
   std::vector<char> bytes;
@@ -571,7 +609,7 @@ struct Payload
 };
 
 // into `p`, whose buffer keeps its capacity across frames
-void format_raw_into(const std::vector<dic_poi>& q, const Options& o, Payload& p)
+void format_raw_into(PoiSpan q, const Options& o, Payload& p)
 {
   p.rows = 0;
   p.bytes.resize(q.size() * kRecordBytes);
@@ -590,7 +628,7 @@ void format_raw_into(const std::vector<dic_poi>& q, const Options& o, Payload& p
   p.bytes.resize((size_t)(c - p.bytes.data()));
 }
 
-Payload format_raw(const std::vector<dic_poi>& q, const Options& o)
+Payload format_raw(PoiSpan q, const Options& o)
 {
   Payload p;
   format_raw_into(q, o, p);
@@ -604,7 +642,7 @@ void append_g6(std::string& s, float v)
   s.append(b, r.ptr);
 }
 
-Payload format_csv(const std::vector<dic_poi>& q, const Options& o)
+Payload format_csv(PoiSpan q, const Options& o)
 {
   std::string s = "x,y,u,v,zncc,uy,vy,ux,vx\n";
   s.reserve(q.size() * 80 + 32);
@@ -628,7 +666,7 @@ Payload format_csv(const std::vector<dic_poi>& q, const Options& o)
   return p;
 }
 
-std::string format_diagnostics(const std::vector<dic_poi>& q)
+std::string format_diagnostics(PoiSpan q)
 {
   std::ostringstream o;
   o.precision(9);
@@ -664,7 +702,7 @@ struct FrameQa
   long long temporal_seed_count = 0;
 };
 
-void fill_qa_stats(const std::vector<dic_poi>& q, FrameQa& qa)
+void fill_qa_stats(PoiSpan q, FrameQa& qa)
 {
   if (q.empty()) return;
   long long valid = 0, finite_it = 0, it_sum = 0;
@@ -978,11 +1016,16 @@ class Preloader
   bool stop_ = false;
 };
 
-// Runs jobs in submission order on one thread; the first failure is kept and rethrown.
+// Runs jobs on `threads` threads, taken in submission order (a job gets the index of the
+// thread that runs it, for per-thread buffers); the first failure is kept and rethrown, and
+// no job starts after it.
 class Writer
 {
  public:
-  Writer() : t_([this] { run(); }) {}
+  explicit Writer(int threads = 1)
+  {
+    for (int t = 0; t < std::max(1, threads); ++t) t_.emplace_back([this, t] { run(t); });
+  }
   ~Writer()
   {
     {
@@ -990,9 +1033,11 @@ class Writer
       done_ = true;
     }
     cv_.notify_all();
-    if (t_.joinable()) t_.join();
+    for (auto& t : t_)
+      if (t.joinable()) t.join();
   }
-  void submit(std::function<void()> job)
+  int threads() const { return (int)t_.size(); }
+  void submit(std::function<void(int)> job)
   {
     std::lock_guard<std::mutex> l(m_);
     q_.push_back(std::move(job));
@@ -1006,7 +1051,8 @@ class Writer
       done_ = true;
     }
     cv_.notify_all();
-    if (t_.joinable()) t_.join();
+    for (auto& t : t_)
+      if (t.joinable()) t.join();
     if (!error_.empty()) throw std::runtime_error(error_);
   }
   void check()
@@ -1016,21 +1062,22 @@ class Writer
   }
 
  private:
-  void run()
+  void run(int me)
   {
     for (;;)
     {
-      std::function<void()> job;
+      std::function<void(int)> job;
       {
         std::unique_lock<std::mutex> l(m_);
         cv_.wait(l, [&] { return !q_.empty() || done_; });
         if (q_.empty()) return;
         job = std::move(q_.front());
         q_.pop_front();
+        if (!error_.empty()) continue;
       }
       try
       {
-        if (error_.empty()) job();
+        job(me);
       }
       catch (const std::exception& ex)
       {
@@ -1039,13 +1086,14 @@ class Writer
       }
     }
   }
-  std::thread t_;
+  std::vector<std::thread> t_;
   std::mutex m_;
   std::condition_variable cv_;
-  std::deque<std::function<void()>> q_;
+  std::deque<std::function<void(int)>> q_;
   bool done_ = false;
   std::string error_;
 };
+
 
 double now_sec()
 {
@@ -1489,11 +1537,16 @@ int run_multi(const std::vector<std::string>& args)
   // outlives the writer thread on every exit path
   std::vector<FrameRecord> frames(entries.size());
   std::mutex frames_m;
-  std::vector<std::vector<dic_poi>> bufs(3, std::vector<dic_poi>((size_t)n));
+  // Two writer threads format and publish frames while the next ones are solved; a frame's
+  // results stay in their page-locked ring slot until its writer is done (the loop keeps at
+  // most kWriters frames unwritten, the ring has two more slots).
+  constexpr int kWriters = 2;
+  std::vector<PinnedPois> bufs;
+  for (int b = 0; b < kWriters + 2; ++b) bufs.emplace_back((size_t)n);
   if (o.diagnostics) fs::create_directories(diag_dir);
   Preloader pre(paths, o.input, o.preload, o.decode_threads);
-  Payload payload;   // the writer thread's output buffer; declared first, so it outlives the writer
-  Writer writer;
+  std::vector<Payload> payloads(kWriters);   // one output buffer per writer thread
+  Writer writer(kWriters);
   bool baseline_ready = false;
   float baseline = 0.f;
   long long depth_mismatches = 0;
@@ -1544,7 +1597,7 @@ int run_multi(const std::vector<std::string>& args)
         next_failed = std::current_exception();
       }
     }
-    std::vector<dic_poi>& res = bufs[k % bufs.size()];
+    PinnedPois& res = bufs[k % bufs.size()];
     dic_frame_report rep{};
     const bool attempted_skip = o.skip_fftcc && k > 0;
     eng.check(dic_sequence_fetch(eng.e, next_enqueued ? 1 : 0, res.data(), &rep), "frame results");
@@ -1594,16 +1647,16 @@ int run_multi(const std::vector<std::string>& args)
         std::cerr << "  [POI-FALLBACK] " << f.output_name << " count=" << rep.repaired_candidates
                   << ", recovered=" << rep.repaired_recovered << ", post_bad_ratio=" << qa.bad_ratio << std::endl;
     }
-    // format + publish on the writer thread; the buffer is reused two frames later, after
-    // the writer is done with it (the queue drains in order and holds at most 2 frames)
+    // format + publish on a writer thread; the ring slot is reused kWriters + 2 frames later,
+    // after its writer is done with it (the loop below)
     const size_t idx = k;
-    const std::vector<dic_poi>* resp = &res;
-    writer.submit([&, idx, resp, f]() mutable {
-      fill_qa_stats(*resp, f.qa);
+    const PoiSpan resp = res;
+    writer.submit([&, idx, resp, f](int me) mutable {
+      fill_qa_stats(resp, f.qa);
       const double t0 = now_sec();
-      Payload& p = payload;   // the writer runs one job at a time: one buffer for every frame
-      if (o.raw) format_raw_into(*resp, o, p);
-      else p = format_csv(*resp, o);
+      Payload& p = payloads[(size_t)me];   // this thread's buffer, reused frame after frame
+      if (o.raw) format_raw_into(resp, o, p);
+      else p = format_csv(resp, o);
       const double t1 = now_sec();
       ledger.publish(root / f.file, p.bytes.data(), p.bytes.size());
       f.rows = p.rows;
@@ -1612,7 +1665,7 @@ int run_multi(const std::vector<std::string>& args)
       f.write_sec = now_sec() - t1;
       if (o.diagnostics)
       {
-        const std::string text = format_diagnostics(*resp);
+        const std::string text = format_diagnostics(resp);
         ledger.publish(diagnostics_file(diag_dir, f.file), text.data(), text.size());
       }
       std::lock_guard<std::mutex> l(frames_m);
@@ -1622,14 +1675,15 @@ int run_multi(const std::vector<std::string>& args)
       std::cerr << "[" << (k + 1) << "/" << entries.size() << "] " << entries[k].tar_path << " -> " << f.file
                 << " (bad_ratio " << qa.bad_ratio << (attempted_skip ? ", skip-FFTCC" : ", FFTCC") << ")" << std::endl;
     ++g_report.frames_processed;
-    // keep the writer at most one frame behind, so that the three-buffer ring is never
-    // overwritten under it
-    if (k >= 1)
+    // keep at most kWriters frames unwritten (frames finish out of order; every earlier
+    // frame was waited for in an earlier iteration), so that no ring slot is refilled under
+    // its writer
+    if (k >= (size_t)kWriters)
       for (;;)
       {
         {
           std::lock_guard<std::mutex> l(frames_m);
-          if (!frames[k - 1].file.empty()) break;
+          if (!frames[k - kWriters].file.empty()) break;
         }
         writer.check();
         std::this_thread::sleep_for(std::chrono::microseconds(200));

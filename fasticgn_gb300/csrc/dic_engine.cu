@@ -1519,6 +1519,24 @@ bool finite_xy(const dic_poi& p) { return std::isfinite(p.x) && std::isfinite(p.
 extern "C" {
 
 const char* dic_version(void) { return kVersion; }
+
+int dic_host_alloc(size_t bytes, void** ptr)
+{
+  if (!ptr) return DIC_ERR_ARGUMENT;
+  *ptr = nullptr;
+  if (cudaMallocHost(ptr, bytes ? bytes : 1) != cudaSuccess)
+  {
+    cudaGetLastError();
+    *ptr = nullptr;
+    return DIC_ERR_MEMORY;
+  }
+  return DIC_OK;
+}
+
+void dic_host_free(void* ptr)
+{
+  if (ptr) cudaFreeHost(ptr);
+}
 int32_t dic_abi_version(void) { return DIC_ABI_VERSION; }
 
 int dic_engine_create(const dic_config* config, dic_engine** out)

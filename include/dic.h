@@ -21,6 +21,7 @@
 #ifndef GB300_DIC_H
 #define GB300_DIC_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -218,6 +219,12 @@ int dic_set_graphs(dic_engine* engine, int32_t enabled);
 #define DIC_PIXELS_STAGED 2
 int dic_stage_frame(dic_engine* engine, const void* pixels, int32_t width, int32_t height, int64_t row_stride_bytes,
                     int32_t dtype);
+/* Page-locked host memory for frames and result buffers (no reference counterpart): frames
+ * staged from it skip the staging copy, and dic_sequence_fetch / dic_sequence_frame results
+ * read into it are direct DMA.  dic_host_alloc returns DIC_ERR_MEMORY when the driver refuses;
+ * dic_host_free(NULL) is a no-op. */
+int dic_host_alloc(size_t bytes, void** ptr);
+void dic_host_free(void* ptr);
 
 /* Uneven batch: several image pairs of different sizes, each with its own subset radius
  * (square, 1..32) and POI queue, solved together (FFTCC seed + IC-GN).  No single call of
