@@ -49,6 +49,7 @@
 #include <functional>
 #include <iostream>
 #include <limits>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <optional>
@@ -1563,16 +1564,26 @@ int run_multi(const std::vector<std::string>& args)
       throw std::runtime_error("target " + entries[k].tar_path + " is not on the reference's grey scale");
     }
   };
+  // DIC_CLI_PROFILE set: per-stage time totals on stderr at the end (diagnostics only)
+  const bool profile = std::getenv("DIC_CLI_PROFILE") != nullptr;
+  double t_get = 0, t_stage = 0, t_enqueue = 0, t_fetch = 0, t_throttle = 0, t_format = 0, t_publish = 0;
+  std::mutex prof_m;
   auto stage = [&](size_t k) {
+    const double a = now_sec();
     Samples t = pre.get(k);
+    const double b = now_sec();
     check_frame(t, k);
     eng.check(dic_stage_frame(eng.e, t.data(), t.width, t.height, t.row_bytes(), t.dtype), "stage frame");
     pre.recycle(std::move(t));   // dic_stage_frame has copied it
+    t_get += b - a;
+    t_stage += now_sec() - b;
   };
   auto enqueue = [&] {
+    const double a = now_sec();
     eng.check(dic_sequence_frame(eng.e, nullptr, ref.width, ref.height, ref.row_bytes(), ref.dtype, DIC_PIXELS_STAGED,
                                  nullptr, nullptr),
               "frame");
+    t_enqueue += now_sec() - a;
   };
   stage(0);
   enqueue();
@@ -1600,7 +1611,9 @@ int run_multi(const std::vector<std::string>& args)
     PinnedPois& res = bufs[k % bufs.size()];
     dic_frame_report rep{};
     const bool attempted_skip = o.skip_fftcc && k > 0;
+    const double tf = now_sec();
     eng.check(dic_sequence_fetch(eng.e, next_enqueued ? 1 : 0, res.data(), &rep), "frame results");
+    t_fetch += now_sec() - tf;
     FrameRecord f;
     f.tar_path = entries[k].tar_path;
     f.output_name = entries[k].output_name;
@@ -1663,6 +1676,11 @@ int run_multi(const std::vector<std::string>& args)
       f.bytes = p.bytes.size();
       f.format_sec = t1 - t0;
       f.write_sec = now_sec() - t1;
+      {
+        std::lock_guard<std::mutex> pl(prof_m);
+        t_format += f.format_sec;
+        t_publish += f.write_sec;
+      }
       if (o.diagnostics)
       {
         const std::string text = format_diagnostics(resp);
@@ -1678,6 +1696,7 @@ int run_multi(const std::vector<std::string>& args)
     // keep at most kWriters frames unwritten (frames finish out of order; every earlier
     // frame was waited for in an earlier iteration), so that no ring slot is refilled under
     // its writer
+    const double tt = now_sec();
     if (k >= (size_t)kWriters)
       for (;;)
       {
@@ -1688,8 +1707,14 @@ int run_multi(const std::vector<std::string>& args)
         writer.check();
         std::this_thread::sleep_for(std::chrono::microseconds(200));
       }
+    t_throttle += now_sec() - tt;
   }
   writer.finish();
+  if (profile)
+    std::fprintf(stderr,
+                 "[profile] frames=%zu decode-wait=%.3f stage=%.3f enqueue=%.3f fetch=%.3f writer-throttle=%.3f "
+                 "format=%.3f publish=%.3f (s; format/publish summed over %d writer threads)\n",
+                 entries.size(), t_get, t_stage, t_enqueue, t_fetch, t_throttle, t_format, t_publish, kWriters);
   if (o.raw)
   {
     const std::string m = manifest_json(ref_path, list_path, out_dir, g.radius, g.grid, o, ref, frames, depth_mismatches);
