@@ -1327,14 +1327,49 @@ Json run_contract(const std::string& ref_path, const std::vector<ListEntry>& ent
   std::map<std::string, Json> seen;
   std::set<std::string> names;
   files.clear();
+  // The distinct inputs' fingerprints (a full XXH3-128 of every file) on up to 8 threads: the
+  // digests do not depend on the order, and the contract is assembled in list order below.
+  // Names and paths are checked in list order first, as before, so the first bad entry is
+  // still the one reported.
+  std::vector<std::string> uniq, canon;
   for (const auto& e : entries)
   {
     check_output_name(e.output_name);
     const std::string file = o.raw ? raw_name(e.output_name) : e.output_name;
     if (!names.insert(file).second) throw std::runtime_error("duplicate output filename: " + file);
-    const std::string path = fs::canonical(e.tar_path).string();
-    auto it = seen.find(path);
-    if (it == seen.end()) it = seen.emplace(path, input_identity(path)).first;
+    canon.push_back(fs::canonical(e.tar_path).string());
+    if (seen.emplace(canon.back(), Json()).second) uniq.push_back(canon.back());
+  }
+  {
+    std::vector<Json> ids(uniq.size());
+    std::vector<std::exception_ptr> errs(uniq.size());   // the first failing input in list order is reported
+    std::atomic<size_t> next{0};
+    const size_t nt = std::min<size_t>({uniq.size(), 8, std::max(1u, std::thread::hardware_concurrency())});
+    std::vector<std::thread> pool;
+    for (size_t t = 0; t < nt; ++t)
+      pool.emplace_back([&] {
+        for (size_t i = next++; i < uniq.size(); i = next++)
+        {
+          try
+          {
+            ids[i] = input_identity(uniq[i]);
+          }
+          catch (...)
+          {
+            errs[i] = std::current_exception();
+          }
+        }
+      });
+    for (auto& t : pool) t.join();
+    for (const auto& e : errs)
+      if (e) std::rethrow_exception(e);
+    for (size_t i = 0; i < uniq.size(); ++i) seen[uniq[i]] = std::move(ids[i]);
+  }
+  for (size_t k = 0; k < entries.size(); ++k)
+  {
+    const auto& e = entries[k];
+    const std::string file = o.raw ? raw_name(e.output_name) : e.output_name;
+    auto it = seen.find(canon[k]);
     Json t = Json::object();
     t["input"] = it->second;
     t["output_name"] = e.output_name;
