@@ -137,7 +137,10 @@ void* dic_stream(dic_engine* engine);
 /* setRefImage / setTarImage (src/icgn2d1_cuda_mvp.h:106-107, src/fftcc2d_cuda.h:91-92):
  * copy a host image (row_stride_bytes >= width * element size) to the device.  Setting
  * the reference invalidates the prepared reference state; setting the target invalidates
- * the B-spline table.  Reference and target must have the same size. */
+ * the B-spline table.  Reference and target must have the same size.  A pageable image is
+ * copied before the call returns; a page-locked one (dic_host_alloc, cudaMallocHost) is read
+ * by DMA on the engine stream, so, as with the reference's images, keep it unchanged until
+ * the next call that returns results (or until the engine stream is synchronised). */
 int dic_set_ref(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
                 int64_t row_stride_bytes, int32_t dtype);
 int dic_set_tar(dic_engine* engine, const void* pixels, int32_t width, int32_t height,
