@@ -503,7 +503,7 @@ struct dic_engine
   // ---------------------------------------------------------------- launch shapes
   // IC-GN runs one warp per POI; what can be tuned is how many POIs a CTA holds (2, 4 or
   // 8 warps) and, for the persistent batch kernel, how many CTAs per SM it launches.
-  // Per-POI results do not depend on either.  shape[persistent][column walk].
+  // Per-POI results do not depend on either.  shape[batch][column walk]: 0 single queues, 1 batches.
   struct IcgnShape
   {
     int warps = 4;
@@ -616,11 +616,13 @@ struct dic_engine
   }
   static constexpr int64_t kTuneMinPois = 2048;
   bool autotune = false;
-  // Untuned default: the persistent form for single queues too.  The grid form of the
-  // column walk (k_icgn<1, 4>) spills a register inside its row loop under the 7-CTA
-  // register cap (a local store and load per row: 14 % of its L1 wavefronts on the 2048²
-  // pair, 3.73 ms against 3.59 ms persistent); the autotuner still times both forms.
-  IcgnShape shape[2][2] = {{{4, 7, 0.f}, {4, 7, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}}};
+  // Untuned default: the persistent form for single queues too (8 CTAs of 4 warps: its
+  // 32-warp residency).  The grid form of the column walk (k_icgn<1, 4>) spills a register
+  // inside its row loop under the 7-CTA register cap (a local store and load per row: 14 %
+  // of its L1 wavefronts on the 2048² pair, 3.73 ms against 3.59 ms persistent with the
+  // four-plane table); the autotuner still times both forms.  shape[0]: single queues,
+  // shape[1]: batches.
+  IcgnShape shape[2][2] = {{{4, 8, 0.f}, {4, 8, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}}};
   bool tuned[2][2] = {};
   DevBuf<dic_poi> tune_q;
   cudaEvent_t tune_ev[2] = {};

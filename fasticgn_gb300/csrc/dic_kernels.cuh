@@ -704,11 +704,12 @@ __device__ __forceinline__ float sample_bspline_tile(const CoefTile& T, const fl
 
 // Rows of the column walk unrolled together (their gathers in flight at once), and the
 // warps per SM the IC-GN launch bounds keep resident (which sets the register budget).
-// The 256-bit coefficient gathers are served from L2, so two rows in flight hide more of
-// their latency (3.48 -> 3.44 ms on the 2048x2048 pair; 3 or 4 rows, or 24 resident warps
-// with more registers, were slower).
+// The 256-bit coefficient gathers are served from L2 and their latency is what the kernel
+// waits on; more resident warps (the persistent form's 32 at 64 registers) hide it better
+// than more rows per warp (two rows at 28 warps: 3.44 ms; one row at 32 warps: 3.33 ms on
+// the 2048x2048 pair; 3 or 4 rows, or 24 warps with more registers, were slower).
 #ifndef DIC_ICGN_ROW_UNROLL
-#define DIC_ICGN_ROW_UNROLL 2
+#define DIC_ICGN_ROW_UNROLL 1
 #endif
 #ifndef DIC_ICGN_RESIDENT_WARPS
 #define DIC_ICGN_RESIDENT_WARPS 28
@@ -917,6 +918,13 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
 // Launch shape: kWarps POIs per CTA (one warp each); the occupancy hint keeps
 // DIC_ICGN_RESIDENT_WARPS (28: 72 registers per thread) warps per SM resident for every shape.
 constexpr int icgn_min_blocks(int warps) { return DIC_ICGN_RESIDENT_WARPS / warps; }
+// The persistent single-queue form keeps 32 warps per SM (64 registers) with one row in
+// flight per lane: its gathers wait on L2, and more warps hide that better than a second
+// row does (3.43 -> 3.33 ms on the 2048x2048 pair; the grid and batch forms spill at 64).
+#ifndef DIC_ICGN_PERSISTENT_RESIDENT_WARPS
+#define DIC_ICGN_PERSISTENT_RESIDENT_WARPS 32
+#endif
+constexpr int icgn_persistent_min_blocks(int warps) { return DIC_ICGN_PERSISTENT_RESIDENT_WARPS / warps; }
 
 template <bool kColumn, int kWarps = 4>
 __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn(IcgnParams P)
@@ -931,8 +939,8 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn(I
 // atomic counter (reset to 0 before the launch), so POIs that need many iterations do not
 // hold a whole CTA back.  Same solver and guards as k_icgn.
 template <bool kColumn, int kWarps = 4>
-__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_persistent(IcgnParams P,
-                                                                                          unsigned long long* next)
+__global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps))
+    k_icgn_persistent(IcgnParams P, unsigned long long* next)
 {
   const int lane = threadIdx.x & 31;
   if (P.enable && *P.enable == 0) return;
@@ -942,7 +950,7 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_p
     if (lane == 0) t = atomicAdd(next, 1ull);
     const int64_t i = (int64_t)__shfl_sync(kFull, t, 0);
     if (!queue_slot_active(P, i)) return;
-    icgn_solve<kColumn>(P, i, lane);
+    icgn_solve<kColumn, false, 1>(P, i, lane);
   }
 }
 
