@@ -1582,6 +1582,11 @@ int run_multi(const std::vector<std::string>& args)
   if (o.diagnostics) fs::create_directories(diag_dir);
   Preloader pre(paths, o.input, o.preload, o.decode_threads);
   std::vector<Payload> payloads(kWriters);   // one output buffer per writer thread
+  // DIC_CLI_PROFILE set: per-stage time totals on stderr at the end (diagnostics only; the
+  // writer jobs add to t_format / t_publish, so these too are declared before the writer)
+  const bool profile = std::getenv("DIC_CLI_PROFILE") != nullptr;
+  double t_get = 0, t_stage = 0, t_enqueue = 0, t_fetch = 0, t_throttle = 0, t_format = 0, t_publish = 0;
+  std::mutex prof_m;
   Writer writer(kWriters);
   bool baseline_ready = false;
   float baseline = 0.f;
@@ -1599,10 +1604,6 @@ int run_multi(const std::vector<std::string>& args)
       throw std::runtime_error("target " + entries[k].tar_path + " is not on the reference's grey scale");
     }
   };
-  // DIC_CLI_PROFILE set: per-stage time totals on stderr at the end (diagnostics only)
-  const bool profile = std::getenv("DIC_CLI_PROFILE") != nullptr;
-  double t_get = 0, t_stage = 0, t_enqueue = 0, t_fetch = 0, t_throttle = 0, t_format = 0, t_publish = 0;
-  std::mutex prof_m;
   auto stage = [&](size_t k) {
     const double a = now_sec();
     Samples t = pre.get(k);
