@@ -459,6 +459,39 @@ struct dic_engine
     queue.ensure((size_t)n);
     DIC_CUDA(cudaMemcpyAsync(queue.ptr, pois, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, stream));
   }
+  // The pair path's queue upload on a side stream, so that it overlaps the reference and
+  // target preparation kernels enqueued after it: the side stream first waits for all
+  // earlier engine-stream work (nothing still reading the queue is overtaken), and
+  // join_queue_upload makes the engine stream wait for the copy before the solvers.
+  cudaStream_t qup_stream = nullptr;
+  cudaEvent_t qup_before = nullptr, qup_done = nullptr;
+  void upload_queue_beside(const dic_poi* pois, int64_t n)
+  {
+    queue.ensure((size_t)n);
+    if (!qup_stream)
+    {
+      DIC_CUDA(cudaStreamCreateWithFlags(&qup_stream, cudaStreamNonBlocking));
+      DIC_CUDA(cudaEventCreateWithFlags(&qup_before, cudaEventDisableTiming));
+      DIC_CUDA(cudaEventCreateWithFlags(&qup_done, cudaEventDisableTiming));
+    }
+    DIC_CUDA(cudaEventRecord(qup_before, stream));
+    DIC_CUDA(cudaStreamWaitEvent(qup_stream, qup_before, 0));
+    DIC_CUDA(cudaMemcpyAsync(queue.ptr, pois, sizeof(dic_poi) * n, cudaMemcpyHostToDevice, qup_stream));
+    DIC_CUDA(cudaEventRecord(qup_done, qup_stream));
+  }
+  void join_queue_upload() { DIC_CUDA(cudaStreamWaitEvent(stream, qup_done, 0)); }
+  void release_queue_upload()
+  {
+    if (qup_stream)
+    {
+      cudaStreamSynchronize(qup_stream);
+      cudaStreamDestroy(qup_stream);
+    }
+    if (qup_before) cudaEventDestroy(qup_before);
+    if (qup_done) cudaEventDestroy(qup_done);
+    qup_stream = nullptr;
+    qup_before = qup_done = nullptr;
+  }
   void download_queue(dic_poi* pois, int64_t n)
   {
     DIC_CUDA(cudaMemcpyAsync(pois, queue.ptr, sizeof(dic_poi) * n, cudaMemcpyDeviceToHost, stream));
@@ -1632,6 +1665,7 @@ void dic_engine_destroy(dic_engine* e)
   e->tune_q.release();
   e->release_staging();
   e->release_frame_outputs();
+  e->release_queue_upload();
   for (int p = 0; p < kPhCount; ++p)
     for (int m = 0; m < dic_engine::kMarks; ++m)
       for (int k = 0; k < 2; ++k)
@@ -1739,7 +1773,11 @@ int dic_process_pair(dic_engine* e, dic_poi* pois, int64_t n)
     if (e->cfg.subset_radius_x != e->cfg.subset_radius_y)
       throw DicError{DIC_ERR_ARGUMENT, "FFTCC2D supports positive square radii only"};
     if (n == 0) return;
-    e->upload_queue(pois, n);
+    // the queue's upload overlaps the reference and target preparation, which do not read it
+    e->upload_queue_beside(pois, n);
+    e->ensure_ref();
+    e->ensure_tar();
+    e->join_queue_upload();
     // FFTCC reads only (x, y, u, v) and writes the seed; the per-POI reference data reads
     // only (x, y).  Launching FFTCC first lets the host's layout check and record (a pass
     // over the queue) run while the GPU works.
