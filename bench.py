@@ -11,11 +11,16 @@ value  = POIs / device time per step, inputs resident in HBM (dic_run_device), L
          (256 MB write) before every timed step, CUDA events on the engine stream.
 e2e    = the same through the C ABI with host buffers (dic_set_ref / dic_set_tar /
          dic_process_pair): pinned host images and POI queue copied in, results copied out.
---impl reference: the reference's CPU path (the oracle restatement, all host threads).
+--impl reference: the reference's CPU path (the oracle restatement, all host threads) on the
+         whole queue of the same pair, every step.
+roofline: the IC-GN gathers are served by L2, so their bound is the L2-to-SM read bandwidth,
+         measured in the same run by dic_read_probe (the gathers' 256-bit loads over an
+         L2-resident buffer); the DRAM side is reported beside it.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes
 import gc
 import json
 import os
@@ -33,8 +38,8 @@ sys.path.insert(0, str(ROOT))
 
 WORKLOAD = {"name": "pair2048_bumps_r15_step4", "width": 2048, "height": 2048, "radius": 15, "step": 4,
             "seed": 4, "conv": 0.001, "max_iter": 10}
-CPU_SAMPLE_STRIDE = 64          # every 64th POI of the queue for the CPU timings
 L2_FLUSH_BYTES = 256 << 20
+STREAM_PARITY_STRIDE = 8        # every 8th POI of a stream frame is re-solved by the CPU oracle
 
 
 def log(*a):
@@ -146,27 +151,27 @@ def grid():
 # ------------------------------------------------------------------------------ CPU legs
 
 def cpu_pair_time(ref, tar, threads):
-    """Reference CPU path on a bounded sample: full-image prep + FFTCC/IC-GN on every 64th POI.
-    Returns (POIs/s extrapolated to the whole queue, detail dict, sample results)."""
+    """Reference CPU path on the whole queue: full-image prep, FFTCC and IC-GN on every POI
+    (OpenMP over POIs, src/oc_icgn.cpp:389-397, src/oc_fftcc.cpp:529-557).
+    Returns (POIs/s, detail dict, results)."""
     from oracle import oracle as O
     w, h, r = WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["radius"]
     reff, tarf = ref.astype(np.float32), tar.astype(np.float32)
     pois = O.grid_pois(w, h, r, WORKLOAD["step"])
-    total = len(pois)
-    sample = np.ascontiguousarray(pois[::CPU_SAMPLE_STRIDE])
     t0 = time.perf_counter()
     gx, gy = O.gradient(reff, threads)
     coef = O.bspline_prepare(tarf, threads)
     t1 = time.perf_counter()
-    O.fftcc2d(reff, tarf, sample, r, threads)
+    O.fftcc2d(reff, tarf, pois, r, threads)
     t2 = time.perf_counter()
-    O.icgn2d1(reff, gx, gy, coef, sample, r, WORKLOAD["conv"], WORKLOAD["max_iter"], threads)
+    O.icgn2d1(reff, gx, gy, coef, pois, r, WORKLOAD["conv"], WORKLOAD["max_iter"], threads)
     t3 = time.perf_counter()
-    per_poi = (t3 - t1) / len(sample)
-    pair_s = (t1 - t0) + per_poi * total
-    detail = {"prep_s": t1 - t0, "fftcc_s_per_poi": (t2 - t1) / len(sample),
-              "icgn_s_per_poi": (t3 - t2) / len(sample), "sample_pois": len(sample), "pair_s": pair_s}
-    return total / pair_s, detail, sample
+    detail = {"prep_s": t1 - t0, "fftcc_s": t2 - t1, "icgn_s": t3 - t2, "pois": len(pois), "pair_s": t3 - t0}
+    return len(pois) / (t3 - t0), detail, pois
+
+
+CPU_SAMPLE = ("the whole queue of the pair every step (254 016 POIs): full-image gradient + B-spline table, "
+              "FFTCC and IC-GN on every POI, OpenMP over POIs on all host threads; own FFT, not FFTW")
 
 
 def run_reference(args):
@@ -175,19 +180,16 @@ def run_reference(args):
     ref, tar = load_pair()
     for _ in range(args.warmup):
         cpu_pair_time(ref, tar, threads)
-    vals, pair_s = [], []
+    pair_s = []
     for _ in range(args.steps):
-        v, d, _ = cpu_pair_time(ref, tar, threads)
-        vals.append(v)
+        _, d, _ = cpu_pair_time(ref, tar, threads)
         pair_s.append(d["pair_s"])
-    value = float(np.mean(vals))
-    sample = (f"full-image gradient + B-spline table, then FFTCC + IC-GN on every {CPU_SAMPLE_STRIDE}th POI "
-              f"({d['sample_pois']} of {len(grid())}), extrapolated to the whole queue; own FFT, not FFTW")
+    value = d["pois"] * len(pair_s) / float(np.sum(pair_s))
     line = {"impl": "reference", "metric": "POIs/s", "value": value, "unit": "POI/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(pair_s)),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": config_block(),
-            "cpu_baseline": {"value": value, "unit": "POI/s", "cores": threads, "kind": "port", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "POI/s", "cores": threads, "kind": "port", "sample": CPU_SAMPLE},
             "e2e": {"value": value, "unit": "POI/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -204,19 +206,23 @@ def config_block():
 # ------------------------------------------------------------------------------ clocks
 
 class ClockSampler:
+    """nvidia-smi every 50 ms for the whole run; the summary keeps the samples taken inside
+    the timed regions (marked with window()), so the clock record belongs to the timing."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    PERIOD_MS = 50
 
     def __init__(self, device_index: int):
         self.dev = device_index
         self.proc = None
-        self.lines = []
+        self.lines = []        # (host time, csv line)
+        self.windows = {}      # name -> [(t0, t1)]
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.PERIOD_MS)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
@@ -226,7 +232,7 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
     def __exit__(self, *exc):
         if self.proc:
@@ -236,25 +242,46 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+    class _Window:
+        def __init__(self, owner, name):
+            self.owner, self.name = owner, name
+
+        def __enter__(self):
+            self.t0 = time.perf_counter()
+
+        def __exit__(self, *exc):
+            # a sample is printed up to one period after it is taken
+            self.owner.windows.setdefault(self.name, []).append(
+                (self.t0, time.perf_counter() + self.owner.PERIOD_MS * 1e-3))
+
+    def window(self, name: str):
+        return self._Window(self, name)
+
+    def summary(self, names=None):
+        spans = [w for n, ws in self.windows.items() if names is None or n in names for w in ws]
+        sm, smax, power, reasons = [], [], [], set()
+        fields = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for t, ln in self.lines:
+            if not any(a <= t <= b for a, b in spans):
+                continue
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
             try:
                 sm.append(float(parts[1]))
                 smax.append(float(parts[2]))
+                power.append(float(parts[3]))
             except ValueError:
                 continue
-            for n, v in zip(names, parts[5:9]):
+            for n, v in zip(fields, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
+        timed_s = sum(b - a - self.PERIOD_MS * 1e-3 for a, b in spans)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "timed_s": timed_s}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "sm_mhz_min": min(sm), "power_w_max": max(power), "timed_s": timed_s,
+                "period_ms": self.PERIOD_MS}
 
 
 # ------------------------------------------------------------------------------ GPU arm
@@ -266,33 +293,102 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel: str):
+def profiled(kernel: str):
+    """ncu figures of one launch of a kernel on this workload (profiles/traffic.json):
+    DRAM bytes per launch and the L2 (lts) throughput percentage, with their source."""
     p = ROOT / "profiles" / "traffic.json"
     if not p.exists():
-        return None
+        return {}
     d = json.loads(p.read_text())
     k = d.get("kernels", {}).get(kernel)
     if not k or d.get("workload") != WORKLOAD["name"]:
-        return None
-    return float(k["dram_bytes_per_launch"])
+        return {}
+    return dict(k, source=d.get("source"))
 
 
-def parity_vs_cpu(result, cpu_sample):
-    """Reference parity-gate statistics of GPU results on the CPU sample's POIs."""
+def measure_read_peak(torch, dev):
+    """L2-to-SM read bandwidth with the gathers' own load (dic_read_probe): a 64 MiB buffer
+    that L2 (126 MB) holds, 40 passes per launch, best of 5 launches after 2 warm-ups, CUDA
+    events on the probe's stream.  The same kernel over a 4 GiB buffer (one pass) gives the
+    HBM read rate for comparison."""
+    from fasticgn_gb300 import _lib
+    L = _lib.load()
+    stream = torch.cuda.Stream(device=dev)
+    sink = torch.zeros(1, dtype=torch.float32, device=dev)
+    out = {}
+    for name, nbytes, repeats in (("l2", 64 << 20, 40), ("hbm", 4 << 30, 1)):
+        buf = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        with torch.cuda.stream(stream):
+            buf.random_(0, 255)
+        best = None
+        for k in range(7):
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                s.record(stream)
+                rc = L.dic_read_probe(dev.index, buf.data_ptr(), nbytes, repeats, sink.data_ptr(), stream.cuda_stream)
+                e.record(stream)
+            if rc != _lib.DIC_OK:
+                raise RuntimeError(f"dic_read_probe failed ({rc})")
+            e.synchronize()
+            if k >= 2:
+                ms = s.elapsed_time(e)
+                best = ms if best is None else min(best, ms)
+        out[name] = {"gbs": nbytes * repeats / (best * 1e-3) / 1e9, "bytes": nbytes, "passes": repeats,
+                     "ms": best}
+        del buf
+    # FP32 FMA rate (the FFTCC kernels' bound), same timing
+    flop = ctypes.c_int64(0)
+    best = None
+    for k in range(7):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            s.record(stream)
+            rc = L.dic_fma_probe(dev.index, 1 << 16, sink.data_ptr(), stream.cuda_stream, ctypes.byref(flop))
+            e.record(stream)
+        if rc != _lib.DIC_OK:
+            raise RuntimeError(f"dic_fma_probe failed ({rc})")
+        e.synchronize()
+        if k >= 2:
+            ms = s.elapsed_time(e)
+            best = ms if best is None else min(best, ms)
+    out["fp32"] = {"tflops": flop.value / (best * 1e-3) / 1e12, "ms": best}
+    torch.cuda.synchronize()
+    return out
+
+
+def parity_vs_cpu(result, cpu_result):
+    """Reference parity-gate statistics of GPU results against the CPU oracle's results on
+    the same POIs (smoke/check_cpu_gpu_parity.py:46-98), plus flag agreement."""
     from oracle import oracle as O
-    g = result[::CPU_SAMPLE_STRIDE]
-    cz, gz = cpu_sample["r"][:, O.R_ZNCC], g["zncc"]
+    cz, gz = cpu_result["r"][:, O.R_ZNCC], result["zncc"]
     both = (cz >= 0) & (gz >= 0) & np.isfinite(cz) & np.isfinite(gz)
-    du = np.abs(cpu_sample["p"][both, O.P_U] - g["u"][both])
-    dv = np.abs(cpu_sample["p"][both, O.P_V] - g["v"][both])
-    return {"sample_pois": int(len(g)), "shared_valid": int(both.sum()),
+    du = np.abs(cpu_result["p"][both, O.P_U] - result["u"][both])
+    dv = np.abs(cpu_result["p"][both, O.P_V] - result["v"][both])
+    neg = lambda z: np.where(np.isfinite(z) & (z < 0), z, 0)   # noqa: E731
+    return {"pois": int(len(result)), "shared_valid": int(both.sum()),
             "median_du": float(np.median(du)), "median_dv": float(np.median(dv)),
             "p99_du": float(np.quantile(du, 0.99)), "p99_dv": float(np.quantile(dv, 0.99)),
             "max_du": float(du.max()), "max_dv": float(dv.max()),
-            "cpu_valid_gpu_valid_agreement": float(np.mean((cz >= 0) == (gz >= 0)))}
+            "cpu_valid_gpu_valid_agreement": float(np.mean((cz >= 0) == (gz >= 0))),
+            "failure_codes_identical": float(np.mean(neg(cz) == neg(gz)))}
 
 
-def measure_uneven(dic, torch, dev, flush, jobs, steps, warmup):
+def stream_parity(frame, tmpl, radius, result, stride=STREAM_PARITY_STRIDE):
+    """A stream frame's GPU results against the CPU oracle solving the same frame from scratch
+    (FFTCC + IC-GN) on every stride-th POI of the template: the converged IC-GN is the judge,
+    whatever seed the stream used."""
+    from oracle import oracle as O
+    ref, tar = frame
+    idx = np.arange(0, len(tmpl), stride)
+    pois = O.make_pois(tmpl["x"][idx], tmpl["y"][idx])
+    O.run_pair(ref.astype(np.float32), tar.astype(np.float32), pois, radius, WORKLOAD["conv"],
+               WORKLOAD["max_iter"], threads=O.default_threads())
+    out = parity_vs_cpu(result[idx], pois)
+    out["sample"] = f"every {stride}th POI of the last timed frame, CPU FFTCC + IC-GN from scratch"
+    return out
+
+
+def measure_uneven(dic, torch, dev, flush, jobs, steps, warmup, clock):
     """The uneven batch through dic_batch_process with device-resident pairs and queues
     (graph replay after the first two calls, autotuned launch shapes), next to the same
     pairs run one at a time through the single-pair device entry point."""
@@ -329,7 +425,8 @@ def measure_uneven(dic, torch, dev, flush, jobs, steps, warmup):
     for _ in range(max(2, warmup)):          # the first call tunes, the second captures the graph
         eager_ms.append(timed(lambda: eng.batch_process_device(djobs)))
     launches0 = eng.stats()["kernel_launches"]
-    graph_ms = [timed(lambda: eng.batch_process_device(djobs)) for _ in range(steps)]
+    with clock.window("uneven_batch"):
+        graph_ms = [timed(lambda: eng.batch_process_device(djobs)) for _ in range(steps)]
     launches = (eng.stats()["kernel_launches"] - launches0) / steps
     batch_out = [qd.cpu().numpy().view(dic.POI_DTYPE).copy() for _, _, _, qd in djobs]
 
@@ -383,7 +480,7 @@ def measure_uneven(dic, torch, dev, flush, jobs, steps, warmup):
     return out
 
 
-def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
+def measure_stream(dic, torch, dev, st, ref, tars, net, flush, clock):
     """A fixed-reference stream through dic_sequence_*: e2e = host frames staged on the side
     stream (dic_stage_frame) and every frame's results read back one frame behind the solve
     (dic_sequence_fetch), host clock, including the read of warm-up frame 1; device =
@@ -414,10 +511,12 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
     t0 = None
     gc.disable()   # no collector pause inside a ~30 ms host-clocked window
     enqueue(0)
+    win = clock.window(st["name"])
     for k in range(len(tars_h)):
         if k == 1:   # frames 0 and 1 solved; the clock covers staging, solving and reading 2..
             torch.cuda.synchronize()
             t0 = time.perf_counter()
+            win.__enter__()
         # frame k is running: stage frame k + 1 (upload on the side stream, straight from the
         # page-locked frame) and enqueue it behind frame k, then read frame k's results one
         # frame back while frame k + 1 runs, so the device never waits for the host
@@ -430,6 +529,7 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
             reports.append(rep)
             results.append(res)
     e2e_s = time.perf_counter() - t0
+    win.__exit__(None, None, None)
     gc.enable()
     timed = len(tars_h) - 2
     # ---- device-resident frames
@@ -442,12 +542,13 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
         s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         s.record(stream)
     l0 = eng.stats()["kernel_launches"]
-    for k in range(2, len(tars_d)):
-        eng.sequence_frame(None, device_ptr=tars_d[k].data_ptr(), width=W, height=H, dtype=_lib.DIC_U16,
-                           report=False)
-    with torch.cuda.stream(stream):
-        e.record(stream)
-    e.synchronize()
+    with clock.window(st["name"]):
+        for k in range(2, len(tars_d)):
+            eng.sequence_frame(None, device_ptr=tars_d[k].data_ptr(), width=W, height=H, dtype=_lib.DIC_U16,
+                               report=False)
+        with torch.cuda.stream(stream):
+            e.record(stream)
+        e.synchronize()
     dev_ms = s.elapsed_time(e)
     launches = (eng.stats()["kernel_launches"] - l0) / timed
     allr = np.concatenate(results)
@@ -463,6 +564,7 @@ def measure_stream(dic, torch, dev, st, ref, tars, net, flush):
            "fallback_rate": float(np.mean([r["repaired_candidates"] for r in reports]) / n),
            "frame_fallbacks": int(sum(r["frame_fallback_used"] for r in reports)),
            "tuning": eng.tuning(),
+           "parity_vs_cpu": stream_parity((ref, tars[-1]), tmpl, R, results[-1]),
            "timing": "e2e: host clock over the timed frames, the next frame uploaded and enqueued while each "
                      "frame runs, every frame's results read one frame behind (uploads and result reads "
                      "included); "
@@ -635,6 +737,7 @@ def run_ours(args):
     streams = load_streams() if rank == 0 and not args.skip_streams else None
     torch.cuda.set_device(local)
     _build.build_lib()
+    clock = ClockSampler(local).__enter__()     # sampled for the whole run; summaries keep timed windows
 
     ref, tar = load_pair()
     W, H, R = WORKLOAD["width"], WORKLOAD["height"], WORKLOAD["radius"]
@@ -677,17 +780,13 @@ def run_ours(args):
 
     kernel_keys = ("ms_prepare_ref", "ms_poi_prepare", "ms_prepare_tar", "ms_fftcc", "ms_proposal", "ms_icgn")
     res = {}
-    clk = None
     for mode in modes:
         for _ in range(args.warmup):
             device_step(mode)
         barrier()
         launches0 = eng.stats()["kernel_launches"]
         times, kern, iters = [], {k: [] for k in kernel_keys}, []
-        sampler = ClockSampler(local) if mode == headline else None
-        if sampler:
-            sampler.__enter__()
-        try:
+        with clock.window(mode):
             for _ in range(args.steps):
                 with torch.cuda.stream(stream):
                     flush.random_(0, 255)           # untimed L2 flush
@@ -703,16 +802,52 @@ def run_ours(args):
                     kern[k].append(st[k])
                 iters.append(st["icgn_iterations"])
             barrier()
-        finally:
-            if sampler:
-                sampler.__exit__(None, None, None)
-                clk = sampler
         ms = rank_max(float(np.sum(times)) / args.steps)
         res[mode] = {"ms_per_step": ms, "value": whole_job_rate(world, P, ms),
                      "launches_per_step": (eng.stats()["kernel_launches"] - launches0) / args.steps,
                      "kernels_ms": {k: float(np.mean(v)) for k, v in kern.items()},
                      "icgn_iterations": float(np.mean(iters)),
                      "result": work_d.cpu().numpy().view(dic.POI_DTYPE).copy()}
+
+    # ---- what any seed can buy: IC-GN alone from seeds at a known distance from the converged
+    # FFTCC-path solution (0 = the solution itself, which IC-GN confirms in one iteration),
+    # on the same resident pair and layout.  The fixed part of a step (reference prep,
+    # per-POI prep, target table) does not depend on the seed.
+    seed_floor = None
+    if "fftcc" in res:
+        base = res["fftcc"]["result"]
+        ok = base["zncc"] >= 0
+        rng = np.random.default_rng(0)
+        seed_floor = {"offsets_px": {}}
+        for off in (0.0, 0.05, 0.2, 0.5):
+            q = tmpl.copy()
+            for f in ("u", "ux", "uy", "v", "vx", "vy"):
+                q[f] = np.where(ok, base[f], 0.0)
+            if off:
+                ang = rng.uniform(0, 2 * np.pi, P)
+                q["u"] += np.where(ok, off * np.cos(ang), 0.0).astype(np.float32)
+                q["v"] += np.where(ok, off * np.sin(ang), 0.0).astype(np.float32)
+            qd = torch.from_numpy(q.view(np.uint8).copy()).to(dev)
+            ms, its = [], []
+            for k in range(args.warmup + args.steps):
+                with torch.cuda.stream(stream):
+                    work_d.copy_(qd)
+                    flush.random_(0, 255)
+                eng.run_device(work_d.data_ptr(), P, _lib.DIC_RUN_ICGN)
+                st = eng.stats()
+                if k >= args.warmup:
+                    ms.append(st["ms_icgn"])
+                    its.append(st["icgn_iterations"] / P)
+            seed_floor["offsets_px"][str(off)] = {"icgn_ms": float(np.mean(ms)), "iterations_per_poi": float(np.mean(its))}
+        fixed = sum(res["fftcc"]["kernels_ms"][k] for k in ("ms_prepare_ref", "ms_poi_prepare", "ms_prepare_tar"))
+        seed_floor["fixed_ms"] = fixed
+        seed_floor["fftcc_step_ms"] = res["fftcc"]["ms_per_step"]
+        # ceiling of learned / FFTCC-seeded throughput for a proposal that costs nothing and
+        # lands at that distance from the solution
+        for off, v in seed_floor["offsets_px"].items():
+            v["ceiling_vs_fftcc_at_zero_proposal_cost"] = res["fftcc"]["ms_per_step"] / (fixed + v["icgn_ms"])
+        seed_floor["note"] = ("IC-GN from the converged FFTCC-path solution moved by the given distance in a random "
+                              "direction (valid POIs); the ceiling adds no proposal time")
 
     # ---- e2e through the host C ABI (pinned host buffers), headline mode
     ref_h = torch.from_numpy(ref).pin_memory()
@@ -734,6 +869,8 @@ def run_ours(args):
         e2e_step()
     e2e_times = []
     gc.disable()   # no collector pause inside a timed step
+    e2e_win = clock.window("e2e")
+    e2e_win.__enter__()
     for _ in range(args.steps):
         q_h.numpy()[:] = tmpl_bytes          # the caller's fresh POI queue (untimed)
         with torch.cuda.stream(stream):
@@ -745,46 +882,60 @@ def run_ours(args):
         e.record(stream)
         e.synchronize()
         e2e_times.append(s.elapsed_time(e))
+    e2e_win.__exit__(None, None, None)
     gc.enable()
     e2e_ms = rank_max(float(np.mean(e2e_times)))
     assert q_np.tobytes() == res[headline]["result"].tobytes(), "host and device entry points disagree"
 
     uneven = None
     if uneven_jobs is not None:
-        uneven = measure_uneven(dic, torch, dev, flush, uneven_jobs, max(5, min(args.steps, 20)), args.warmup)
+        uneven = measure_uneven(dic, torch, dev, flush, uneven_jobs, max(5, min(args.steps, 20)), args.warmup, clock)
     config1 = measure_config1(dic, torch, dev) if rank == 0 else None
     stream_lines = None
     cli_line = None
     if streams is not None:
-        stream_lines = {st["name"]: measure_stream(dic, torch, dev, st, *streams[st["name"]], net, flush)
+        stream_lines = {st["name"]: measure_stream(dic, torch, dev, st, *streams[st["name"]], net, flush, clock)
                         for st in STREAMS}
         if rank == 0:
             st0 = STREAMS[0]
             cli_line = measure_cli(st0, *streams[st0["name"]])
 
+    peaks = measure_read_peak(torch, dev) if rank == 0 else None
+    clock.__exit__(None, None, None)
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel (IC-GN; gather model: 64 B texel + 12 B reference per sample and iteration, 224 B per POI)
+    # ---- roofline of the dominant kernel (IC-GN).  Gather model per launch: 64 B of B-spline
+    # texel per warped sample per iteration + 12 B of reference/gradients per sample + 224 B per
+    # POI.  L2 serves the gathers (98.9 % hit; DRAM carries only the compulsory table and
+    # planes), so the bound is the L2-to-SM read bandwidth measured above with the same loads.
     N = (2 * R + 1) ** 2
     H0 = res[headline]
     icgn_ms = H0["kernels_ms"]["ms_icgn"]
     alg_bytes = 64.0 * N * H0["icgn_iterations"] + P * (12.0 * N + 144 + 8 + 32 + 40)
-    peak, peak_kind = measured_peak_hbm()
+    hbm_peak, hbm_kind = measured_peak_hbm()
     achieved = alg_bytes / (icgn_ms * 1e-3) / 1e9
-    traffic = profiled_traffic("k_icgn")
-    roofline = {"kernel": "k_icgn", "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-                "algorithmic_bytes_per_launch": alg_bytes,
+    prof = profiled("k_icgn")
+    traffic = prof.get("dram_bytes_per_launch")
+    roofline = {"kernel": "k_icgn", "bound": "l2", "achieved": achieved, "peak": peaks["l2"]["gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["l2"]["gbs"],
+                "peak_source": (f"measured in this run: dic_read_probe, 256-bit loads over a {peaks['l2']['bytes'] >> 20} "
+                                f"MiB L2-resident buffer x {peaks['l2']['passes']} passes (of measured)"),
+                "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes, "icgn_ms": icgn_ms,
+                "l2_busy_pct_ncu": prof.get("lts_throughput_pct"),
+                "hbm": {"achieved": (traffic / (icgn_ms * 1e-3) / 1e9) if traffic else None, "peak": hbm_peak,
+                        "frac": (traffic / (icgn_ms * 1e-3) / 1e9 / hbm_peak) if traffic else None,
+                        "peak_source": hbm_kind, "note": "DRAM bytes per launch (ncu) over the IC-GN time"},
+                "read_probe": peaks, "profile_source": prof.get("source"),
                 "model": "64 B B-spline texel per warped sample per iteration + 12 B ref/grad per sample "
-                         "+ 224 B per-POI record/IO; the gathers are served on chip, see profiles/"}
+                         "+ 224 B per-POI record/IO"}
 
     # ---- the other hot kernels against their own bounds (FLOP models per POI)
     M = 2 * R
     fftcc_flop = 2 * (2.5 * M * M * np.log2(M * M)) + 6 * M * (M // 2 + 1) + 4 * M * M
-    fp32_peak = 152 * 128 * 2 * 2.07e9 / 1e12       # nominal FP32: 152 SMs x 128 FMA/clk at 2.07 GHz
+    fp32_peak = peaks["fp32"]["tflops"]             # measured in this run by dic_fma_probe
     try:
         bf16_peak = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"])
         bf16_src = "measured"
@@ -792,7 +943,8 @@ def run_ours(args):
         bf16_peak, bf16_src = 1900.0, "fallback"
     other = {"k_fftcc": {"bound": "fp32", "flop_per_poi": fftcc_flop,
                          "achieved": fftcc_flop * P / (H0["kernels_ms"]["ms_fftcc"] * 1e-3) / 1e12,
-                         "peak": fp32_peak, "unit": "TFLOP/s", "peak_source": "nominal"}}
+                         "peak": fp32_peak, "unit": "TFLOP/s",
+                         "peak_source": "measured in this run: dic_fma_probe, 8 independent FMA chains per thread"}}
     if "learned" in res:
         cnn_flop = 2 * (256 * 32 * 18 + 64 * 32 * 288 + 16 * 32 * 288 + 4 * 32 * 288 + 128 * 256 + 256 * 6)
         other["k_proposal_fused"] = {"bound": "tensor", "flop_per_poi": cnn_flop,
@@ -801,10 +953,10 @@ def run_ours(args):
     for v in other.values():
         v["frac"] = v["achieved"] / v["peak"]
 
-    # ---- CPU baseline on a bounded sample, and parity of each GPU mode on that sample
+    # ---- CPU baseline on the whole queue, and parity of each GPU mode against its results
     from oracle import oracle as O
     threads = O.default_threads()
-    cpu_value, cpu_detail, cpu_sample = cpu_pair_time(ref, tar, threads)
+    cpu_value, cpu_detail, cpu_result = cpu_pair_time(ref, tar, threads)
     seed_modes = {}
     for mode, r in res.items():
         ok = r["result"]["zncc"] >= 0
@@ -817,7 +969,7 @@ def run_ours(args):
                                                                    (r["result"]["v0"] == np.round(r["result"]["v0"]))))
                                                      if mode == "learned" else None),
                             "kernel_launches_per_step": r["launches_per_step"],
-                            "parity_vs_cpu": parity_vs_cpu(r["result"], cpu_sample)}
+                            "parity_vs_cpu": parity_vs_cpu(r["result"], cpu_result)}
     h2d = ref.nbytes + tar.nbytes + tmpl.nbytes
     cfg = config_block()
     cfg["seed_method"] = {"fftcc": "FFTCC", "learned": "learned proposal CNN (FFTCC fallback)"}[headline]
@@ -832,14 +984,14 @@ def run_ours(args):
         "roofline": roofline,
         "roofline_other_kernels": other,
         "cpu_baseline": {"value": cpu_value, "unit": "POI/s", "cores": threads, "kind": "port",
-                         "sample": f"full-image prep + FFTCC/IC-GN on every {CPU_SAMPLE_STRIDE}th POI "
-                                   f"({cpu_detail['sample_pois']} POIs), extrapolated; own FFT, not FFTW",
-                         "detail": cpu_detail},
-        "clocks": clk.summary() if clk else None,
+                         "sample": CPU_SAMPLE, "detail": cpu_detail},
+        "clocks": clock.summary(),
+        "clocks_headline": clock.summary([headline]),
         "gpu_launches": int(round(H0["launches_per_step"] * args.steps)),
         "icgn_launch_shape": eng.tuning()["icgn_column"],
         "seed_modes": seed_modes,
         "learned_vs_fftcc": (seed_modes["learned"]["value"] / seed_modes["fftcc"]["value"]) if "learned" in seed_modes else None,
+        "seed_floor": seed_floor,
         "parity_vs_cpu": seed_modes[headline]["parity_vs_cpu"],
         "config1_pair512": config1,
         "uneven_batch": uneven,

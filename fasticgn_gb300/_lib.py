@@ -67,11 +67,11 @@ class DicBatchReport(ctypes.Structure):
 
 class DicLaunchShape(ctypes.Structure):
     _fields_ = [("warps_per_cta", ctypes.c_int32), ("ctas_per_sm", ctypes.c_int32), ("tuned", ctypes.c_int32),
-                ("ms", ctypes.c_float), ("tile", ctypes.c_int32)]
+                ("ms", ctypes.c_float), ("tile", ctypes.c_int32), ("warps_per_poi", ctypes.c_int32)]
 
 
 class DicTuning(ctypes.Structure):
-    _fields_ = [("icgn", DicLaunchShape * 2), ("batch", DicLaunchShape * 2)]
+    _fields_ = [("icgn", DicLaunchShape * 3), ("batch", DicLaunchShape * 3)]
 
 
 class DicStats(ctypes.Structure):
@@ -108,6 +108,8 @@ SIGNATURES = {
     "dic_process_frame_history": (ctypes.c_int, [_vp, _vp, _i64, _vp, _vp, ctypes.POINTER(DicFramePolicy),
                                                  ctypes.POINTER(DicFrameReport)]),
     "dic_run_device": (ctypes.c_int, [_vp, _vp, _i64, _i32]),
+    "dic_process_pair_multi": (ctypes.c_int, [ctypes.POINTER(_vp), _i32, _vp, _i64, _vp]),
+    "dic_split_rows": (ctypes.c_int, [_vp, _i64, _i32, _vp]),
     "dic_sequence_begin": (ctypes.c_int, [_vp, _vp, _i64, ctypes.POINTER(DicFramePolicy)]),
     "dic_stage_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32]),
     "dic_sequence_frame": (ctypes.c_int, [_vp, _vp, _i32, _i32, _i64, _i32, _i32, _vp,
@@ -123,6 +125,8 @@ SIGNATURES = {
     "dic_read_plane": (ctypes.c_int, [_vp, _i32, _vp, _i64]),
     "dic_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(DicStats)]),
     "dic_set_timing": (ctypes.c_int, [_vp, _i32]),
+    "dic_read_probe": (ctypes.c_int, [_i32, _vp, _i64, _i32, _vp, _vp]),
+    "dic_fma_probe": (ctypes.c_int, [_i32, _i32, _vp, _vp, ctypes.POINTER(_i64)]),
     "dic_cnn_param_count": (_i64, []),
     "dic_cnn_create": (ctypes.c_int, [_i32, ctypes.POINTER(_vp)]),
     "dic_cnn_destroy": (None, [_vp]),

@@ -20,8 +20,9 @@
 // files, --durability picks rename or fsync, and --verify-only <dir> audits a directory
 // without computing (:3785-4060, :4613-4760).
 //
-// Not provided: --dual-gpu (one GPU), --kernel legacy and --fftcc cpu.  Asking for them is an
-// error with a message saying so.
+// Not provided: --dual-gpu (one GPU) and --fftcc cpu.  Asking for them is an error with a
+// message saying so.  --kernel legacy selects the IC-GN grid launch form (one CTA per POI
+// group) instead of the persistent work queue; the results are the same bytes.
 //
 // Host threads and streams: a decode thread reads ahead (--preload, the default); while frame
 // k is solved, frame k+1 is staged (copied to pinned memory, uploaded on the engine's upload
@@ -206,6 +207,7 @@ struct Options
   bool skip_fftcc = true, poi_fallback = true, preload = true;
   bool temporal = false;   // --temporal-extrapolation
   int decode_threads = 1;
+  bool legacy_kernel = false;   // --kernel legacy: the grid launch form (one CTA per POI group)
   bool keep(int x, int y) const
   {
     if (roi && (x < roi_x1 || x > roi_x2 || y < roi_y1 || y > roi_y2)) return false;
@@ -313,8 +315,16 @@ bool parse_common(const std::vector<std::string>& a, size_t& i, Options& o, std:
   {
     auto v = value("--kernel");
     if (!v) return false;
-    if (*v == "warp") return true;
-    if (*v == "legacy") return unsupported("--kernel legacy");
+    if (*v == "warp")
+    {
+      o.legacy_kernel = false;
+      return true;
+    }
+    if (*v == "legacy")
+    {
+      o.legacy_kernel = true;
+      return true;
+    }
     err = "--kernel must be legacy or warp, got '" + *v + "'";
     return false;
   }
@@ -500,7 +510,7 @@ void print_usage(std::ostream& out, bool full)
   out << "GB300 DIC engine command line (" << kTool << ")\n"
       << "Usage: " << kTool << " <ref_image> <tar_image> <subset_radius> <grid_space> <output_path>\n"
       << "       [--subset-size N] [--gpu-device N] [--max-iter M] [--conv-threshold T] [--line y1,y2] [--threads N]\n"
-      << "       [--output-format csv|raw] [--diagnostics|--diagnostics-dir DIR] [--kernel warp] [--fftcc gpu]\n"
+      << "       [--output-format csv|raw] [--diagnostics|--diagnostics-dir DIR] [--kernel warp|legacy] [--fftcc gpu]\n"
       << "       [--input-depth 8|12|16|auto] [--input-align right|left|auto] [--input-normalize none|to-8|to-16|unit]\n"
       << "       [--output-roi x1,y1,x2,y2] [--output-step N] [--durability rename|fsync] [--quiet]\n"
       << "   or: " << kTool << " --multi-frame --ref <ref_image> --tar-list <tar_list.txt> --output-dir <output_dir>\n"
@@ -521,7 +531,8 @@ void print_usage(std::ostream& out, bool full)
     out << "Defaults: --max-iter 10, --conv-threshold 0.001, --gpu-device 0, --output-format csv, --input-depth 8,\n"
         << "  --input-normalize none, --skip-fftcc on, --poi-fallback on, --temporal-extrapolation off, --preload on,\n"
         << "  --durability rename.\n"
-        << "Not available here: --dual-gpu, --kernel legacy, --fftcc cpu (one GPU).\n"
+        << "Not available here: --dual-gpu, --fftcc cpu (one GPU).  --kernel legacy runs the IC-GN grid launch\n"
+        << "  form instead of the persistent work queue (same results).\n"
         << "Exit status: 0 success (--verify-only: the directory is complete and verified); 1 any usage, input,\n"
         << "  compute or output error (--verify-only: the directory is not complete, or could not be read).\n";
 }
@@ -745,7 +756,7 @@ std::string engine_block(const Options& o, int device)
     << "    \"version\": " << jstr(kVersion) << ",\n"
     << "    \"git_dirty\": " << git_dirty_json() << ",\n"
     << "    \"icgn_backend\": \"cuda\",\n"
-    << "    \"icgn_kernel\": \"warp\",\n"
+    << "    \"icgn_kernel\": " << (o.legacy_kernel ? "\"legacy\"" : "\"warp\"") << ",\n"
     << "    \"oob_policy\": \"geometric-v1\",\n"
     << "    \"fftcc_backend\": \"gpu\",\n"
     << "    \"skip_fftcc\": " << (o.skip_fftcc ? "true" : "false") << ",\n"
@@ -903,6 +914,21 @@ struct Engine
     if (rc != DIC_OK)
       throw std::runtime_error("cannot create the DIC engine on CUDA device " + std::to_string(o.device) +
                                " (status " + std::to_string(rc) + ")");
+    if (o.legacy_kernel)
+    {
+      // --kernel legacy: every walk in the grid form, one CTA of 4 warps per POI group, each
+      // POI solved to completion by its own CTA slot (the reference's legacy kernel is
+      // block-per-POI); the default is the persistent work-queue form.  Same results.
+      for (int walk = 0; walk < 3; ++walk)
+      {
+        dic_launch_shape sh{};
+        sh.warps_per_cta = 4;
+        sh.ctas_per_sm = 0;
+        sh.warps_per_poi = 1;
+        if (dic_set_launch_shape(e, walk, &sh) != DIC_OK)
+          throw std::runtime_error(std::string("--kernel legacy: ") + dic_last_error(e));
+      }
+    }
   }
   ~Engine()
   {
@@ -1301,7 +1327,7 @@ Json run_contract(const std::string& ref_path, const std::vector<ListEntry>& ent
   op["radius"] = g.radius;
   op["step"] = g.grid;
   op["dual_gpu"] = false;
-  op["kernel"] = "warp";
+  op["kernel"] = o.legacy_kernel ? "legacy" : "warp";
   op["fftcc"] = "gpu";
   op["max_iteration"] = o.max_iter;
   op["convergence"] = (double)o.conv;
@@ -1684,8 +1710,10 @@ int run_multi(const std::vector<std::string>& args)
     {
       ++g_report.fallback_frames;
       if (!o.quiet)
-        std::cerr << "  [FALLBACK] " << f.output_name << " reason=bad_ratio > baseline + margin bad_ratio="
-                  << (float)rep.bad_before_repair / (float)n << ", post_fallback_bad_ratio=" << qa.bad_ratio << std::endl;
+        std::cerr << "  [FALLBACK] " << f.output_name << " reason=bad_ratio > baseline + margin"
+                  << " bad_ratio=" << (float)rep.bad_before_repair / (float)n << ", baseline_bad_ratio=" << baseline
+                  << ", margin=" << kSkipFftccBadRatioMargin << ", fallback_threshold=" << qa.fallback_threshold
+                  << ", post_fallback_bad_ratio=" << qa.bad_ratio << ", re-ran FFTCC + ICGN" << std::endl;
     }
     if (rep.repaired_candidates > 0)
     {

@@ -11,6 +11,7 @@
 #include <mutex>
 #include <set>
 #include <string>
+#include <thread>
 #include <vector>
 #include <algorithm>
 
@@ -286,6 +287,7 @@ struct dic_engine
   DevBuf<unsigned char> raw_ref, raw_tar;
   DevBuf<float> ref_f32, tar_f32;
   DevBuf<float4> ref_pack, coef;
+  DevBuf<float> lattice;   // coefficient [0][0] of every texel (the integer-translation fast path)
 
   // prepared layout
   std::vector<int> layout_x, layout_y;   // host copy of a host-defined layout
@@ -413,7 +415,7 @@ struct dic_engine
   {
     dim3 grid((w + kPrepTile - 1) / kPrepTile, (h + kPrepTile - 1) / kPrepTile);
     k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_tar.ptr), w, h, scale(),
-                                               tar_f32.ptr, coef.ptr);
+                                               tar_f32.ptr, coef.ptr, lattice.ptr);
     check_launch("k_prepare_tar");
   }
 
@@ -442,6 +444,7 @@ struct dic_engine
     const size_t px = (size_t)w * h;
     tar_f32.ensure(px);
     coef.ensure(px * 4);
+    lattice.ensure(px);
     mark(kPhTar, 0);
     switch (tar_dtype)
     {
@@ -534,16 +537,26 @@ struct dic_engine
   }
 
   // ---------------------------------------------------------------- launch shapes
-  // IC-GN runs one warp per POI; what can be tuned is how many POIs a CTA holds (2, 4 or
-  // 8 warps) and, for the persistent batch kernel, how many CTAs per SM it launches.
-  // Per-POI results do not depend on either.  shape[batch][column walk]: 0 single queues, 1 batches.
+  // What can be tuned: how many warps a CTA holds (2, 4 or 8), one CTA per group of POIs or
+  // a persistent launch (and, for the batch kernel, how many CTAs per SM), the staging tile
+  // (column walk) and the warps per POI (pair walk: 1 or 2).  Per-POI results depend on
+  // none of them.  shape[batch][walk]: batch 0 single queues, 1 batches; walk kWalkFlat,
+  // kWalkColumn, kWalkPair.
   struct IcgnShape
   {
     int warps = 4;
     int ctas_per_sm = 7;     // persistent launches: resident CTAs per SM (0: one CTA per kWarps POIs)
     float ms = 0.f;
     int tile = 0;            // column walk: 0 gathers from the table; 1, 2: k_icgn_tile (kTileKinds)
+    int poi_warps = 1;       // pair walk: warps per POI
   };
+  static constexpr int kWalkFlat = 0, kWalkColumn = 1, kWalkPair = 2;
+  // the subset walk of a radius: column walk up to 32 columns, pair walk up to 64, else flat
+  static int walk_of(int rx)
+  {
+    const int sw = 2 * rx + 1;
+    return sw <= 32 ? kWalkColumn : sw <= kPairMaxWidth ? kWalkPair : kWalkFlat;
+  }
   // TMA-staged tile forms: POIs (warps) per CTA, block width and height in texels, CTAs per SM
   // (shared memory: 2 planes x 32 B per texel, 110.7 KB and 163.9 KB)
   struct TileKind
@@ -655,8 +668,8 @@ struct dic_engine
   // of its L1 wavefronts on the 2048² pair, 3.73 ms against 3.59 ms persistent with the
   // four-plane table); the autotuner still times both forms.  shape[0]: single queues,
   // shape[1]: batches.
-  IcgnShape shape[2][2] = {{{4, 8, 0.f}, {4, 8, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}}};
-  bool tuned[2][2] = {};
+  IcgnShape shape[2][3] = {{{4, 8, 0.f}, {4, 8, 0.f}, {4, 8, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}}};
+  bool tuned[2][3] = {};
   DevBuf<dic_poi> tune_q;
   cudaEvent_t tune_ev[2] = {};
 
@@ -690,6 +703,22 @@ struct dic_engine
     return warps == 2 ? max_ctas_single<false, 2>() : warps == 8 ? max_ctas_single<false, 8>()
                                                                   : max_ctas_single<false, 4>();
   }
+  template <int PW, int W>
+  static int max_ctas_pair(bool batch)
+  {
+    int b = 0;
+    if (batch)
+      DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_pair<PW, W>, W * 32, 0));
+    else
+      DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_pair_persistent<PW, W>, W * 32, 0));
+    return std::max(b, 1);
+  }
+  static int occupancy_pair(bool batch, int poi_warps, int warps)
+  {
+    if (poi_warps == 2)
+      return warps == 2 ? max_ctas_pair<2, 2>(batch) : warps == 8 ? max_ctas_pair<2, 8>(batch) : max_ctas_pair<2, 4>(batch);
+    return warps == 2 ? max_ctas_pair<1, 2>(batch) : warps == 8 ? max_ctas_pair<1, 8>(batch) : max_ctas_pair<1, 4>(batch);
+  }
   static int occupancy(bool persistent, bool column, int warps)
   {
     if (column) return warps == 2 ? max_ctas<true, 2>(persistent) : warps == 8 ? max_ctas<true, 8>(persistent)
@@ -717,8 +746,57 @@ struct dic_engine
         (unsigned)std::min<int64_t>((int64_t)sms * kTileKinds[kind].ctas, (p.n + W - 1) / W);
     k_icgn_tile<W, BX, BY><<<grid, W * 32, tile_smem_bytes<BX, BY>(), stream>>>(q, m, icgn_next.ptr, wait_flag());
   }
-  void launch_icgn(const IcgnParams& p, bool column, const IcgnShape& sh)
+  void launch_icgn_pair(const IcgnParams& p, const IcgnShape& sh)
   {
+    const int warps = sh.warps, pw = sh.poi_warps == 2 ? 2 : 1;
+    const int slots = warps / pw;
+    if (sh.ctas_per_sm > 0)
+    {
+      icgn_next.ensure(1);
+      DIC_CUDA(cudaMemsetAsync(icgn_next.ptr, 0, sizeof(unsigned long long), stream));
+      int sms = 0;
+      DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+      const unsigned grid = (unsigned)std::min<int64_t>((int64_t)sms * sh.ctas_per_sm, (p.n + slots - 1) / slots);
+#define DIC_PAIR_PERSIST(PW, W) k_icgn_pair_persistent<PW, W><<<grid, W * 32, 0, stream>>>(p, icgn_next.ptr)
+      if (pw == 2)
+      {
+        if (warps == 2) DIC_PAIR_PERSIST(2, 2);
+        else if (warps == 8) DIC_PAIR_PERSIST(2, 8);
+        else DIC_PAIR_PERSIST(2, 4);
+      }
+      else
+      {
+        if (warps == 2) DIC_PAIR_PERSIST(1, 2);
+        else if (warps == 8) DIC_PAIR_PERSIST(1, 8);
+        else DIC_PAIR_PERSIST(1, 4);
+      }
+#undef DIC_PAIR_PERSIST
+      return;
+    }
+    const unsigned blocks = (unsigned)((p.n + slots - 1) / slots);
+#define DIC_PAIR_GRID(PW, W) k_icgn_pair<PW, W><<<blocks, W * 32, 0, stream>>>(p)
+    if (pw == 2)
+    {
+      if (warps == 2) DIC_PAIR_GRID(2, 2);
+      else if (warps == 8) DIC_PAIR_GRID(2, 8);
+      else DIC_PAIR_GRID(2, 4);
+    }
+    else
+    {
+      if (warps == 2) DIC_PAIR_GRID(1, 2);
+      else if (warps == 8) DIC_PAIR_GRID(1, 8);
+      else DIC_PAIR_GRID(1, 4);
+    }
+#undef DIC_PAIR_GRID
+  }
+  void launch_icgn(const IcgnParams& p, int walk, const IcgnShape& sh)
+  {
+    if (walk == kWalkPair)
+    {
+      launch_icgn_pair(p, sh);
+      return;
+    }
+    const bool column = walk == kWalkColumn;
     const int warps = sh.warps;
     if (sh.tile && column)
     {
@@ -779,12 +857,34 @@ struct dic_engine
     unsigned long long* next;
     unsigned long long* iter_sum;
   };
-  void launch_batch(const BatchLaunch& b, bool column, const IcgnShape& sh)
+  void launch_batch(const BatchLaunch& b, int walk, const IcgnShape& sh)
   {
     int sms = 0;
     DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
     const unsigned grid = (unsigned)(sms * sh.ctas_per_sm);
     const float mi = (float)cfg.max_iteration;
+    if (walk == kWalkPair)
+    {
+#define DIC_BATCH_PAIR(PW, W)                                                                                      \
+  k_icgn_batch_pair<PW, W><<<grid, W * 32, 0, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next, \
+                                                       cfg.conv_criterion, mi, b.iter_sum)
+      if (sh.poi_warps == 2)
+      {
+        if (sh.warps == 2) DIC_BATCH_PAIR(2, 2);
+        else if (sh.warps == 8) DIC_BATCH_PAIR(2, 8);
+        else DIC_BATCH_PAIR(2, 4);
+      }
+      else
+      {
+        if (sh.warps == 2) DIC_BATCH_PAIR(1, 2);
+        else if (sh.warps == 8) DIC_BATCH_PAIR(1, 8);
+        else DIC_BATCH_PAIR(1, 4);
+      }
+#undef DIC_BATCH_PAIR
+      check_launch("k_icgn_batch_pair");
+      return;
+    }
+    const bool column = walk == kWalkColumn;
 #define DIC_BATCH_LAUNCH(C, W)                                                                                     \
   k_icgn_batch<C, W><<<grid, W * 32, 0, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,       \
                                                   cfg.conv_criterion, mi, b.iter_sum)
@@ -817,8 +917,9 @@ struct dic_engine
   }
   // Times every candidate shape on a copy of the seeded queue (best of two runs) and keeps
   // the fastest.  The queue itself is not touched.
-  void tune_icgn(const IcgnParams& p0, bool column)
+  void tune_icgn(const IcgnParams& p0, int walk)
   {
+    const bool column = walk == kWalkColumn;
     tune_q.ensure((size_t)p0.n);
     IcgnParams p = p0;
     p.pois = tune_q.ptr;
@@ -828,7 +929,11 @@ struct dic_engine
     std::vector<IcgnShape> cand;
     for (int warps : {2, 4, 8})
       for (int persistent = 0; persistent < 2; ++persistent)
-        cand.push_back(IcgnShape{warps, persistent ? occupancy_single(column, warps) : 0, 0.f, 0});
+        if (walk == kWalkPair)
+          for (int pw : {1, 2})
+            cand.push_back(IcgnShape{warps, persistent ? occupancy_pair(false, pw, warps) : 0, 0.f, 0, pw});
+        else
+          cand.push_back(IcgnShape{warps, persistent ? occupancy_single(column, warps) : 0, 0.f, 0});
     // the TMA-staged tile forms (column walk, where the driver provides tensor maps)
     if (column && encode_tiled())
       for (int kind = 1; kind <= 2; ++kind)
@@ -839,15 +944,15 @@ struct dic_engine
       for (int rep = 0; rep < 2; ++rep)
       {
         DIC_CUDA(cudaMemcpyAsync(tune_q.ptr, p0.pois, sizeof(dic_poi) * p0.n, cudaMemcpyDeviceToDevice, stream));
-        t = std::min(t, time_once([&] { launch_icgn(p, column, sh); }));
+        t = std::min(t, time_once([&] { launch_icgn(p, walk, sh); }));
       }
-      if (t < best.ms) best = IcgnShape{sh.warps, sh.ctas_per_sm, t, sh.tile};
+      if (t < best.ms) best = IcgnShape{sh.warps, sh.ctas_per_sm, t, sh.tile, sh.poi_warps};
     }
     check_wait_error();
-    shape[0][column] = best;
-    tuned[0][column] = true;
+    shape[0][walk] = best;
+    tuned[0][walk] = true;
   }
-  void tune_batch(const BatchLaunch& b0, bool column, int64_t total)
+  void tune_batch(const BatchLaunch& b0, int walk, int64_t total)
   {
     tune_q.ensure((size_t)total);
     BatchLaunch b = b0;
@@ -856,24 +961,27 @@ struct dic_engine
     IcgnShape best;
     best.ms = INFINITY;
     for (int warps : {2, 4, 8})
-    {
-      const int full = occupancy(true, column, warps);
-      for (int ctas : {full, std::max(1, (3 * full) / 4)})
+      for (int pw : {1, 2})
       {
-        const IcgnShape sh{warps, ctas, 0.f};
-        float t = INFINITY;
-        for (int rep = 0; rep < 2; ++rep)
+        if (walk != kWalkPair && pw == 2) continue;
+        const int full =
+            walk == kWalkPair ? occupancy_pair(true, pw, warps) : occupancy(true, walk == kWalkColumn, warps);
+        for (int ctas : {full, std::max(1, (3 * full) / 4)})
         {
-          DIC_CUDA(cudaMemcpyAsync(tune_q.ptr + b.begin, b0.pois + b.begin, sizeof(dic_poi) * (b.end - b.begin),
-                                   cudaMemcpyDeviceToDevice, stream));
-          DIC_CUDA(cudaMemsetAsync(b.next, 0, sizeof(unsigned long long), stream));
-          t = std::min(t, time_once([&] { launch_batch(b, column, sh); }));
+          const IcgnShape sh{warps, ctas, 0.f, 0, pw};
+          float t = INFINITY;
+          for (int rep = 0; rep < 2; ++rep)
+          {
+            DIC_CUDA(cudaMemcpyAsync(tune_q.ptr + b.begin, b0.pois + b.begin, sizeof(dic_poi) * (b.end - b.begin),
+                                     cudaMemcpyDeviceToDevice, stream));
+            DIC_CUDA(cudaMemsetAsync(b.next, 0, sizeof(unsigned long long), stream));
+            t = std::min(t, time_once([&] { launch_batch(b, walk, sh); }));
+          }
+          if (t < best.ms) best = IcgnShape{warps, ctas, t, 0, pw};
         }
-        if (t < best.ms) best = IcgnShape{warps, ctas, t};
       }
-    }
-    shape[1][column] = best;
-    tuned[1][column] = true;
+    shape[1][walk] = best;
+    tuned[1][walk] = true;
     DIC_CUDA(cudaMemsetAsync(b0.next, 0, sizeof(unsigned long long), stream));
   }
 
@@ -930,6 +1038,7 @@ struct dic_engine
     p.n_dev = n_dev;
     p.enable = enable;
     p.coef = coef.ptr;
+    p.lattice = lattice.ptr;
     p.ref_pack = ref_pack.ptr;
     p.poi_ref = poi_ref.ptr;
     p.slot = d_slots;
@@ -942,10 +1051,10 @@ struct dic_engine
     p.conv = cfg.conv_criterion;
     p.max_iter = (float)(max_iter_override > 0 ? max_iter_override : cfg.max_iteration);
     p.iter_sum = counters.ptr;
-    const bool column = 2 * p.rx + 1 <= 32;
-    if (autotune && !tuned[0][column] && n >= kTuneMinPois && !capturing()) tune_icgn(p, column);
+    const int walk = walk_of(p.rx);
+    if (autotune && !tuned[0][walk] && n >= kTuneMinPois && !capturing()) tune_icgn(p, walk);
     mark(kPhIcgn, 0);
-    launch_icgn(p, column, shape[0][column]);
+    launch_icgn(p, walk, shape[0][walk]);
     check_launch("k_icgn");
     mark(kPhIcgn, 1);
     icgn_pois = n;
@@ -1246,9 +1355,11 @@ struct dic_engine
     DevBuf<unsigned char> raw_ref, raw_tar;
     DevBuf<float> ref_f32, tar_f32;
     DevBuf<float4> ref_pack, coef;
+    DevBuf<float> lattice;
     void release()
     {
       raw_ref.release(); raw_tar.release(); ref_f32.release(); tar_f32.release(); ref_pack.release(); coef.release();
+      lattice.release();
     }
   };
   std::vector<JobBufs> jobs_mem;
@@ -1265,14 +1376,15 @@ struct dic_engine
                                                J.ref_pack.ptr);
     check_launch("k_prepare_ref");
     k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_t), bw, bh, scale(), J.tar_f32.ptr,
-                                               J.coef.ptr);
+                                               J.coef.ptr, J.lattice.ptr);
     check_launch("k_prepare_tar");
   }
 
-  // Batch plan: column-walk jobs (2r + 1 <= 32) first, then wider subsets, stable otherwise.
+  // Batch plan: column-walk jobs (2r + 1 <= 32) first, then the pair walk's (33 to 64
+  // columns), then wider subsets, stable otherwise.
   std::vector<int> b_order;
   std::vector<int64_t> b_first;
-  int64_t b_total = 0, b_col_end = 0;
+  int64_t b_total = 0, b_col_end = 0, b_pair_end = 0;
   std::vector<dic_job> b_key;           // jobs of the captured batch graph (device pointers)
   bool b_key_seen = false;
   cudaGraphExec_t batch_graph = nullptr;
@@ -1282,24 +1394,30 @@ struct dic_engine
   {
     b_order.resize(nj);
     for (int j = 0; j < nj; ++j) b_order[j] = j;
-    std::stable_sort(b_order.begin(), b_order.end(), [&](int a, int b) {
-      return (2 * jobs[a].subset_radius + 1 <= 32) > (2 * jobs[b].subset_radius + 1 <= 32);
-    });
+    // walk rank: column 0, pair 1, flat 2
+    const auto rank = [&](int j) {
+      const int wk = walk_of(jobs[j].subset_radius);
+      return wk == kWalkColumn ? 0 : wk == kWalkPair ? 1 : 2;
+    };
+    std::stable_sort(b_order.begin(), b_order.end(), [&](int a, int b) { return rank(a) < rank(b); });
     b_first.assign(nj, 0);
     b_total = 0;
     b_col_end = 0;
+    b_pair_end = 0;
     for (int k = 0; k < nj; ++k)
     {
       const dic_job& J = jobs[b_order[k]];
       b_first[k] = b_total;
       b_total += J.count;
-      if (2 * J.subset_radius + 1 <= 32) b_col_end = b_total;
+      const int r = rank(b_order[k]);
+      if (r == 0) b_col_end = b_total;
+      if (r <= 1) b_pair_end = b_total;
     }
     if ((int)jobs_mem.size() < nj) jobs_mem.resize(nj);
     bq.ensure((size_t)std::max<int64_t>(b_total, 1));
     bpoi.ensure((size_t)std::max<int64_t>(b_total, 1));
     bjobs.ensure((size_t)nj);
-    bnext.ensure(2);
+    bnext.ensure(3);
     counters.ensure(1);
     std::vector<BatchJob> table(nj);
     for (int k = 0; k < nj; ++k)
@@ -1314,7 +1432,8 @@ struct dic_engine
       M.tar_f32.ensure(px);
       M.ref_pack.ensure(px);
       M.coef.ensure(px * 4);
-      table[k] = BatchJob{M.coef.ptr, M.ref_pack.ptr, b_first[k], J.width, J.height, J.subset_radius,
+      M.lattice.ensure(px);
+      table[k] = BatchJob{M.coef.ptr, M.lattice.ptr, M.ref_pack.ptr, b_first[k], J.width, J.height, J.subset_radius,
                           J.subset_radius};
     }
     DIC_CUDA(cudaMemcpyAsync(bjobs.ptr, table.data(), sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, stream));
@@ -1352,18 +1471,21 @@ struct dic_engine
       FftccParams fp{M.ref_f32.ptr, M.tar_f32.ptr, q, J.count, J.width, J.height};
       fftcc_launch(fp, r);
     }
-    DIC_CUDA(cudaMemsetAsync(bnext.ptr, 0, 2 * sizeof(unsigned long long), stream));
+    DIC_CUDA(cudaMemsetAsync(bnext.ptr, 0, 3 * sizeof(unsigned long long), stream));
     BatchLaunch col{bjobs.ptr, nj, bq.ptr, bpoi.ptr, 0, b_col_end, bnext.ptr, counters.ptr};
-    BatchLaunch flat{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_col_end, b_total, bnext.ptr + 1, counters.ptr};
+    BatchLaunch pair{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_col_end, b_pair_end, bnext.ptr + 2, counters.ptr};
+    BatchLaunch flat{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_pair_end, b_total, bnext.ptr + 1, counters.ptr};
     const bool cap = capturing();
     if (autotune && !cap)
     {
-      if (b_col_end >= kTuneMinPois && !tuned[1][1]) tune_batch(col, true, b_total);
-      if (b_total - b_col_end >= kTuneMinPois && !tuned[1][0]) tune_batch(flat, false, b_total);
+      if (b_col_end >= kTuneMinPois && !tuned[1][kWalkColumn]) tune_batch(col, kWalkColumn, b_total);
+      if (b_pair_end - b_col_end >= kTuneMinPois && !tuned[1][kWalkPair]) tune_batch(pair, kWalkPair, b_total);
+      if (b_total - b_pair_end >= kTuneMinPois && !tuned[1][kWalkFlat]) tune_batch(flat, kWalkFlat, b_total);
     }
     mark(kPhIcgn, 0);
-    if (b_col_end > 0) launch_batch(col, true, shape[1][1]);
-    if (b_total > b_col_end) launch_batch(flat, false, shape[1][0]);
+    if (b_col_end > 0) launch_batch(col, kWalkColumn, shape[1][kWalkColumn]);
+    if (b_pair_end > b_col_end) launch_batch(pair, kWalkPair, shape[1][kWalkPair]);
+    if (b_total > b_pair_end) launch_batch(flat, kWalkFlat, shape[1][kWalkFlat]);
     mark(kPhIcgn, 1);
     for (int k = 0; k < nj; ++k)
     {
@@ -1640,6 +1762,7 @@ void dic_engine_destroy(dic_engine* e)
   e->tar_f32.release();
   e->ref_pack.release();
   e->coef.release();
+  e->lattice.release();
   e->poi_ref.release();
   e->queue.release();
   e->slots.release();
@@ -1775,8 +1898,22 @@ int dic_process_pair(dic_engine* e, dic_poi* pois, int64_t n)
     if (n == 0) return;
     // the queue's upload overlaps the reference and target preparation, which do not read it
     e->upload_queue_beside(pois, n);
+    // If the preparation throws (an allocation or a launch fails), the copy is still joined
+    // to the engine stream and waited for before the error returns: later engine work on
+    // the queue buffer stays ordered after it, and the caller may free its source at once.
+    struct JoinOnError
+    {
+      dic_engine* e;
+      ~JoinOnError()
+      {
+        if (!e) return;
+        cudaStreamWaitEvent(e->stream, e->qup_done, 0);
+        cudaEventSynchronize(e->qup_done);
+      }
+    } join_on_error{e};
     e->ensure_ref();
     e->ensure_tar();
+    join_on_error.e = nullptr;
     e->join_queue_upload();
     // FFTCC reads only (x, y, u, v) and writes the seed; the per-POI reference data reads
     // only (x, y).  Launching FFTCC first lets the host's layout check and record (a pass
@@ -1790,6 +1927,46 @@ int dic_process_pair(dic_engine* e, dic_poi* pois, int64_t n)
     e->run_icgn(e->queue.ptr, n, nullptr);
     e->download_queue(pois, n);
   });
+}
+
+int dic_split_rows(const dic_poi* pois, int64_t n, int32_t parts, int64_t* starts)
+{
+  if (parts < 1 || n < 0 || (n > 0 && !pois) || !starts) return DIC_ERR_ARGUMENT;
+  // Cut k at the first row start at or after k * n / parts, so that no row of POIs (equal y,
+  // contiguous in buildPoiQueue order) is split between two parts.
+  starts[0] = 0;
+  for (int32_t k = 1; k < parts; ++k)
+  {
+    int64_t c = std::max<int64_t>(starts[k - 1], (int64_t)((__int128)n * k / parts));
+    while (c > 0 && c < n && pois[c].y == pois[c - 1].y) ++c;
+    starts[k] = c;
+  }
+  starts[parts] = n;
+  return DIC_OK;
+}
+
+int dic_process_pair_multi(dic_engine* const* engines, int32_t count, dic_poi* pois, int64_t n, int64_t* band_starts)
+{
+  if (!engines || count < 1 || n < 0 || (n > 0 && !pois)) return DIC_ERR_ARGUMENT;
+  for (int32_t k = 0; k < count; ++k)
+    if (!engines[k]) return DIC_ERR_ARGUMENT;
+  std::vector<int64_t> starts(count + 1);
+  const int rc = dic_split_rows(pois, n, count, starts.data());
+  if (rc != DIC_OK) return rc;
+  if (band_starts) std::copy(starts.begin(), starts.end(), band_starts);
+  // one host thread per engine (each engine keeps its one-thread-per-handle rule); the bands
+  // are disjoint ranges of the caller's queue, so the results land in queue order
+  std::vector<int> status(count, DIC_OK);
+  std::vector<std::thread> workers;
+  workers.reserve(count);
+  for (int32_t k = 0; k < count; ++k)
+    workers.emplace_back([&, k] {
+      status[k] = dic_process_pair(engines[k], pois + starts[k], starts[k + 1] - starts[k]);
+    });
+  for (auto& w : workers) w.join();
+  for (int32_t k = 0; k < count; ++k)
+    if (status[k] != DIC_OK) return status[k];
+  return DIC_OK;
 }
 
 int dic_run_device(dic_engine* e, dic_poi* d_pois, int64_t n, int32_t flags)
@@ -2111,28 +2288,29 @@ int dic_get_tuning(dic_engine* e, dic_tuning* out)
   return guarded(e, [&] {
     if (!out) throw DicError{DIC_ERR_ARGUMENT, "get_tuning: null output"};
     for (int pers = 0; pers < 2; ++pers)
-      for (int col = 0; col < 2; ++col)
+      for (int walk = 0; walk < 3; ++walk)
       {
-        dic_launch_shape& d = pers ? out->batch[col] : out->icgn[col];
-        const auto& s = e->shape[pers][col];
+        dic_launch_shape& d = pers ? out->batch[walk] : out->icgn[walk];
+        const auto& s = e->shape[pers][walk];
         d.warps_per_cta = s.warps;
         d.ctas_per_sm = s.ctas_per_sm;
-        d.tuned = e->tuned[pers][col] ? 1 : 0;
+        d.tuned = e->tuned[pers][walk] ? 1 : 0;
         d.ms = s.ms;
         d.tile = s.tile;
+        d.warps_per_poi = walk == dic_engine::kWalkPair ? s.poi_warps : 1;
       }
   }, false);
 }
 
-int dic_set_launch_shape(dic_engine* e, int32_t column_walk, const dic_launch_shape* shape)
+int dic_set_launch_shape(dic_engine* e, int32_t walk, const dic_launch_shape* shape)
 {
   return guarded(e, [&] {
     if (!shape) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: null shape"};
-    const int col = column_walk ? 1 : 0;
+    if (walk < 0 || walk > 2) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: walk must be 0 (flat), 1 (column) or 2 (pair)"};
     dic_engine::IcgnShape sh;
     if (shape->tile != 0)
     {
-      if (shape->tile < 0 || shape->tile > 2 || !col)
+      if (shape->tile < 0 || shape->tile > 2 || walk != dic_engine::kWalkColumn)
         throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0, or 1 or 2 with the column walk"};
       const auto& k = dic_engine::kTileKinds[shape->tile];
       sh = dic_engine::IcgnShape{k.warps, k.ctas, 0.f, shape->tile};
@@ -2142,10 +2320,13 @@ int dic_set_launch_shape(dic_engine* e, int32_t column_walk, const dic_launch_sh
       if (shape->warps_per_cta != 2 && shape->warps_per_cta != 4 && shape->warps_per_cta != 8)
         throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: warps_per_cta must be 2, 4 or 8"};
       if (shape->ctas_per_sm < 0) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: ctas_per_sm must be >= 0"};
-      sh = dic_engine::IcgnShape{shape->warps_per_cta, shape->ctas_per_sm, 0.f, 0};
+      const int pw = shape->warps_per_poi == 0 ? 1 : shape->warps_per_poi;
+      if (pw != 1 && !(pw == 2 && walk == dic_engine::kWalkPair))
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: warps_per_poi must be 1, or 2 with the pair walk"};
+      sh = dic_engine::IcgnShape{shape->warps_per_cta, shape->ctas_per_sm, 0.f, 0, pw};
     }
-    e->shape[0][col] = sh;
-    e->tuned[0][col] = false;
+    e->shape[0][walk] = sh;
+    e->tuned[0][walk] = false;
     if (e->seq_graph)
     {
       // a captured sequence frame holds the previous launch
@@ -2221,6 +2402,92 @@ int dic_set_timing(dic_engine* e, int32_t enabled)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------- read-bandwidth probe
+// The denominator of the IC-GN gather roofline.  The gathers read 32-byte halves of
+// coefficient texels with 256-bit non-coherent loads and are served by L2 (the table's
+// working set of a few thousand POIs in flight fits there; DRAM carries only the
+// compulsory bytes), so their bound is the L2-to-SM read bandwidth, measured here with
+// the same load instruction: every thread streams 32-byte chunks of a buffer that L2 holds,
+// four loads in flight, `repeats` passes per launch.
+namespace
+{
+__global__ void __launch_bounds__(256) k_read_probe(const float4* __restrict__ buf, int64_t chunks, int repeats,
+                                                    float* __restrict__ sink)
+{
+  const int64_t T = (int64_t)gridDim.x * blockDim.x;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float acc = 0.f;
+  for (int rep = 0; rep < repeats; ++rep)
+  {
+    int64_t j = t;
+    for (; j + 3 * T < chunks; j += 4 * T)
+    {
+      float4 a0, b0, a1, b1, a2, b2, a3, b3;
+      ldg_256(buf + 2 * j, a0, b0);
+      ldg_256(buf + 2 * (j + T), a1, b1);
+      ldg_256(buf + 2 * (j + 2 * T), a2, b2);
+      ldg_256(buf + 2 * (j + 3 * T), a3, b3);
+      acc += (a0.x + b0.w) + (a1.x + b1.w) + (a2.x + b2.w) + (a3.x + b3.w);
+    }
+    for (; j < chunks; j += T)
+    {
+      float4 a, b;
+      ldg_256(buf + 2 * j, a, b);
+      acc += a.x + b.w;
+    }
+  }
+  if (acc == 1.2345678e-30f) *sink = acc;   // keeps the loads; never true for finite data of sane size
+}
+
+// FP32 FMA issue rate (the FFTCC kernels' bound): eight independent FMA chains per thread,
+// 8 CTAs of 256 threads per SM, `iterations` rounds of eight FMAs (16 FLOP each round-lane).
+__global__ void __launch_bounds__(256) k_fma_probe(int iterations, float seed, float* __restrict__ sink)
+{
+  float a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = seed + (float)(threadIdx.x + k);
+  const float m = 0.999999f, c = 1e-7f;
+  for (int it = 0; it < iterations; ++it)
+  {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fmaf(a[k], m, c);
+  }
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc += a[k];
+  if (acc == 1.2345678e-30f) *sink = acc;
+}
+}  // namespace
+
+extern "C" int dic_fma_probe(int32_t device, int32_t iterations, float* device_sink, void* stream,
+                             int64_t* flop_out)
+{
+  if (!device_sink || iterations < 1 || !flop_out) return DIC_ERR_ARGUMENT;
+  int sms = 0;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return DIC_ERR_CUDA;
+  const unsigned blocks = (unsigned)(sms * 8);
+  k_fma_probe<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(iterations, 1.f, device_sink);
+  *flop_out = (int64_t)blocks * 256 * iterations * 8 * 2;
+  return cudaGetLastError() == cudaSuccess ? DIC_OK : DIC_ERR_CUDA;
+}
+
+extern "C" int dic_read_probe(int32_t device, const void* device_buf, int64_t bytes, int32_t repeats,
+                              float* device_sink, void* stream)
+{
+  if (!device_buf || !device_sink || bytes < 32 || repeats < 1 || (reinterpret_cast<uintptr_t>(device_buf) & 31))
+    return DIC_ERR_ARGUMENT;
+  int sms = 0;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return DIC_ERR_CUDA;
+  // 8 resident CTAs of 256 threads per SM: 64 warps, the SM's limit
+  k_read_probe<<<(unsigned)(sms * 8), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      static_cast<const float4*>(device_buf), bytes / 32, repeats, device_sink);
+  return cudaGetLastError() == cudaSuccess ? DIC_OK : DIC_ERR_CUDA;
+}
 
 // ---------------------------------------------------------------- proposal network ABI
 namespace
@@ -2475,6 +2742,17 @@ extern "C" int dic_process_pair_noalloc(const dic_config* cfg, const void* d_ref
     return DIC_ERR_ARGUMENT;
   }
   const size_t px = (size_t)w * h;
+  // Bound each term before the sum, so that no product or sum of huge sizes can wrap and
+  // pass the capacity check (88 bytes of planes per pixel, one PoiRef per POI).
+  if (px > kNoAllocScratchBytes / 88 || (uint64_t)n > kNoAllocScratchBytes / sizeof(PoiRef))
+  {
+    noalloc_error(error_text, error_capacity,
+                  "dic_process_pair_noalloc: " + std::to_string(w) + "x" + std::to_string(h) + " with " +
+                      std::to_string(n) + " POIs exceeds the fixed scratch of " +
+                      std::to_string(kNoAllocScratchBytes) +
+                      " bytes (88 bytes per pixel + 224 bytes per POI, each plane rounded up to 256 bytes)");
+    return DIC_ERR_ARGUMENT;
+  }
   const size_t off_ref = 0, off_pack = off_ref + align256(px * sizeof(float));
   const size_t off_tar = off_pack + align256(px * sizeof(float4));
   const size_t off_coef = off_tar + align256(px * sizeof(float));
@@ -2524,7 +2802,7 @@ extern "C" int dic_process_pair_noalloc(const dic_config* cfg, const void* d_ref
       case DIC_U16: noalloc_prepare<uint16_t>(d_ref, d_tar, w, h, scale, ref_f32, ref_pack, tar_f32, coef, s); break;
       default: noalloc_prepare<float>(d_ref, d_tar, w, h, scale, ref_f32, ref_pack, tar_f32, coef, s); break;
     }
-    const int wpb = 4;
+    constexpr int wpb = 4;
     const unsigned blocks = (unsigned)((n + wpb - 1) / wpb);
     k_poi_prepare<<<blocks, wpb * 32, 0, s>>>(ref_pack, w, h, d_pois, n, r, r, poi_ref);
     FftccParams fp{ref_f32, tar_f32, d_pois, n, w, h};
@@ -2555,6 +2833,8 @@ extern "C" int dic_process_pair_noalloc(const dic_config* cfg, const void* d_ref
     ip.iter_sum = nullptr;
     if (2 * r + 1 <= 32)
       k_icgn<true><<<blocks, wpb * 32, 0, s>>>(ip);
+    else if (2 * r + 1 <= kPairMaxWidth)
+      k_icgn_pair<1, wpb><<<blocks, wpb * 32, 0, s>>>(ip);
     else
       k_icgn<false><<<blocks, wpb * 32, 0, s>>>(ip);
     DIC_CUDA(cudaGetLastError());

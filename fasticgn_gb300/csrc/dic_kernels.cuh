@@ -22,6 +22,16 @@ namespace dic
 
 constexpr int kWarp = 32;
 constexpr unsigned kFull = 0xffffffffu;
+// Widest subset (columns) of the pair walk: two column classes of at most 32 each.
+#ifndef DIC_PAIR_MAX_WIDTH
+#define DIC_PAIR_MAX_WIDTH 64
+#endif
+constexpr int kPairMaxWidth = DIC_PAIR_MAX_WIDTH;
+// Column of lane l in class k of the pair walk: interleaved (2 l + k) or halves (32 k + l).
+#ifndef DIC_PAIR_HALVES
+#define DIC_PAIR_HALVES 0
+#endif
+__host__ __device__ constexpr int pair_column(int lane, int k) { return DIC_PAIR_HALVES ? 32 * k + lane : 2 * lane + k; }
 
 // --------------------------------------------------------------------------------------
 // Per-POI reference record, built once per (reference, layout) by k_poi_prepare.
@@ -148,7 +158,7 @@ __global__ void __launch_bounds__(256) k_prepare_ref(const T* __restrict__ raw, 
 template <typename T>
 __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, int w, int h, float scale,
                                                      float* __restrict__ tar_f32,
-                                                     float4* __restrict__ coef)
+                                                     float4* __restrict__ coef, float* __restrict__ lattice = nullptr)
 {
   __shared__ float tile[kPrepTile + 3][kPrepTile + 3 + 1];
   const int bx = blockIdx.x * kPrepTile, by = blockIdx.y * kPrepTile;
@@ -172,6 +182,7 @@ __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, 
   {
     const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     dst[0] = z; dst[1] = z; dst[2 * plane] = z; dst[2 * plane + 1] = z;
+    if (lattice) lattice[o] = 0.f;
     return;
   }
   float q[4][4];
@@ -196,6 +207,8 @@ __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, 
 #pragma unroll
   for (int k = 0; k < 4; ++k)
     dst[(k >> 1) * 2 * plane + (k & 1)] = make_float4(p[3 - k][3], p[3 - k][2], p[3 - k][1], p[3 - k][0]);
+  // the interpolant at the texel's own integer position (dx = dy = 0): coefficient [0][0]
+  if (lattice) lattice[o] = p[3][3];
 }
 
 // --------------------------------------------------------------------------------------
@@ -399,6 +412,96 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
     }
     if (lane == 0) rec->t0 = t0;
   }
+  else if (sw <= kPairMaxWidth)
+  {
+    // Pair walk (33 to 64 columns): column classes c = 2 lane + k, each walked like the
+    // column walk and butterfly-reduced on its own, class totals added in class order --
+    // the order in which the IC-GN pair walk forms its target-side sums.
+    const float4* base = ref_pack + (size_t)(cy - ry) * w + cx - rx;
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+    {
+      const int c = pair_column(lane, k);
+      if (c < sw)
+        for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&base[(size_t)r * w + c].x);
+    }
+    sum = warp_sum(sum);
+    const float t0 = sum / (float)size;
+#pragma unroll 1
+    for (int k = 0; k < 2; ++k)
+    {
+      const int c = pair_column(lane, k);
+      float pn = 0.f, ps = 0.f, pS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, pG[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+      float Qxx[3] = {0.f, 0.f, 0.f}, Qyy[3] = {0.f, 0.f, 0.f}, Qxy[3] = {0.f, 0.f, 0.f};
+      if (c < sw)
+      {
+        const float4* col = base + c;
+        for (int r = 0; r < 2 * ry + 1; ++r)
+        {
+          const float fly = (float)(r - ry);
+          const float4 v = __ldg(&col[(size_t)r * w]);
+          const float rc = v.x - t0;
+          pn = fmaf(rc, rc, pn);
+          ps += rc;
+          const float grc = __fmul_rn(v.y, rc), hrc = __fmul_rn(v.z, rc);
+          pG[0] = __fadd_rn(pG[0], grc);
+          pG[2] = fmaf(grc, fly, pG[2]);
+          pG[3] = __fadd_rn(pG[3], hrc);
+          pG[5] = fmaf(hrc, fly, pG[5]);
+          pS[0] += v.y;
+          pS[2] = fmaf(v.y, fly, pS[2]);
+          pS[3] += v.z;
+          pS[5] = fmaf(v.z, fly, pS[5]);
+          const float xx = v.y * v.y, yy = v.z * v.z, xy = v.y * v.z;
+          const float xxl = xx * fly, yyl = yy * fly, xyl = xy * fly;
+          Qxx[0] += xx; Qxx[1] += xxl; Qxx[2] = fmaf(xxl, fly, Qxx[2]);
+          Qyy[0] += yy; Qyy[1] += yyl; Qyy[2] = fmaf(yyl, fly, Qyy[2]);
+          Qxy[0] += xy; Qxy[1] += xyl; Qxy[2] = fmaf(xyl, fly, Qxy[2]);
+        }
+      }
+      const float lx = (float)(c - rx), lx2 = lx * lx;
+      pG[1] = lx * pG[0];
+      pG[4] = lx * pG[3];
+      pS[1] = lx * pS[0];
+      pS[4] = lx * pS[3];
+      float pH[21] = {Qxx[0], lx * Qxx[0], lx2 * Qxx[0], Qxx[1], lx * Qxx[1], Qxx[2],
+                      Qxy[0], lx * Qxy[0], Qxy[1], Qyy[0],
+                      lx * Qxy[0], lx2 * Qxy[0], lx * Qxy[1], lx * Qyy[0], lx2 * Qyy[0],
+                      Qxy[1], lx * Qxy[1], Qxy[2], Qyy[1], lx * Qyy[1], Qyy[2]};
+      pn = warp_sum(pn);
+      ps = warp_sum(ps);
+#pragma unroll
+      for (int a = 0; a < 6; ++a) { pS[a] = warp_sum(pS[a]); pG[a] = warp_sum(pG[a]); }
+#pragma unroll
+      for (int t = 0; t < 21; ++t) pH[t] = warp_sum(pH[t]);
+      if (k == 0)
+      {
+        nsq = pn;
+        src = ps;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) { S[a] = pS[a]; G[a] = pG[a]; }
+#pragma unroll
+        for (int t = 0; t < 21; ++t) H[t] = pH[t];
+      }
+      else
+      {
+        nsq = __fadd_rn(nsq, pn);
+        src = __fadd_rn(src, ps);
+#pragma unroll
+        for (int a = 0; a < 6; ++a) { S[a] = __fadd_rn(S[a], pS[a]); G[a] = __fadd_rn(G[a], pG[a]); }
+#pragma unroll
+        for (int t = 0; t < 21; ++t) H[t] = __fadd_rn(H[t], pH[t]);
+      }
+    }
+    if (lane == 0) rec->t0 = t0;
+#pragma unroll
+    for (int a = 0; a < 6; ++a) { out_sums.S[a] = S[a]; out_sums.G[a] = G[a]; }
+#pragma unroll
+    for (int t = 0; t < 21; ++t) out_sums.H[t] = H[t];
+    out_sums.nsq = nsq;
+    out_sums.src = src;
+    return true;   // already reduced
+  }
   else
   {
     DIC_FOR_EACH_SAMPLE(lane, rx, ry, sum += __ldg(&ref_pack[(size_t)(cy + ly) * w + cx + lx].x);)
@@ -584,6 +687,7 @@ constexpr uint32_t kWaitPolls = 1u << 22;
 struct IcgnParams
 {
   const float4* coef;      // tar B-spline table: 2 planes of W*H texels x 2 float4
+  const float* lattice = nullptr;   // coefficient [0][0] of every texel (nullable, see on_lattice)
   const float4* ref_pack;  // {ref, gx, gy, 0}
   const PoiRef* poi_ref;   // per layout slot
   const int64_t* slot;     // queue index -> layout slot (nullptr: identity)
@@ -631,6 +735,18 @@ __device__ __forceinline__ void compose_update(float (&W)[6], const float (&dp)[
   W[3] = a3 * i0 + a4 * i3 + a5 * i6;
   W[4] = a3 * i1 + a4 * i4 + a5 * i7;
   W[5] = a3 * i2 + a4 * i5 + a5 * i8;
+}
+
+// Lattice samples.  A warp that is a pure integer translation (ux = uy = vx = vy = 0, u, v
+// and the POI's x, y integers: every FFTCC seed) puts every sample on a texel's own
+// integer position, where dx = dy = 0 and the bicubic polynomial reduces to its constant
+// coefficient [0][0] -- fmaf(c, 0, r) = r, so the full evaluation returns exactly that
+// float.  Those iterations read it from the one-float-per-texel lattice plane (4 B per
+// sample instead of two 32 B coefficient rows) with the same result.
+__device__ __forceinline__ bool on_lattice(const float (&W)[6], float px, float py)
+{
+  return W[0] == 1.f && W[1] == 0.f && W[3] == 0.f && W[4] == 1.f && W[2] == rintf(W[2]) && W[5] == rintf(W[5]) &&
+         px == rintf(px) && py == rintf(py);
 }
 
 // 32 bytes of read-only global memory in one 256-bit load (p 32-byte aligned)
@@ -761,6 +877,7 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
     ++it;
     float A0 = 0.f, A1 = 0.f, A2 = 0.f, B[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     bool bad = false;
+    const bool lat = !kTile && P.lattice && on_lattice(W, px, py);   // warp-uniform
     if constexpr (column_walk)
     {
       if (col_active)
@@ -780,6 +897,8 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
           float t;
           if constexpr (kTile)
             t = sample_bspline_tile(T, coef, plane, w, gxp, gyp);
+          else if (lat)
+            t = __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp));
           else
             t = sample_bspline(coef, plane, w, gxp, gyp);
           const float4 rv = __ldg(ref_col + (size_t)r * w);
@@ -809,7 +928,8 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
           bad = true;
         else
         {
-          const float t = sample_bspline(coef, plane, w, gxp, gyp);
+          const float t = lat ? __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp))
+                              : sample_bspline(coef, plane, w, gxp, gyp);
           const float4 rv = __ldg(ref_pack + (size_t)(cy + ly) * w + (cx + lx));
           const float tau = t - t0;
           const float rc = rv.x - t0;
@@ -951,6 +1071,280 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps
     const int64_t i = (int64_t)__shfl_sync(kFull, t, 0);
     if (!queue_slot_active(P, i)) return;
     icgn_solve<kColumn, false, 1>(P, i, lane);
+  }
+}
+
+// --------------------------------------------------------------------------------------
+// Pair walk: IC-GN for subsets of 33 to 64 columns (subset radius 16 to 31), one or two
+// warps per POI.  The columns form two interleaved classes, c = 2 l + k for lane l and
+// class k; each class is walked like the column walk (the lane's lx is constant, so the
+// lx-weighted sums factor out of the row loop) and butterfly-reduced on its own, and the
+// two class totals are added in class order.  With one warp per POI the warp walks both
+// classes in turn; with two, warp k of the pair walks class k and the pair exchanges its
+// class totals through shared memory (double-buffered by iteration parity, one named
+// barrier per iteration).  The sums are the same bits either way, so results do not depend
+// on the warps per POI; k_poi_prepare forms the per-POI constants in the same class order,
+// which keeps the exact self-match.
+// --------------------------------------------------------------------------------------
+// barrier of the two warps of a pair (ids 1.., 0 is __syncthreads)
+__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+
+// The nine single-pass sums of column class k under warp W, butterfly-reduced (s: A0, A1,
+// A2, B0..B5).  Returns (warp-uniformly) whether a sample of the class failed the range test.
+__device__ __forceinline__ bool pair_class_sums(const IcgnParams& P, int k, int lane, float px, float py, int cx,
+                                                int cy, float t0, const float (&W)[6], float (&s)[9])
+{
+  const int rx = P.rx, ry = P.ry, w = P.w;
+  const int c = pair_column(lane, k);
+  const float flx = (float)(c - rx);
+  const float xmax = (float)(P.w - 2), ymax = (float)(P.h - 2);
+  const size_t plane = (size_t)P.w * P.h;
+  float A0 = 0.f, A1 = 0.f, A2 = 0.f, B[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  bool bad = false;
+  const bool lat = P.lattice && on_lattice(W, px, py);
+  if (c < 2 * rx + 1)
+  {
+    const float4* __restrict__ ref_col = P.ref_pack + (size_t)(cy - ry) * w + cx + (c - rx);
+    const float ax = fmaf(W[0], flx, W[2]), ay = fmaf(W[3], flx, W[5]);
+    for (int r = 0; r < 2 * ry + 1; ++r)
+    {
+      const float fly = (float)(r - ry);
+      const float gxp = px + fmaf(W[1], fly, ax);
+      const float gyp = py + fmaf(W[4], fly, ay);
+      if (!(gxp >= 1.f && gyp >= 1.f && gxp < xmax && gyp < ymax))
+      {
+        bad = true;
+        continue;
+      }
+      const float t = lat ? __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp)) : sample_bspline(P.coef, plane, w, gxp, gyp);
+      const float4 rv = __ldg(ref_col + (size_t)r * w);
+      const float tau = t - t0;
+      const float rc = rv.x - t0;
+      A0 += tau;
+      A1 = fmaf(tau, tau, A1);
+      A2 = fmaf(tau, rc, A2);
+      const float gt = __fmul_rn(rv.y, tau), ht = __fmul_rn(rv.z, tau);
+      B[0] = __fadd_rn(B[0], gt);
+      B[2] = fmaf(gt, fly, B[2]);
+      B[3] = __fadd_rn(B[3], ht);
+      B[5] = fmaf(ht, fly, B[5]);
+    }
+  }
+  B[1] = flx * B[0];
+  B[4] = flx * B[3];
+  const bool any_bad = __any_sync(kFull, bad);
+  s[0] = warp_sum(A0);
+  s[1] = warp_sum(A1);
+  s[2] = warp_sum(A2);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) s[3 + a] = warp_sum(B[a]);
+  return any_bad;
+}
+
+// Whether a sample of column class k lies outside the interpolatable range (warp-uniform).
+__device__ __forceinline__ bool pair_class_oob(const IcgnParams& P, int k, int lane, float px, float py,
+                                               const float (&W)[6])
+{
+  const int c = pair_column(lane, k), ry = P.ry;
+  const float flx = (float)(c - P.rx);
+  const float xmax = (float)(P.w - 2), ymax = (float)(P.h - 2);
+  bool oob = false;
+  if (c < 2 * P.rx + 1)
+  {
+    const float ax = fmaf(W[0], flx, W[2]), ay = fmaf(W[3], flx, W[5]);
+    for (int r = 0; r < 2 * ry + 1; ++r)
+    {
+      const float fly = (float)(r - ry);
+      const float gxp = px + fmaf(W[1], fly, ax), gyp = py + fmaf(W[4], fly, ay);
+      if (gxp < 1.f || gyp < 1.f || gxp >= xmax || gyp >= ymax) oob = true;
+    }
+  }
+  return __any_sync(kFull, oob);
+}
+
+// Shared exchange area of one POI pair: [iteration parity][class][9 sums + bad flag], and
+// the two classes' out-of-range flags.
+struct PairExchange
+{
+  float sums[2][2][10];
+  int oob[2];
+};
+
+// One POI (queue index i) on one warp (kPoiWarps 1) or on the two warps of a pair
+// (kPoiWarps 2: this warp walks class `cls`, barrier `bar` joins the pair).  Same rules,
+// status codes and outputs as icgn_solve; class 0's lane 0 writes the record.
+template <int kPoiWarps>
+__device__ __forceinline__ void icgn_solve_pair(const IcgnParams& P, int64_t i, int lane, int cls,
+                                                PairExchange* xch, int bar)
+{
+  dic_poi* poi = P.pois + i;
+  const float px = poi->x, py = poi->y;
+  const float u_in = poi->u, ux_in = poi->ux, uy_in = poi->uy;
+  const float v_in = poi->v, vx_in = poi->vx, vy_in = poi->vy;
+  const float zncc_in = poi->zncc;
+  const int w = P.w, h = P.h, rx = P.rx, ry = P.ry;
+  // Entry test (src/oc_icgn.cpp:184-191); both warps of a pair take the same branch.
+  if (py - ry < 0 || px - rx < 0 || py + ry > h - 1 || px + rx > w - 1 || fabsf(u_in) >= w ||
+      fabsf(v_in) >= h || zncc_in < 0 || isnan(u_in) || isnan(v_in))
+  {
+    if (cls == 0 && lane == 0) poi->zncc = zncc_in >= 0 ? -3.f : zncc_in;
+    return;
+  }
+  const PoiRef* R = P.poi_ref + (P.slot ? P.slot[i] : i);
+  const float t0 = R->t0;
+  const int size = (2 * rx + 1) * (2 * ry + 1);
+  const float inv_size = 1.f / (float)size;
+  const int cx = (int)px, cy = (int)py;
+  float W[6] = {1.f + ux_in, uy_in, u_in, vx_in, 1.f + vy_in, v_in};
+  const float rx2 = (float)(rx * rx), ry2 = (float)(ry * ry);
+  int it = 0;
+  float conv = 0.f, znssd = 0.f;
+  int status = 0;
+  do
+  {
+    ++it;
+    float s[9];
+    bool bad;
+    if constexpr (kPoiWarps == 1)
+    {
+      float s1[9];
+      bad = pair_class_sums(P, 0, lane, px, py, cx, cy, t0, W, s);
+      bad = pair_class_sums(P, 1, lane, px, py, cx, cy, t0, W, s1) || bad;
+#pragma unroll
+      for (int j = 0; j < 9; ++j) s[j] = __fadd_rn(s[j], s1[j]);
+    }
+    else
+    {
+      float mine[9];
+      const bool b = pair_class_sums(P, cls, lane, px, py, cx, cy, t0, W, mine);
+      float* slot = xch->sums[it & 1][cls];
+      if (lane == 0)
+      {
+#pragma unroll
+        for (int j = 0; j < 9; ++j) slot[j] = mine[j];
+        slot[9] = b ? 1.f : 0.f;
+      }
+      pair_sync(bar);
+      const float* s0 = xch->sums[it & 1][0];
+      const float* s1 = xch->sums[it & 1][1];
+#pragma unroll
+      for (int j = 0; j < 9; ++j) s[j] = __fadd_rn(s0[j], s1[j]);
+      bad = s0[9] != 0.f || s1[9] != 0.f;
+    }
+    if (bad)
+    {
+      // Rare path: the CPU's order (src/oc_icgn.cpp:266-301), out of range before NaN.
+      bool oob;
+      if constexpr (kPoiWarps == 1)
+        oob = pair_class_oob(P, 0, lane, px, py, W) || pair_class_oob(P, 1, lane, px, py, W);
+      else
+      {
+        const bool mo = pair_class_oob(P, cls, lane, px, py, W);
+        if (lane == 0) xch->oob[cls] = mo ? 1 : 0;
+        pair_sync(bar);
+        oob = xch->oob[0] != 0 || xch->oob[1] != 0;
+      }
+      status = oob ? -3 : -5;
+      break;
+    }
+    const float A0 = s[0], A1 = s[1], A2 = s[2];
+    const float ref_norm = R->ref_norm, ref_norm_sq = R->ref_norm_sq, sum_rc = R->sum_rc;
+    const float mean_tau = A0 * inv_size;
+    const float tnorm_sq = fmaf(-A0, mean_tau, A1);
+    const float tar_norm = tnorm_sq > 0.f ? sqrtf(tnorm_sq) : __int_as_float(0x7fc00000);
+    const float sc = ref_norm / tar_norm;
+    const float tc_rc = fmaf(-mean_tau, sum_rc, A2);
+    const float esq = sc * sc * tnorm_sq - 2.f * sc * tc_rc + ref_norm_sq;
+    znssd = esq / (ref_norm * ref_norm);
+    const int row = lane < 6 ? lane : 0;
+    const float S_l = R->S[row], G_l = R->G[row];
+    float num_l = 0.f;
+#pragma unroll
+    for (int a = 0; a < 6; ++a)
+      if (lane == a) num_l = sc * fmaf(-mean_tau, S_l, s[3 + a]) - G_l;
+    float dp_l = 0.f;
+#pragma unroll
+    for (int c = 0; c < 6; ++c)
+    {
+      const float nc = __shfl_sync(kFull, num_l, c);
+      dp_l += R->inv_h[row * 6 + c] * nc;
+    }
+    float dp[6];
+#pragma unroll
+    for (int a = 0; a < 6; ++a) dp[a] = __shfl_sync(kFull, dp_l, a);
+    compose_update(W, dp);
+    conv = sqrtf(dp[0] * dp[0] + dp[1] * dp[1] * rx2 + dp[2] * dp[2] * ry2 + dp[3] * dp[3] +
+                 dp[4] * dp[4] * rx2 + dp[5] * dp[5] * ry2);
+  } while ((float)it < P.max_iter && conv >= P.conv);
+
+  if (cls != 0 || lane != 0) return;
+  if (P.iter_sum) atomicAdd(P.iter_sum, (unsigned long long)it);
+  if (status == -3) { poi->zncc = -3.f; return; }
+  if (status == -5) { poi->zncc = -5.f; return; }
+  float u = W[2], ux = W[0] - 1.f, uy = W[1], v = W[5], vx = W[3], vy = W[4] - 1.f;
+  float zncc = 0.5f * (2.f - znssd);
+  if (conv >= P.conv && (float)it >= P.max_iter) zncc = -4.f;
+  const float u_init = poi->u, v_init = poi->v;
+  if (isnan(zncc) || isnan(u) || isnan(v))
+  {
+    u = u_init;
+    v = v_init;
+    zncc = -5.f;
+  }
+  poi->u = u; poi->ux = ux; poi->uy = uy;
+  poi->v = v; poi->vx = vx; poi->vy = vy;
+  poi->u0 = u_init;
+  poi->v0 = v_init;
+  poi->zncc = zncc;
+  poi->iteration = (float)it;
+  poi->convergence = conv;
+}
+
+// Launch shapes of the pair walk: kWarps warps per CTA, kPoiWarps (1 or 2) per POI, 28
+// resident warps per SM (72 registers: one warp walking both classes keeps the first
+// class's nine totals live through the second).  The grid form takes POIs
+// blockIdx.x * (kWarps / kPoiWarps) + slot; the persistent form
+// draws them from an atomic counter (the pair's class-0 warp fetches, double-buffered by
+// fetch parity, a named barrier per fetch).
+template <int kPoiWarps, int kWarps>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_pair(IcgnParams P)
+{
+  constexpr int kSlots = kWarps / kPoiWarps;
+  __shared__ PairExchange xch[kSlots];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = warp / kPoiWarps, cls = warp % kPoiWarps;
+  const int64_t i = (int64_t)blockIdx.x * kSlots + slot;
+  if (!queue_slot_active(P, i)) return;   // uniform over a pair
+  icgn_solve_pair<kPoiWarps>(P, i, lane, cls, &xch[slot], 1 + slot);
+}
+
+template <int kPoiWarps, int kWarps>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
+    k_icgn_pair_persistent(IcgnParams P, unsigned long long* next)
+{
+  constexpr int kSlots = kWarps / kPoiWarps;
+  __shared__ PairExchange xch[kSlots];
+  __shared__ long long fetched[kSlots][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = warp / kPoiWarps, cls = warp % kPoiWarps;
+  if (P.enable && *P.enable == 0) return;
+  for (unsigned f = 0;; ++f)
+  {
+    int64_t i;
+    if constexpr (kPoiWarps == 1)
+    {
+      unsigned long long t = 0;
+      if (lane == 0) t = atomicAdd(next, 1ull);
+      i = (int64_t)__shfl_sync(kFull, t, 0);
+    }
+    else
+    {
+      if (cls == 0 && lane == 0) fetched[slot][f & 1] = (long long)atomicAdd(next, 1ull);
+      pair_sync(1 + slot);
+      i = (int64_t)fetched[slot][f & 1];
+    }
+    if (!queue_slot_active(P, i)) return;
+    icgn_solve_pair<kPoiWarps>(P, i, lane, cls, &xch[slot], 1 + slot);
   }
 }
 
@@ -1126,6 +1520,7 @@ __global__ void __launch_bounds__(kWarps * 32) k_icgn_tile(IcgnParams P, const _
 struct BatchJob
 {
   const float4* coef;
+  const float* lattice;
   const float4* ref_pack;
   int64_t first;   // first queue index of the job
   int w, h, rx, ry;
@@ -1154,6 +1549,7 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_b
     const BatchJob& J = jobs[j];
     IcgnParams P;
     P.coef = J.coef;
+    P.lattice = J.lattice;
     P.ref_pack = J.ref_pack;
     P.poi_ref = poi_ref;
     P.slot = nullptr;
@@ -1167,6 +1563,68 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_b
     P.max_iter = max_iter;
     P.iter_sum = iter_sum;
     icgn_solve<kColumn, false, 1>(P, k, lane);
+  }
+}
+
+// Job lookup of the batch kernels: the last job whose first queue index is <= k.
+__device__ __forceinline__ int batch_job_of(const BatchJob* __restrict__ jobs, int njobs, int64_t k)
+{
+  int j = 0, hi = njobs - 1;
+  while (j < hi)
+  {
+    const int mid = (j + hi + 1) >> 1;
+    if (jobs[mid].first <= k) j = mid;
+    else hi = mid - 1;
+  }
+  return j;
+}
+
+// The persistent multi-job launch for the jobs whose subsets take the pair walk (33 to 64
+// columns), one or two warps per POI (see k_icgn_pair_persistent).
+template <int kPoiWarps, int kWarps>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
+    k_icgn_batch_pair(const BatchJob* __restrict__ jobs, int njobs, dic_poi* pois, const PoiRef* poi_ref,
+                      int64_t begin, int64_t end, unsigned long long* next, float conv, float max_iter,
+                      unsigned long long* iter_sum)
+{
+  constexpr int kSlots = kWarps / kPoiWarps;
+  __shared__ PairExchange xch[kSlots];
+  __shared__ long long fetched[kSlots][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = warp / kPoiWarps, cls = warp % kPoiWarps;
+  for (unsigned f = 0;; ++f)
+  {
+    int64_t k;
+    if constexpr (kPoiWarps == 1)
+    {
+      unsigned long long t = 0;
+      if (lane == 0) t = atomicAdd(next, 1ull);
+      k = begin + (int64_t)__shfl_sync(kFull, t, 0);
+    }
+    else
+    {
+      if (cls == 0 && lane == 0) fetched[slot][f & 1] = (long long)atomicAdd(next, 1ull);
+      pair_sync(1 + slot);
+      k = begin + (int64_t)fetched[slot][f & 1];
+    }
+    if (k >= end) return;
+    const BatchJob& J = jobs[batch_job_of(jobs, njobs, k)];
+    IcgnParams P;
+    P.coef = J.coef;
+    P.lattice = J.lattice;
+    P.ref_pack = J.ref_pack;
+    P.poi_ref = poi_ref;
+    P.slot = nullptr;
+    P.pois = pois;
+    P.n = end;
+    P.w = J.w;
+    P.h = J.h;
+    P.rx = J.rx;
+    P.ry = J.ry;
+    P.conv = conv;
+    P.max_iter = max_iter;
+    P.iter_sum = iter_sum;
+    icgn_solve_pair<kPoiWarps>(P, k, lane, cls, &xch[slot], 1 + slot);
   }
 }
 

@@ -298,14 +298,19 @@ class Engine:
 
         def shape(s):
             return {f: getattr(s, f) for f, _ in s._fields_}
-        return {"icgn_flat": shape(t.icgn[0]), "icgn_column": shape(t.icgn[1]),
-                "batch_flat": shape(t.batch[0]), "batch_column": shape(t.batch[1])}
+        return {"icgn_flat": shape(t.icgn[0]), "icgn_column": shape(t.icgn[1]), "icgn_pair": shape(t.icgn[2]),
+                "batch_flat": shape(t.batch[0]), "batch_column": shape(t.batch[1]), "batch_pair": shape(t.batch[2])}
 
-    def set_launch_shape(self, column_walk: bool, warps_per_cta: int = 4, ctas_per_sm: int = 0, tile: int = 0) -> None:
-        """Fixes the single-queue IC-GN launch of one subset walk (dic_set_launch_shape):
-        ``tile`` 1 or 2 selects the TMA-staged coefficient tile forms (column walk only)."""
-        s = _lib.DicLaunchShape(warps_per_cta, ctas_per_sm, 0, 0.0, tile)
-        self._call(self._L.dic_set_launch_shape(self._h, int(bool(column_walk)), ctypes.byref(s)))
+    WALK_FLAT, WALK_COLUMN, WALK_PAIR = 0, 1, 2
+
+    def set_launch_shape(self, walk: int, warps_per_cta: int = 4, ctas_per_sm: int = 0, tile: int = 0,
+                         warps_per_poi: int = 1) -> None:
+        """Fixes the single-queue IC-GN launch of one subset walk (dic_set_launch_shape): walk 1
+        column (subsets up to 32 wide), 2 pair (33 to 64), 0 flat (wider); ``tile`` 1 or 2 selects
+        the TMA-staged coefficient tile forms (column walk only), ``warps_per_poi`` 2 the
+        two-warp pair walk.  A bool walk is read as column (True) or flat (False)."""
+        s = _lib.DicLaunchShape(warps_per_cta, ctas_per_sm, 0, 0.0, tile, warps_per_poi)
+        self._call(self._L.dic_set_launch_shape(self._h, int(walk), ctypes.byref(s)))
 
     def set_graphs(self, enabled: bool) -> None:
         self._call(self._L.dic_set_graphs(self._h, int(bool(enabled))))
@@ -331,6 +336,31 @@ class Engine:
         s = DicStats()
         self._call(self._L.dic_get_stats(self._h, ctypes.byref(s)))
         return {f: getattr(s, f) for f, _ in s._fields_}
+
+
+def split_rows(queue: np.ndarray, parts: int) -> np.ndarray:
+    """Row-band partition of a queue (dic_split_rows): parts + 1 boundaries, every inner one at
+    the first change of y at or after k * len / parts, so no row of POIs is split."""
+    q = _check_queue(queue)
+    starts = np.zeros(int(parts) + 1, dtype=np.int64)
+    rc = _lib.load().dic_split_rows(q.ctypes.data, len(q), int(parts), starts.ctypes.data)
+    if rc != _lib.DIC_OK:
+        raise ValueError("split_rows: bad arguments")
+    return starts
+
+
+def process_pair_multi(engines, queue: np.ndarray) -> np.ndarray:
+    """One pair over several engines (one per GPU), each solving a row band of the queue from
+    its own host thread (dic_process_pair_multi); the queue is updated in place, in queue
+    order.  Returns the band boundaries."""
+    q = _check_queue(queue)
+    arr = (ctypes.c_void_p * len(engines))(*[e._h for e in engines])
+    starts = np.zeros(len(engines) + 1, dtype=np.int64)
+    rc = _lib.load().dic_process_pair_multi(arr, len(engines), q.ctypes.data, len(q), starts.ctypes.data)
+    if rc != _lib.DIC_OK:
+        failed = next((e for e in engines if _lib.load().dic_last_error(e._h)), engines[0])
+        _lib.raise_for(rc, failed._h)
+    return starts
 
 
 class ICGN2D1:

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define DIC_ABI_VERSION 1
+#define DIC_ABI_VERSION 2
 
 typedef enum dic_status
 {
@@ -169,6 +169,20 @@ int dic_icgn(dic_engine* engine, dic_poi* pois, int64_t count);
  * (opencorr_cli_cuda_mvp.cpp:3187-3196, the non-skip branch of processFrame). */
 int dic_process_pair(dic_engine* engine, dic_poi* pois, int64_t count);
 
+/* Several GPUs on one pair: the dual-device mode of ICGN2D1CudaMvp (src/icgn2d1_cuda_mvp.cu:
+ * 2922-2933 halves the queue between two devices), for any number of engines.  The queue is
+ * cut into contiguous bands at row boundaries (dic_split_rows) and each engine solves its band
+ * with dic_process_pair from its own host thread; no data moves between devices and the
+ * results land in place, in queue order, identical to a single engine's.  Every engine must
+ * hold the same reference and target (dic_set_ref / dic_set_tar) and configuration.
+ * band_starts (nullable) receives the count + 1 band boundaries.  Returns the first failing
+ * engine's status (its dic_last_error holds the message). */
+int dic_process_pair_multi(dic_engine* const* engines, int32_t count, dic_poi* pois, int64_t n, int64_t* band_starts);
+/* The row-band partition used above: starts[0] = 0 <= starts[1] <= ... <= starts[parts] = n,
+ * each inner cut at the first row start (a change of y) at or after k * n / parts.  Host
+ * only; no device is touched. */
+int dic_split_rows(const dic_poi* pois, int64_t n, int32_t parts, int64_t* starts);
+
 /* processFrame (opencorr_cli_cuda_mvp.cpp:3024-3210): with policy->skip_fftcc and
  * prev_results (count entries) the queue is seeded from the previous frame and solved by
  * IC-GN alone, then repaired per POI or per frame as the policy says; otherwise FFTCC +
@@ -260,14 +274,17 @@ typedef struct dic_batch_report
 int dic_batch_process(dic_engine* engine, const dic_job* jobs, int32_t njobs, int32_t pixels_on_device,
                       dic_batch_report* report);
 
-/* Launch-shape autotuner (no reference counterpart).  IC-GN runs one warp per POI; when
- * enabled, the first IC-GN launch of each kind (per-queue / persistent batch, column walk
- * for subsets up to 32 columns / flat walk) with at least 2048 POIs times the candidate
- * shapes -- 2, 4 or 8 POIs (warps) per CTA; for a single queue a grid of one CTA per
- * POI group or a persistent work-queue launch at full occupancy; for a batch full or 3/4
- * occupancy in CTAs per SM -- on a copy of its seeded queue and keeps the fastest for the
- * engine's lifetime.  Results do not depend on the shape.  Enabling (again) clears what
- * was learnt.  Tuning never runs inside a graph capture. */
+/* Launch-shape autotuner (no reference counterpart).  IC-GN walks a subset in one of three
+ * ways: the column walk (up to 32 columns, one warp per POI, lane = column), the pair walk
+ * (33 to 64 columns: two interleaved column classes, one or two warps per POI) and the
+ * flat walk (wider, one warp per POI).  When enabled, the first IC-GN launch of each kind
+ * (per-queue / persistent batch, per walk) with at least 2048 POIs times the candidate
+ * shapes -- 2, 4 or 8 warps per CTA; for the pair walk 1 or 2 warps per POI; for a single
+ * queue a grid of one CTA per POI group or a persistent work-queue launch at full
+ * occupancy; for a batch full or 3/4 occupancy in CTAs per SM -- on a copy of its seeded
+ * queue and keeps the fastest for the engine's lifetime.  Results do not depend on the
+ * shape.  Enabling (again) clears what was learnt.  Tuning never runs inside a graph
+ * capture. */
 typedef struct dic_launch_shape
 {
   int32_t warps_per_cta;
@@ -279,22 +296,27 @@ typedef struct dic_launch_shape
                             1 (4 warps, 48x36 texels, 2 CTAs/SM) or 2 (8 warps, 64x40, 1 CTA/SM)
                             stage the block a chunk of consecutive POIs warps onto in shared memory
                             by TMA; warps_per_cta and ctas_per_sm then follow the tile kind */
+  int32_t warps_per_poi; /* pair walk: 1 (one warp walks both column classes) or 2 (one warp per
+                            class, class sums exchanged through shared memory); 1 elsewhere
+                            (0 is read as 1) */
 } dic_launch_shape;
 
 typedef struct dic_tuning
 {
-  dic_launch_shape icgn[2];    /* [0] flat walk, [1] column walk */
-  dic_launch_shape batch[2];
+  dic_launch_shape icgn[3];    /* [0] flat walk, [1] column walk, [2] pair walk */
+  dic_launch_shape batch[3];
 } dic_tuning;
 
 int dic_set_autotune(dic_engine* engine, int32_t enabled);
 int dic_get_tuning(dic_engine* engine, dic_tuning* out);
 /* No reference counterpart: fixes the single-queue IC-GN launch shape of one subset walk
- * (column_walk 1: subsets at most 32 wide, 0: wider), e.g. to compare the gather and the
- * TMA-staged tile forms.  warps_per_cta in {2, 4, 8}, ctas_per_sm >= 0, tile in {0, 1, 2}
- * (tile > 0 only with column_walk 1); tuned and ms are ignored.  Results do not depend on
- * the shape.  An enabled autotuner may replace it on the next large queue. */
-int dic_set_launch_shape(dic_engine* engine, int32_t column_walk, const dic_launch_shape* shape);
+ * (walk 1: column walk, subsets at most 32 wide; 2: pair walk, 33 to 64; 0: flat walk,
+ * wider), e.g. to compare the gather and the TMA-staged tile forms, or one and two warps per
+ * POI.  warps_per_cta in {2, 4, 8}, ctas_per_sm >= 0, tile in {0, 1, 2} (tile > 0 only with
+ * walk 1), warps_per_poi in {0, 1, 2} (2 only with walk 2); tuned and ms are ignored.
+ * Results do not depend on the shape.  An enabled autotuner may replace it on the next large
+ * queue. */
+int dic_set_launch_shape(dic_engine* engine, int32_t walk, const dic_launch_shape* shape);
 
 /* Device-resident variant: pois points to device memory (count records) and the call only
  * enqueues work on the engine stream (dic_get_stats or a stream sync waits for it).  flags
@@ -357,6 +379,21 @@ int dic_process_pair_learned(dic_engine* engine, dic_poi* pois, int64_t count, d
 int dic_get_stats(const dic_engine* engine, dic_stats* out);
 /* Turns per-phase CUDA-event timing on (1) or off (0).  On by default. */
 int dic_set_timing(dic_engine* engine, int32_t enabled);
+
+/* No reference counterpart: measurement support.  Enqueues on `stream` (a cudaStream_t) one
+ * kernel on `device` that reads `bytes` (rounded down to 32) of device memory `repeats` times
+ * with the 256-bit non-coherent loads the IC-GN gathers use, four in flight per thread, 8
+ * CTAs of 256 threads per SM; device_sink (one float) is written only in a case that never
+ * occurs for finite data.  Timed by the caller with events on `stream`: for a buffer that fits
+ * in L2 (tens of MB, after one warm-up launch) bytes x repeats / time is the L2-to-SM read
+ * bandwidth that bounds the gathers.  device_buf must be 32-byte aligned. */
+int dic_read_probe(int32_t device, const void* device_buf, int64_t bytes, int32_t repeats, float* device_sink,
+                   void* stream);
+/* No reference counterpart: measurement support.  Enqueues on `stream` one kernel on `device`
+ * that runs eight independent FP32 FMA chains per thread for `iterations` rounds (8 CTAs of
+ * 256 threads per SM); *flop_out receives the FLOP count of the launch (2 per FMA).  Timed by
+ * the caller with events on `stream`, it gives the FP32 peak the FFTCC kernels are held to. */
+int dic_fma_probe(int32_t device, int32_t iterations, float* device_sink, void* stream, int64_t* flop_out);
 
 /* Allocation-free pair solve (FFTCC seed + IC-GN).  No counterpart in the reference: its
  * solvers allocate their device buffers themselves.

@@ -8,8 +8,12 @@ The reference's own CPU implementation cannot be compiled here: its sources incl
 OpenCV and FFTW headers and none of the three is installed.  What does compile from the
 reference tree is the xxHash header it vendors (third_party/xxhash/xxhash.h, header-only):
 build_xxh3_ref() compiles oracle/xxh3_check.c against it where it lies into
-oracle/_ref/xxh3_ref, the checker for the output ledger's XXH3-128 (only where the
-reference tree is present; the golden digests it produced are committed under tests/golden).
+oracle/_ref/xxh3_ref, the checker for the output ledger's XXH3-128 (only where a reference
+checkout is named; the golden digests it produced are committed under tests/golden).
+
+The checkout is named by the --reference argument or the DIC_REFERENCE environment variable:
+
+    DIC_REFERENCE=/path/to/FastICGN python oracle/build.py
 """
 from __future__ import annotations
 
@@ -36,15 +40,23 @@ def build_oracle(force: bool = False, verbose: bool = False) -> Path:
     return LIB
 
 
-REF_ROOT = Path("/root/reference")
 REF_DIR = HERE / "_ref"
 
 
-def build_xxh3_ref(force: bool = False, verbose: bool = False) -> Path | None:
-    """oracle/_ref/xxh3_ref from the reference's vendored xxhash.h; None without the tree."""
-    header_dir = REF_ROOT / "third_party" / "xxhash"
-    src = HERE / "xxh3_check.c"
+def reference_root(reference: str | os.PathLike | None = None) -> Path | None:
+    """The reference checkout: the argument, else $DIC_REFERENCE, else None."""
+    root = reference or os.environ.get("DIC_REFERENCE")
+    return Path(root) if root else None
+
+
+def build_xxh3_ref(force: bool = False, verbose: bool = False, reference=None) -> Path | None:
+    """oracle/_ref/xxh3_ref from the reference's vendored xxhash.h; None without a checkout."""
     exe = REF_DIR / "xxh3_ref"
+    root = reference_root(reference)
+    if root is None:
+        return exe if exe.exists() else None
+    header_dir = root / "third_party" / "xxhash"
+    src = HERE / "xxh3_check.c"
     if not (header_dir / "xxhash.h").exists():
         return exe if exe.exists() else None
     if not force and exe.exists() and exe.stat().st_mtime >= src.stat().st_mtime:
@@ -60,5 +72,10 @@ def build_xxh3_ref(force: bool = False, verbose: bool = False) -> Path | None:
 
 
 if __name__ == "__main__":
-    print(build_oracle(force="--force" in sys.argv, verbose=True))
-    print(build_xxh3_ref(force="--force" in sys.argv, verbose=True))
+    import argparse
+    ap = argparse.ArgumentParser(description="build the oracle (and the xxHash checker from a reference checkout)")
+    ap.add_argument("--force", action="store_true")
+    ap.add_argument("--reference", default=None, help="reference checkout (default: $DIC_REFERENCE)")
+    a = ap.parse_args()
+    print(build_oracle(force=a.force, verbose=True))
+    print(build_xxh3_ref(force=a.force, verbose=True, reference=a.reference))

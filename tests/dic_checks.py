@@ -125,3 +125,37 @@ def block_relation(x, y, radius, block_x, block_y, side):
         overlap = (x + radius >= x0) & (x - radius <= x1) & (y + radius >= block_y) & (y - radius <= y1)
         rel = np.where(inside, 2, np.where(overlap & (rel < 2), np.maximum(rel, 1), rel))
     return rel
+
+
+def failure_codes(z):
+    """The failure flag of each POI: its negative zncc (-3, -4, -5, or a negative incoming
+    value kept by the entry test), 0 for a solved POI."""
+    z = np.asarray(z)
+    return np.where(np.isfinite(z) & (z < 0), z, 0)
+
+
+def flags_agree(cpu, gpu):
+    """Converged/failed flags of two runs over the same queue (dicts or structured arrays with
+    u0, v0, zncc).  Returns (fraction of POIs whose FFTCC seeds agree, number of POIs with the
+    same seed and different flags).  Integer FFTCC peaks may differ only on exact ties of the
+    correlation map; from the same seed the flags must be identical."""
+    same = (np.asarray(cpu["u0"]) == np.asarray(gpu["u0"])) & (np.asarray(cpu["v0"]) == np.asarray(gpu["v0"]))
+    diff = failure_codes(cpu["zncc"]) != failure_codes(gpu["zncc"])
+    return float(same.mean()) if len(same) else 1.0, int((diff & same).sum())
+
+
+def flag_differences(cpu, gpu, limit=8):
+    """(cpu code, gpu code, cpu iterations, gpu iterations) of up to `limit` POIs whose
+    failure flags differ, for messages."""
+    fc, fg = failure_codes(cpu["zncc"]), failure_codes(gpu["zncc"])
+    idx = np.flatnonzero(fc != fg)[:limit]
+    it_c = cpu.get("iteration", np.full(len(fc), np.nan))
+    it_g = gpu.get("iteration", np.full(len(fg), np.nan))
+    return [(float(fc[i]), float(fg[i]), float(it_c[i]), float(it_g[i])) for i in idx]
+
+
+def assert_flags_agree(cpu, gpu, min_same_seed=0.999):
+    same, bad = flags_agree(cpu, gpu)
+    assert same >= min_same_seed, f"FFTCC seeds agree on {same:.5f} of the POIs"
+    assert bad == 0, (f"{bad} POIs with the same seed have different failure flags "
+                      f"(cpu code, gpu code, cpu iterations, gpu iterations): {flag_differences(cpu, gpu)}")

@@ -66,7 +66,7 @@ def test_struct_layouts_match_header(tmp_path):
 def test_version_and_abi(libpath):
     from fasticgn_gb300 import _lib
     L = _lib.load()
-    assert L.dic_abi_version() == 1
+    assert L.dic_abi_version() == 2
     assert b"sm_103a" in L.dic_version()
 
 

@@ -13,11 +13,13 @@ pytestmark = pytest.mark.gpu
 
 def _jobs():
     """Jobs of the uneven batch's kind at test sizes: per-pair affine fields with 20 % flat
-    patches (u8), plus a 12-bit u16 pair and a float32 pair with smooth bump fields."""
+    patches (u8) -- radii 10 and 15 (column walk), 20 and 30 (pair walk), 32 (flat walk) --
+    plus a 12-bit u16 pair and a float32 pair with smooth bump fields."""
     from fasticgn_gb300 import speckle
     rng = np.random.default_rng(71)
     out = []
-    for w, h, r, n in [(384, 320, 10, 4000), (640, 512, 15, 16000), (300, 420, 20, 1500), (320, 320, 30, 600)]:
+    for w, h, r, n in [(384, 320, 10, 4000), (640, 512, 15, 16000), (300, 420, 20, 1500), (320, 320, 30, 600),
+                       (300, 280, 32, 300)]:
         p = speckle.pair_uneven(rng, w, h, r, n)
         out.append((p.ref, p.tar, r, p.step))
     pr = speckle.pair_bumps(seed=73, width=300, height=260, max_disp=6.0, max_strain=0.01)
@@ -140,5 +142,5 @@ def test_autotuner_keeps_results(dic):
             e.process_pair(qq)
             out.append(qq)
         np.testing.assert_array_equal(out[0].view(np.uint8), out[1].view(np.uint8))
-        key = "icgn_column" if r == 15 else "icgn_flat"
+        key = "icgn_column" if r == 15 else "icgn_pair"
         assert e2.tuning()[key]["tuned"] == 1, e2.tuning()

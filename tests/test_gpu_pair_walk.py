@@ -1,0 +1,102 @@
+"""The pair walk (subsets of 33 to 64 columns, subset radius 16 to 31): two interleaved
+column classes, each reduced on its own and added in class order, walked by one or two
+warps per POI.
+
+* every launch shape (one or two warps per POI, 2 / 4 / 8 warps per CTA, grid or
+  persistent) gives the same bytes;
+* same-seed IC-GN against the CPU oracle within the reference parity gate, with identical
+  failure flags and iteration counts;
+* the exact self-match of the per-POI prep and the IC-GN sums: a target equal to the
+  reference gives zncc == 1 exactly on every textured subset.
+"""
+import numpy as np
+import pytest
+
+import dic_checks as C
+
+pytestmark = pytest.mark.gpu
+
+SHAPES = [dict(warps_per_cta=4, ctas_per_sm=0, warps_per_poi=1), dict(warps_per_cta=4, ctas_per_sm=0, warps_per_poi=2),
+          dict(warps_per_cta=2, ctas_per_sm=16, warps_per_poi=1), dict(warps_per_cta=8, ctas_per_sm=4, warps_per_poi=2),
+          dict(warps_per_cta=2, ctas_per_sm=16, warps_per_poi=2), dict(warps_per_cta=8, ctas_per_sm=0, warps_per_poi=1)]
+
+
+@pytest.mark.parametrize("radius", [16, 20, 25, 31])
+def test_pair_walk_shapes_give_the_same_bytes(dic, radius):
+    from fasticgn_gb300 import speckle
+    pr = speckle.pair_bumps(seed=40 + radius, width=416, height=384, max_disp=5.0, max_strain=0.01)
+    outs = []
+    for sh in SHAPES:
+        with dic.Engine(radius) as e:
+            e.set_launch_shape(2, **sh)
+            e.set_ref(pr.ref)
+            e.set_tar(pr.tar)
+            q = dic.grid_queue(416, 384, radius, 5)
+            e.process_pair(q)
+            assert e.tuning()["icgn_pair"]["warps_per_poi"] == sh["warps_per_poi"]
+        outs.append(q)
+    ok = outs[0]["zncc"] >= 0
+    assert ok.mean() > 0.9
+    for sh, q in zip(SHAPES[1:], outs[1:]):
+        assert q.tobytes() == outs[0].tobytes(), sh
+
+
+def _to_oracle(O, q):
+    pois = np.zeros(len(q), dtype=O.POI2D_DTYPE)
+    pois["x"], pois["y"] = q["x"], q["y"]
+    for name, idx in (("u", O.P_U), ("ux", O.P_UX), ("uy", O.P_UY), ("v", O.P_V), ("vx", O.P_VX), ("vy", O.P_VY)):
+        pois["p"][:, idx] = q[name]
+    for name, idx in (("u0", O.R_U0), ("v0", O.R_V0), ("zncc", O.R_ZNCC), ("iteration", O.R_ITER)):
+        pois["r"][:, idx] = q[name]
+    return pois
+
+
+@pytest.mark.parametrize("radius", [20, 31])
+def test_pair_walk_matches_oracle_same_seed(dic, oracle_mod, radius):
+    O = oracle_mod
+    from fasticgn_gb300 import speckle
+    pr = speckle.pair_affine(seed=radius, width=448, height=416)
+    ref, tar = pr.ref.astype(np.float32), pr.tar.astype(np.float32)
+    q = dic.grid_queue(448, 416, radius, 6)
+    oq = _to_oracle(O, q)
+    O.fftcc2d(ref, tar, oq, radius)
+    g = q.copy()
+    for f, idx in (("u", O.P_U), ("ux", O.P_UX), ("uy", O.P_UY), ("v", O.P_V), ("vx", O.P_VX), ("vy", O.P_VY)):
+        g[f] = oq["p"][:, idx]
+    g["zncc"] = oq["r"][:, O.R_ZNCC]
+    icgn = dic.ICGN2D1(radius, radius, 0.001, 10)
+    icgn.setImages(pr.ref, pr.tar)
+    icgn.compute(g)
+    gx, gy = O.gradient(ref)
+    O.icgn2d1(ref, gx, gy, O.bspline_prepare(tar), oq, radius)
+    cpu = {"u": oq["p"][:, O.P_U], "v": oq["p"][:, O.P_V], "zncc": oq["r"][:, O.R_ZNCC]}
+    res = C.compare_frame(cpu, {"u": g["u"], "v": g["v"], "zncc": g["zncc"]})
+    assert res["pass"], res
+    assert np.array_equal(C.failure_codes(cpu["zncc"]), C.failure_codes(g["zncc"]))
+    assert np.mean(oq["r"][:, O.R_ITER] == g["iteration"]) >= 0.98
+    both = (cpu["zncc"] >= 0) & (g["zncc"] >= 0)
+    np.testing.assert_allclose(g["zncc"][both], cpu["zncc"][both], atol=1e-4)
+
+
+@pytest.mark.parametrize("radius", [16, 22])
+def test_pair_walk_exact_self_match(dic, golden, radius):
+    """Target = reference: s = 1, ZNSSD = 0 and dp = 0 bit for bit, so every subset clear of
+    the constant blocks ends at zncc == 1 with u = v = 0 after one iteration; subsets inside a
+    block end -5 as on the CPU."""
+    g = golden("zero_texture")
+    ref = g["ref"]
+    h, w = ref.shape
+    q = dic.grid_queue(w, h, radius, 2)
+    with dic.Engine(radius) as e:
+        for pw in (1, 2):
+            e.set_launch_shape(2, warps_per_cta=4, ctas_per_sm=0, warps_per_poi=pw)
+            e.set_ref(ref)
+            e.set_tar(ref)
+            qq = q.copy()
+            e.process_pair(qq)
+            rel = C.block_relation(qq["x"], qq["y"], radius, g["block_x"], int(g["block_y"]), int(g["block_side"]))
+            outside = rel == 0
+            assert outside.sum() > 50
+            assert np.all(qq["zncc"][outside] == 1.0)
+            assert np.all(qq["u"][outside] == 0.0) and np.all(qq["v"][outside] == 0.0)
+            assert np.all(qq["iteration"][outside] == 1.0)

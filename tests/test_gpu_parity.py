@@ -215,6 +215,7 @@ def test_pair_parity_config1(dic, oracle_mod, affine_pair):
     O.run_pair(affine_pair.ref.astype(np.float32), affine_pair.tar.astype(np.float32), oq, 15)
     res = C.compare_frame(fields(from_oracle(O, oq, q)), fields(q))
     assert res["pass"], res
+    C.assert_flags_agree(fields(from_oracle(O, oq, q)), fields(q))
     ut, vt = affine_pair.field(q["x"].astype(np.float64), q["y"].astype(np.float64))
     ok = q["zncc"] >= 0
     assert np.sqrt(np.mean((q["u"][ok] - ut[ok]) ** 2)) < 0.02
@@ -241,6 +242,7 @@ def test_golden_accuracy_and_parity(dic, oracle_mod, golden, case):
         O.run_pair(ref.astype(np.float32), tar.astype(np.float32), oq, radius)
         res = C.compare_frame(fields(from_oracle(O, oq, q)), fields(q), min_shared_valid=50)
         assert res["pass"], (case, k, res)
+        C.assert_flags_agree(fields(from_oracle(O, oq, q)), fields(q))
 
 
 def test_whole_pixel_shifts_exact(dic, golden):
@@ -370,6 +372,7 @@ def test_u16_12bit_and_scale(dic, oracle_mod):
     O.run_pair(ref.astype(np.float32), tar.astype(np.float32), oq, 12)
     res = C.compare_frame(fields(from_oracle(O, oq, q)), fields(q))
     assert res["pass"], res
+    C.assert_flags_agree(fields(from_oracle(O, oq, q)), fields(q))
     q2 = dic.grid_queue(256, 256, 12, 8)
     e2 = dic.Engine(12, input_scale=1.0 / 16.0)
     e2.set_ref((ref.astype(np.uint32) << 4).astype(np.uint16))
@@ -402,3 +405,44 @@ def test_oversize_image_rejected(dic):
     assert b"2^31" in L.dic_last_error(e._h)
     e.set_ref(np.zeros((64, 64), np.uint8))   # the engine is still usable
     e.close()
+
+
+@pytest.mark.parametrize("case", ["u8_dark", "u16_bright"])
+def test_illumination_change_pair(dic, oracle_mod, case):
+    """Target = a * I + b (a brightness and contrast change, which ZNCC / ZNSSD is invariant
+    to): 0.6 I - 20 DN on 8-bit data and 1.4 I + 600 DN on 12-bit data.  The IC-GN kernels form
+    the zero-mean sums from offsets to the reference mean in one pass; against the oracle's
+    two-pass Eigen arithmetic the results stay within the parity gate with identical flags,
+    and the displacements still match the truth."""
+    O = oracle_mod
+    from fasticgn_gb300 import speckle
+    if case == "u8_dark":
+        pr = speckle.pair_affine(seed=7, width=512, height=512)
+        ref = pr.ref
+        tar = np.clip(np.rint(0.6 * pr.tar.astype(np.float64) - 20.0), 0, 255).astype(np.uint8)
+        assert pr.tar.min() >= 34      # no clipping: the change is exactly affine before rounding
+        field, radius, step = pr.field, 15, 7
+    else:
+        ref, frames = speckle.stream_frames(width=512, height=512, frames=200, which=[150])
+        _, t12, field = frames[0]
+        tar = np.rint(1.4 * t12.astype(np.float64) + 600.0).astype(np.uint16)
+        radius, step = 15, 7
+    h, w = ref.shape
+    q = dic.grid_queue(w, h, radius, step)
+    oq = to_oracle(O, q)
+    e = dic.Engine(radius)
+    e.set_ref(ref)
+    e.set_tar(tar)
+    e.process_pair(q)
+    e.close()
+    O.run_pair(ref.astype(np.float32), tar.astype(np.float32), oq, radius)
+    cpu = fields(from_oracle(O, oq, q))
+    res = C.compare_frame(cpu, fields(q))
+    assert res["pass"], (case, res)
+    C.assert_flags_agree(cpu, fields(q))
+    ok = q["zncc"] >= 0
+    assert ok.mean() > 0.95
+    np.testing.assert_allclose(q["zncc"][ok & (cpu["zncc"] >= 0)], cpu["zncc"][ok & (cpu["zncc"] >= 0)], atol=1e-4)
+    ut, vt = field(q["x"].astype(np.float64), q["y"].astype(np.float64))
+    assert np.sqrt(np.mean((q["u"][ok] - ut[ok]) ** 2)) < 0.03
+    assert np.sqrt(np.mean((q["v"][ok] - vt[ok]) ** 2)) < 0.03

@@ -2,7 +2,9 @@
 flags are bit-identical to the gather form's, whether its chunk's block fits the tile (texels
 from shared memory), partly fits (texels outside it from the global table) or does not fit at
 all (the whole chunk from the global table), also inside a graph-captured sequence frame and
-under the autotuner."""
+under the autotuner.  The tile form always evaluates the full bicubic polynomial, while the
+gather form takes the first (integer-translation) iteration of every FFTCC-seeded POI from
+the lattice plane, so these comparisons also show that the lattice samples are exact."""
 import numpy as np
 import pytest
 
@@ -73,12 +75,15 @@ def test_autotuner_times_tile_forms(dic):
 
 def test_launch_shape_arguments(dic):
     e = dic.Engine(15)
-    for kw in (dict(column_walk=True, tile=3), dict(column_walk=False, tile=1),
-               dict(column_walk=True, warps_per_cta=3), dict(column_walk=True, ctas_per_sm=-1)):
+    for kw in (dict(walk=1, tile=3), dict(walk=0, tile=1), dict(walk=2, tile=1),
+               dict(walk=1, warps_per_cta=3), dict(walk=1, ctas_per_sm=-1), dict(walk=3),
+               dict(walk=1, warps_per_poi=2), dict(walk=2, warps_per_poi=3)):
         with pytest.raises((ValueError, RuntimeError)):
             e.set_launch_shape(**kw)
     e.set_launch_shape(True, warps_per_cta=2, ctas_per_sm=0)
     assert e.tuning()["icgn_column"]["warps_per_cta"] == 2 and e.tuning()["icgn_column"]["tile"] == 0
+    e.set_launch_shape(2, warps_per_cta=8, ctas_per_sm=4, warps_per_poi=2)
+    assert e.tuning()["icgn_pair"]["warps_per_poi"] == 2 and e.tuning()["icgn_pair"]["warps_per_cta"] == 8
     e.close()
 
 
@@ -103,3 +108,36 @@ def test_tile_copy_timeout_is_reported(dic, monkeypatch):
     e.close()
     got, _, _ = solve(dic, pr, 15, 4, tile=1)
     np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8))
+
+
+def test_lattice_samples_equal_the_polynomial(dic, oracle_mod):
+    """IC-GN from integer-translation seeds (the FFTCC seeds) reads its first iteration's samples
+    from the lattice plane; the oracle evaluates the full polynomial at those points.  One
+    iteration from a whole-pixel shift gives the CPU's flags, displacement and ZNCC to within
+    the rounding of the single-pass sums."""
+    O = oracle_mod
+    from fasticgn_gb300 import speckle
+    pr = speckle.pair_affine(seed=12, width=256, height=224)
+    ref = pr.ref
+    tar = np.zeros_like(ref)
+    tar[:, 3:] = ref[:, :-3]            # a whole-pixel shift of 3 px in x
+    q = dic.grid_queue(256, 224, 12, 5)
+    q["u"] = 3.0
+    oq = O.make_pois(q["x"], q["y"])
+    oq["p"][:, O.P_U] = 3.0
+    icgn = dic.ICGN2D1(12, 12, 0.001, 1)           # one iteration: the lattice iteration alone
+    icgn.setImages(ref, tar)
+    icgn.compute(q)
+    r32, t32 = ref.astype(np.float32), tar.astype(np.float32)
+    gx, gy = O.gradient(r32)
+    O.icgn2d1(r32, gx, gy, O.bspline_prepare(t32), oq, 12, 0.001, 1)
+    inside = (q["x"] - 12 - 2 > 3) & (q["zncc"] >= 0)
+    assert inside.sum() > 100
+    cz = oq["r"][:, O.R_ZNCC]
+    assert np.array_equal(C_failure(q["zncc"]), C_failure(cz))
+    np.testing.assert_allclose(q["u"][inside], oq["p"][inside, O.P_U], atol=2e-5)
+    np.testing.assert_allclose(q["zncc"][inside], cz[inside], atol=2e-6)
+
+
+def C_failure(z):
+    return np.where(np.isfinite(z) & (z < 0), z, 0)

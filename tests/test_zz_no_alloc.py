@@ -5,8 +5,11 @@ lends its plug-ins buffers, or a camera loop that an allocation's device synchro
 would stall).  The test calls it through the C ABI with caller-owned device buffers, twice
 in a row on the same scratch array, and checks each result against the engine entry point
 on the same pair within the reference parity gate's tolerance (median |du|,|dv| <= 1e-3 px,
-p99 <= 1e-2 px, max <= 0.5 px, identical failure flags).  The file sorts last so that a
-run stopping at the first failure has run every other test before it.
+p99 <= 1e-2 px, max <= 0.5 px, identical failure flags wherever both started from the same
+FFTCC peak).  The radii cover every kernel the entry point can reach: the line-DFT FFTCC
+for 2r < 8 and 2r > 32, the register FFTCC for 2r = 8..32, the column-walk IC-GN for
+subsets up to 31 wide and the flat walk beyond.  The file sorts last so that a run stopping
+at the first failure has run every other test before it.
 """
 import ctypes
 
@@ -22,15 +25,16 @@ def _fields(q):
     return {k: q[k] for k in q.dtype.names}
 
 
-def test_noalloc_matches_engine_twice(dic):
+@pytest.mark.parametrize("radius", [3, 4, 7, 11, 15, 16, 17, 21, 32])
+def test_noalloc_matches_engine_twice(dic, radius):
     torch = pytest.importorskip("torch")
     from fasticgn_gb300 import _lib, speckle
 
     L = _lib.load()
     pr = speckle.pair_affine(seed=9, width=320, height=288)
     h, w = pr.ref.shape
-    radius = 15
-    want = dic.grid_queue(w, h, radius, 6)
+    step = 6 if radius <= 16 else 9
+    want = dic.grid_queue(w, h, radius, step)
     with dic.Engine(radius) as e:
         e.set_ref(pr.ref)
         e.set_tar(pr.tar)
@@ -42,7 +46,7 @@ def test_noalloc_matches_engine_twice(dic):
     stream = torch.cuda.current_stream()
     err = ctypes.create_string_buffer(256)
     for call in range(2):
-        q = dic.grid_queue(w, h, radius, 6)
+        q = dic.grid_queue(w, h, radius, step)
         q_d = torch.from_numpy(q.view(np.uint8).copy()).cuda()
         torch.cuda.synchronize()
         rc = L.dic_process_pair_noalloc(ctypes.byref(cfg), ref_d.data_ptr(), tar_d.data_ptr(), w, h, _lib.DIC_U8,
@@ -50,9 +54,17 @@ def test_noalloc_matches_engine_twice(dic):
         assert rc == _lib.DIC_OK, err.value
         stream.synchronize()
         got = q_d.cpu().numpy().view(dic.POI_DTYPE)
-        res = C.compare_frame(_fields(want), _fields(got))
-        assert res["pass"], (call, res)
-        assert np.array_equal(np.where(want["zncc"] < 0, want["zncc"], 0), np.where(got["zncc"] < 0, got["zncc"], 0))
+        # small subsets (r = 3, 7x7) leave few valid POIs on this speckle: gate on what there is
+        valid = int((want["zncc"] >= 0).sum())
+        res = C.compare_frame(_fields(want), _fields(got), min_shared_valid=min(100, valid // 2))
+        assert res["pass"], (radius, call, res)
+        # the two entry points run different FFTCC kernels; their integer peaks may differ only
+        # on exact ties of the correlation map, and from the same peak the flags are identical
+        same_seed = (want["u0"] == got["u0"]) & (want["v0"] == got["v0"])
+        assert same_seed.mean() >= 0.995, (radius, call, same_seed.mean())
+        flags_w = np.where(want["zncc"] < 0, want["zncc"], 0)[same_seed]
+        flags_g = np.where(got["zncc"] < 0, got["zncc"], 0)[same_seed]
+        assert np.array_equal(flags_w, flags_g), (radius, call)
 
 
 def test_noalloc_rejects_oversize(dic):
@@ -69,3 +81,14 @@ def test_noalloc_rejects_oversize(dic):
                                     q.data_ptr(), 10, None, err, len(err))
     assert rc == _lib.DIC_ERR_ARGUMENT
     assert b"scratch" in err.value
+    # sizes whose byte counts would wrap a 64-bit sum are rejected before any arithmetic on them
+    err2 = ctypes.create_string_buffer(256)
+    rc = L.dic_process_pair_noalloc(ctypes.byref(cfg), img.data_ptr(), img.data_ptr(), 2 ** 31 - 1, 2 ** 31 - 1,
+                                    _lib.DIC_F32, q.data_ptr(), 10, None, err2, len(err2))
+    assert rc == _lib.DIC_ERR_ARGUMENT
+    assert b"scratch" in err2.value
+    err3 = ctypes.create_string_buffer(256)
+    rc = L.dic_process_pair_noalloc(ctypes.byref(cfg), img.data_ptr(), img.data_ptr(), 64, 64, _lib.DIC_U8,
+                                    q.data_ptr(), 2 ** 62, None, err3, len(err3))
+    assert rc == _lib.DIC_ERR_ARGUMENT
+    assert b"scratch" in err3.value
