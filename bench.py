@@ -352,6 +352,22 @@ def measure_read_peak(torch, dev):
             ms = s.elapsed_time(e)
             best = ms if best is None else min(best, ms)
     out["fp32"] = {"tflops": flop.value / (best * 1e-3) / 1e12, "ms": best}
+    # shared-memory load bandwidth (the pixel-sampled IC-GN's sample path), same timing
+    nbytes = ctypes.c_int64(0)
+    best = None
+    for k in range(7):
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            s.record(stream)
+            rc = L.dic_smem_probe(dev.index, 1 << 12, sink.data_ptr(), stream.cuda_stream, ctypes.byref(nbytes))
+            e.record(stream)
+        if rc != _lib.DIC_OK:
+            raise RuntimeError(f"dic_smem_probe failed ({rc})")
+        e.synchronize()
+        if k >= 2:
+            ms = s.elapsed_time(e)
+            best = ms if best is None else min(best, ms)
+    out["smem"] = {"gbs": nbytes.value / (best * 1e-3) / 1e9, "bytes": nbytes.value, "ms": best}
     torch.cuda.synchronize()
     return out
 
@@ -813,6 +829,35 @@ def run_ours(args):
     # FFTCC-path solution (0 = the solution itself, which IC-GN confirms in one iteration),
     # on the same resident pair and layout.  The fixed part of a step (reference prep,
     # per-POI prep, target table) does not depend on the seed.
+    # ---- the same FFTCC-seeded step with IC-GN sampling the B-spline coefficient table
+    # (DIC_SAMPLE_TABLE, k_icgn_persistent) instead of staged pixels: the previous form,
+    # timed the same way for the comparison and its L2 gather roofline
+    table_form = None
+    if "fftcc" in res:
+        eng.set_sampling(_lib.DIC_SAMPLE_TABLE)
+        for _ in range(args.warmup):
+            device_step("fftcc")
+        barrier()
+        times, icgn, its = [], [], []
+        for _ in range(max(3, args.steps // 4)):
+            with torch.cuda.stream(stream):
+                flush.random_(0, 255)
+                s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                s.record(stream)
+            device_step("fftcc")
+            with torch.cuda.stream(stream):
+                e.record(stream)
+            e.synchronize()
+            times.append(s.elapsed_time(e))
+            st = eng.stats()
+            icgn.append(st["ms_icgn"])
+            its.append(st["icgn_iterations"])
+        same = np.array_equal(work_d.cpu().numpy().view(dic.POI_DTYPE)["zncc"] < 0, res["fftcc"]["result"]["zncc"] < 0)
+        table_form = {"ms_per_step": float(np.mean(times)), "value": whole_job_rate(world, P, float(np.mean(times))),
+                      "ms_icgn": float(np.mean(icgn)), "icgn_iterations": float(np.mean(its)),
+                      "flags_equal_to_pixel_form": bool(same), "tuning": eng.tuning()["icgn_column"]}
+        eng.set_sampling(_lib.DIC_SAMPLE_PIXELS)
+
     seed_floor = None
     if "fftcc" in res:
         base = res["fftcc"]["result"]
@@ -907,30 +952,52 @@ def run_ours(args):
             dist.destroy_process_group()
         return
 
-    # ---- roofline of the dominant kernel (IC-GN).  Gather model per launch: 64 B of B-spline
-    # texel per warped sample per iteration + 12 B of reference/gradients per sample + 224 B per
-    # POI.  L2 serves the gathers (98.9 % hit; DRAM carries only the compulsory table and
-    # planes), so the bound is the L2-to-SM read bandwidth measured above with the same loads.
+    # ---- roofline of the dominant kernel, IC-GN under pixel sampling (k_icgn_px).  Each warped
+    # sample reads its 4 x 4 pixel support (16 x 4 B) from the POI's window in shared memory;
+    # an iteration on the pixel lattice (the first one from an integer FFTCC seed) reads one
+    # pixel per sample.  The reference texel (16 B) per sample per iteration comes through
+    # L1/L2, and each POI's window (bx x by floats) is staged once from L2 by TMA.  The bound
+    # is the shared-memory load bandwidth, measured in this run by dic_smem_probe; ncu shows
+    # the kernel limited by instruction issue below it (issue_active_pct_ncu).
     N = (2 * R + 1) ** 2
     H0 = res[headline]
     icgn_ms = H0["kernels_ms"]["ms_icgn"]
-    alg_bytes = 64.0 * N * H0["icgn_iterations"] + P * (12.0 * N + 144 + 8 + 32 + 40)
-    hbm_peak, hbm_kind = measured_peak_hbm()
-    achieved = alg_bytes / (icgn_ms * 1e-3) / 1e9
-    prof = profiled("k_icgn")
+    iters = H0["icgn_iterations"]
+    lattice_iters = float(np.sum(H0["result"]["iteration"] >= 1)) if headline == "fftcc" else 0.0
+    smem_bytes = N * (64.0 * (iters - lattice_iters) + 4.0 * lattice_iters)
+    wx, wy = ((2 * R + 1 + 3 + 2 + 1 + 3) + 3) // 4 * 4, 2 * R + 1 + 3 + 2 + 1
+    l2_bytes = 16.0 * N * iters + P * (4.0 * wx * wy + 224 + 2 * 56)
+    achieved = smem_bytes / (icgn_ms * 1e-3) / 1e9
+    prof = profiled("k_icgn_px")
     traffic = prof.get("dram_bytes_per_launch")
-    roofline = {"kernel": "k_icgn", "bound": "l2", "achieved": achieved, "peak": peaks["l2"]["gbs"], "unit": "GB/s",
-                "frac": achieved / peaks["l2"]["gbs"],
-                "peak_source": (f"measured in this run: dic_read_probe, 256-bit loads over a {peaks['l2']['bytes'] >> 20} "
-                                f"MiB L2-resident buffer x {peaks['l2']['passes']} passes (of measured)"),
-                "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes, "icgn_ms": icgn_ms,
-                "l2_busy_pct_ncu": prof.get("lts_throughput_pct"),
+    hbm_peak, hbm_kind = measured_peak_hbm()
+    roofline = {"kernel": "k_icgn_px", "bound": "smem", "achieved": achieved, "peak": peaks["smem"]["gbs"],
+                "unit": "GB/s", "frac": achieved / peaks["smem"]["gbs"],
+                "peak_source": ("measured in this run: dic_smem_probe, conflict-free 32-float warp loads from "
+                                "shared memory, 8 CTAs of 256 threads per SM (of measured)"),
+                "traffic": traffic, "algorithmic_bytes_per_launch": smem_bytes, "icgn_ms": icgn_ms,
+                "model": "64 B of pixels per warped sample per iteration from the staged window (4 B on the "
+                         "pixel lattice); per-launch counts from the step's own iteration total",
+                "issue_active_pct_ncu": prof.get("issue_active_pct"),
+                "limiter_ncu": prof.get("limiter"),
+                "l2": {"achieved": l2_bytes / (icgn_ms * 1e-3) / 1e9, "peak": peaks["l2"]["gbs"],
+                       "frac": l2_bytes / (icgn_ms * 1e-3) / 1e9 / peaks["l2"]["gbs"],
+                       "model": "16 B reference texel per sample per iteration + one pixel window, the "
+                                "record and the queue per POI", "busy_pct_ncu": prof.get("lts_throughput_pct")},
                 "hbm": {"achieved": (traffic / (icgn_ms * 1e-3) / 1e9) if traffic else None, "peak": hbm_peak,
                         "frac": (traffic / (icgn_ms * 1e-3) / 1e9 / hbm_peak) if traffic else None,
                         "peak_source": hbm_kind, "note": "DRAM bytes per launch (ncu) over the IC-GN time"},
-                "read_probe": peaks, "profile_source": prof.get("source"),
-                "model": "64 B B-spline texel per warped sample per iteration + 12 B ref/grad per sample "
-                         "+ 224 B per-POI record/IO"}
+                "read_probe": peaks, "profile_source": prof.get("source")}
+    if table_form is not None:
+        # the table form's gathers: 64 B of coefficients per sample per iteration (4 B on the
+        # lattice plane) + 16 B reference texel, served by L2
+        t_bytes = N * (64.0 * (iters - lattice_iters) + 4.0 * lattice_iters) + 16.0 * N * iters + P * (224 + 2 * 56)
+        t_ach = t_bytes / (table_form["ms_icgn"] * 1e-3) / 1e9
+        table_form["l2_roofline"] = {"kernel": "k_icgn_persistent", "bound": "l2", "achieved": t_ach,
+                                     "peak": peaks["l2"]["gbs"], "frac": t_ach / peaks["l2"]["gbs"],
+                                     "model": "64 B coefficient texel per sample per iteration (4 B lattice) + "
+                                              "16 B reference texel + record per POI"}
+        roofline["table_form"] = table_form
 
     # ---- the other hot kernels against their own bounds (FLOP models per POI)
     M = 2 * R
@@ -988,7 +1055,7 @@ def run_ours(args):
         "clocks": clock.summary(),
         "clocks_headline": clock.summary([headline]),
         "gpu_launches": int(round(H0["launches_per_step"] * args.steps)),
-        "icgn_launch_shape": eng.tuning()["icgn_column"],
+        "icgn_launch_shape": eng.tuning()["icgn_column_px"],
         "seed_modes": seed_modes,
         "learned_vs_fftcc": (seed_modes["learned"]["value"] / seed_modes["fftcc"]["value"]) if "learned" in seed_modes else None,
         "seed_floor": seed_floor,

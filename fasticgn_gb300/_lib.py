@@ -23,6 +23,7 @@ DIC_U8, DIC_U16, DIC_F32 = 1, 2, 3
 DIC_RUN_FFTCC, DIC_RUN_ICGN, DIC_RUN_PREPARE, DIC_RUN_LEARNED = 1, 2, 4, 8
 DIC_PIXELS_STAGED = 2
 DIC_PLANE_REF, DIC_PLANE_REF_PACK, DIC_PLANE_TAR, DIC_PLANE_TAR_COEF = 1, 2, 3, 4
+DIC_SAMPLE_TABLE, DIC_SAMPLE_PIXELS = 0, 1
 
 # struct dic_poi (include/dic.h), 56 bytes
 POI_DTYPE = np.dtype([
@@ -71,7 +72,7 @@ class DicLaunchShape(ctypes.Structure):
 
 
 class DicTuning(ctypes.Structure):
-    _fields_ = [("icgn", DicLaunchShape * 3), ("batch", DicLaunchShape * 3)]
+    _fields_ = [("icgn", DicLaunchShape * 4), ("batch", DicLaunchShape * 4)]
 
 
 class DicStats(ctypes.Structure):
@@ -122,11 +123,13 @@ SIGNATURES = {
     "dic_set_autotune": (ctypes.c_int, [_vp, _i32]),
     "dic_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(DicTuning)]),
     "dic_set_launch_shape": (ctypes.c_int, [_vp, _i32, ctypes.POINTER(DicLaunchShape)]),
+    "dic_set_sampling": (ctypes.c_int, [_vp, _i32]),
     "dic_read_plane": (ctypes.c_int, [_vp, _i32, _vp, _i64]),
     "dic_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(DicStats)]),
     "dic_set_timing": (ctypes.c_int, [_vp, _i32]),
     "dic_read_probe": (ctypes.c_int, [_i32, _vp, _i64, _i32, _vp, _vp]),
     "dic_fma_probe": (ctypes.c_int, [_i32, _i32, _vp, _vp, ctypes.POINTER(_i64)]),
+    "dic_smem_probe": (ctypes.c_int, [_i32, _i32, _vp, _vp, ctypes.POINTER(_i64)]),
     "dic_cnn_param_count": (_i64, []),
     "dic_cnn_create": (ctypes.c_int, [_i32, ctypes.POINTER(_vp)]),
     "dic_cnn_destroy": (None, [_vp]),

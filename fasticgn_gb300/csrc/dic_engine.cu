@@ -411,11 +411,11 @@ struct dic_engine
     check_launch("k_prepare_ref");
   }
   template <typename T>
-  void launch_prepare_tar()
+  void launch_prepare_tar(bool table)
   {
     dim3 grid((w + kPrepTile - 1) / kPrepTile, (h + kPrepTile - 1) / kPrepTile);
     k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_tar.ptr), w, h, scale(),
-                                               tar_f32.ptr, coef.ptr, lattice.ptr);
+                                               tar_f32.ptr, table ? coef.ptr : nullptr, lattice.ptr);
     check_launch("k_prepare_tar");
   }
 
@@ -436,24 +436,36 @@ struct dic_engine
     mark(kPhRef, 1);
     ref_dirty = false;
   }
-  void ensure_tar()
+  // Sampling of the target in IC-GN (DIC_SAMPLE_*): the B-spline coefficient table, or the
+  // pixels themselves (column walk; other walks keep the table).
+  int sampling = DIC_SAMPLE_PIXELS;
+  bool pixel_walk() const { return sampling == DIC_SAMPLE_PIXELS && walk_of(cfg.subset_radius_x) == kWalkColumn; }
+  bool table_ready = false;   // coef / lattice hold the current target's table
+  // The target's float plane, plus its coefficient table when IC-GN samples the table (or
+  // `table` asks for it).
+  void ensure_tar(bool table = false)
   {
     if (!tar_set) throw DicError{DIC_ERR_STATE, "target image must be set first"};
     if (!ref_set) throw DicError{DIC_ERR_STATE, "reference image must be set first"};
-    if (!tar_dirty) return;
+    table = table || !pixel_walk();
+    if (!tar_dirty && (table_ready || !table)) return;
     const size_t px = (size_t)w * h;
     tar_f32.ensure(px);
-    coef.ensure(px * 4);
-    lattice.ensure(px);
+    if (table)
+    {
+      coef.ensure(px * 4);
+      lattice.ensure(px);
+    }
     mark(kPhTar, 0);
     switch (tar_dtype)
     {
-      case DIC_U8: launch_prepare_tar<uint8_t>(); break;
-      case DIC_U16: launch_prepare_tar<uint16_t>(); break;
-      default: launch_prepare_tar<float>(); break;
+      case DIC_U8: launch_prepare_tar<uint8_t>(table); break;
+      case DIC_U16: launch_prepare_tar<uint16_t>(table); break;
+      default: launch_prepare_tar<float>(table); break;
     }
     mark(kPhTar, 1);
     tar_dirty = false;
+    table_ready = table;
   }
 
   // ---------------------------------------------------------------- layout
@@ -551,6 +563,8 @@ struct dic_engine
     int poi_warps = 1;       // pair walk: warps per POI
   };
   static constexpr int kWalkFlat = 0, kWalkColumn = 1, kWalkPair = 2;
+  // the column walk's launches under pixel sampling (k_icgn_px), tuned separately
+  static constexpr int kWalkColumnPx = 3;
   // the subset walk of a radius: column walk up to 32 columns, pair walk up to 64, else flat
   static int walk_of(int rx)
   {
@@ -587,7 +601,7 @@ struct dic_engine
   {
     alignas(128) CUtensorMap map;
     const void* base = nullptr;
-    int w = 0, h = 0;
+    int w = 0, h = 0, bx = 0, by = 0;
   };
   TileMap tile_maps[3];
   // Bounded waits inside kernels report here instead of hanging: bit 0, a k_icgn_tile CTA
@@ -642,7 +656,7 @@ struct dic_engine
   }
   static std::string wait_error_text(int flag)
   {
-    std::string t = (flag & 1) ? "k_icgn_tile: a TMA tile copy did not complete in time" : "";
+    std::string t = (flag & 1) ? "k_icgn_tile / k_icgn_px: a TMA tile copy did not complete in time" : "";
     if (flag & 2) t += std::string(t.empty() ? "" : "; ") + "k_proposal_fused: a tensor-core product did not complete in time";
     return t + "; results are invalid";
   }
@@ -668,8 +682,9 @@ struct dic_engine
   // of its L1 wavefronts on the 2048² pair, 3.73 ms against 3.59 ms persistent with the
   // four-plane table); the autotuner still times both forms.  shape[0]: single queues,
   // shape[1]: batches.
-  IcgnShape shape[2][3] = {{{4, 8, 0.f}, {4, 8, 0.f}, {4, 8, 0.f}}, {{4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}}};
-  bool tuned[2][3] = {};
+  IcgnShape shape[2][4] = {{{4, 8, 0.f}, {4, 8, 0.f}, {4, 8, 0.f}, {4, 0, 0.f, 1}},
+                           {{4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}}};
+  bool tuned[2][4] = {};
   DevBuf<dic_poi> tune_q;
   cudaEvent_t tune_ev[2] = {};
 
@@ -728,6 +743,116 @@ struct dic_engine
   }
   DevBuf<unsigned long long> icgn_next;   // work counter of the persistent single-queue launch
 
+  // k_icgn_px: dynamic shared memory of one CTA (the warps' windows plus alignment room)
+  static size_t px_smem(int warps, int rx, int ry) { return 128 + (size_t)warps * px_window_bytes(rx, ry); }
+  // the shared-memory opt-in of the three k_icgn_px widths (per engine, so per device): the
+  // device's per-block maximum, set once outside any capture
+  bool px_attr_set = false;
+  void px_attributes()
+  {
+    if (px_attr_set) return;
+    int optin = 0;
+    DIC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, cfg.device));
+    auto opt_in = [optin](const void* k) {
+      cudaFuncAttributes fa{};
+      DIC_CUDA(cudaFuncGetAttributes(&fa, k));   // the dynamic maximum leaves room for the static part
+      DIC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+    };
+    opt_in((const void*)k_icgn_px<2>);
+    opt_in((const void*)k_icgn_px<4>);
+    opt_in((const void*)k_icgn_px<8>);
+    opt_in((const void*)k_icgn_batch_px<2>);
+    opt_in((const void*)k_icgn_batch_px<4>);
+    opt_in((const void*)k_icgn_batch_px<8>);
+    px_attr_set = true;
+  }
+  template <int W>
+  static int max_ctas_px(size_t smem)
+  {
+    int b = 0;
+    DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_px<W>, W * 32, smem));
+    return b;
+  }
+  int occupancy_batch_px(int warps, size_t smem)
+  {
+    px_attributes();
+    int b = 0;
+    if (warps == 2) DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<2>, 64, smem));
+    else if (warps == 8) DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<8>, 256, smem));
+    else DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<4>, 128, smem));
+    if (b < 1) throw DicError{DIC_ERR_ARGUMENT, "IC-GN pixel windows of this subset radius do not fit in shared memory"};
+    return b;
+  }
+  // resident CTAs per SM of a k_icgn_px width, cached per (warps, staged, radius)
+  struct PxOcc
+  {
+    int warps = 0, staged = 0, rx = -1, ry = -1, ctas = 0;
+  };
+  PxOcc px_occ[6];
+  int occupancy_px(int warps, bool staged, int rx, int ry)
+  {
+    const int slot = (warps == 2 ? 0 : warps == 4 ? 1 : 2) * 2 + (staged ? 1 : 0);
+    PxOcc& o = px_occ[slot];
+    if (o.warps == warps && o.rx == rx && o.ry == ry) return o.ctas;
+    px_attributes();
+    const size_t smem = staged ? px_smem(warps, rx, ry) : 0;
+    const int b = warps == 2 ? max_ctas_px<2>(smem) : warps == 8 ? max_ctas_px<8>(smem) : max_ctas_px<4>(smem);
+    if (b < 1) throw DicError{DIC_ERR_ARGUMENT, "IC-GN pixel windows of this subset radius do not fit in shared memory"};
+    o = PxOcc{warps, staged ? 1 : 0, rx, ry, b};
+    return b;
+  }
+  // the 2-D map {x, y} of the target plane, box {bx, by} (only for rows of a multiple of 16 bytes)
+  TileMap px_map;
+  const CUtensorMap* tar_map(const float* plane, int tw, int th, int bx, int by)
+  {
+    if ((tw * sizeof(float)) % 16 != 0) return nullptr;
+    EncodeTiledFn fn = encode_tiled();
+    if (!fn) return nullptr;
+    TileMap& m = px_map;
+    if (m.base == plane && m.w == tw && m.h == th && m.bx == bx && m.by == by) return &m.map;
+    const cuuint64_t dims[2] = {(cuuint64_t)tw, (cuuint64_t)th};
+    const cuuint64_t strides[1] = {(cuuint64_t)tw * sizeof(float)};
+    const cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult r = fn(&m.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(plane), dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS)
+    {
+      m.base = nullptr;
+      throw DicError{DIC_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")"};
+    }
+    m.base = plane;
+    m.w = tw;
+    m.h = th;
+    m.bx = bx;
+    m.by = by;
+    return &m.map;
+  }
+  // shape.tile: 1 stages each POI's pixel window in shared memory, 0 reads the global plane
+  void launch_px(const IcgnParams& p, const IcgnShape& sh)
+  {
+    icgn_next.ensure(1);
+    DIC_CUDA(cudaMemsetAsync(icgn_next.ptr, 0, sizeof(unsigned long long), stream));
+    int sms = 0;
+    DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+    const int warps = sh.warps;
+    px_attributes();
+    const size_t smem = sh.tile ? px_smem(warps, p.rx, p.ry) : 0;
+    const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_px(warps, sh.tile != 0, p.rx, p.ry);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * ctas, (p.n + warps - 1) / warps));
+    const CUtensorMap* m = sh.tile ? tar_map(p.tar, p.w, p.h, px_window_x(p.rx), px_window_y(p.ry)) : nullptr;
+    CUtensorMap none{};
+    IcgnParams q = p;
+    q.wait_polls = wait_polls;
+    q.wait_test = wait_test & 1;
+    const int mode = sh.tile ? (m ? 2 : 1) : 0;   // 2: TMA, 1: warp copies, 0: no window
+#define DIC_PX_LAUNCH(W) k_icgn_px<W><<<grid, W * 32, smem, stream>>>(q, m ? *m : none, mode, icgn_next.ptr, wait_flag())
+    if (warps == 2) DIC_PX_LAUNCH(2);
+    else if (warps == 8) DIC_PX_LAUNCH(8);
+    else DIC_PX_LAUNCH(4);
+#undef DIC_PX_LAUNCH
+  }
   bool tile_attr_set[3] = {};   // per engine, so per device: the shared-memory opt-in of each tile form
   template <int W, int BX, int BY>
   void launch_tile(const IcgnParams& p, int kind, int sms)
@@ -791,6 +916,11 @@ struct dic_engine
   }
   void launch_icgn(const IcgnParams& p, int walk, const IcgnShape& sh)
   {
+    if (walk == kWalkColumnPx)
+    {
+      launch_px(p, sh);
+      return;
+    }
     if (walk == kWalkPair)
     {
       launch_icgn_pair(p, sh);
@@ -861,8 +991,26 @@ struct dic_engine
   {
     int sms = 0;
     DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
-    const unsigned grid = (unsigned)(sms * sh.ctas_per_sm);
     const float mi = (float)cfg.max_iteration;
+    if (walk == kWalkColumnPx)
+    {
+      // windows sized for the largest radius of the launch's jobs
+      px_attributes();
+      const uint32_t win = (uint32_t)px_window_bytes(b_col_rmax, b_col_rmax);
+      const size_t smem = 128 + (size_t)sh.warps * win;
+      const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_batch_px(sh.warps, smem);
+      const unsigned grid = (unsigned)(sms * ctas);
+#define DIC_BATCH_PX(W)                                                                                            \
+  k_icgn_batch_px<W><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,     \
+                                                     cfg.conv_criterion, mi, b.iter_sum, win)
+      if (sh.warps == 2) DIC_BATCH_PX(2);
+      else if (sh.warps == 8) DIC_BATCH_PX(8);
+      else DIC_BATCH_PX(4);
+#undef DIC_BATCH_PX
+      check_launch("k_icgn_batch_px");
+      return;
+    }
+    const unsigned grid = (unsigned)(sms * sh.ctas_per_sm);
     if (walk == kWalkPair)
     {
 #define DIC_BATCH_PAIR(PW, W)                                                                                      \
@@ -929,7 +1077,9 @@ struct dic_engine
     std::vector<IcgnShape> cand;
     for (int warps : {2, 4, 8})
       for (int persistent = 0; persistent < 2; ++persistent)
-        if (walk == kWalkPair)
+        if (walk == kWalkColumnPx)
+          cand.push_back(IcgnShape{warps, 0, 0.f, persistent});   // windows staged, or not
+        else if (walk == kWalkPair)
           for (int pw : {1, 2})
             cand.push_back(IcgnShape{warps, persistent ? occupancy_pair(false, pw, warps) : 0, 0.f, 0, pw});
         else
@@ -964,8 +1114,10 @@ struct dic_engine
       for (int pw : {1, 2})
       {
         if (walk != kWalkPair && pw == 2) continue;
-        const int full =
-            walk == kWalkPair ? occupancy_pair(true, pw, warps) : occupancy(true, walk == kWalkColumn, warps);
+        const int full = walk == kWalkColumnPx
+                             ? occupancy_batch_px(warps, 128 + (size_t)warps * px_window_bytes(b_col_rmax, b_col_rmax))
+                             : walk == kWalkPair ? occupancy_pair(true, pw, warps)
+                                                 : occupancy(true, walk == kWalkColumn, warps);
         for (int ctas : {full, std::max(1, (3 * full) / 4)})
         {
           const IcgnShape sh{warps, ctas, 0.f, 0, pw};
@@ -1039,6 +1191,7 @@ struct dic_engine
     p.enable = enable;
     p.coef = coef.ptr;
     p.lattice = lattice.ptr;
+    p.tar = tar_f32.ptr;
     p.ref_pack = ref_pack.ptr;
     p.poi_ref = poi_ref.ptr;
     p.slot = d_slots;
@@ -1051,7 +1204,7 @@ struct dic_engine
     p.conv = cfg.conv_criterion;
     p.max_iter = (float)(max_iter_override > 0 ? max_iter_override : cfg.max_iteration);
     p.iter_sum = counters.ptr;
-    const int walk = walk_of(p.rx);
+    const int walk = pixel_walk() ? kWalkColumnPx : walk_of(p.rx);
     if (autotune && !tuned[0][walk] && n >= kTuneMinPois && !capturing()) tune_icgn(p, walk);
     mark(kPhIcgn, 0);
     launch_icgn(p, walk, shape[0][walk]);
@@ -1369,14 +1522,14 @@ struct dic_engine
   DevBuf<unsigned long long> bnext;
 
   template <typename T>
-  void prep_planes(const unsigned char* raw_r, const unsigned char* raw_t, int bw, int bh, JobBufs& J)
+  void prep_planes(const unsigned char* raw_r, const unsigned char* raw_t, int bw, int bh, JobBufs& J, bool table)
   {
     dim3 grid((bw + kPrepTile - 1) / kPrepTile, (bh + kPrepTile - 1) / kPrepTile);
     k_prepare_ref<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_r), bw, bh, scale(), J.ref_f32.ptr,
                                                J.ref_pack.ptr);
     check_launch("k_prepare_ref");
     k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_t), bw, bh, scale(), J.tar_f32.ptr,
-                                               J.coef.ptr, J.lattice.ptr);
+                                               table ? J.coef.ptr : nullptr, J.lattice.ptr);
     check_launch("k_prepare_tar");
   }
 
@@ -1385,6 +1538,9 @@ struct dic_engine
   std::vector<int> b_order;
   std::vector<int64_t> b_first;
   int64_t b_total = 0, b_col_end = 0, b_pair_end = 0;
+  int b_col_rmax = 0;                   // largest subset radius among the column-walk jobs
+  // pixel sampling covers the batch's column-walk jobs; the others sample the table
+  bool job_table(int radius) const { return sampling != DIC_SAMPLE_PIXELS || walk_of(radius) != kWalkColumn; }
   std::vector<dic_job> b_key;           // jobs of the captured batch graph (device pointers)
   bool b_key_seen = false;
   cudaGraphExec_t batch_graph = nullptr;
@@ -1404,6 +1560,7 @@ struct dic_engine
     b_total = 0;
     b_col_end = 0;
     b_pair_end = 0;
+    b_col_rmax = 0;
     for (int k = 0; k < nj; ++k)
     {
       const dic_job& J = jobs[b_order[k]];
@@ -1411,6 +1568,7 @@ struct dic_engine
       b_total += J.count;
       const int r = rank(b_order[k]);
       if (r == 0) b_col_end = b_total;
+      if (r == 0) b_col_rmax = std::max(b_col_rmax, J.subset_radius);
       if (r <= 1) b_pair_end = b_total;
     }
     if ((int)jobs_mem.size() < nj) jobs_mem.resize(nj);
@@ -1431,10 +1589,13 @@ struct dic_engine
       M.ref_f32.ensure(px);
       M.tar_f32.ensure(px);
       M.ref_pack.ensure(px);
-      M.coef.ensure(px * 4);
-      M.lattice.ensure(px);
+      if (job_table(J.subset_radius))
+      {
+        M.coef.ensure(px * 4);
+        M.lattice.ensure(px);
+      }
       table[k] = BatchJob{M.coef.ptr, M.lattice.ptr, M.ref_pack.ptr, b_first[k], J.width, J.height, J.subset_radius,
-                          J.subset_radius};
+                          J.subset_radius, M.tar_f32.ptr};
     }
     DIC_CUDA(cudaMemcpyAsync(bjobs.ptr, table.data(), sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, stream));
   }
@@ -1455,11 +1616,12 @@ struct dic_engine
                                  (size_t)J.width * es, J.height, in_kind, stream));
       DIC_CUDA(cudaMemcpy2DAsync(M.raw_tar.ptr, (size_t)J.width * es, J.tar, (size_t)J.row_stride_bytes,
                                  (size_t)J.width * es, J.height, in_kind, stream));
+      const bool table = job_table(J.subset_radius);
       switch (J.dtype)
       {
-        case DIC_U8: prep_planes<uint8_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M); break;
-        case DIC_U16: prep_planes<uint16_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M); break;
-        default: prep_planes<float>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M); break;
+        case DIC_U8: prep_planes<uint8_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table); break;
+        case DIC_U16: prep_planes<uint16_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table); break;
+        default: prep_planes<float>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table); break;
       }
       if (J.count == 0) continue;
       const int r = J.subset_radius;
@@ -1476,14 +1638,15 @@ struct dic_engine
     BatchLaunch pair{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_col_end, b_pair_end, bnext.ptr + 2, counters.ptr};
     BatchLaunch flat{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_pair_end, b_total, bnext.ptr + 1, counters.ptr};
     const bool cap = capturing();
+    const int col_walk = sampling == DIC_SAMPLE_PIXELS ? kWalkColumnPx : kWalkColumn;
     if (autotune && !cap)
     {
-      if (b_col_end >= kTuneMinPois && !tuned[1][kWalkColumn]) tune_batch(col, kWalkColumn, b_total);
+      if (b_col_end >= kTuneMinPois && !tuned[1][col_walk]) tune_batch(col, col_walk, b_total);
       if (b_pair_end - b_col_end >= kTuneMinPois && !tuned[1][kWalkPair]) tune_batch(pair, kWalkPair, b_total);
       if (b_total - b_pair_end >= kTuneMinPois && !tuned[1][kWalkFlat]) tune_batch(flat, kWalkFlat, b_total);
     }
     mark(kPhIcgn, 0);
-    if (b_col_end > 0) launch_batch(col, kWalkColumn, shape[1][kWalkColumn]);
+    if (b_col_end > 0) launch_batch(col, col_walk, shape[1][col_walk]);
     if (b_pair_end > b_col_end) launch_batch(pair, kWalkPair, shape[1][kWalkPair]);
     if (b_total > b_pair_end) launch_batch(flat, kWalkFlat, shape[1][kWalkFlat]);
     mark(kPhIcgn, 1);
@@ -2288,7 +2451,7 @@ int dic_get_tuning(dic_engine* e, dic_tuning* out)
   return guarded(e, [&] {
     if (!out) throw DicError{DIC_ERR_ARGUMENT, "get_tuning: null output"};
     for (int pers = 0; pers < 2; ++pers)
-      for (int walk = 0; walk < 3; ++walk)
+      for (int walk = 0; walk < 4; ++walk)
       {
         dic_launch_shape& d = pers ? out->batch[walk] : out->icgn[walk];
         const auto& s = e->shape[pers][walk];
@@ -2306,9 +2469,19 @@ int dic_set_launch_shape(dic_engine* e, int32_t walk, const dic_launch_shape* sh
 {
   return guarded(e, [&] {
     if (!shape) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: null shape"};
-    if (walk < 0 || walk > 2) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: walk must be 0 (flat), 1 (column) or 2 (pair)"};
+    if (walk < 0 || walk > 3)
+      throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: walk must be 0 (flat), 1 (column), 2 (pair) or 3 (column, pixel sampling)"};
     dic_engine::IcgnShape sh;
-    if (shape->tile != 0)
+    if (walk == dic_engine::kWalkColumnPx)
+    {
+      if (shape->warps_per_cta != 2 && shape->warps_per_cta != 4 && shape->warps_per_cta != 8)
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: warps_per_cta must be 2, 4 or 8"};
+      if (shape->ctas_per_sm < 0) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: ctas_per_sm must be >= 0"};
+      if (shape->tile != 0 && shape->tile != 1)
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0 or 1 with walk 3"};
+      sh = dic_engine::IcgnShape{shape->warps_per_cta, shape->ctas_per_sm, 0.f, shape->tile};
+    }
+    else if (shape->tile != 0)
     {
       if (shape->tile < 0 || shape->tile > 2 || walk != dic_engine::kWalkColumn)
         throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0, or 1 or 2 with the column walk"};
@@ -2330,6 +2503,23 @@ int dic_set_launch_shape(dic_engine* e, int32_t walk, const dic_launch_shape* sh
     if (e->seq_graph)
     {
       // a captured sequence frame holds the previous launch
+      cudaGraphExecDestroy(e->seq_graph);
+      e->seq_graph = nullptr;
+    }
+  });
+}
+
+int dic_set_sampling(dic_engine* e, int32_t mode)
+{
+  return guarded(e, [&] {
+    if (mode != DIC_SAMPLE_TABLE && mode != DIC_SAMPLE_PIXELS)
+      throw DicError{DIC_ERR_ARGUMENT, "set_sampling: mode must be DIC_SAMPLE_TABLE or DIC_SAMPLE_PIXELS"};
+    if (mode == e->sampling) return;
+    e->sampling = mode;
+    e->drop_batch_graph();   // a captured batch holds the previous kernels
+    if (e->seq_graph)
+    {
+      // a captured sequence frame holds the previous solver
       cudaGraphExecDestroy(e->seq_graph);
       e->seq_graph = nullptr;
     }
@@ -2365,7 +2555,7 @@ int dic_read_plane(dic_engine* e, int32_t plane, void* dst, int64_t bytes)
       case DIC_PLANE_REF: e->ensure_ref(); src = e->ref_f32.ptr; size = px * sizeof(float); break;
       case DIC_PLANE_REF_PACK: e->ensure_ref(); src = e->ref_pack.ptr; size = px * sizeof(float4); break;
       case DIC_PLANE_TAR: e->ensure_tar(); src = e->tar_f32.ptr; size = px * sizeof(float); break;
-      case DIC_PLANE_TAR_COEF: e->ensure_tar(); src = e->coef.ptr; size = px * 4 * sizeof(float4); break;
+      case DIC_PLANE_TAR_COEF: e->ensure_tar(true); src = e->coef.ptr; size = px * 4 * sizeof(float4); break;
       default: throw DicError{DIC_ERR_ARGUMENT, "read_plane: unknown plane"};
     }
     if ((size_t)bytes != size) throw DicError{DIC_ERR_ARGUMENT, "read_plane: size mismatch"};
@@ -2458,7 +2648,42 @@ __global__ void __launch_bounds__(256) k_fma_probe(int iterations, float seed, f
   for (int k = 0; k < 8; ++k) acc += a[k];
   if (acc == 1.2345678e-30f) *sink = acc;
 }
+
+// Shared-memory load bandwidth (the pixel-sampled IC-GN's sample path): every warp reads
+// 32 consecutive floats per load (one wavefront, no bank conflicts) from a 16 KB block,
+// 16 loads per pass, `repeats` passes; 8 CTAs of 256 threads per SM.
+__global__ void __launch_bounds__(256) k_smem_probe(int repeats, float* __restrict__ sink)
+{
+  __shared__ float buf[4096 + 32];
+  for (int i = threadIdx.x; i < 4096 + 32; i += 256) buf[i] = (float)i;
+  __syncthreads();
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int rep = 0; rep < repeats; ++rep)
+  {
+    // the pass's offset (0 or 32 floats) keeps the loads from being hoisted out of the loop
+    const volatile float* a = buf + threadIdx.x + ((rep & 1) << 5);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k & 7] += a[256 * k];
+  }
+  float t = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) t += acc[k];
+  if (t == 1.2345678e-30f) *sink = t;
+}
 }  // namespace
+
+extern "C" int dic_smem_probe(int32_t device, int32_t repeats, float* device_sink, void* stream, int64_t* bytes_out)
+{
+  if (!device_sink || repeats < 1 || !bytes_out) return DIC_ERR_ARGUMENT;
+  int sms = 0;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return DIC_ERR_CUDA;
+  const unsigned blocks = (unsigned)(sms * 8);
+  k_smem_probe<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(repeats, device_sink);
+  *bytes_out = (int64_t)blocks * 256 * 16 * 4 * repeats;
+  return cudaGetLastError() == cudaSuccess ? DIC_OK : DIC_ERR_CUDA;
+}
 
 extern "C" int dic_fma_probe(int32_t device, int32_t iterations, float* device_sink, void* stream,
                              int64_t* flop_out)

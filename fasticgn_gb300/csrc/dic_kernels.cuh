@@ -176,6 +176,7 @@ __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, 
   if (x >= w || y >= h) return;
   const size_t o = (size_t)y * w + x;
   tar_f32[o] = tile[ty + 1][tx + 1];
+  if (!coef) return;   // pixel sampling: no table
   const size_t plane = (size_t)w * h;
   float4* dst = coef + 2 * o;   // row k at dst[(k >> 1) * 2 * plane + (k & 1)]
   if (x < 1 || y < 1 || x >= w - 2 || y >= h - 2)
@@ -338,6 +339,8 @@ struct PoiSums
 
 // Entry test, mean (written to rec->t0), and the warp-reduced sums of one POI.  Returns false
 // (after writing valid = 0) when the reference subset leaves the image.
+// (The mean pass reads ref_pack, not the 4-byte grey-level plane: its lines stay in L1 for
+// the second pass; reading the plane instead was slower, 0.60 -> 0.70 ms on the 2048x2048 pair.)
 __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, int w, int h, float px, float py,
                                          int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums)
 {
@@ -688,6 +691,7 @@ struct IcgnParams
 {
   const float4* coef;      // tar B-spline table: 2 planes of W*H texels x 2 float4
   const float* lattice = nullptr;   // coefficient [0][0] of every texel (nullable, see on_lattice)
+  const float* tar = nullptr;       // target plane (pixel sampling, k_icgn_px)
   const float4* ref_pack;  // {ref, gx, gy, 0}
   const PoiRef* poi_ref;   // per layout slot
   const int64_t* slot;     // queue index -> layout slot (nullptr: identity)
@@ -818,6 +822,132 @@ __device__ __forceinline__ float sample_bspline_tile(const CoefTile& T, const fl
   return fmaf(fmaf(fmaf(r3, dy, r2), dy, r1), dy, r0);
 }
 
+// --------------------------------------------------------------------------------------
+// Pixel sampling.  The bicubic value at (ix + dx, iy + dy) is the texel's polynomial
+// sum_{a,b} P[3-a][3-b] dy^a dx^b with P = BC q BC^T over the 4 x 4 pixels q[n][m] =
+// I(iy - 1 + n, ix - 1 + m) (k_prepare_tar).  Regrouped by pixel it is
+//   sum_n wy[n] sum_m wx[m] q[n][m],   w[m](d) = sum_b BC[3-b][m] d^b,
+// the B-spline weights of the BC matrix.  Evaluated that way a sample reads 16 pixels (4 B
+// each) instead of the texel's 16 coefficients (64 B), so a warp's whole warped subset fits
+// in a few KB of shared memory (k_icgn_px) and the coefficient table is not needed.  The
+// polynomial is the same, the rounding is not: results agree with the table forms to float
+// rounding, not bit for bit.  At d = 0 the weights are exactly (0, 1, 0, 0) (BC's last row),
+// so a sample on the lattice returns the pixel itself, as the table does.
+// --------------------------------------------------------------------------------------
+// The weights of both axes at once, d = (dx, dy): w[m] = (wx[m], wy[m]).  Packed FP32 pairs
+// (fma.rn.f32x2, sm_100 and later) round each half like the scalar operation, so the
+// values are the scalar Horner forms' bit for bit, in half the instructions.
+__device__ __forceinline__ float2 k2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ void bspline_weights2(float2 d, float2 (&w)[4])
+{
+  w[0] = __fmul2_rn(__ffma2_rn(__ffma2_rn(k2(-144.0f / 336.0f), d, k2(342.0f / 336.0f)), d, k2(-198.0f / 336.0f)), d);
+  w[1] = __ffma2_rn(__ffma2_rn(__ffma2_rn(k2(384.0f / 336.0f), d, k2(-702.0f / 336.0f)), d, k2(-18.0f / 336.0f)), d,
+                    k2(1.0f));
+  w[2] = __fmul2_rn(__ffma2_rn(__ffma2_rn(k2(-384.0f / 336.0f), d, k2(450.0f / 336.0f)), d, k2(270.0f / 336.0f)), d);
+  w[3] = __fmul2_rn(__ffma2_rn(__ffma2_rn(k2(144.0f / 336.0f), d, k2(-90.0f / 336.0f)), d, k2(-54.0f / 336.0f)), d);
+}
+
+// The dynamic shared memory of the pixel-window kernels (k_icgn_px, k_icgn_batch_px) as
+// floats: indexing it with 32-bit offsets keeps the window loads in the shared window's own
+// 32-bit addressing, and as ordinary loads the compiler keeps them after the copy's mbarrier
+// wait.
+extern __shared__ __align__(128) float px_smem[];
+
+// A warp's block of the target plane in shared memory: pixels [ox, ox + bx) x [oy, oy + by),
+// rows of bx floats, from px_smem[s].  bx = 0: nothing staged.
+struct PixelTile
+{
+  int s = 0;
+  int ox = 0, oy = 0, bx = 0, by = 0;
+};
+
+// sum_n wy[n] sum_m wx[m] q[n][m] with w[m] = (wx[m], wy[m]), pixels from a load functor
+// ld(n, m).  (Packing the row sums as FP32 pairs needs the x weights broadcast into pairs,
+// which costs the moves it saves: 2.96 against 2.94 ms of IC-GN on the 2048x2048 pair.)
+template <class Ld>
+__device__ __forceinline__ float eval_pixels(const float2 (&w)[4], Ld ld)
+{
+  float h[4];
+#pragma unroll
+  for (int n = 0; n < 4; ++n)
+    h[n] = fmaf(w[3].x, ld(n, 3), fmaf(w[2].x, ld(n, 2), fmaf(w[1].x, ld(n, 1), w[0].x * ld(n, 0))));
+  return fmaf(w[3].y, h[3], fmaf(w[2].y, h[2], fmaf(w[1].y, h[1], w[0].y * h[0])));
+}
+
+// The weights of a sample and the window address of its 4 x 4 support's first pixel.
+__device__ __forceinline__ void pixel_setup(float gxp, float gyp, float2 (&w)[4], int& ix, int& iy)
+{
+  const float fx = floorf(gxp), fy = floorf(gyp);
+  ix = (int)fx;
+  iy = (int)fy;
+  bspline_weights2(make_float2(gxp - fx, gyp - fy), w);
+}
+
+__device__ __forceinline__ float sample_pixels(const PixelTile& T, const float* __restrict__ tar, int w, float gxp,
+                                               float gyp)
+{
+  float2 wt[4];
+  int ix, iy;
+  pixel_setup(gxp, gyp, wt, ix, iy);
+  const int tx = ix - 1 - T.ox, ty = iy - 1 - T.oy;
+  if (tx >= 0 && ty >= 0 && tx <= T.bx - 4 && ty <= T.by - 4)
+  {
+    const int a = T.s + (ty * T.bx + tx);
+    const int row = T.bx;
+    return eval_pixels(wt, [&](int n, int m) { return px_smem[a + n * row + m]; });
+  }
+  const float* g = tar + ((size_t)(iy - 1) * w + (ix - 1));   // images < 2^31 pixels
+  return eval_pixels(wt, [&](int n, int m) { return __ldg(g + (size_t)n * w + m); });
+}
+
+// A sample whose support lies in the window (the caller has checked): no tests.
+__device__ __forceinline__ float sample_window(const PixelTile& T, int row, float gxp, float gyp)
+{
+  float2 wt[4];
+  int ix, iy;
+  pixel_setup(gxp, gyp, wt, ix, iy);
+  const int a = T.s + ((iy - 1 - T.oy) * T.bx + (ix - 1 - T.ox));
+  return eval_pixels(wt, [&](int n, int m) { return px_smem[a + n * row + m]; });
+}
+
+// Column walk under pixel sampling: whether every sample of the current warp lies in the
+// interpolation range and has its support inside the window.  Sample coordinates are
+// px + fmaf(W1, ly, fmaf(W0, lx, W2)) (y likewise), rounded monotone functions of lx and of
+// ly, so their extremes are the subset's corners, computed here with the same expression;
+// lanes 0-3 take one corner each.  Warp-uniform.
+__device__ __forceinline__ bool window_covers(const float (&W)[6], float px, float py, int rx, int ry, float xmax,
+                                              float ymax, const PixelTile& T, int lane)
+{
+  bool ok = true;
+  if (lane < 4)
+  {
+    const float flx = (lane & 1) ? (float)rx : (float)-rx, fly = (lane & 2) ? (float)ry : (float)-ry;
+    const float gxp = px + fmaf(W[1], fly, fmaf(W[0], flx, W[2]));
+    const float gyp = py + fmaf(W[4], fly, fmaf(W[3], flx, W[5]));
+    ok = gxp >= 1.f && gyp >= 1.f && gxp < xmax && gyp < ymax;
+    if (ok)
+    {
+      const int tx = (int)floorf(gxp) - 1 - T.ox, ty = (int)floorf(gyp) - 1 - T.oy;
+      ok = tx >= 0 && ty >= 0 && tx <= T.bx - 4 && ty <= T.by - 4;
+    }
+  }
+  return __all_sync(kFull, ok);
+}
+
+// the pixel at an integer sample (the lattice case of sample_pixels)
+__device__ __forceinline__ float pixel_at(const PixelTile& T, const float* __restrict__ tar, int w, float gxp,
+                                          float gyp)
+{
+  const int ix = (int)gxp, iy = (int)gyp;
+  const int tx = ix - T.ox, ty = iy - T.oy;
+  if (tx >= 0 && ty >= 0 && tx < T.bx && ty < T.by) return px_smem[T.s + ty * T.bx + tx];
+  return __ldg(tar + ((size_t)iy * w + ix));
+}
+
+// Sample sources of icgn_solve: the global coefficient table, a coefficient block staged
+// in shared memory (k_icgn_tile), or the target pixels (k_icgn_px).
+constexpr int kSrcTable = 0, kSrcCoefTile = 1, kSrcPixels = 2;
+
 // Rows of the column walk unrolled together (their gathers in flight at once), and the
 // warps per SM the IC-GN launch bounds keep resident (which sets the register budget).
 // The 256-bit coefficient gathers are served from L2 and their latency is what the kernel
@@ -835,8 +965,8 @@ constexpr int kIcgnRowUnroll = DIC_ICGN_ROW_UNROLL;
 // One POI (queue index i) on the calling warp; shared by the per-queue launch (k_icgn) and
 // the persistent multi-job launch (k_icgn_batch, which keeps one row in flight: its job
 // lookup leaves no registers for two without spilling).
-template <bool kColumn, bool kTile = false, int kRowUnroll = kIcgnRowUnroll>
-__device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int lane, const CoefTile& T = CoefTile{})
+template <bool kColumn, int kSrc = kSrcTable, int kRowUnroll = kIcgnRowUnroll, class Tile = CoefTile>
+__device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int lane, const Tile& T = Tile{})
 {
   dic_poi* poi = P.pois + i;
   const float px = poi->x, py = poi->y;
@@ -877,10 +1007,46 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
     ++it;
     float A0 = 0.f, A1 = 0.f, A2 = 0.f, B[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     bool bad = false;
-    const bool lat = !kTile && P.lattice && on_lattice(W, px, py);   // warp-uniform
+    const bool lat = kSrc != kSrcCoefTile && (kSrc == kSrcPixels || P.lattice) && on_lattice(W, px, py);   // warp-uniform
     if constexpr (column_walk)
     {
-      if (col_active)
+      bool fast = false;
+      if constexpr (kSrc == kSrcPixels)
+        fast = !lat && window_covers(W, px, py, rx, ry, xmax, ymax, T, lane);
+      if (fast)
+      {
+        if constexpr (kSrc == kSrcPixels)
+          if (col_active)
+          {
+            // every sample in range and in the window: no per-sample tests
+            const float ax = fmaf(W[0], flx_col, W[2]), ay = fmaf(W[3], flx_col, W[5]);
+            const int row = T.bx;
+            // (Loading the reference texel a row ahead of its use shortens the L2 waits but
+            // costs the registers that keep 32 warps resident: 3.27 against 2.94 ms.)
+            const float4* rp = ref_col;
+#pragma unroll kRowUnroll
+            for (int r = 0; r < 2 * ry + 1; ++r)
+            {
+              const float4 cur = __ldg(rp);
+              rp += w;
+              const float fly = (float)(r - ry);
+              const float gxp = px + fmaf(W[1], fly, ax);
+              const float gyp = py + fmaf(W[4], fly, ay);
+              const float t = sample_window(T, row, gxp, gyp);
+              const float tau = t - t0;
+              const float rc = cur.x - t0;
+              A0 += tau;
+              A1 = fmaf(tau, tau, A1);
+              A2 = fmaf(tau, rc, A2);
+              const float gt = __fmul_rn(cur.y, tau), ht = __fmul_rn(cur.z, tau);
+              B[0] = __fadd_rn(B[0], gt);
+              B[2] = fmaf(gt, fly, B[2]);
+              B[3] = __fadd_rn(B[3], ht);
+              B[5] = fmaf(ht, fly, B[5]);
+            }
+          }
+      }
+      else if (col_active)
       {
         const float ax = fmaf(W[0], flx_col, W[2]), ay = fmaf(W[3], flx_col, W[5]);
 #pragma unroll kRowUnroll
@@ -895,8 +1061,10 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
             continue;
           }
           float t;
-          if constexpr (kTile)
+          if constexpr (kSrc == kSrcCoefTile)
             t = sample_bspline_tile(T, coef, plane, w, gxp, gyp);
+          else if constexpr (kSrc == kSrcPixels)
+            t = lat ? pixel_at(T, P.tar, w, gxp, gyp) : sample_pixels(T, P.tar, w, gxp, gyp);
           else if (lat)
             t = __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp));
           else
@@ -928,8 +1096,11 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
           bad = true;
         else
         {
-          const float t = lat ? __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp))
-                              : sample_bspline(coef, plane, w, gxp, gyp);
+          float t;
+          if constexpr (kSrc == kSrcPixels)
+            t = lat ? pixel_at(T, P.tar, w, gxp, gyp) : sample_pixels(T, P.tar, w, gxp, gyp);
+          else
+            t = lat ? __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp)) : sample_bspline(coef, plane, w, gxp, gyp);
           const float4 rv = __ldg(ref_pack + (size_t)(cy + ly) * w + (cx + lx));
           const float tau = t - t0;
           const float rc = rv.x - t0;
@@ -1070,7 +1241,7 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps
     if (lane == 0) t = atomicAdd(next, 1ull);
     const int64_t i = (int64_t)__shfl_sync(kFull, t, 0);
     if (!queue_slot_active(P, i)) return;
-    icgn_solve<kColumn, false, 1>(P, i, lane);
+    icgn_solve<kColumn, kSrcTable, 1>(P, i, lane);
   }
 }
 
@@ -1505,8 +1676,173 @@ __global__ void __launch_bounds__(kWarps * 32) k_icgn_tile(IcgnParams P, const _
     }
     else
       T.bx = 0;   // nothing staged: every texel from the global table
-    if (active) icgn_solve<true, true>(P, i, lane, T);
+    if (active) icgn_solve<true, kSrcCoefTile>(P, i, lane, T);
     __syncthreads();   // every read of this block before the next copy overwrites it
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int c0, int c1, uint32_t bar)
+{
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+// --------------------------------------------------------------------------------------
+// IC-GN from target pixels staged per warp (column walk, pixel sampling).  Persistent CTAs;
+// every warp takes the next POI from the atomic counter and works alone: it bounds the
+// POI's warped subset at the incoming warp (corners, the 4 x 4 pixel support -1..+2, and
+// kPxMargin pixels for the updates to come), and when that block fits its bx x by window
+// it stages the block in its own shared memory -- one cp.async.bulk.tensor.2d issued by
+// lane 0 (map {x, y} over the f32 target plane, box {bx, by}; the x origin is rounded
+// down to a multiple of 4 pixels, TMA's 16-byte rule; pixels outside the image read as
+// zero and are never sampled: the range test rejects their samples first), or, where the
+// plane's row pitch is not a multiple of 16 bytes, a warp-wide copy.  The POI then
+// iterates on shared memory: 16 pixel loads per sample, 4 B each, against the table's
+// two 32-byte coefficient gathers from L2.  Samples whose support leaves the block (an
+// update that walked further than the margin) read the global plane; both give the same
+// bits.  A POI's window is ~6.7 KB at subset radius 15 and stays for all its iterations.
+// The wait on the copy is bounded: a warp that times out sets bit 0 of `err`, waits
+// (bounded) for the copy still in flight, and leaves.
+// --------------------------------------------------------------------------------------
+constexpr int kPxMargin = 1;
+
+// window of one warp for a subset radius: the support of the subset with the margin and
+// the x alignment slack, x rounded up to a multiple of 4 pixels
+__host__ __device__ constexpr int px_window_x(int rx) { return ((2 * rx + 1 + 3 + 2 * kPxMargin + 1 + 3) + 3) & ~3; }
+__host__ __device__ constexpr int px_window_y(int ry) { return 2 * ry + 1 + 3 + 2 * kPxMargin + 1; }
+__host__ __device__ constexpr size_t px_window_bytes(int rx, int ry)
+{
+  return ((size_t)px_window_x(rx) * px_window_y(ry) * sizeof(float) + 127) & ~(size_t)127;
+}
+
+// Stages POI i's window for the calling warp (px_smem[win_f...], shared address win) and fills T.
+// mode 2: one TMA copy (map, the warp's mbarrier bar and its phase parity); 1: warp copies;
+// 0: nothing staged (T.bx = 0, every sample from the global plane).  Returns false when the
+// TMA copy did not arrive within P.wait_polls polls: bit 0 of err is set, lane 0 waits once
+// more (bounded) for the copy in flight, and the caller leaves.
+__device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lane, int mode, int win_f,
+                                         uint32_t win, const CUtensorMap* map, uint32_t bar, uint32_t& parity,
+                                         int* err, PixelTile& T)
+{
+  const int rx = P.rx, ry = P.ry, w = P.w, h = P.h;
+  const int bx = px_window_x(rx), by = px_window_y(ry);
+  int ox = 0, oy = 0, fits = 0;
+  if (lane == 0 && mode != 0)
+  {
+    const dic_poi* poi = P.pois + i;
+    const float px = poi->x, py = poi->y, u = poi->u, v = poi->v;
+    const float W0 = 1.f + poi->ux, W1 = poi->uy, W3 = poi->vx, W4 = 1.f + poi->vy;
+    // only POIs the solver will sample (the entry test passes a non-negative incoming zncc)
+    if (poi->zncc >= 0.f && isfinite(u) && isfinite(v) && isfinite(W0) && isfinite(W1) && isfinite(W3) &&
+        isfinite(W4) && fabsf(u) < w && fabsf(v) < h)
+    {
+      float x0 = 3.4e38f, x1 = -3.4e38f, y0 = 3.4e38f, y1 = -3.4e38f;
+#pragma unroll
+      for (int k = 0; k < 4; ++k)
+      {
+        const float lx = (k & 1) ? (float)rx : (float)-rx, ly = (k & 2) ? (float)ry : (float)-ry;
+        const float gx = px + (W0 * lx + W1 * ly + u), gy = py + (W3 * lx + W4 * ly + v);
+        x0 = fminf(x0, gx); x1 = fmaxf(x1, gx);
+        y0 = fminf(y0, gy); y1 = fmaxf(y1, gy);
+      }
+      if (x0 > -1e6f && x1 < 1e6f && y0 > -1e6f && y1 < 1e6f)
+      {
+        const int ax = (int)floorf(x0) - 1 - kPxMargin, ay = (int)floorf(y0) - 1 - kPxMargin;
+        const int ex = (int)floorf(x1) + 2 + kPxMargin, ey = (int)floorf(y1) + 2 + kPxMargin;
+        ox = ax & ~3;   // floor to a multiple of 4 (two's complement)
+        oy = ay;
+        fits = ex - ox < bx && ey - oy < by;
+      }
+    }
+    if (fits)
+    {
+      fence_proxy_async_smem();   // this warp's reads of the previous window come first
+      if (mode == 2)
+      {
+        mbar_arrive_expect_tx(bar, (uint32_t)(bx * by * sizeof(float)));
+        if (!P.wait_test) tma_load_2d(win, map, ox, oy, bar);
+      }
+    }
+  }
+  ox = __shfl_sync(kFull, ox, 0);
+  oy = __shfl_sync(kFull, oy, 0);
+  fits = __shfl_sync(kFull, fits, 0);
+  T.s = win_f;
+  T.ox = ox;
+  T.oy = oy;
+  T.bx = 0;
+  T.by = 0;
+  if (!fits) return true;
+  if (mode == 2)
+  {
+    const bool done = mbar_wait_bounded(bar, parity, P.wait_polls);
+    parity ^= 1u;
+    if (!__all_sync(kFull, done))
+    {
+      if (lane == 0)
+      {
+        atomicOr(err, 1);
+        mbar_wait_bounded(bar, parity ^ 1u, P.wait_polls);   // the copy in flight, once more
+      }
+      return false;
+    }
+  }
+  else
+  {
+    // rows of the window by the whole warp; pixels outside the image as zero
+    for (int r = 0; r < by; ++r)
+    {
+      const int gy = oy + r;
+      for (int c = lane; c < bx; c += 32)
+      {
+        const int gx = ox + c;
+        px_smem[win_f + r * bx + c] = (gx >= 0 && gx < w && gy >= 0 && gy < h) ? __ldg(P.tar + ((size_t)gy * w + gx)) : 0.f;
+      }
+    }
+    __syncwarp();
+  }
+  T.bx = bx;
+  T.by = by;
+  return true;
+}
+
+// the calling warp's window in the dynamic shared memory (128-byte aligned slots of win_bytes),
+// as a float offset into px_smem and as a shared-window address
+__device__ __forceinline__ int px_window(int warp, size_t win_bytes, uint32_t& addr)
+{
+  const uint32_t base = smem_addr(px_smem);
+  const uint32_t off = ((128u - (base & 127u)) & 127u) + (uint32_t)(warp * win_bytes);
+  addr = base + off;
+  return (int)(off / sizeof(float));
+}
+
+// use_map: 2 windows staged by TMA, 1 staged by warp copies, 0 no windows (every sample from
+// the global plane)
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps))
+    k_icgn_px(IcgnParams P, const __grid_constant__ CUtensorMap map, int use_map, unsigned long long* next, int* err)
+{
+  __shared__ __align__(8) unsigned long long bars[kWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (P.enable && *P.enable == 0) return;
+  uint32_t win = 0;
+  const int win_f = px_window(warp, px_window_bytes(P.rx, P.ry), win);
+  const uint32_t bar = smem_addr(&bars[warp]);
+  if (lane == 0) mbar_init(bar, 1);
+  __syncwarp();
+  uint32_t parity = 0;
+  for (;;)
+  {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(next, 1ull);
+    const int64_t i = (int64_t)__shfl_sync(kFull, t, 0);
+    if (!queue_slot_active(P, i)) return;
+    PixelTile T;
+    if (!px_stage(P, i, lane, use_map, win_f, win, &map, bar, parity, err, T)) return;
+    icgn_solve<true, kSrcPixels, 1, PixelTile>(P, i, lane, T);
+    __syncwarp();   // every lane's reads of this window before the next copy overwrites it
   }
 }
 
@@ -1524,6 +1860,7 @@ struct BatchJob
   const float4* ref_pack;
   int64_t first;   // first queue index of the job
   int w, h, rx, ry;
+  const float* tar = nullptr;   // target plane (pixel sampling)
 };
 
 template <bool kColumn, int kWarps = 4>
@@ -1562,7 +1899,7 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps)) k_icgn_b
     P.conv = conv;
     P.max_iter = max_iter;
     P.iter_sum = iter_sum;
-    icgn_solve<kColumn, false, 1>(P, k, lane);
+    icgn_solve<kColumn, kSrcTable, 1>(P, k, lane);
   }
 }
 
@@ -1577,6 +1914,48 @@ __device__ __forceinline__ int batch_job_of(const BatchJob* __restrict__ jobs, i
     else hi = mid - 1;
   }
   return j;
+}
+
+// Uneven batches under pixel sampling (column-walk jobs): the persistent multi-job drain of
+// k_icgn_batch with k_icgn_px's per-warp windows, staged by warp copies (the jobs' planes
+// differ, so no one tensor map serves them); win_bytes is the window slot of the largest
+// radius in the launch.  Same bits as each job's single-pair pixel solve.
+template <int kWarps>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
+    k_icgn_batch_px(const BatchJob* __restrict__ jobs, int njobs, dic_poi* pois, const PoiRef* poi_ref, int64_t begin,
+                    int64_t end, unsigned long long* next, float conv, float max_iter, unsigned long long* iter_sum,
+                    uint32_t win_bytes)
+{
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t win = 0, parity = 0;
+  const int win_f = px_window(warp, win_bytes, win);
+  for (;;)
+  {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(next, 1ull);
+    const int64_t k = begin + (int64_t)__shfl_sync(kFull, t, 0);
+    if (k >= end) return;
+    const BatchJob& J = jobs[batch_job_of(jobs, njobs, k)];
+    IcgnParams P;
+    P.coef = nullptr;
+    P.tar = J.tar;
+    P.ref_pack = J.ref_pack;
+    P.poi_ref = poi_ref;
+    P.slot = nullptr;
+    P.pois = pois;
+    P.n = end;
+    P.w = J.w;
+    P.h = J.h;
+    P.rx = J.rx;
+    P.ry = J.ry;
+    P.conv = conv;
+    P.max_iter = max_iter;
+    P.iter_sum = iter_sum;
+    PixelTile T;
+    px_stage(P, k, lane, 1, win_f, win, nullptr, 0, parity, nullptr, T);   // warp copies: no wait to time out
+    icgn_solve<true, kSrcPixels, 1, PixelTile>(P, k, lane, T);
+    __syncwarp();
+  }
 }
 
 // The persistent multi-job launch for the jobs whose subsets take the pair walk (33 to 64
@@ -1634,11 +2013,30 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
 // k = k1 + N1*k2.  After full unrolling every twiddle index is a constant, so twiddles are
 // read straight from the constant bank.
 // --------------------------------------------------------------------------------------
+#ifndef DIC_FFT_PACKED
+#define DIC_FFT_PACKED 0
+#endif
+#if DIC_FFT_PACKED
+// complex add / subtract / real scale as packed FP32 pairs (each half rounded as the scalar op)
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b)
+{
+  unsigned long long ra, rb, rd;
+  memcpy(&ra, &a, 8);
+  memcpy(&rb, &b, 8);
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+  float2 d;
+  memcpy(&d, &rd, 8);
+  return d;
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
+#else
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 __device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // -i * a
 
 __host__ __device__ constexpr bool is_prime(int n)

@@ -303,20 +303,38 @@ typedef struct dic_launch_shape
 
 typedef struct dic_tuning
 {
-  dic_launch_shape icgn[3];    /* [0] flat walk, [1] column walk, [2] pair walk */
-  dic_launch_shape batch[3];
+  dic_launch_shape icgn[4];    /* [0] flat walk, [1] column walk, [2] pair walk, [3] column walk with
+                                  pixel sampling (k_icgn_px, see dic_set_sampling) */
+  dic_launch_shape batch[4];   /* [3] the column walk under pixel sampling (k_icgn_batch_px) */
 } dic_tuning;
 
 int dic_set_autotune(dic_engine* engine, int32_t enabled);
 int dic_get_tuning(dic_engine* engine, dic_tuning* out);
 /* No reference counterpart: fixes the single-queue IC-GN launch shape of one subset walk
  * (walk 1: column walk, subsets at most 32 wide; 2: pair walk, 33 to 64; 0: flat walk,
- * wider), e.g. to compare the gather and the TMA-staged tile forms, or one and two warps per
- * POI.  warps_per_cta in {2, 4, 8}, ctas_per_sm >= 0, tile in {0, 1, 2} (tile > 0 only with
- * walk 1), warps_per_poi in {0, 1, 2} (2 only with walk 2); tuned and ms are ignored.
+ * wider; 3: the column walk under pixel sampling), e.g. to compare the gather and the
+ * TMA-staged tile forms, or one and two warps per POI.  warps_per_cta in {2, 4, 8},
+ * ctas_per_sm >= 0, tile in {0, 1, 2} (tile > 0 only with walk 1; with walk 3, tile 1
+ * stages each POI's pixel window in shared memory and 0 reads the plane in global memory,
+ * ctas_per_sm 0 = full occupancy), warps_per_poi in {0, 1, 2} (2 only with walk 2); tuned
+ * and ms are ignored.
  * Results do not depend on the shape.  An enabled autotuner may replace it on the next large
  * queue. */
 int dic_set_launch_shape(dic_engine* engine, int32_t walk, const dic_launch_shape* shape);
+
+/* No reference counterpart: how IC-GN reads the target's bicubic interpolant.
+ * DIC_SAMPLE_TABLE evaluates BicubicBspline::compute's polynomial from the per-texel
+ * coefficient table (src/oc_cubic_bspline.cpp:134-181; 64 B per texel, gathered from L2 per
+ * sample).  DIC_SAMPLE_PIXELS (the default) evaluates the same polynomial regrouped by pixel,
+ * sum_n wy[n] sum_m wx[m] I(iy-1+n, ix-1+m) with the B-spline weights of the BC matrix, from
+ * the 4 x 4 pixels around the texel, each POI's window staged once in shared memory
+ * (k_icgn_px) and no coefficient table built.  It applies to the column walk (subsets at
+ * most 32 columns wide); wider subsets keep the table.  The two differ by float rounding
+ * only (both within the parity gate against the CPU; flags agree); samples on the pixel
+ * lattice give the pixel itself either way.  Takes effect at the next solve. */
+#define DIC_SAMPLE_TABLE 0
+#define DIC_SAMPLE_PIXELS 1
+int dic_set_sampling(dic_engine* engine, int32_t mode);
 
 /* Device-resident variant: pois points to device memory (count records) and the call only
  * enqueues work on the engine stream (dic_get_stats or a stream sync waits for it).  flags
@@ -394,6 +412,12 @@ int dic_read_probe(int32_t device, const void* device_buf, int64_t bytes, int32_
  * 256 threads per SM); *flop_out receives the FLOP count of the launch (2 per FMA).  Timed by
  * the caller with events on `stream`, it gives the FP32 peak the FFTCC kernels are held to. */
 int dic_fma_probe(int32_t device, int32_t iterations, float* device_sink, void* stream, int64_t* flop_out);
+/* No reference counterpart: measurement support.  Enqueues on `stream` one kernel on `device`
+ * whose warps read 32 consecutive floats of shared memory per load (one conflict-free
+ * wavefront), 16 loads per pass, `repeats` passes, 8 CTAs of 256 threads per SM; *bytes_out
+ * receives the bytes the launch loads.  Timed by the caller with events on `stream`, it gives
+ * the shared-memory load bandwidth the pixel-sampled IC-GN (k_icgn_px) is held to. */
+int dic_smem_probe(int32_t device, int32_t repeats, float* device_sink, void* stream, int64_t* bytes_out);
 
 /* Allocation-free pair solve (FFTCC seed + IC-GN).  No counterpart in the reference: its
  * solvers allocate their device buffers themselves.

@@ -164,3 +164,37 @@ def run_sequence(ref, targets, template, radius, skip=True, poi_fallback=True, t
         out.append((q, info))
         prev2, prev = prev, q
     return out
+
+
+LEARNED_MAX_ITER = 6       # IC-GN budget from a proposal seed
+LEARNED_ACCEPT = 0.9       # ZNCC a proposal-seeded result must reach
+
+
+def learned_policy(solver, template, seeds):
+    """The learned-seed policy (no reference counterpart; the engine's enqueue_learned):
+    IC-GN from the proposal's seeds with at most LEARNED_MAX_ITER iterations, then every POI
+    that did not reach ZNCC LEARNED_ACCEPT (failed, NaN, or below it) is solved again from the
+    template by FFTCC + IC-GN with the full budget, and that result replaces the first one.
+    `seeds` holds the six first-order parameters per POI (u, ux, uy, v, vx, vy), e.g. the
+    network's own output, so the oracle runs from the seeds the GPU ran from.  Returns
+    (queue, number of fallback POIs)."""
+    q = template.copy()
+    for k, idx in enumerate((O.P_U, O.P_UX, O.P_UY, O.P_V, O.P_VX, O.P_VY)):
+        q["p"][:, idx] = seeds[:, k]
+    q["r"] = 0.0
+    q["e"] = 0.0
+    full = solver.max_iter
+    solver.max_iter = min(LEARNED_MAX_ITER, full)
+    try:
+        solver.icgn(q)
+    finally:
+        solver.max_iter = full
+    z = q["r"][:, O.R_ZNCC]
+    with np.errstate(invalid="ignore"):
+        cands = np.flatnonzero(~(z >= LEARNED_ACCEPT))
+    if len(cands):
+        fq = np.ascontiguousarray(template[cands])
+        solver.fftcc(fq)
+        solver.icgn(fq)
+        q[cands] = fq
+    return q, len(cands)

@@ -134,14 +134,27 @@ def failure_codes(z):
     return np.where(np.isfinite(z) & (z < 0), z, 0)
 
 
-def flags_agree(cpu, gpu):
+def flags_agree(cpu, gpu, conv=1e-3):
     """Converged/failed flags of two runs over the same queue (dicts or structured arrays with
-    u0, v0, zncc).  Returns (fraction of POIs whose FFTCC seeds agree, number of POIs with the
-    same seed and different flags).  Integer FFTCC peaks may differ only on exact ties of the
-    correlation map; from the same seed the flags must be identical."""
+    u0, v0, zncc, and iteration / convergence where present).  Returns (fraction of POIs whose
+    FFTCC seeds agree, number of POIs with the same seed and different flags, how many of those
+    are iteration-cap boundary cases).  Integer FFTCC peaks may differ only on exact ties of the
+    correlation map; from the same seed the flags must be identical, except where both runs
+    used the whole iteration budget and the last step's size lies within a factor of two of the
+    criterion: whether such a POI ends converged (0) or at the cap (-4) is decided by float
+    rounding of a slowly converging iteration, on either side."""
     same = (np.asarray(cpu["u0"]) == np.asarray(gpu["u0"])) & (np.asarray(cpu["v0"]) == np.asarray(gpu["v0"]))
-    diff = failure_codes(cpu["zncc"]) != failure_codes(gpu["zncc"])
-    return float(same.mean()) if len(same) else 1.0, int((diff & same).sum())
+    fc, fg = failure_codes(cpu["zncc"]), failure_codes(gpu["zncc"])
+    diff = (fc != fg) & same
+    boundary = np.zeros(len(fc), dtype=bool)
+    if all(k in cpu and k in gpu for k in ("iteration", "convergence")):
+        ic, ig = np.asarray(cpu["iteration"]), np.asarray(gpu["iteration"])
+        cap = max(float(np.nanmax(ic)) if len(ic) else 0.0, float(np.nanmax(ig)) if len(ig) else 0.0)
+        cc, cg = np.asarray(cpu["convergence"]), np.asarray(gpu["convergence"])
+        with np.errstate(invalid="ignore"):
+            boundary = ((ic == cap) & (ig == cap) & np.isin(fc, (0, -4)) & np.isin(fg, (0, -4))
+                        & (cc >= 0.5 * conv) & (cc <= 2 * conv) & (cg >= 0.5 * conv) & (cg <= 2 * conv))
+    return float(same.mean()) if len(same) else 1.0, int(diff.sum()), int((diff & boundary).sum())
 
 
 def flag_differences(cpu, gpu, limit=8):
@@ -154,8 +167,12 @@ def flag_differences(cpu, gpu, limit=8):
     return [(float(fc[i]), float(fg[i]), float(it_c[i]), float(it_g[i])) for i in idx]
 
 
-def assert_flags_agree(cpu, gpu, min_same_seed=0.999):
-    same, bad = flags_agree(cpu, gpu)
+def assert_flags_agree(cpu, gpu, min_same_seed=0.999, max_boundary=1e-3):
+    """Same-seed flags identical, up to iteration-cap boundary cases (flags_agree) on at most
+    `max_boundary` of the POIs."""
+    same, bad, boundary = flags_agree(cpu, gpu)
     assert same >= min_same_seed, f"FFTCC seeds agree on {same:.5f} of the POIs"
-    assert bad == 0, (f"{bad} POIs with the same seed have different failure flags "
-                      f"(cpu code, gpu code, cpu iterations, gpu iterations): {flag_differences(cpu, gpu)}")
+    n = max(len(np.asarray(cpu["zncc"])), 1)
+    assert bad == boundary and boundary <= max_boundary * n, (
+        f"{bad} POIs with the same seed have different failure flags, {boundary} of them at the iteration cap "
+        f"(cpu code, gpu code, cpu iterations, gpu iterations): {flag_differences(cpu, gpu)}")

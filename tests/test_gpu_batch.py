@@ -126,8 +126,8 @@ def test_autotuner_keeps_results(dic):
     for x, y in zip(a, b):
         np.testing.assert_array_equal(x.view(np.uint8), y.view(np.uint8))
     t = tuned.tuning()
-    assert t["batch_column"]["tuned"] and t["batch_column"]["warps_per_cta"] in (2, 4, 8), t
-    assert t["batch_column"]["ctas_per_sm"] >= 1 and t["batch_column"]["ms"] > 0, t
+    assert t["batch_column_px"]["tuned"] and t["batch_column_px"]["warps_per_cta"] in (2, 4, 8), t
+    assert t["batch_column_px"]["ctas_per_sm"] >= 1 and t["batch_column_px"]["ms"] > 0, t
 
     pr = speckle.pair_bumps(seed=90, width=512, height=512, max_disp=6.0, max_strain=0.01)
     for r in (15, 20):
@@ -142,5 +142,5 @@ def test_autotuner_keeps_results(dic):
             e.process_pair(qq)
             out.append(qq)
         np.testing.assert_array_equal(out[0].view(np.uint8), out[1].view(np.uint8))
-        key = "icgn_column" if r == 15 else "icgn_pair"
+        key = "icgn_column_px" if r == 15 else "icgn_pair"
         assert e2.tuning()[key]["tuned"] == 1, e2.tuning()

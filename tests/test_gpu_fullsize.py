@@ -93,9 +93,27 @@ def test_stream2048_12bit_sequence_matches_policy_oracle(dic, oracle_mod, stream
         assert rep["fftcc_used"] == int(repaired), (k, rep)
 
 
+def proposal_seeds(dic, net, ref, tar, tmpl):
+    """The network's seeds for one frame (the fused kernel the engine runs), as (n, 6) float32
+    columns u, ux, uy, v, vx, vy."""
+    import torch
+    rf = torch.from_numpy(ref.astype(np.float32)).cuda()
+    tf = torch.from_numpy(tar.astype(np.float32)).cuda()
+    qd = torch.from_numpy(tmpl.view(np.uint8).copy()).cuda()
+    net.seed(rf, tf, qd, len(tmpl))
+    s = qd.cpu().numpy().view(dic.POI_DTYPE)
+    return np.stack([s[k] for k in ("u", "ux", "uy", "v", "vx", "vy")], axis=1).astype(np.float32)
+
+
 def test_crack1024_learned_sequence_matches_oracle(dic, oracle_mod, crack1024):
+    """Displacements against the CPU path (FFTCC + IC-GN, the judge of the proposal); failure
+    flags against the oracle's run of the same learned-seed policy from the same proposal
+    seeds (oracle/frame_policy.learned_policy): a POI's outcome depends on where IC-GN
+    starts, so flags are compared from identical starting points."""
     O = oracle_mod
+    pytest.importorskip("torch")
     from fasticgn_gb300 import proposal, speckle
+    from oracle import frame_policy as FP
     if not proposal.WEIGHTS.exists():
         pytest.skip("no trained weights")
     ref, tars = crack1024
@@ -113,22 +131,23 @@ def test_crack1024_learned_sequence_matches_oracle(dic, oracle_mod, crack1024):
         rep = e.sequence_frame(tar, res)
         got.append((res, rep))
     e.close()
+    seeds = [proposal_seeds(dic, net, ref, tar, tmpl) for tar in tars]
     net.close()
-    _, _, p0, direction = speckle.crack_setup(5, 1024, 1024)
-    near = speckle.crack_distance(tmpl["x"], tmpl["y"], (p0, direction)) <= radius + 2
+    solver = FP.Solver(ref, radius)
     for k, (tar, (g, rep)) in enumerate(zip(tars, got)):
+        solver.set_tar(tar)
         pois = to_oracle(O, tmpl)
-        O.run_pair(ref.astype(np.float32), tar.astype(np.float32), pois, radius)
+        solver.fftcc(pois)
+        solver.icgn(pois)
         cpu = oracle_fields(O, pois)
         r = C.compare_frame(cpu, {"u": g["u"], "v": g["v"], "zncc": g["zncc"]})
         assert r["pass"], (k, r)
-        agree = C.failure_codes(cpu["zncc"]) == C.failure_codes(g["zncc"])
-        # away from the crack the flags agree; POIs whose subsets straddle the displacement
-        # jump have no unique minimum, and a different seed may settle in another one
-        far = np.flatnonzero(~near & ~agree)
-        detail = [(float(C.failure_codes(cpu["zncc"])[i]), float(C.failure_codes(g["zncc"])[i]),
-                   float(pois["r"][i, O.R_ITER]), float(g["iteration"][i]), float(cpu["zncc"][i]), float(g["zncc"][i]))
-                  for i in far[:10]]
-        assert agree[~near].mean() >= 0.999, (k, agree[~near].mean(), detail)
-        assert agree.mean() >= 0.99, (k, agree.mean())
+        same, fallbacks = FP.learned_policy(solver, to_oracle(O, tmpl), seeds[k])
+        fc, fg = C.failure_codes(same["r"][:, O.R_ZNCC]), C.failure_codes(g["zncc"])
+        agree = fc == fg
+        detail = [(float(fc[i]), float(fg[i]), float(same["r"][i, O.R_ITER]), float(g["iteration"][i]))
+                  for i in np.flatnonzero(~agree)[:10]]
+        assert agree.mean() >= 0.999, (k, agree.mean(), detail)
+        # the fallback set is the same policy's: POIs below ZNCC 0.9 after the capped IC-GN
+        assert abs(rep["repaired_candidates"] - fallbacks) <= max(5, 0.002 * len(tmpl)), (rep, fallbacks)
         assert rep["repaired_candidates"] < 0.2 * len(tmpl), rep

@@ -1,4 +1,4 @@
-"""GPU tests of the TMA-staged IC-GN (k_icgn_tile): each POI's result, iteration count and
+"""GPU tests of the TMA-staged IC-GN (k_icgn_tile, table sampling): each POI's result, iteration count and
 flags are bit-identical to the gather form's, whether its chunk's block fits the tile (texels
 from shared memory), partly fits (texels outside it from the global table) or does not fit at
 all (the whole chunk from the global table), also inside a graph-captured sequence frame and
@@ -14,6 +14,7 @@ pytestmark = pytest.mark.gpu
 def solve(dic, pr, radius, step, tile=None, autotune=False):
     q = dic.grid_queue(pr.ref.shape[1], pr.ref.shape[0], radius, step)
     e = dic.Engine(radius)
+    e.set_sampling(dic._lib.DIC_SAMPLE_TABLE)
     if tile is not None:
         e.set_launch_shape(True, tile=tile)
     e.set_autotune(autotune)
@@ -47,6 +48,7 @@ def test_tile_form_in_sequence_graph(dic):
     outs = []
     for tile in (None, 1):
         e = dic.Engine(15)
+        e.set_sampling(dic._lib.DIC_SAMPLE_TABLE)
         e.set_graphs(True)
         if tile:
             e.set_launch_shape(True, tile=tile)
@@ -76,7 +78,7 @@ def test_autotuner_times_tile_forms(dic):
 def test_launch_shape_arguments(dic):
     e = dic.Engine(15)
     for kw in (dict(walk=1, tile=3), dict(walk=0, tile=1), dict(walk=2, tile=1),
-               dict(walk=1, warps_per_cta=3), dict(walk=1, ctas_per_sm=-1), dict(walk=3),
+               dict(walk=1, warps_per_cta=3), dict(walk=1, ctas_per_sm=-1), dict(walk=4), dict(walk=3, tile=2),
                dict(walk=1, warps_per_poi=2), dict(walk=2, warps_per_poi=3)):
         with pytest.raises((ValueError, RuntimeError)):
             e.set_launch_shape(**kw)
@@ -97,6 +99,7 @@ def test_tile_copy_timeout_is_reported(dic, monkeypatch):
     monkeypatch.setenv("DIC_TEST_WAIT_FAULT", "1")
     e = dic.Engine(15)
     monkeypatch.delenv("DIC_TEST_WAIT_FAULT")
+    e.set_sampling(_lib.DIC_SAMPLE_TABLE)
     e.set_launch_shape(True, tile=1)
     e.set_autotune(False)
     e.set_ref(pr.ref)

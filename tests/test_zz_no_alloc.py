@@ -36,6 +36,7 @@ def test_noalloc_matches_engine_twice(dic, radius):
     step = 6 if radius <= 16 else 9
     want = dic.grid_queue(w, h, radius, step)
     with dic.Engine(radius) as e:
+        e.set_sampling(_lib.DIC_SAMPLE_TABLE)   # the entry point's IC-GN samples the coefficient table
         e.set_ref(pr.ref)
         e.set_tar(pr.tar)
         e.process_pair(want)
