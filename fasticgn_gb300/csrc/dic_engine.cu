@@ -758,28 +758,37 @@ struct dic_engine
       DIC_CUDA(cudaFuncGetAttributes(&fa, k));   // the dynamic maximum leaves room for the static part
       DIC_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
     };
-    opt_in((const void*)k_icgn_px<2>);
-    opt_in((const void*)k_icgn_px<4>);
-    opt_in((const void*)k_icgn_px<8>);
-    opt_in((const void*)k_icgn_batch_px<2>);
-    opt_in((const void*)k_icgn_batch_px<4>);
-    opt_in((const void*)k_icgn_batch_px<8>);
+    opt_in((const void*)k_icgn_px<2, 2>);
+    opt_in((const void*)k_icgn_px<4, 2>);
+    opt_in((const void*)k_icgn_px<8, 2>);
+    opt_in((const void*)k_icgn_px<2, 1>);
+    opt_in((const void*)k_icgn_px<4, 1>);
+    opt_in((const void*)k_icgn_px<8, 1>);
+    opt_in((const void*)k_icgn_batch_px<2, 2>);
+    opt_in((const void*)k_icgn_batch_px<4, 2>);
+    opt_in((const void*)k_icgn_batch_px<8, 2>);
+    opt_in((const void*)k_icgn_batch_px<2, 1>);
+    opt_in((const void*)k_icgn_batch_px<4, 1>);
+    opt_in((const void*)k_icgn_batch_px<8, 1>);
     px_attr_set = true;
   }
   template <int W>
   static int max_ctas_px(size_t smem)
   {
     int b = 0;
-    DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_px<W>, W * 32, smem));
+    if (smem)
+      DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_px<W, 2>, W * 32, smem));
+    else
+      DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_px<W, 0>, W * 32, smem));
     return b;
   }
   int occupancy_batch_px(int warps, size_t smem)
   {
     px_attributes();
     int b = 0;
-    if (warps == 2) DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<2>, 64, smem));
-    else if (warps == 8) DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<8>, 256, smem));
-    else DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<4>, 128, smem));
+    if (warps == 2) DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<2, 2>, 64, smem));
+    else if (warps == 8) DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<8, 2>, 256, smem));
+    else DIC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_px<4, 2>, 128, smem));
     if (b < 1) throw DicError{DIC_ERR_ARGUMENT, "IC-GN pixel windows of this subset radius do not fit in shared memory"};
     return b;
   }
@@ -829,7 +838,8 @@ struct dic_engine
     m.by = by;
     return &m.map;
   }
-  // shape.tile: 1 stages each POI's pixel window in shared memory, 0 reads the global plane
+  // shape.tile: 1 stages each POI's pixel window in shared memory by TMA (by warp copies where
+  // the plane's row pitch is not a multiple of 16 bytes), 2 by warp copies, 0 reads the global plane
   void launch_px(const IcgnParams& p, const IcgnShape& sh)
   {
     icgn_next.ensure(1);
@@ -841,16 +851,24 @@ struct dic_engine
     const size_t smem = sh.tile ? px_smem(warps, p.rx, p.ry) : 0;
     const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_px(warps, sh.tile != 0, p.rx, p.ry);
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * ctas, (p.n + warps - 1) / warps));
-    const CUtensorMap* m = sh.tile ? tar_map(p.tar, p.w, p.h, px_window_x(p.rx), px_window_y(p.ry)) : nullptr;
+    const CUtensorMap* m = sh.tile == 1 ? tar_map(p.tar, p.w, p.h, px_window_x(p.rx), px_window_y(p.ry)) : nullptr;
     CUtensorMap none{};
     IcgnParams q = p;
     q.wait_polls = wait_polls;
     q.wait_test = wait_test & 1;
     const int mode = sh.tile ? (m ? 2 : 1) : 0;   // 2: TMA, 1: warp copies, 0: no window
-#define DIC_PX_LAUNCH(W) k_icgn_px<W><<<grid, W * 32, smem, stream>>>(q, m ? *m : none, mode, icgn_next.ptr, wait_flag())
-    if (warps == 2) DIC_PX_LAUNCH(2);
-    else if (warps == 8) DIC_PX_LAUNCH(8);
-    else DIC_PX_LAUNCH(4);
+#define DIC_PX_LAUNCH(W, M) k_icgn_px<W, M><<<grid, W * 32, smem, stream>>>(q, m ? *m : none, icgn_next.ptr, wait_flag())
+#define DIC_PX_MODES(W)                       \
+  do                                          \
+  {                                           \
+    if (mode == 2) DIC_PX_LAUNCH(W, 2);      \
+    else if (mode == 1) DIC_PX_LAUNCH(W, 1); \
+    else DIC_PX_LAUNCH(W, 0);                 \
+  } while (0)
+    if (warps == 2) DIC_PX_MODES(2);
+    else if (warps == 8) DIC_PX_MODES(8);
+    else DIC_PX_MODES(4);
+#undef DIC_PX_MODES
 #undef DIC_PX_LAUNCH
   }
   bool tile_attr_set[3] = {};   // per engine, so per device: the shared-memory opt-in of each tile form
@@ -1000,12 +1018,21 @@ struct dic_engine
       const size_t smem = 128 + (size_t)sh.warps * win;
       const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_batch_px(sh.warps, smem);
       const unsigned grid = (unsigned)(sms * ctas);
-#define DIC_BATCH_PX(W)                                                                                            \
-  k_icgn_batch_px<W><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,     \
-                                                     cfg.conv_criterion, mi, b.iter_sum, win)
-      if (sh.warps == 2) DIC_BATCH_PX(2);
-      else if (sh.warps == 8) DIC_BATCH_PX(8);
-      else DIC_BATCH_PX(4);
+#define DIC_BATCH_PX(W, M)                                                                                         \
+  k_icgn_batch_px<W, M><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,  \
+                                                        cfg.conv_criterion, mi, b.iter_sum, win, wait_polls, wait_flag())
+      if (b_col_maps)
+      {
+        if (sh.warps == 2) DIC_BATCH_PX(2, 2);
+        else if (sh.warps == 8) DIC_BATCH_PX(8, 2);
+        else DIC_BATCH_PX(4, 2);
+      }
+      else
+      {
+        if (sh.warps == 2) DIC_BATCH_PX(2, 1);
+        else if (sh.warps == 8) DIC_BATCH_PX(8, 1);
+        else DIC_BATCH_PX(4, 1);
+      }
 #undef DIC_BATCH_PX
       check_launch("k_icgn_batch_px");
       return;
@@ -1078,7 +1105,11 @@ struct dic_engine
     for (int warps : {2, 4, 8})
       for (int persistent = 0; persistent < 2; ++persistent)
         if (walk == kWalkColumnPx)
-          cand.push_back(IcgnShape{warps, 0, 0.f, persistent});   // windows staged, or not
+        {
+          // windows staged by TMA, or not staged; and staged by warp copies
+          cand.push_back(IcgnShape{warps, 0, 0.f, persistent});
+          if (persistent) cand.push_back(IcgnShape{warps, 0, 0.f, 2});
+        }
         else if (walk == kWalkPair)
           for (int pw : {1, 2})
             cand.push_back(IcgnShape{warps, persistent ? occupancy_pair(false, pw, warps) : 0, 0.f, 0, pw});
@@ -1539,6 +1570,9 @@ struct dic_engine
   std::vector<int64_t> b_first;
   int64_t b_total = 0, b_col_end = 0, b_pair_end = 0;
   int b_col_rmax = 0;                   // largest subset radius among the column-walk jobs
+  DevBuf<CUtensorMap> bmaps;            // the jobs' target-plane tensor maps (pixel sampling)
+  bool b_col_maps = false;              // every pixel-sampled job has one (TMA windows), else warp copies
+  std::vector<CUtensorMap> b_maps_host; // their host copy (kept alive for the asynchronous upload)
   // pixel sampling covers the batch's column-walk jobs; the others sample the table
   bool job_table(int radius) const { return sampling != DIC_SAMPLE_PIXELS || walk_of(radius) != kWalkColumn; }
   std::vector<dic_job> b_key;           // jobs of the captured batch graph (device pointers)
@@ -1596,6 +1630,37 @@ struct dic_engine
       }
       table[k] = BatchJob{M.coef.ptr, M.lattice.ptr, M.ref_pack.ptr, b_first[k], J.width, J.height, J.subset_radius,
                           J.subset_radius, M.tar_f32.ptr};
+    }
+    // tensor maps of the pixel-sampled jobs' target planes (window copies by TMA), in device
+    // memory beside the job table
+    bmaps.ensure((size_t)nj);
+    std::vector<TileMap> maps(nj);
+    bool any_map = false;
+    b_col_maps = encode_tiled() != nullptr;
+    for (int k = 0; k < nj; ++k)
+    {
+      const dic_job& J = jobs[b_order[k]];
+      const int r = J.subset_radius;
+      if (job_table(r)) continue;
+      if ((J.width * sizeof(float)) % 16 != 0) b_col_maps = false;
+      if ((J.width * sizeof(float)) % 16 != 0 || !encode_tiled()) continue;
+      const cuuint64_t dims[2] = {(cuuint64_t)J.width, (cuuint64_t)J.height};
+      const cuuint64_t strides[1] = {(cuuint64_t)J.width * sizeof(float)};
+      const cuuint32_t box[2] = {(cuuint32_t)px_window_x(r), (cuuint32_t)px_window_y(r)};
+      const cuuint32_t estr[2] = {1, 1};
+      const CUresult res = encode_tiled()(&maps[k].map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, jobs_mem[k].tar_f32.ptr, dims,
+                                          strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                          CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (res != CUDA_SUCCESS)
+        throw DicError{DIC_ERR_CUDA, "cuTensorMapEncodeTiled failed (" + std::to_string((int)res) + ")"};
+      table[k].map = bmaps.ptr + k;
+      any_map = true;
+    }
+    if (any_map)
+    {
+      b_maps_host.resize(nj);
+      for (int k = 0; k < nj; ++k) b_maps_host[k] = maps[k].map;
+      DIC_CUDA(cudaMemcpyAsync(bmaps.ptr, b_maps_host.data(), sizeof(CUtensorMap) * nj, cudaMemcpyHostToDevice, stream));
     }
     DIC_CUDA(cudaMemcpyAsync(bjobs.ptr, table.data(), sizeof(BatchJob) * nj, cudaMemcpyHostToDevice, stream));
   }
@@ -1945,6 +2010,7 @@ void dic_engine_destroy(dic_engine* e)
   e->bq.release();
   e->bpoi.release();
   e->bjobs.release();
+  e->bmaps.release();
   e->bnext.release();
   e->icgn_next.release();
   e->wait_err.release();
@@ -2477,8 +2543,8 @@ int dic_set_launch_shape(dic_engine* e, int32_t walk, const dic_launch_shape* sh
       if (shape->warps_per_cta != 2 && shape->warps_per_cta != 4 && shape->warps_per_cta != 8)
         throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: warps_per_cta must be 2, 4 or 8"};
       if (shape->ctas_per_sm < 0) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: ctas_per_sm must be >= 0"};
-      if (shape->tile != 0 && shape->tile != 1)
-        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0 or 1 with walk 3"};
+      if (shape->tile < 0 || shape->tile > 2)
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0, 1 or 2 with walk 3"};
       sh = dic_engine::IcgnShape{shape->warps_per_cta, shape->ctas_per_sm, 0.f, shape->tile};
     }
     else if (shape->tile != 0)

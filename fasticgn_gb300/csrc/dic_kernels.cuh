@@ -339,8 +339,9 @@ struct PoiSums
 
 // Entry test, mean (written to rec->t0), and the warp-reduced sums of one POI.  Returns false
 // (after writing valid = 0) when the reference subset leaves the image.
-// (The mean pass reads ref_pack, not the 4-byte grey-level plane: its lines stay in L1 for
-// the second pass; reading the plane instead was slower, 0.60 -> 0.70 ms on the 2048x2048 pair.)
+// (The mean pass re-reads the subset from ref_pack, whose lines the second pass then finds in
+// L1.  Forming the means from precomputed horizontal window sums instead saved 0.01 ms of the
+// 0.60 ms prep on the 2048x2048 pair and cost 0.03 ms to build the sums: dropped.)
 __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, int w, int h, float px, float py,
                                          int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums)
 {
@@ -1718,14 +1719,18 @@ __host__ __device__ constexpr size_t px_window_bytes(int rx, int ry)
 }
 
 // Stages POI i's window for the calling warp (px_smem[win_f...], shared address win) and fills T.
-// mode 2: one TMA copy (map, the warp's mbarrier bar and its phase parity); 1: warp copies;
-// 0: nothing staged (T.bx = 0, every sample from the global plane).  Returns false when the
-// TMA copy did not arrive within P.wait_polls polls: bit 0 of err is set, lane 0 waits once
-// more (bounded) for the copy in flight, and the caller leaves.
-__device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lane, int mode, int win_f,
-                                         uint32_t win, const CUtensorMap* map, uint32_t bar, uint32_t& parity,
-                                         int* err, PixelTile& T)
+// kMode 2: one TMA copy (map, the warp's mbarrier bar and its phase parity); 1: warp copies;
+// 0: nothing staged (T.bx = 0, every sample from the global plane).  A compile-time mode keeps
+// each kernel form to its own staging code (the copy loop's registers slowed the TMA form by
+// 7 % when both were compiled into one kernel).  Returns false when the TMA copy did not
+// arrive within P.wait_polls polls: bit 0 of err is set, lane 0 waits once more (bounded) for
+// the copy in flight, and the caller leaves.
+template <int kMode>
+__device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lane, int win_f, uint32_t win,
+                                         const CUtensorMap* map, uint32_t bar, uint32_t& parity, int* err,
+                                         PixelTile& T)
 {
+  constexpr int mode = kMode;
   const int rx = P.rx, ry = P.ry, w = P.w, h = P.h;
   const int bx = px_window_x(rx), by = px_window_y(ry);
   int ox = 0, oy = 0, fits = 0;
@@ -1791,14 +1796,24 @@ __device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lan
   }
   else
   {
-    // rows of the window by the whole warp; pixels outside the image as zero
-    for (int r = 0; r < by; ++r)
+    // rows of the window by the whole warp, eight rows' loads in flight before their stores;
+    // pixels outside the image as zero
+    for (int c = lane; c < bx; c += 32)
     {
-      const int gy = oy + r;
-      for (int c = lane; c < bx; c += 32)
+      const int gx = ox + c;
+      const bool xin = gx >= 0 && gx < w;
+      for (int r0 = 0; r0 < by; r0 += 8)
       {
-        const int gx = ox + c;
-        px_smem[win_f + r * bx + c] = (gx >= 0 && gx < w && gy >= 0 && gy < h) ? __ldg(P.tar + ((size_t)gy * w + gx)) : 0.f;
+        float v[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+          const int gy = oy + r0 + j;
+          v[j] = (xin && r0 + j < by && gy >= 0 && gy < h) ? __ldg(P.tar + ((size_t)gy * w + gx)) : 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (r0 + j < by) px_smem[win_f + (r0 + j) * bx + c] = v[j];
       }
     }
     __syncwarp();
@@ -1818,11 +1833,11 @@ __device__ __forceinline__ int px_window(int warp, size_t win_bytes, uint32_t& a
   return (int)(off / sizeof(float));
 }
 
-// use_map: 2 windows staged by TMA, 1 staged by warp copies, 0 no windows (every sample from
+// kMode: 2 windows staged by TMA, 1 staged by warp copies, 0 no windows (every sample from
 // the global plane)
-template <int kWarps>
+template <int kWarps, int kMode>
 __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps))
-    k_icgn_px(IcgnParams P, const __grid_constant__ CUtensorMap map, int use_map, unsigned long long* next, int* err)
+    k_icgn_px(IcgnParams P, const __grid_constant__ CUtensorMap map, unsigned long long* next, int* err)
 {
   __shared__ __align__(8) unsigned long long bars[kWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1840,7 +1855,7 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps
     const int64_t i = (int64_t)__shfl_sync(kFull, t, 0);
     if (!queue_slot_active(P, i)) return;
     PixelTile T;
-    if (!px_stage(P, i, lane, use_map, win_f, win, &map, bar, parity, err, T)) return;
+    if (!px_stage<kMode>(P, i, lane, win_f, win, &map, bar, parity, err, T)) return;
     icgn_solve<true, kSrcPixels, 1, PixelTile>(P, i, lane, T);
     __syncwarp();   // every lane's reads of this window before the next copy overwrites it
   }
@@ -1860,7 +1875,8 @@ struct BatchJob
   const float4* ref_pack;
   int64_t first;   // first queue index of the job
   int w, h, rx, ry;
-  const float* tar = nullptr;   // target plane (pixel sampling)
+  const float* tar = nullptr;          // target plane (pixel sampling)
+  const CUtensorMap* map = nullptr;    // its 2-D map in device memory for the window copies (null: warp copies)
 };
 
 template <bool kColumn, int kWarps = 4>
@@ -1917,18 +1933,25 @@ __device__ __forceinline__ int batch_job_of(const BatchJob* __restrict__ jobs, i
 }
 
 // Uneven batches under pixel sampling (column-walk jobs): the persistent multi-job drain of
-// k_icgn_batch with k_icgn_px's per-warp windows, staged by warp copies (the jobs' planes
-// differ, so no one tensor map serves them); win_bytes is the window slot of the largest
-// radius in the launch.  Same bits as each job's single-pair pixel solve.
-template <int kWarps>
+// k_icgn_batch with k_icgn_px's per-warp windows.  Each job's plane has its own tensor map in
+// device memory (BatchJob::map, encoded by the host before the launch), so the windows are
+// TMA copies as in k_icgn_px; a job without one (row pitch not a multiple of 16 bytes) is
+// staged by warp copies.  win_bytes is the window slot of the largest radius in the launch.
+// Same bits as each job's single-pair pixel solve.  The copy wait is bounded as in k_icgn_px.
+// kMode 2: every job has a map (TMA windows); 1: warp copies for all.
+template <int kWarps, int kMode>
 __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
     k_icgn_batch_px(const BatchJob* __restrict__ jobs, int njobs, dic_poi* pois, const PoiRef* poi_ref, int64_t begin,
                     int64_t end, unsigned long long* next, float conv, float max_iter, unsigned long long* iter_sum,
-                    uint32_t win_bytes)
+                    uint32_t win_bytes, uint32_t wait_polls, int* err)
 {
+  __shared__ __align__(8) unsigned long long bars[kWarps];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t win = 0, parity = 0;
   const int win_f = px_window(warp, win_bytes, win);
+  const uint32_t bar = smem_addr(&bars[warp]);
+  if (lane == 0) mbar_init(bar, 1);
+  __syncwarp();
   for (;;)
   {
     unsigned long long t = 0;
@@ -1951,8 +1974,9 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
     P.conv = conv;
     P.max_iter = max_iter;
     P.iter_sum = iter_sum;
+    P.wait_polls = wait_polls;
     PixelTile T;
-    px_stage(P, k, lane, 1, win_f, win, nullptr, 0, parity, nullptr, T);   // warp copies: no wait to time out
+    if (!px_stage<kMode>(P, k, lane, win_f, win, J.map, bar, parity, err, T)) return;
     icgn_solve<true, kSrcPixels, 1, PixelTile>(P, k, lane, T);
     __syncwarp();
   }
@@ -2013,11 +2037,9 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
 // k = k1 + N1*k2.  After full unrolling every twiddle index is a constant, so twiddles are
 // read straight from the constant bank.
 // --------------------------------------------------------------------------------------
-#ifndef DIC_FFT_PACKED
-#define DIC_FFT_PACKED 0
-#endif
-#if DIC_FFT_PACKED
-// complex add / subtract / real scale as packed FP32 pairs (each half rounded as the scalar op)
+// Complex add / subtract / real scale as packed FP32 pairs (add/sub/mul.rn.f32x2, sm_100 and
+// later; each half rounded as the scalar operation): the FFTCC line transforms issue half the
+// instructions for their butterflies (k_fftcc2<30> 0.756 -> 0.674 ms on the 2048x2048 pair).
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b)
 {
@@ -2030,11 +2052,6 @@ __device__ __forceinline__ float2 csub(float2 a, float2 b)
   return d;
 }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
-#else
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
-__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __device__ __forceinline__ float2 mul_mi(float2 a) { return make_float2(a.y, -a.x); }  // -i * a

@@ -314,10 +314,10 @@ int dic_get_tuning(dic_engine* engine, dic_tuning* out);
  * (walk 1: column walk, subsets at most 32 wide; 2: pair walk, 33 to 64; 0: flat walk,
  * wider; 3: the column walk under pixel sampling), e.g. to compare the gather and the
  * TMA-staged tile forms, or one and two warps per POI.  warps_per_cta in {2, 4, 8},
- * ctas_per_sm >= 0, tile in {0, 1, 2} (tile > 0 only with walk 1; with walk 3, tile 1
- * stages each POI's pixel window in shared memory and 0 reads the plane in global memory,
- * ctas_per_sm 0 = full occupancy), warps_per_poi in {0, 1, 2} (2 only with walk 2); tuned
- * and ms are ignored.
+ * ctas_per_sm >= 0, tile in {0, 1, 2} (tile > 0 only with walks 1 and 3; with walk 3, tile
+ * 1 stages each POI's pixel window in shared memory by TMA, 2 by warp copies, and 0 reads
+ * the plane in global memory, ctas_per_sm 0 = full occupancy), warps_per_poi in {0, 1, 2}
+ * (2 only with walk 2); tuned and ms are ignored.
  * Results do not depend on the shape.  An enabled autotuner may replace it on the next large
  * queue. */
 int dic_set_launch_shape(dic_engine* engine, int32_t walk, const dic_launch_shape* shape);

@@ -38,14 +38,14 @@ def solve(dic, ref, tar, radius, step, sampling=None, shape=None, autotune=False
 
 @pytest.mark.parametrize("radius,step,width", [(15, 4, 384), (10, 3, 320), (7, 2, 256), (12, 5, 382), (3, 6, 200)])
 def test_pixel_forms_agree_bit_for_bit(dic, radius, step, width):
-    """Staged (TMA, or warp copies for the 382-wide image) and unstaged windows, every CTA
-    width: identical records.  Displacements up to 9 px with 2 % strain put some updates
+    """Staged (TMA, or warp copies for the 382-wide image; tile 2 always by warp copies) and
+    unstaged windows, every CTA width: identical records.  Displacements up to 9 px with 2 % strain put some updates
     outside their windows (global reads inside a staged solve)."""
     from fasticgn_gb300 import speckle
     pr = speckle.pair_bumps(seed=200 + radius, width=width, height=300, max_disp=9.0, max_strain=0.02)
     want, st0, _ = solve(dic, pr.ref, pr.tar, radius, step, shape=dict(warps_per_cta=4, tile=1))
     for warps in (2, 4, 8):
-        for tile in (0, 1):
+        for tile in (0, 1, 2):
             got, st, tun = solve(dic, pr.ref, pr.tar, radius, step, shape=dict(warps_per_cta=warps, tile=tile))
             assert tun["icgn_column_px"]["warps_per_cta"] == warps and tun["icgn_column_px"]["tile"] == tile
             np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8), err_msg=f"{warps} {tile}")

@@ -78,7 +78,7 @@ def test_autotuner_times_tile_forms(dic):
 def test_launch_shape_arguments(dic):
     e = dic.Engine(15)
     for kw in (dict(walk=1, tile=3), dict(walk=0, tile=1), dict(walk=2, tile=1),
-               dict(walk=1, warps_per_cta=3), dict(walk=1, ctas_per_sm=-1), dict(walk=4), dict(walk=3, tile=2),
+               dict(walk=1, warps_per_cta=3), dict(walk=1, ctas_per_sm=-1), dict(walk=4), dict(walk=3, tile=3),
                dict(walk=1, warps_per_poi=2), dict(walk=2, warps_per_poi=3)):
         with pytest.raises((ValueError, RuntimeError)):
             e.set_launch_shape(**kw)

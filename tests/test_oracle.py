@@ -184,3 +184,39 @@ def test_policy_temporal_seed_rules(oracle_mod):
     assert q["p"][4, O.P_U] == 0.0 and np.all(q["r"][:, O.R_ZNCC] == 0.0)
     q0, c0 = FP.seed_from_previous(tmpl, prev, prev2, temporal=False)
     assert c0 == 0 and q0["p"][0, O.P_U] == np.float32(1.0)
+
+
+def test_policy_learned_seed_fallback(oracle_mod):
+    """The restated learned-seed policy (oracle/frame_policy.learned_policy): POIs whose seeds
+    IC-GN confirms within 6 iterations keep that result; POIs whose seed is far off (the 6-
+    iteration budget runs out, the result leaves the range, or ZNCC ends below 0.9) are solved
+    again from the template by FFTCC + IC-GN, which then equals the plain FFTCC path."""
+    O = oracle_mod
+    from fasticgn_gb300 import speckle
+    from oracle import frame_policy as FP
+    pr = speckle.pair_affine(seed=21, width=192, height=160)
+    ref, tar = pr.ref.astype(np.float32), pr.tar.astype(np.float32)
+    tmpl = O.grid_pois(192, 160, 12, 9)
+    plain = tmpl.copy()
+    solver = FP.Solver(ref, 12)
+    solver.set_tar(tar)
+    solver.fftcc(plain)
+    solver.icgn(plain)
+    ok = plain["r"][:, O.R_ZNCC] >= 0.9
+    assert ok.mean() > 0.8
+    seeds = np.stack([plain["p"][:, k] for k in (O.P_U, O.P_UX, O.P_UY, O.P_V, O.P_VX, O.P_VY)], axis=1)
+    seeds[~ok] = 0.0
+    bad = np.zeros(len(tmpl), dtype=bool)
+    bad[::3] = True                       # a third of the seeds 9 px off: beyond what IC-GN recovers
+    seeds[bad, 0] += 9.0
+    q, fallbacks = FP.learned_policy(solver, tmpl, seeds.astype(np.float32))
+    z = q["r"][:, O.R_ZNCC]
+    good = ok & ~bad
+    # converged seeds: confirmed in a few iterations, at the plain path's solution
+    assert np.all(q["r"][good, O.R_ITER] <= 3)
+    assert np.max(np.abs(q["p"][good, O.P_U] - plain["p"][good, O.P_U])) < 1e-3
+    # the displaced seeds fell back, and their results are the plain path's, bit for bit
+    fb = q["r"][:, O.R_U0] == np.round(q["r"][:, O.R_U0])
+    assert fallbacks >= bad.sum() * 0.9 and np.all(fb[bad & ok])
+    np.testing.assert_array_equal(q[bad & ok].view(np.uint8), plain[bad & ok].view(np.uint8))
+    assert np.all((z[ok] >= 0.9))
