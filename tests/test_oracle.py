@@ -220,3 +220,31 @@ def test_policy_learned_seed_fallback(oracle_mod):
     assert fallbacks >= bad.sum() * 0.9 and np.all(fb[bad & ok])
     np.testing.assert_array_equal(q[bad & ok].view(np.uint8), plain[bad & ok].view(np.uint8))
     assert np.all((z[ok] >= 0.9))
+
+
+def test_flag_agreement_rule():
+    """The flag rule the GPU parity tests apply (tests/dic_checks.py): from the same seed the
+    failure codes must be identical, except for POIs that used the whole iteration budget on
+    both sides with a last step within a factor of two of the criterion (0 against -4)."""
+    n = 2000
+    cpu = {"u0": np.zeros(n, np.float32), "v0": np.zeros(n, np.float32), "zncc": np.full(n, 0.95, np.float32),
+           "iteration": np.full(n, 4.0, np.float32), "convergence": np.full(n, 2e-4, np.float32)}
+    gpu = {k: v.copy() for k, v in cpu.items()}
+    assert C.flags_agree(cpu, gpu) == (1.0, 0, 0)
+    # a cap-boundary flip: both at 10 iterations, last steps 0.9e-3 and 1.1e-3
+    for d, z, c in ((cpu, 0.97, 0.9e-3), (gpu, -4.0, 1.1e-3)):
+        d["iteration"][7] = 10.0
+        d["zncc"][7] = z
+        d["convergence"][7] = c
+    assert C.flags_agree(cpu, gpu) == (1.0, 1, 1)
+    C.assert_flags_agree(cpu, gpu)
+    # a flip away from the cap is a parity failure
+    gpu["zncc"][9] = -5.0
+    assert C.flags_agree(cpu, gpu) == (1.0, 2, 1)
+    with pytest.raises(AssertionError):
+        C.assert_flags_agree(cpu, gpu)
+    # different FFTCC seeds are not compared
+    gpu["zncc"][9] = 0.95
+    gpu["u0"][11] = 1.0
+    gpu["zncc"][11] = -3.0
+    assert C.flags_agree(cpu, gpu)[1:] == (1, 1)
