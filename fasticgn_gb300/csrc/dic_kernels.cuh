@@ -27,9 +27,13 @@ constexpr unsigned kFull = 0xffffffffu;
 #define DIC_PAIR_MAX_WIDTH 64
 #endif
 constexpr int kPairMaxWidth = DIC_PAIR_MAX_WIDTH;
-// Column of lane l in class k of the pair walk: interleaved (2 l + k) or halves (32 k + l).
+// Column of lane l in class k of the pair walk: halves (32 k + l; the default) or interleaved
+// (2 l + k).  Halves keep a warp's texel loads on consecutive columns, one contiguous run per
+// coefficient plane; interleaved classes balance the two classes' lanes but stride the loads
+// by two texels.  Measured on the uneven batch's r 20 / 30 jobs: halves 16.7 ms, interleaved
+// 19.1 ms, the flat walk 17.7 ms; those pairs one at a time 48.6 / 57.9 / 47.5 ms.
 #ifndef DIC_PAIR_HALVES
-#define DIC_PAIR_HALVES 0
+#define DIC_PAIR_HALVES 1
 #endif
 __host__ __device__ constexpr int pair_column(int lane, int k) { return DIC_PAIR_HALVES ? 32 * k + lane : 2 * lane + k; }
 
@@ -1248,8 +1252,8 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps
 
 // --------------------------------------------------------------------------------------
 // Pair walk: IC-GN for subsets of 33 to 64 columns (subset radius 16 to 31), one or two
-// warps per POI.  The columns form two interleaved classes, c = 2 l + k for lane l and
-// class k; each class is walked like the column walk (the lane's lx is constant, so the
+// warps per POI.  The columns form two classes, c = pair_column(l, k) for lane l and class k
+// (the halves 32 k + l); each class is walked like the column walk (the lane's lx is constant, so the
 // lx-weighted sums factor out of the row loop) and butterfly-reduced on its own, and the
 // two class totals are added in class order.  With one warp per POI the warp walks both
 // classes in turn; with two, warp k of the pair walks class k and the pair exchanges its

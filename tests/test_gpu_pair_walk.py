@@ -1,6 +1,6 @@
-"""The pair walk (subsets of 33 to 64 columns, subset radius 16 to 31): two interleaved
-column classes, each reduced on its own and added in class order, walked by one or two
-warps per POI.
+"""The pair walk (subsets of 33 to 64 columns, subset radius 16 to 31): two column classes
+(columns 0-31 and 32 on), each reduced on its own and added in class order, walked by one
+or two warps per POI.
 
 * every launch shape (one or two warps per POI, 2 / 4 / 8 warps per CTA, grid or
   persistent) gives the same bytes;
