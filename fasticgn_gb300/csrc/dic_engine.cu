@@ -411,11 +411,12 @@ struct dic_engine
     check_launch("k_prepare_ref");
   }
   template <typename T>
-  void launch_prepare_tar(bool table)
+  void launch_prepare_tar(bool table, bool pitched)
   {
     dim3 grid((w + kPrepTile - 1) / kPrepTile, (h + kPrepTile - 1) / kPrepTile);
     k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_tar.ptr), w, h, scale(),
-                                               tar_f32.ptr, table ? coef.ptr : nullptr, lattice.ptr);
+                                               tar_f32.ptr, table ? coef.ptr : nullptr, lattice.ptr,
+                                               pitched ? tar_px.ptr : nullptr, px_pitch(w));
     check_launch("k_prepare_tar");
   }
 
@@ -441,14 +442,21 @@ struct dic_engine
   int sampling = DIC_SAMPLE_PIXELS;
   bool pixel_walk() const { return sampling == DIC_SAMPLE_PIXELS && walk_of(cfg.subset_radius_x) == kWalkColumn; }
   bool table_ready = false;   // coef / lattice hold the current target's table
+  // Pixel sampling stages windows by TMA, whose rows must start on 16-byte boundaries: where W
+  // is not a multiple of 4 floats the target is also written with a padded pitch (tar_px).
+  DevBuf<float> tar_px;
+  bool px_ready = false;       // tar_px holds the current target
+  bool pitched_target() const { return pixel_walk() && (w & 3) != 0; }
+  const float* px_plane() const { return pitched_target() ? tar_px.ptr : tar_f32.ptr; }
   // The target's float plane, plus its coefficient table when IC-GN samples the table (or
-  // `table` asks for it).
+  // `table` asks for it), plus the padded-pitch plane pixel sampling needs for odd widths.
   void ensure_tar(bool table = false)
   {
     if (!tar_set) throw DicError{DIC_ERR_STATE, "target image must be set first"};
     if (!ref_set) throw DicError{DIC_ERR_STATE, "reference image must be set first"};
     table = table || !pixel_walk();
-    if (!tar_dirty && (table_ready || !table)) return;
+    const bool pitched = pitched_target();
+    if (!tar_dirty && (table_ready || !table) && (px_ready || !pitched)) return;
     const size_t px = (size_t)w * h;
     tar_f32.ensure(px);
     if (table)
@@ -456,16 +464,18 @@ struct dic_engine
       coef.ensure(px * 4);
       lattice.ensure(px);
     }
+    if (pitched) tar_px.ensure((size_t)px_pitch(w) * h);
     mark(kPhTar, 0);
     switch (tar_dtype)
     {
-      case DIC_U8: launch_prepare_tar<uint8_t>(table); break;
-      case DIC_U16: launch_prepare_tar<uint16_t>(table); break;
-      default: launch_prepare_tar<float>(table); break;
+      case DIC_U8: launch_prepare_tar<uint8_t>(table, pitched); break;
+      case DIC_U16: launch_prepare_tar<uint16_t>(table, pitched); break;
+      default: launch_prepare_tar<float>(table, pitched); break;
     }
     mark(kPhTar, 1);
     tar_dirty = false;
     table_ready = table;
+    px_ready = pitched;
   }
 
   // ---------------------------------------------------------------- layout
@@ -601,7 +611,7 @@ struct dic_engine
   {
     alignas(128) CUtensorMap map;
     const void* base = nullptr;
-    int w = 0, h = 0, bx = 0, by = 0;
+    int w = 0, h = 0, bx = 0, by = 0, pitch = 0;
   };
   TileMap tile_maps[3];
   // Bounded waits inside kernels report here instead of hanging: bit 0, a k_icgn_tile CTA
@@ -812,15 +822,15 @@ struct dic_engine
   }
   // the 2-D map {x, y} of the target plane, box {bx, by} (only for rows of a multiple of 16 bytes)
   TileMap px_map;
-  const CUtensorMap* tar_map(const float* plane, int tw, int th, int bx, int by)
+  const CUtensorMap* tar_map(const float* plane, int tw, int th, int pitch, int bx, int by)
   {
-    if ((tw * sizeof(float)) % 16 != 0) return nullptr;
+    if ((pitch * sizeof(float)) % 16 != 0) return nullptr;
     EncodeTiledFn fn = encode_tiled();
     if (!fn) return nullptr;
     TileMap& m = px_map;
-    if (m.base == plane && m.w == tw && m.h == th && m.bx == bx && m.by == by) return &m.map;
+    if (m.base == plane && m.w == tw && m.h == th && m.pitch == pitch && m.bx == bx && m.by == by) return &m.map;
     const cuuint64_t dims[2] = {(cuuint64_t)tw, (cuuint64_t)th};
-    const cuuint64_t strides[1] = {(cuuint64_t)tw * sizeof(float)};
+    const cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
     const cuuint32_t box[2] = {(cuuint32_t)bx, (cuuint32_t)by};
     const cuuint32_t estr[2] = {1, 1};
     const CUresult r = fn(&m.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(plane), dims, strides, box, estr,
@@ -834,6 +844,7 @@ struct dic_engine
     m.base = plane;
     m.w = tw;
     m.h = th;
+    m.pitch = pitch;
     m.bx = bx;
     m.by = by;
     return &m.map;
@@ -851,7 +862,8 @@ struct dic_engine
     const size_t smem = sh.tile ? px_smem(warps, p.rx, p.ry) : 0;
     const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_px(warps, sh.tile != 0, p.rx, p.ry);
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * ctas, (p.n + warps - 1) / warps));
-    const CUtensorMap* m = sh.tile == 1 ? tar_map(p.tar, p.w, p.h, px_window_x(p.rx), px_window_y(p.ry)) : nullptr;
+    const CUtensorMap* m =
+        sh.tile == 1 ? tar_map(p.tar, p.w, p.h, px_pitch(p.w), px_window_x(p.rx), px_window_y(p.ry)) : nullptr;
     CUtensorMap none{};
     IcgnParams q = p;
     q.wait_polls = wait_polls;
@@ -1222,7 +1234,7 @@ struct dic_engine
     p.enable = enable;
     p.coef = coef.ptr;
     p.lattice = lattice.ptr;
-    p.tar = tar_f32.ptr;
+    p.tar = px_plane();
     p.ref_pack = ref_pack.ptr;
     p.poi_ref = poi_ref.ptr;
     p.slot = d_slots;
@@ -1539,11 +1551,11 @@ struct dic_engine
     DevBuf<unsigned char> raw_ref, raw_tar;
     DevBuf<float> ref_f32, tar_f32;
     DevBuf<float4> ref_pack, coef;
-    DevBuf<float> lattice;
+    DevBuf<float> lattice, tar_px;
     void release()
     {
       raw_ref.release(); raw_tar.release(); ref_f32.release(); tar_f32.release(); ref_pack.release(); coef.release();
-      lattice.release();
+      lattice.release(); tar_px.release();
     }
   };
   std::vector<JobBufs> jobs_mem;
@@ -1553,14 +1565,16 @@ struct dic_engine
   DevBuf<unsigned long long> bnext;
 
   template <typename T>
-  void prep_planes(const unsigned char* raw_r, const unsigned char* raw_t, int bw, int bh, JobBufs& J, bool table)
+  void prep_planes(const unsigned char* raw_r, const unsigned char* raw_t, int bw, int bh, JobBufs& J, bool table,
+                   bool pitched)
   {
     dim3 grid((bw + kPrepTile - 1) / kPrepTile, (bh + kPrepTile - 1) / kPrepTile);
     k_prepare_ref<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_r), bw, bh, scale(), J.ref_f32.ptr,
                                                J.ref_pack.ptr);
     check_launch("k_prepare_ref");
     k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_t), bw, bh, scale(), J.tar_f32.ptr,
-                                               table ? J.coef.ptr : nullptr, J.lattice.ptr);
+                                               table ? J.coef.ptr : nullptr, J.lattice.ptr,
+                                               pitched ? J.tar_px.ptr : nullptr, px_pitch(bw));
     check_launch("k_prepare_tar");
   }
 
@@ -1575,6 +1589,8 @@ struct dic_engine
   std::vector<CUtensorMap> b_maps_host; // their host copy (kept alive for the asynchronous upload)
   // pixel sampling covers the batch's column-walk jobs; the others sample the table
   bool job_table(int radius) const { return sampling != DIC_SAMPLE_PIXELS || walk_of(radius) != kWalkColumn; }
+  // a pixel-sampled job whose width is not a multiple of 4 floats gets a padded-pitch plane
+  bool job_pitched(int radius, int width) const { return !job_table(radius) && (width & 3) != 0; }
   std::vector<dic_job> b_key;           // jobs of the captured batch graph (device pointers)
   bool b_key_seen = false;
   cudaGraphExec_t batch_graph = nullptr;
@@ -1628,8 +1644,10 @@ struct dic_engine
         M.coef.ensure(px * 4);
         M.lattice.ensure(px);
       }
+      const bool pitched = job_pitched(J.subset_radius, J.width);
+      if (pitched) M.tar_px.ensure((size_t)px_pitch(J.width) * J.height);
       table[k] = BatchJob{M.coef.ptr, M.lattice.ptr, M.ref_pack.ptr, b_first[k], J.width, J.height, J.subset_radius,
-                          J.subset_radius, M.tar_f32.ptr};
+                          J.subset_radius, pitched ? M.tar_px.ptr : M.tar_f32.ptr};
     }
     // tensor maps of the pixel-sampled jobs' target planes (window copies by TMA), in device
     // memory beside the job table
@@ -1641,14 +1659,12 @@ struct dic_engine
     {
       const dic_job& J = jobs[b_order[k]];
       const int r = J.subset_radius;
-      if (job_table(r)) continue;
-      if ((J.width * sizeof(float)) % 16 != 0) b_col_maps = false;
-      if ((J.width * sizeof(float)) % 16 != 0 || !encode_tiled()) continue;
+      if (job_table(r) || !encode_tiled()) continue;
       const cuuint64_t dims[2] = {(cuuint64_t)J.width, (cuuint64_t)J.height};
-      const cuuint64_t strides[1] = {(cuuint64_t)J.width * sizeof(float)};
+      const cuuint64_t strides[1] = {(cuuint64_t)px_pitch(J.width) * sizeof(float)};
       const cuuint32_t box[2] = {(cuuint32_t)px_window_x(r), (cuuint32_t)px_window_y(r)};
       const cuuint32_t estr[2] = {1, 1};
-      const CUresult res = encode_tiled()(&maps[k].map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, jobs_mem[k].tar_f32.ptr, dims,
+      const CUresult res = encode_tiled()(&maps[k].map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(table[k].tar), dims,
                                           strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                           CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
       if (res != CUDA_SUCCESS)
@@ -1681,12 +1697,12 @@ struct dic_engine
                                  (size_t)J.width * es, J.height, in_kind, stream));
       DIC_CUDA(cudaMemcpy2DAsync(M.raw_tar.ptr, (size_t)J.width * es, J.tar, (size_t)J.row_stride_bytes,
                                  (size_t)J.width * es, J.height, in_kind, stream));
-      const bool table = job_table(J.subset_radius);
+      const bool table = job_table(J.subset_radius), pitched = job_pitched(J.subset_radius, J.width);
       switch (J.dtype)
       {
-        case DIC_U8: prep_planes<uint8_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table); break;
-        case DIC_U16: prep_planes<uint16_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table); break;
-        default: prep_planes<float>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table); break;
+        case DIC_U8: prep_planes<uint8_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched); break;
+        case DIC_U16: prep_planes<uint16_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched); break;
+        default: prep_planes<float>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched); break;
       }
       if (J.count == 0) continue;
       const int r = J.subset_radius;
@@ -1988,6 +2004,7 @@ void dic_engine_destroy(dic_engine* e)
   e->raw_tar.release();
   e->ref_f32.release();
   e->tar_f32.release();
+  e->tar_px.release();
   e->ref_pack.release();
   e->coef.release();
   e->lattice.release();

@@ -159,10 +159,13 @@ __global__ void __launch_bounds__(256) k_prepare_ref(const T* __restrict__ raw, 
 // IC-GN time on GB300, same values (the texel-major 64 B layout spreads a warp load over
 // 16 cache lines).
 // --------------------------------------------------------------------------------------
+// tar_px (nullable): the float plane again with rows of `pitch` floats (a multiple of 4), for
+// the pixel-sampled IC-GN's TMA windows when W itself is not a multiple of 4.
 template <typename T>
 __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, int w, int h, float scale,
                                                      float* __restrict__ tar_f32,
-                                                     float4* __restrict__ coef, float* __restrict__ lattice = nullptr)
+                                                     float4* __restrict__ coef, float* __restrict__ lattice = nullptr,
+                                                     float* __restrict__ tar_px = nullptr, int pitch = 0)
 {
   __shared__ float tile[kPrepTile + 3][kPrepTile + 3 + 1];
   const int bx = blockIdx.x * kPrepTile, by = blockIdx.y * kPrepTile;
@@ -180,6 +183,7 @@ __global__ void __launch_bounds__(256) k_prepare_tar(const T* __restrict__ raw, 
   if (x >= w || y >= h) return;
   const size_t o = (size_t)y * w + x;
   tar_f32[o] = tile[ty + 1][tx + 1];
+  if (tar_px) tar_px[(size_t)y * pitch + x] = tile[ty + 1][tx + 1];
   if (!coef) return;   // pixel sampling: no table
   const size_t plane = (size_t)w * h;
   float4* dst = coef + 2 * o;   // row k at dst[(k >> 1) * 2 * plane + (k & 1)]
@@ -696,7 +700,7 @@ struct IcgnParams
 {
   const float4* coef;      // tar B-spline table: 2 planes of W*H texels x 2 float4
   const float* lattice = nullptr;   // coefficient [0][0] of every texel (nullable, see on_lattice)
-  const float* tar = nullptr;       // target plane (pixel sampling, k_icgn_px)
+  const float* tar = nullptr;       // target plane (pixel sampling, k_icgn_px): rows of px_pitch(w) floats
   const float4* ref_pack;  // {ref, gx, gy, 0}
   const PoiRef* poi_ref;   // per layout slot
   const int64_t* slot;     // queue index -> layout slot (nullptr: identity)
@@ -839,6 +843,11 @@ __device__ __forceinline__ float sample_bspline_tile(const CoefTile& T, const fl
 // rounding, not bit for bit.  At d = 0 the weights are exactly (0, 1, 0, 0) (BC's last row),
 // so a sample on the lattice returns the pixel itself, as the table does.
 // --------------------------------------------------------------------------------------
+// Row pitch (floats) of the target plane the pixel-sampled IC-GN reads: W rounded up to a
+// multiple of 4, so every row starts on the 16-byte boundary TMA needs (the plane itself where
+// W is a multiple of 4, a padded copy otherwise).
+__host__ __device__ constexpr int px_pitch(int w) { return (w + 3) & ~3; }
+
 // The weights of both axes at once, d = (dx, dy): w[m] = (wx[m], wy[m]).  Packed FP32 pairs
 // (fma.rn.f32x2, sm_100 and later) round each half like the scalar operation, so the
 // values are the scalar Horner forms' bit for bit, in half the instructions.
@@ -859,7 +868,9 @@ __device__ __forceinline__ void bspline_weights2(float2 d, float2 (&w)[4])
 extern __shared__ __align__(128) float px_smem[];
 
 // A warp's block of the target plane in shared memory: pixels [ox, ox + bx) x [oy, oy + by),
-// rows of bx floats, from px_smem[s].  bx = 0: nothing staged.
+// rows of bx floats, from px_smem[s].  bx = 0: nothing staged.  (A compile-time row pitch,
+// which turns the 16 loads of a sample into one base plus immediate offsets, was measured
+// slower: 3.06 against 2.77 ms of IC-GN on the 2048x2048 pair.)
 struct PixelTile
 {
   int s = 0;
@@ -888,7 +899,7 @@ __device__ __forceinline__ void pixel_setup(float gxp, float gyp, float2 (&w)[4]
   bspline_weights2(make_float2(gxp - fx, gyp - fy), w);
 }
 
-__device__ __forceinline__ float sample_pixels(const PixelTile& T, const float* __restrict__ tar, int w, float gxp,
+__device__ __forceinline__ float sample_pixels(const PixelTile& T, const float* __restrict__ tar, int pitch, float gxp,
                                                float gyp)
 {
   float2 wt[4];
@@ -901,8 +912,8 @@ __device__ __forceinline__ float sample_pixels(const PixelTile& T, const float* 
     const int row = T.bx;
     return eval_pixels(wt, [&](int n, int m) { return px_smem[a + n * row + m]; });
   }
-  const float* g = tar + ((size_t)(iy - 1) * w + (ix - 1));   // images < 2^31 pixels
-  return eval_pixels(wt, [&](int n, int m) { return __ldg(g + (size_t)n * w + m); });
+  const float* g = tar + ((size_t)(iy - 1) * pitch + (ix - 1));   // images < 2^31 pixels
+  return eval_pixels(wt, [&](int n, int m) { return __ldg(g + (size_t)n * pitch + m); });
 }
 
 // A sample whose support lies in the window (the caller has checked): no tests.
@@ -940,13 +951,60 @@ __device__ __forceinline__ bool window_covers(const float (&W)[6], float px, flo
 }
 
 // the pixel at an integer sample (the lattice case of sample_pixels)
-__device__ __forceinline__ float pixel_at(const PixelTile& T, const float* __restrict__ tar, int w, float gxp,
+__device__ __forceinline__ float pixel_at(const PixelTile& T, const float* __restrict__ tar, int pitch, float gxp,
                                           float gyp)
 {
   const int ix = (int)gxp, iy = (int)gyp;
   const int tx = ix - T.ox, ty = iy - T.oy;
   if (tx >= 0 && ty >= 0 && tx < T.bx && ty < T.by) return px_smem[T.s + ty * T.bx + tx];
-  return __ldg(tar + ((size_t)iy * w + ix));
+  return __ldg(tar + ((size_t)iy * pitch + ix));
+}
+
+// The column walk's checked row loop under pixel sampling, for iterations whose samples are
+// not all inside the range and the window: per-sample range tests, window or global-plane
+// reads, the same sums in the same order as the fast loop.  Returns the sums (A0, A1, A2, B0,
+// B2, B3, B5) and whether a sample left the range.  (The fast loop's code generation is
+// sensitive to this rare path: written as this function and inlined, k_icgn_px runs 2.80 ms
+// on the 2048x2048 pair; as a call, 2.84 ms; as the same loop written inside icgn_solve with
+// the padded pitch, 3.00 ms.)
+struct ColumnSums
+{
+  float A0, A1, A2, B0, B2, B3, B5;
+  int bad;
+};
+__device__ __forceinline__ ColumnSums px_column_checked(const float* __restrict__ tar, int w, int h, PixelTile T,
+                                                     const float4* __restrict__ ref_col, float px, float py, float W0,
+                                                     float W1, float W2, float W3, float W4, float W5, float flx_col,
+                                                     float t0, int ry, int lat)
+{
+  ColumnSums c{0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0};
+  const float xmax = (float)(w - 2), ymax = (float)(h - 2);
+  const int pitch = px_pitch(w);
+  const float ax = fmaf(W0, flx_col, W2), ay = fmaf(W3, flx_col, W5);
+  for (int r = 0; r < 2 * ry + 1; ++r)
+  {
+    const float fly = (float)(r - ry);
+    const float gxp = px + fmaf(W1, fly, ax);
+    const float gyp = py + fmaf(W4, fly, ay);
+    if (!(gxp >= 1.f && gyp >= 1.f && gxp < xmax && gyp < ymax))
+    {
+      c.bad = 1;
+      continue;
+    }
+    const float t = lat ? pixel_at(T, tar, pitch, gxp, gyp) : sample_pixels(T, tar, pitch, gxp, gyp);
+    const float4 rv = __ldg(ref_col + (size_t)r * w);
+    const float tau = t - t0;
+    const float rc = rv.x - t0;
+    c.A0 += tau;
+    c.A1 = fmaf(tau, tau, c.A1);
+    c.A2 = fmaf(tau, rc, c.A2);
+    const float gt = __fmul_rn(rv.y, tau), ht = __fmul_rn(rv.z, tau);
+    c.B0 = __fadd_rn(c.B0, gt);
+    c.B2 = fmaf(gt, fly, c.B2);
+    c.B3 = __fadd_rn(c.B3, ht);
+    c.B5 = fmaf(ht, fly, c.B5);
+  }
+  return c;
 }
 
 // Sample sources of icgn_solve: the global coefficient table, a coefficient block staged
@@ -1051,6 +1109,22 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
             }
           }
       }
+      else if (kSrc == kSrcPixels && col_active)
+      {
+        if constexpr (kSrc == kSrcPixels)
+        {
+          const ColumnSums c = px_column_checked(P.tar, w, h, T, ref_col, px, py, W[0], W[1], W[2], W[3], W[4], W[5],
+                                                 flx_col, t0, ry, lat ? 1 : 0);
+          A0 = c.A0;
+          A1 = c.A1;
+          A2 = c.A2;
+          B[0] = c.B0;
+          B[2] = c.B2;
+          B[3] = c.B3;
+          B[5] = c.B5;
+          bad = c.bad != 0;
+        }
+      }
       else if (col_active)
       {
         const float ax = fmaf(W[0], flx_col, W[2]), ay = fmaf(W[3], flx_col, W[5]);
@@ -1068,8 +1142,6 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
           float t;
           if constexpr (kSrc == kSrcCoefTile)
             t = sample_bspline_tile(T, coef, plane, w, gxp, gyp);
-          else if constexpr (kSrc == kSrcPixels)
-            t = lat ? pixel_at(T, P.tar, w, gxp, gyp) : sample_pixels(T, P.tar, w, gxp, gyp);
           else if (lat)
             t = __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp));
           else
@@ -1103,7 +1175,7 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
         {
           float t;
           if constexpr (kSrc == kSrcPixels)
-            t = lat ? pixel_at(T, P.tar, w, gxp, gyp) : sample_pixels(T, P.tar, w, gxp, gyp);
+            t = lat ? pixel_at(T, P.tar, px_pitch(w), gxp, gyp) : sample_pixels(T, P.tar, px_pitch(w), gxp, gyp);
           else
             t = lat ? __ldg(P.lattice + ((size_t)(int)gyp * w + (int)gxp)) : sample_bspline(coef, plane, w, gxp, gyp);
           const float4 rv = __ldg(ref_pack + (size_t)(cy + ly) * w + (cx + lx));
@@ -1712,6 +1784,10 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
 // (bounded) for the copy still in flight, and leaves.
 // --------------------------------------------------------------------------------------
 constexpr int kPxMargin = 1;
+#ifndef DIC_PX_ROW_UNROLL
+#define DIC_PX_ROW_UNROLL 1
+#endif
+constexpr int kPxRowUnroll = DIC_PX_ROW_UNROLL;   // rows of the pixel walk unrolled together
 
 // window of one warp for a subset radius: the support of the subset with the margin and
 // the x alignment slack, x rounded up to a multiple of 4 pixels
@@ -1813,7 +1889,7 @@ __device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lan
         for (int j = 0; j < 8; ++j)
         {
           const int gy = oy + r0 + j;
-          v[j] = (xin && r0 + j < by && gy >= 0 && gy < h) ? __ldg(P.tar + ((size_t)gy * w + gx)) : 0.f;
+          v[j] = (xin && r0 + j < by && gy >= 0 && gy < h) ? __ldg(P.tar + ((size_t)gy * px_pitch(w) + gx)) : 0.f;
         }
 #pragma unroll
         for (int j = 0; j < 8; ++j)
@@ -1860,7 +1936,7 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps
     if (!queue_slot_active(P, i)) return;
     PixelTile T;
     if (!px_stage<kMode>(P, i, lane, win_f, win, &map, bar, parity, err, T)) return;
-    icgn_solve<true, kSrcPixels, 1, PixelTile>(P, i, lane, T);
+    icgn_solve<true, kSrcPixels, kPxRowUnroll, PixelTile>(P, i, lane, T);
     __syncwarp();   // every lane's reads of this window before the next copy overwrites it
   }
 }
@@ -1879,7 +1955,7 @@ struct BatchJob
   const float4* ref_pack;
   int64_t first;   // first queue index of the job
   int w, h, rx, ry;
-  const float* tar = nullptr;          // target plane (pixel sampling)
+  const float* tar = nullptr;          // target plane (pixel sampling), rows of px_pitch(w) floats
   const CUtensorMap* map = nullptr;    // its 2-D map in device memory for the window copies (null: warp copies)
 };
 
@@ -1942,9 +2018,10 @@ __device__ __forceinline__ int batch_job_of(const BatchJob* __restrict__ jobs, i
 // TMA copies as in k_icgn_px; a job without one (row pitch not a multiple of 16 bytes) is
 // staged by warp copies.  win_bytes is the window slot of the largest radius in the launch.
 // Same bits as each job's single-pair pixel solve.  The copy wait is bounded as in k_icgn_px.
-// kMode 2: every job has a map (TMA windows); 1: warp copies for all.
+// kMode 2: every job has a map (TMA windows); 1: warp copies for all.  32 resident warps per
+// SM (64 registers, no spills), as k_icgn_px.
 template <int kWarps, int kMode>
-__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
+__global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps))
     k_icgn_batch_px(const BatchJob* __restrict__ jobs, int njobs, dic_poi* pois, const PoiRef* poi_ref, int64_t begin,
                     int64_t end, unsigned long long* next, float conv, float max_iter, unsigned long long* iter_sum,
                     uint32_t win_bytes, uint32_t wait_polls, int* err)
