@@ -40,7 +40,7 @@ def cli(dic):
 ZERO_TEXTURE_CODE = pytest.mark.xfail(
     strict=True,
     reason="the gate expects -3 for zero-texture subsets from a CUDA build (the reference CUDA kernel's extra "
-           "reference-side rejection); this engine follows the CPU path, the north star's judge, which gives -5 "
+           "reference-side rejection); this engine follows the CPU path, the parity oracle, which gives -5 "
            "(tests/test_gpu_parity.py::test_zero_texture_cpu_rule)")
 
 
