@@ -1182,20 +1182,21 @@ struct dic_engine
 
   // ---------------------------------------------------------------- solvers
   // FFTCC launch for an explicit plane pair and (square) radius.
-  void fftcc_launch(const FftccParams& p, int r)
+  void fftcc_launch(const FftccParams& p, int r, cudaStream_t on = nullptr)
   {
+    cudaStream_t st = on ? on : stream;
     const unsigned blocks = (unsigned)((p.n + 3) / 4);
     switch (2 * r)
     {
 #define DIC_FFTCC_CASE2(M) \
-  case M: k_fftcc2<M><<<(unsigned)((p.n + 3) / 4), 64, 0, stream>>>(p); break;
+  case M: k_fftcc2<M><<<(unsigned)((p.n + 3) / 4), 64, 0, st>>>(p); break;
       DIC_FFTCC_CASE2(8) DIC_FFTCC_CASE2(10) DIC_FFTCC_CASE2(12) DIC_FFTCC_CASE2(14) DIC_FFTCC_CASE2(16)
       DIC_FFTCC_CASE2(18) DIC_FFTCC_CASE2(20) DIC_FFTCC_CASE2(22) DIC_FFTCC_CASE2(24) DIC_FFTCC_CASE2(26)
       DIC_FFTCC_CASE2(28) DIC_FFTCC_CASE2(30)
 #undef DIC_FFTCC_CASE2
-      case 32: k_fftcc<32><<<blocks, 128, 0, stream>>>(p); break;
+      case 32: k_fftcc<32><<<blocks, 128, 0, st>>>(p); break;
 #define DIC_FFTCC_BIG(M) \
-  case M: k_fftcc_big<M><<<(unsigned)p.n, 128, (size_t)M * (M + 1) * sizeof(float2), stream>>>(p); break;
+  case M: k_fftcc_big<M><<<(unsigned)p.n, 128, (size_t)M * (M + 1) * sizeof(float2), st>>>(p); break;
       // 2r = 2 x prime (34, 38, 46, 58, 62) stays on the line-DFT kernel below
       DIC_FFTCC_BIG(36) DIC_FFTCC_BIG(40) DIC_FFTCC_BIG(42) DIC_FFTCC_BIG(44) DIC_FFTCC_BIG(48)
       DIC_FFTCC_BIG(50) DIC_FFTCC_BIG(52) DIC_FFTCC_BIG(54) DIC_FFTCC_BIG(56) DIC_FFTCC_BIG(60) DIC_FFTCC_BIG(64)
@@ -1203,7 +1204,7 @@ struct dic_engine
       default:
         if (r < 1 || 2 * r > kMaxTwiddleN)
           throw DicError{DIC_ERR_ARGUMENT, "FFTCC supports subset radius 1..32 on this engine"};
-        k_fftcc_large<<<(unsigned)p.n, 256, (size_t)2 * (2 * r) * (2 * r + 1) * sizeof(float2), stream>>>(p, 2 * r);
+        k_fftcc_large<<<(unsigned)p.n, 256, (size_t)2 * (2 * r) * (2 * r + 1) * sizeof(float2), st>>>(p, 2 * r);
     }
     check_launch("k_fftcc");
   }
@@ -1566,15 +1567,15 @@ struct dic_engine
 
   template <typename T>
   void prep_planes(const unsigned char* raw_r, const unsigned char* raw_t, int bw, int bh, JobBufs& J, bool table,
-                   bool pitched)
+                   bool pitched, cudaStream_t st)
   {
     dim3 grid((bw + kPrepTile - 1) / kPrepTile, (bh + kPrepTile - 1) / kPrepTile);
-    k_prepare_ref<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_r), bw, bh, scale(), J.ref_f32.ptr,
+    k_prepare_ref<T><<<grid, 256, 0, st>>>(reinterpret_cast<const T*>(raw_r), bw, bh, scale(), J.ref_f32.ptr,
                                                J.ref_pack.ptr);
     check_launch("k_prepare_ref");
-    k_prepare_tar<T><<<grid, 256, 0, stream>>>(reinterpret_cast<const T*>(raw_t), bw, bh, scale(), J.tar_f32.ptr,
-                                               table ? J.coef.ptr : nullptr, J.lattice.ptr,
-                                               pitched ? J.tar_px.ptr : nullptr, px_pitch(bw));
+    k_prepare_tar<T><<<grid, 256, 0, st>>>(reinterpret_cast<const T*>(raw_t), bw, bh, scale(), J.tar_f32.ptr,
+                                           table ? J.coef.ptr : nullptr, J.lattice.ptr,
+                                           pitched ? J.tar_px.ptr : nullptr, px_pitch(bw));
     check_launch("k_prepare_tar");
   }
 
@@ -1683,36 +1684,74 @@ struct dic_engine
 
   // Everything from pixel upload to results, on the engine stream (capturable when the
   // pixels and queues are device memory).
+  // Side streams of the batch's per-job preparation: each job's chain (uploads, planes,
+  // per-POI prep, FFTCC) touches only that job's buffers and queue slice, so the chains run
+  // side by side (in a captured batch they become parallel graph branches) and small jobs'
+  // kernels share the GPU instead of running one after another.
+  static constexpr int kBatchLanes = 4;
+  cudaStream_t b_lane[kBatchLanes] = {};
+  cudaEvent_t b_fork = nullptr, b_join[kBatchLanes] = {};
+  void batch_lanes()
+  {
+    if (b_fork) return;
+    for (int l = 0; l < kBatchLanes; ++l)
+    {
+      DIC_CUDA(cudaStreamCreateWithFlags(&b_lane[l], cudaStreamNonBlocking));
+      DIC_CUDA(cudaEventCreateWithFlags(&b_join[l], cudaEventDisableTiming));
+    }
+    DIC_CUDA(cudaEventCreateWithFlags(&b_fork, cudaEventDisableTiming));
+  }
+  void release_batch_lanes()
+  {
+    for (int l = 0; l < kBatchLanes; ++l)
+    {
+      if (b_lane[l]) cudaStreamDestroy(b_lane[l]);
+      if (b_join[l]) cudaEventDestroy(b_join[l]);
+      b_lane[l] = nullptr;
+      b_join[l] = nullptr;
+    }
+    if (b_fork) cudaEventDestroy(b_fork);
+    b_fork = nullptr;
+  }
   void enqueue_batch(const dic_job* jobs, int nj, bool on_device)
   {
     const cudaMemcpyKind in_kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     mark(kPhFrame, 0);
     DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
+    batch_lanes();
+    DIC_CUDA(cudaEventRecord(b_fork, stream));
+    for (int l = 0; l < kBatchLanes; ++l) DIC_CUDA(cudaStreamWaitEvent(b_lane[l], b_fork, 0));
     for (int k = 0; k < nj; ++k)
     {
       const dic_job& J = jobs[b_order[k]];
       JobBufs& M = jobs_mem[k];
+      cudaStream_t st = b_lane[k % kBatchLanes];
       const int es = dtype_size(J.dtype);
       DIC_CUDA(cudaMemcpy2DAsync(M.raw_ref.ptr, (size_t)J.width * es, J.ref, (size_t)J.row_stride_bytes,
-                                 (size_t)J.width * es, J.height, in_kind, stream));
+                                 (size_t)J.width * es, J.height, in_kind, st));
       DIC_CUDA(cudaMemcpy2DAsync(M.raw_tar.ptr, (size_t)J.width * es, J.tar, (size_t)J.row_stride_bytes,
-                                 (size_t)J.width * es, J.height, in_kind, stream));
+                                 (size_t)J.width * es, J.height, in_kind, st));
       const bool table = job_table(J.subset_radius), pitched = job_pitched(J.subset_radius, J.width);
       switch (J.dtype)
       {
-        case DIC_U8: prep_planes<uint8_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched); break;
-        case DIC_U16: prep_planes<uint16_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched); break;
-        default: prep_planes<float>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched); break;
+        case DIC_U8: prep_planes<uint8_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched, st); break;
+        case DIC_U16: prep_planes<uint16_t>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched, st); break;
+        default: prep_planes<float>(M.raw_ref.ptr, M.raw_tar.ptr, J.width, J.height, M, table, pitched, st); break;
       }
       if (J.count == 0) continue;
       const int r = J.subset_radius;
       dic_poi* q = bq.ptr + b_first[k];
-      DIC_CUDA(cudaMemcpyAsync(q, J.pois, sizeof(dic_poi) * J.count, in_kind, stream));
-      k_poi_prepare32<<<(unsigned)((J.count + kPrepPois - 1) / kPrepPois), kPrepWarps * 32, 0, stream>>>(
+      DIC_CUDA(cudaMemcpyAsync(q, J.pois, sizeof(dic_poi) * J.count, in_kind, st));
+      k_poi_prepare32<<<(unsigned)((J.count + kPrepPois - 1) / kPrepPois), kPrepWarps * 32, 0, st>>>(
           M.ref_pack.ptr, J.width, J.height, q, J.count, r, r, bpoi.ptr + b_first[k]);
       check_launch("k_poi_prepare32");
       FftccParams fp{M.ref_f32.ptr, M.tar_f32.ptr, q, J.count, J.width, J.height};
-      fftcc_launch(fp, r);
+      fftcc_launch(fp, r, st);
+    }
+    for (int l = 0; l < kBatchLanes; ++l)
+    {
+      DIC_CUDA(cudaEventRecord(b_join[l], b_lane[l]));
+      DIC_CUDA(cudaStreamWaitEvent(stream, b_join[l], 0));
     }
     DIC_CUDA(cudaMemsetAsync(bnext.ptr, 0, 3 * sizeof(unsigned long long), stream));
     BatchLaunch col{bjobs.ptr, nj, bq.ptr, bpoi.ptr, 0, b_col_end, bnext.ptr, counters.ptr};
@@ -2033,6 +2072,7 @@ void dic_engine_destroy(dic_engine* e)
   e->wait_err.release();
   e->tune_q.release();
   e->release_staging();
+  e->release_batch_lanes();
   e->release_frame_outputs();
   e->release_queue_upload();
   for (int p = 0; p < kPhCount; ++p)
