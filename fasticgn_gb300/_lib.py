@@ -72,7 +72,7 @@ class DicLaunchShape(ctypes.Structure):
 
 
 class DicTuning(ctypes.Structure):
-    _fields_ = [("icgn", DicLaunchShape * 4), ("batch", DicLaunchShape * 4)]
+    _fields_ = [("icgn", DicLaunchShape * 5), ("batch", DicLaunchShape * 5)]
 
 
 class DicStats(ctypes.Structure):

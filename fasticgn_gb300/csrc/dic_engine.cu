@@ -438,9 +438,17 @@ struct dic_engine
     ref_dirty = false;
   }
   // Sampling of the target in IC-GN (DIC_SAMPLE_*): the B-spline coefficient table, or the
-  // pixels themselves (column walk; other walks keep the table).
+  // pixels themselves (column and pair walks; the flat walk keeps the table).
   int sampling = DIC_SAMPLE_PIXELS;
-  bool pixel_walk() const { return sampling == DIC_SAMPLE_PIXELS && walk_of(cfg.subset_radius_x) == kWalkColumn; }
+  bool pixel_radius(int rx) const { return sampling == DIC_SAMPLE_PIXELS && walk_of(rx) != kWalkFlat; }
+  bool pixel_walk() const { return pixel_radius(cfg.subset_radius_x); }
+  // the launch kind (shape slot) of a radius's IC-GN under the current sampling
+  int icgn_walk(int rx) const
+  {
+    const int wk = walk_of(rx);
+    if (!pixel_radius(rx)) return wk;
+    return wk == kWalkColumn ? kWalkColumnPx : kWalkPairPx;
+  }
   bool table_ready = false;   // coef / lattice hold the current target's table
   // Pixel sampling stages windows by TMA, whose rows must start on 16-byte boundaries: where W
   // is not a multiple of 4 floats the target is also written with a padded pitch (tar_px).
@@ -549,8 +557,8 @@ struct dic_engine
     {
       mark(kPhPoi, 0);
       const unsigned blocks = (unsigned)((n + kPrepPois - 1) / kPrepPois);
-      k_poi_prepare32<<<blocks, kPrepWarps * 32, 0, stream>>>(ref_pack.ptr, w, h, src, n, cfg.subset_radius_x,
-                                                              cfg.subset_radius_y, poi_ref.ptr);
+      k_poi_prepare32<<<blocks, kPrepWarps * 32, 0, stream>>>(ref_pack.ptr, ref_f32.ptr, w, h, src, n,
+                                                              cfg.subset_radius_x, cfg.subset_radius_y, poi_ref.ptr);
       check_launch("k_poi_prepare32");
       mark(kPhPoi, 1);
     }
@@ -573,8 +581,9 @@ struct dic_engine
     int poi_warps = 1;       // pair walk: warps per POI
   };
   static constexpr int kWalkFlat = 0, kWalkColumn = 1, kWalkPair = 2;
-  // the column walk's launches under pixel sampling (k_icgn_px), tuned separately
-  static constexpr int kWalkColumnPx = 3;
+  // the column and pair walks' launches under pixel sampling (k_icgn_px, k_icgn_pair_px and
+  // their batch forms), tuned separately
+  static constexpr int kWalkColumnPx = 3, kWalkPairPx = 4, kWalks = 5;
   // the subset walk of a radius: column walk up to 32 columns, pair walk up to 64, else flat
   static int walk_of(int rx)
   {
@@ -692,9 +701,9 @@ struct dic_engine
   // of its L1 wavefronts on the 2048² pair, 3.73 ms against 3.59 ms persistent with the
   // four-plane table); the autotuner still times both forms.  shape[0]: single queues,
   // shape[1]: batches.
-  IcgnShape shape[2][4] = {{{4, 8, 0.f}, {4, 8, 0.f}, {4, 8, 0.f}, {4, 0, 0.f, 1}},
-                           {{4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}}};
-  bool tuned[2][4] = {};
+  IcgnShape shape[2][kWalks] = {{{4, 8, 0.f}, {4, 8, 0.f}, {4, 8, 0.f}, {4, 0, 0.f, 1}, {4, 0, 0.f, 1, 2}},
+                                {{4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {4, 0, 0.f, 0, 2}}};
+  bool tuned[2][kWalks] = {};
   DevBuf<dic_poi> tune_q;
   cudaEvent_t tune_ev[2] = {};
 
@@ -780,6 +789,17 @@ struct dic_engine
     opt_in((const void*)k_icgn_batch_px<2, 1>);
     opt_in((const void*)k_icgn_batch_px<4, 1>);
     opt_in((const void*)k_icgn_batch_px<8, 1>);
+#define DIC_PAIR_PX_OPT(PW, W)                                \
+  opt_in((const void*)k_icgn_pair_px<PW, W, 2>);              \
+  opt_in((const void*)k_icgn_pair_px<PW, W, 1>);              \
+  opt_in((const void*)k_icgn_batch_pair_px<PW, W, 2>)
+    DIC_PAIR_PX_OPT(1, 2);
+    DIC_PAIR_PX_OPT(1, 4);
+    DIC_PAIR_PX_OPT(1, 8);
+    DIC_PAIR_PX_OPT(2, 2);
+    DIC_PAIR_PX_OPT(2, 4);
+    DIC_PAIR_PX_OPT(2, 8);
+#undef DIC_PAIR_PX_OPT
     px_attr_set = true;
   }
   template <int W>
@@ -883,6 +903,88 @@ struct dic_engine
 #undef DIC_PX_MODES
 #undef DIC_PX_LAUNCH
   }
+  // Pair walk under pixel sampling: the dynamic shared memory of one CTA (a window per POI slot)
+  // and its resident CTAs per SM (cached per form, width and size).
+  static size_t pair_px_smem(int warps, int poi_warps, size_t win) { return 128 + (size_t)(warps / poi_warps) * win; }
+  template <int PW, int W>
+  static int max_ctas_pair_px(bool batch, size_t smem)
+  {
+    int b = 0;
+    if (batch)
+      DIC_CUDA(smem ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_pair_px<PW, W, 2>, W * 32, smem)
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_batch_pair_px<PW, W, 0>, W * 32, 0));
+    else
+      DIC_CUDA(smem ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_pair_px<PW, W, 2>, W * 32, smem)
+                    : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_icgn_pair_px<PW, W, 0>, W * 32, 0));
+    return b;
+  }
+  struct PairPxOcc
+  {
+    int batch, poi_warps, warps;
+    size_t smem;
+    int ctas;
+  };
+  std::vector<PairPxOcc> pair_px_occ;
+  int occupancy_pair_px(bool batch, int poi_warps, int warps, size_t smem)
+  {
+    for (const PairPxOcc& o : pair_px_occ)
+      if (o.batch == (batch ? 1 : 0) && o.poi_warps == poi_warps && o.warps == warps && o.smem == smem) return o.ctas;
+    px_attributes();
+    int b;
+    if (poi_warps == 2)
+      b = warps == 2 ? max_ctas_pair_px<2, 2>(batch, smem) : warps == 8 ? max_ctas_pair_px<2, 8>(batch, smem)
+                                                                           : max_ctas_pair_px<2, 4>(batch, smem);
+    else
+      b = warps == 2 ? max_ctas_pair_px<1, 2>(batch, smem) : warps == 8 ? max_ctas_pair_px<1, 8>(batch, smem)
+                                                                           : max_ctas_pair_px<1, 4>(batch, smem);
+    if (b < 1) throw DicError{DIC_ERR_ARGUMENT, "IC-GN pixel windows of this subset radius do not fit in shared memory"};
+    pair_px_occ.push_back(PairPxOcc{batch ? 1 : 0, poi_warps, warps, smem, b});
+    return b;
+  }
+  // shape.tile as in launch_px: 1 TMA windows (warp copies where no map), 2 warp copies, 0 none;
+  // shape.poi_warps 1 or 2
+  void launch_pair_px(const IcgnParams& p, const IcgnShape& sh)
+  {
+    icgn_next.ensure(1);
+    DIC_CUDA(cudaMemsetAsync(icgn_next.ptr, 0, sizeof(unsigned long long), stream));
+    int sms = 0;
+    DIC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cfg.device));
+    const int warps = sh.warps, pw = sh.poi_warps == 2 ? 2 : 1, slots = warps / pw;
+    px_attributes();
+    const size_t smem = sh.tile ? pair_px_smem(warps, pw, px_window_bytes(p.rx, p.ry)) : 0;
+    const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_pair_px(false, pw, warps, smem);
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * ctas, (p.n + slots - 1) / slots));
+    const CUtensorMap* m =
+        sh.tile == 1 ? tar_map(p.tar, p.w, p.h, px_pitch(p.w), px_window_x(p.rx), px_window_y(p.ry)) : nullptr;
+    CUtensorMap none{};
+    IcgnParams q = p;
+    q.wait_polls = wait_polls;
+    q.wait_test = wait_test & 1;
+    const int mode = sh.tile ? (m ? 2 : 1) : 0;
+#define DIC_PAIR_PX_LAUNCH(PW, W, M) \
+  k_icgn_pair_px<PW, W, M><<<grid, W * 32, smem, stream>>>(q, m ? *m : none, icgn_next.ptr, wait_flag())
+#define DIC_PAIR_PX_MODES(PW, W)                     \
+  do                                                 \
+  {                                                  \
+    if (mode == 2) DIC_PAIR_PX_LAUNCH(PW, W, 2);     \
+    else if (mode == 1) DIC_PAIR_PX_LAUNCH(PW, W, 1); \
+    else DIC_PAIR_PX_LAUNCH(PW, W, 0);               \
+  } while (0)
+    if (pw == 2)
+    {
+      if (warps == 2) DIC_PAIR_PX_MODES(2, 2);
+      else if (warps == 8) DIC_PAIR_PX_MODES(2, 8);
+      else DIC_PAIR_PX_MODES(2, 4);
+    }
+    else
+    {
+      if (warps == 2) DIC_PAIR_PX_MODES(1, 2);
+      else if (warps == 8) DIC_PAIR_PX_MODES(1, 8);
+      else DIC_PAIR_PX_MODES(1, 4);
+    }
+#undef DIC_PAIR_PX_MODES
+#undef DIC_PAIR_PX_LAUNCH
+  }
   bool tile_attr_set[3] = {};   // per engine, so per device: the shared-memory opt-in of each tile form
   template <int W, int BX, int BY>
   void launch_tile(const IcgnParams& p, int kind, int sms)
@@ -949,6 +1051,11 @@ struct dic_engine
     if (walk == kWalkColumnPx)
     {
       launch_px(p, sh);
+      return;
+    }
+    if (walk == kWalkPairPx)
+    {
+      launch_pair_px(p, sh);
       return;
     }
     if (walk == kWalkPair)
@@ -1049,6 +1156,42 @@ struct dic_engine
       check_launch("k_icgn_batch_px");
       return;
     }
+    if (walk == kWalkPairPx)
+    {
+      // windows sized for the largest radius of the launch's jobs
+      px_attributes();
+      const int pw = sh.poi_warps == 2 ? 2 : 1;
+      const uint32_t win = (uint32_t)px_window_bytes(b_pair_rmax, b_pair_rmax);
+      const size_t smem = b_col_maps ? pair_px_smem(sh.warps, pw, win) : 0;
+      const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_pair_px(true, pw, sh.warps, smem);
+      const unsigned grid = (unsigned)(sms * ctas);
+#define DIC_BATCH_PAIR_PX(PW, W, M)                                                                                  \
+  k_icgn_batch_pair_px<PW, W, M><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, \
+                                                                 b.next, cfg.conv_criterion, mi, b.iter_sum, win,     \
+                                                                 wait_polls, wait_flag())
+#define DIC_BATCH_PAIR_PX_W(PW)                                \
+  do                                                           \
+  {                                                            \
+    if (b_col_maps)                                            \
+    {                                                          \
+      if (sh.warps == 2) DIC_BATCH_PAIR_PX(PW, 2, 2);          \
+      else if (sh.warps == 8) DIC_BATCH_PAIR_PX(PW, 8, 2);     \
+      else DIC_BATCH_PAIR_PX(PW, 4, 2);                        \
+    }                                                          \
+    else                                                       \
+    {                                                          \
+      if (sh.warps == 2) DIC_BATCH_PAIR_PX(PW, 2, 0);          \
+      else if (sh.warps == 8) DIC_BATCH_PAIR_PX(PW, 8, 0);     \
+      else DIC_BATCH_PAIR_PX(PW, 4, 0);                        \
+    }                                                          \
+  } while (0)
+      if (pw == 2) DIC_BATCH_PAIR_PX_W(2);
+      else DIC_BATCH_PAIR_PX_W(1);
+#undef DIC_BATCH_PAIR_PX_W
+#undef DIC_BATCH_PAIR_PX
+      check_launch("k_icgn_batch_pair_px");
+      return;
+    }
     const unsigned grid = (unsigned)(sms * sh.ctas_per_sm);
     if (walk == kWalkPair)
     {
@@ -1125,6 +1268,13 @@ struct dic_engine
         else if (walk == kWalkPair)
           for (int pw : {1, 2})
             cand.push_back(IcgnShape{warps, persistent ? occupancy_pair(false, pw, warps) : 0, 0.f, 0, pw});
+        else if (walk == kWalkPairPx)
+        {
+          // windows staged by TMA or not staged, one or two warps per POI (always persistent)
+          if (persistent)
+            for (int pw : {1, 2})
+              for (int tile : {1, 0}) cand.push_back(IcgnShape{warps, 0, 0.f, tile, pw});
+        }
         else
           cand.push_back(IcgnShape{warps, persistent ? occupancy_single(column, warps) : 0, 0.f, 0});
     // the TMA-staged tile forms (column walk, where the driver provides tensor maps)
@@ -1156,11 +1306,15 @@ struct dic_engine
     for (int warps : {2, 4, 8})
       for (int pw : {1, 2})
       {
-        if (walk != kWalkPair && pw == 2) continue;
-        const int full = walk == kWalkColumnPx
-                             ? occupancy_batch_px(warps, 128 + (size_t)warps * px_window_bytes(b_col_rmax, b_col_rmax))
-                             : walk == kWalkPair ? occupancy_pair(true, pw, warps)
-                                                 : occupancy(true, walk == kWalkColumn, warps);
+        if (walk != kWalkPair && walk != kWalkPairPx && pw == 2) continue;
+        const int full =
+            walk == kWalkColumnPx
+                ? occupancy_batch_px(warps, 128 + (size_t)warps * px_window_bytes(b_col_rmax, b_col_rmax))
+            : walk == kWalkPairPx
+                ? occupancy_pair_px(true, pw, warps,
+                                    b_col_maps ? pair_px_smem(warps, pw, px_window_bytes(b_pair_rmax, b_pair_rmax)) : 0)
+            : walk == kWalkPair ? occupancy_pair(true, pw, warps)
+                                : occupancy(true, walk == kWalkColumn, warps);
         for (int ctas : {full, std::max(1, (3 * full) / 4)})
         {
           const IcgnShape sh{warps, ctas, 0.f, 0, pw};
@@ -1248,7 +1402,7 @@ struct dic_engine
     p.conv = cfg.conv_criterion;
     p.max_iter = (float)(max_iter_override > 0 ? max_iter_override : cfg.max_iteration);
     p.iter_sum = counters.ptr;
-    const int walk = pixel_walk() ? kWalkColumnPx : walk_of(p.rx);
+    const int walk = icgn_walk(p.rx);
     if (autotune && !tuned[0][walk] && n >= kTuneMinPois && !capturing()) tune_icgn(p, walk);
     mark(kPhIcgn, 0);
     launch_icgn(p, walk, shape[0][walk]);
@@ -1585,11 +1739,12 @@ struct dic_engine
   std::vector<int64_t> b_first;
   int64_t b_total = 0, b_col_end = 0, b_pair_end = 0;
   int b_col_rmax = 0;                   // largest subset radius among the column-walk jobs
+  int b_pair_rmax = 0;                  // and among the pair-walk jobs
   DevBuf<CUtensorMap> bmaps;            // the jobs' target-plane tensor maps (pixel sampling)
-  bool b_col_maps = false;              // every pixel-sampled job has one (TMA windows), else warp copies
+  bool b_col_maps = false;              // every pixel-sampled job has one (TMA windows), else warp copies / none
   std::vector<CUtensorMap> b_maps_host; // their host copy (kept alive for the asynchronous upload)
-  // pixel sampling covers the batch's column-walk jobs; the others sample the table
-  bool job_table(int radius) const { return sampling != DIC_SAMPLE_PIXELS || walk_of(radius) != kWalkColumn; }
+  // pixel sampling covers the batch's column- and pair-walk jobs; the flat walk's sample the table
+  bool job_table(int radius) const { return !pixel_radius(radius); }
   // a pixel-sampled job whose width is not a multiple of 4 floats gets a padded-pitch plane
   bool job_pitched(int radius, int width) const { return !job_table(radius) && (width & 3) != 0; }
   std::vector<dic_job> b_key;           // jobs of the captured batch graph (device pointers)
@@ -1612,6 +1767,7 @@ struct dic_engine
     b_col_end = 0;
     b_pair_end = 0;
     b_col_rmax = 0;
+    b_pair_rmax = 0;
     for (int k = 0; k < nj; ++k)
     {
       const dic_job& J = jobs[b_order[k]];
@@ -1620,6 +1776,7 @@ struct dic_engine
       const int r = rank(b_order[k]);
       if (r == 0) b_col_end = b_total;
       if (r == 0) b_col_rmax = std::max(b_col_rmax, J.subset_radius);
+      if (r == 1) b_pair_rmax = std::max(b_pair_rmax, J.subset_radius);
       if (r <= 1) b_pair_end = b_total;
     }
     if ((int)jobs_mem.size() < nj) jobs_mem.resize(nj);
@@ -1743,7 +1900,7 @@ struct dic_engine
       dic_poi* q = bq.ptr + b_first[k];
       DIC_CUDA(cudaMemcpyAsync(q, J.pois, sizeof(dic_poi) * J.count, in_kind, st));
       k_poi_prepare32<<<(unsigned)((J.count + kPrepPois - 1) / kPrepPois), kPrepWarps * 32, 0, st>>>(
-          M.ref_pack.ptr, J.width, J.height, q, J.count, r, r, bpoi.ptr + b_first[k]);
+          M.ref_pack.ptr, M.ref_f32.ptr, J.width, J.height, q, J.count, r, r, bpoi.ptr + b_first[k]);
       check_launch("k_poi_prepare32");
       FftccParams fp{M.ref_f32.ptr, M.tar_f32.ptr, q, J.count, J.width, J.height};
       fftcc_launch(fp, r, st);
@@ -1759,15 +1916,16 @@ struct dic_engine
     BatchLaunch flat{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_pair_end, b_total, bnext.ptr + 1, counters.ptr};
     const bool cap = capturing();
     const int col_walk = sampling == DIC_SAMPLE_PIXELS ? kWalkColumnPx : kWalkColumn;
+    const int pair_walk = sampling == DIC_SAMPLE_PIXELS ? kWalkPairPx : kWalkPair;
     if (autotune && !cap)
     {
       if (b_col_end >= kTuneMinPois && !tuned[1][col_walk]) tune_batch(col, col_walk, b_total);
-      if (b_pair_end - b_col_end >= kTuneMinPois && !tuned[1][kWalkPair]) tune_batch(pair, kWalkPair, b_total);
+      if (b_pair_end - b_col_end >= kTuneMinPois && !tuned[1][pair_walk]) tune_batch(pair, pair_walk, b_total);
       if (b_total - b_pair_end >= kTuneMinPois && !tuned[1][kWalkFlat]) tune_batch(flat, kWalkFlat, b_total);
     }
     mark(kPhIcgn, 0);
     if (b_col_end > 0) launch_batch(col, col_walk, shape[1][col_walk]);
-    if (b_pair_end > b_col_end) launch_batch(pair, kWalkPair, shape[1][kWalkPair]);
+    if (b_pair_end > b_col_end) launch_batch(pair, pair_walk, shape[1][pair_walk]);
     if (b_total > b_pair_end) launch_batch(flat, kWalkFlat, shape[1][kWalkFlat]);
     mark(kPhIcgn, 1);
     for (int k = 0; k < nj; ++k)
@@ -2574,7 +2732,7 @@ int dic_get_tuning(dic_engine* e, dic_tuning* out)
   return guarded(e, [&] {
     if (!out) throw DicError{DIC_ERR_ARGUMENT, "get_tuning: null output"};
     for (int pers = 0; pers < 2; ++pers)
-      for (int walk = 0; walk < 4; ++walk)
+      for (int walk = 0; walk < dic_engine::kWalks; ++walk)
       {
         dic_launch_shape& d = pers ? out->batch[walk] : out->icgn[walk];
         const auto& s = e->shape[pers][walk];
@@ -2583,7 +2741,7 @@ int dic_get_tuning(dic_engine* e, dic_tuning* out)
         d.tuned = e->tuned[pers][walk] ? 1 : 0;
         d.ms = s.ms;
         d.tile = s.tile;
-        d.warps_per_poi = walk == dic_engine::kWalkPair ? s.poi_warps : 1;
+        d.warps_per_poi = walk == dic_engine::kWalkPair || walk == dic_engine::kWalkPairPx ? s.poi_warps : 1;
       }
   }, false);
 }
@@ -2592,17 +2750,21 @@ int dic_set_launch_shape(dic_engine* e, int32_t walk, const dic_launch_shape* sh
 {
   return guarded(e, [&] {
     if (!shape) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: null shape"};
-    if (walk < 0 || walk > 3)
-      throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: walk must be 0 (flat), 1 (column), 2 (pair) or 3 (column, pixel sampling)"};
+    if (walk < 0 || walk >= dic_engine::kWalks)
+      throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: walk must be 0 (flat), 1 (column), 2 (pair), 3 (column, "
+                                       "pixel sampling) or 4 (pair, pixel sampling)"};
     dic_engine::IcgnShape sh;
-    if (walk == dic_engine::kWalkColumnPx)
+    if (walk == dic_engine::kWalkColumnPx || walk == dic_engine::kWalkPairPx)
     {
       if (shape->warps_per_cta != 2 && shape->warps_per_cta != 4 && shape->warps_per_cta != 8)
         throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: warps_per_cta must be 2, 4 or 8"};
       if (shape->ctas_per_sm < 0) throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: ctas_per_sm must be >= 0"};
       if (shape->tile < 0 || shape->tile > 2)
-        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0, 1 or 2 with walk 3"};
-      sh = dic_engine::IcgnShape{shape->warps_per_cta, shape->ctas_per_sm, 0.f, shape->tile};
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: tile must be 0, 1 or 2 with walks 3 and 4"};
+      const int pw = shape->warps_per_poi == 0 ? 1 : shape->warps_per_poi;
+      if (pw != 1 && !(pw == 2 && walk == dic_engine::kWalkPairPx))
+        throw DicError{DIC_ERR_ARGUMENT, "set_launch_shape: warps_per_poi must be 1, or 2 with the pair walks"};
+      sh = dic_engine::IcgnShape{shape->warps_per_cta, shape->ctas_per_sm, 0.f, shape->tile, pw};
     }
     else if (shape->tile != 0)
     {
@@ -3152,7 +3314,7 @@ extern "C" int dic_process_pair_noalloc(const dic_config* cfg, const void* d_ref
     }
     constexpr int wpb = 4;
     const unsigned blocks = (unsigned)((n + wpb - 1) / wpb);
-    k_poi_prepare<<<blocks, wpb * 32, 0, s>>>(ref_pack, w, h, d_pois, n, r, r, poi_ref);
+    k_poi_prepare<<<blocks, wpb * 32, 0, s>>>(ref_pack, ref_f32, w, h, d_pois, n, r, r, poi_ref);
     FftccParams fp{ref_f32, tar_f32, d_pois, n, w, h};
     switch (2 * r)
     {

@@ -346,12 +346,25 @@ struct PoiSums
 };
 
 // Entry test, mean (written to rec->t0), and the warp-reduced sums of one POI.  Returns false
-// (after writing valid = 0) when the reference subset leaves the image.
-// (The mean pass re-reads the subset from ref_pack, whose lines the second pass then finds in
-// L1.  Forming the means from precomputed horizontal window sums instead saved 0.01 ms of the
-// 0.60 ms prep on the 2048x2048 pair and cost 0.03 ms to build the sums: dropped.)
-__device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, int w, int h, float px, float py,
-                                         int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums)
+// (after writing valid = 0) when the reference subset leaves the image.  The mean pass reads
+// the grey levels from the float plane ref_plane (the same values as ref_pack's .x, 4 B per
+// sample instead of a 16-byte stride).  (Forming the means from precomputed horizontal window
+// sums instead saved 0.01 ms of the 0.60 ms prep on the 2048x2048 pair and cost 0.03 ms to
+// build the sums: dropped.)
+#ifndef DIC_PREP_MEAN_PLANE
+#define DIC_PREP_MEAN_PLANE 1
+#endif
+__device__ __forceinline__ float ref_grey(const float4* __restrict__ ref_pack, const float* __restrict__ ref_plane,
+                                         size_t o)
+{
+  if constexpr (DIC_PREP_MEAN_PLANE != 0)
+    return __ldg(ref_plane + o);
+  else
+    return __ldg(&ref_pack[o].x);
+}
+__device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, const float* __restrict__ ref_plane,
+                                         int w, int h, float px, float py, int rx, int ry, int lane,
+                                         PoiRef* __restrict__ rec, PoiSums& out_sums)
 {
   // Entry-test geometry of src/oc_icgn.cpp:184-185.
   if (!(py - ry >= 0 && px - rx >= 0 && py + ry <= h - 1 && px + rx <= w - 1))
@@ -368,9 +381,10 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
   for (int t = 0; t < 21; ++t) H[t] = 0.f;
   if (sw <= 32)
   {
-    const float4* col = ref_pack + (size_t)(cy - ry) * w + cx + (lane - rx);
+    const size_t col0 = (size_t)(cy - ry) * w + cx + (lane - rx);
+    const float4* col = ref_pack + col0;
     if (lane < sw)
-      for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&col[(size_t)r * w].x);
+      for (int r = 0; r < 2 * ry + 1; ++r) sum += ref_grey(ref_pack, ref_plane, col0 + (size_t)r * w);
     sum = warp_sum(sum);
     const float t0 = sum / (float)size;
     float Qxx[3] = {0.f, 0.f, 0.f}, Qyy[3] = {0.f, 0.f, 0.f}, Qxy[3] = {0.f, 0.f, 0.f};
@@ -429,13 +443,14 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
     // Pair walk (33 to 64 columns): column classes c = 2 lane + k, each walked like the
     // column walk and butterfly-reduced on its own, class totals added in class order --
     // the order in which the IC-GN pair walk forms its target-side sums.
-    const float4* base = ref_pack + (size_t)(cy - ry) * w + cx - rx;
+    const size_t base0 = (size_t)(cy - ry) * w + cx - rx;
+    const float4* base = ref_pack + base0;
 #pragma unroll
     for (int k = 0; k < 2; ++k)
     {
       const int c = pair_column(lane, k);
       if (c < sw)
-        for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&base[(size_t)r * w + c].x);
+        for (int r = 0; r < 2 * ry + 1; ++r) sum += ref_grey(ref_pack, ref_plane, base0 + (size_t)r * w + c);
     }
     sum = warp_sum(sum);
     const float t0 = sum / (float)size;
@@ -516,7 +531,7 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
   }
   else
   {
-    DIC_FOR_EACH_SAMPLE(lane, rx, ry, sum += __ldg(&ref_pack[(size_t)(cy + ly) * w + cx + lx].x);)
+    DIC_FOR_EACH_SAMPLE(lane, rx, ry, sum += ref_grey(ref_pack, ref_plane, (size_t)(cy + ly) * w + cx + lx);)
     sum = warp_sum(sum);
     const float t0 = sum / (float)size;
     DIC_FOR_EACH_SAMPLE(lane, rx, ry,
@@ -576,7 +591,8 @@ __device__ __forceinline__ void poi_write_sums(const PoiSums& q, int size, int l
   }
 }
 
-__global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ ref_pack, int w, int h,
+__global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ ref_pack,
+                                                     const float* __restrict__ ref_plane, int w, int h,
                                                      const dic_poi* __restrict__ pois, int64_t n,
                                                      int rx, int ry, PoiRef* __restrict__ out)
 {
@@ -585,7 +601,7 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
   if (i >= n) return;
   PoiRef* rec = out + i;
   PoiSums q;
-  if (!poi_sums(ref_pack, w, h, pois[i].x, pois[i].y, rx, ry, lane, rec, q)) return;
+  if (!poi_sums(ref_pack, ref_plane, w, h, pois[i].x, pois[i].y, rx, ry, lane, rec, q)) return;
   // Every lane holds the same sums (butterfly reductions), so the LU runs uniformly and
   // lane c < 6 solves and writes column c of the inverse.
   float hf[6][6];
@@ -614,7 +630,8 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
 // leaves through shared memory as one 144 B run per POI.
 // --------------------------------------------------------------------------------------
 constexpr int kPrepPois = 32, kPrepWarps = 4;   // (8 warps per 32 POIs: 0.72 against 0.60 ms at 2048^2)
-__global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4* __restrict__ ref_pack, int w,
+__global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4* __restrict__ ref_pack,
+                                                                  const float* __restrict__ ref_plane, int w,
                                                                   int h, const dic_poi* __restrict__ pois,
                                                                   int64_t n, int rx, int ry,
                                                                   PoiRef* __restrict__ out)
@@ -633,7 +650,7 @@ __global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4*
     if (i < n)
     {
       PoiSums q;
-      live = poi_sums(ref_pack, w, h, pois[i].x, pois[i].y, rx, ry, lane, out + i, q);
+      live = poi_sums(ref_pack, ref_plane, w, h, pois[i].x, pois[i].y, rx, ry, lane, out + i, q);
       if (live)
       {
         poi_write_sums(q, size, lane, out + i);
@@ -1389,6 +1406,73 @@ __device__ __forceinline__ bool pair_class_sums(const IcgnParams& P, int k, int 
   return any_bad;
 }
 
+// The same nine sums under pixel sampling (T: the POI's staged window).  `fast`: every sample of
+// the subset lies in the interpolation range and has its support in the window (window_covers,
+// once per iteration), so the rows run without tests; otherwise the checked loop of the column
+// walk (px_column_checked: range tests, window or global plane; `lat` on the pixel lattice).
+// Same sums in the same order as pair_class_sums, same bits in either loop.
+__device__ __forceinline__ bool pair_class_sums_px(const IcgnParams& P, const PixelTile& T, int k, int lane, float px,
+                                                   float py, int cx, int cy, float t0, const float (&W)[6], bool fast,
+                                                   bool lat, float (&s)[9])
+{
+  const int rx = P.rx, ry = P.ry, w = P.w;
+  const int c = pair_column(lane, k);
+  const float flx = (float)(c - rx);
+  float A0 = 0.f, A1 = 0.f, A2 = 0.f, B[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  bool bad = false;
+  if (c < 2 * rx + 1)
+  {
+    const float4* __restrict__ ref_col = P.ref_pack + (size_t)(cy - ry) * w + cx + (c - rx);
+    if (fast)
+    {
+      const float ax = fmaf(W[0], flx, W[2]), ay = fmaf(W[3], flx, W[5]);
+      const int row = T.bx;
+      const float4* rp = ref_col;
+      const auto accumulate = [&](float t, const float4& cur, float fly) {
+        const float tau = t - t0;
+        const float rc = cur.x - t0;
+        A0 += tau;
+        A1 = fmaf(tau, tau, A1);
+        A2 = fmaf(tau, rc, A2);
+        const float gt = __fmul_rn(cur.y, tau), ht = __fmul_rn(cur.z, tau);
+        B[0] = __fadd_rn(B[0], gt);
+        B[2] = fmaf(gt, fly, B[2]);
+        B[3] = __fadd_rn(B[3], ht);
+        B[5] = fmaf(ht, fly, B[5]);
+      };
+      for (int r = 0; r < 2 * ry + 1; ++r)
+      {
+        const float4 cur = __ldg(rp);
+        rp += w;
+        const float fly = (float)(r - ry);
+        accumulate(sample_window(T, row, px + fmaf(W[1], fly, ax), py + fmaf(W[4], fly, ay)), cur, fly);
+      }
+    }
+    else
+    {
+      const ColumnSums cs = px_column_checked(P.tar, w, P.h, T, ref_col, px, py, W[0], W[1], W[2], W[3], W[4], W[5],
+                                              flx, t0, ry, lat ? 1 : 0);
+      A0 = cs.A0;
+      A1 = cs.A1;
+      A2 = cs.A2;
+      B[0] = cs.B0;
+      B[2] = cs.B2;
+      B[3] = cs.B3;
+      B[5] = cs.B5;
+      bad = cs.bad != 0;
+    }
+  }
+  B[1] = flx * B[0];
+  B[4] = flx * B[3];
+  const bool any_bad = __any_sync(kFull, bad);
+  s[0] = warp_sum(A0);
+  s[1] = warp_sum(A1);
+  s[2] = warp_sum(A2);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) s[3 + a] = warp_sum(B[a]);
+  return any_bad;
+}
+
 // Whether a sample of column class k lies outside the interpolatable range (warp-uniform).
 __device__ __forceinline__ bool pair_class_oob(const IcgnParams& P, int k, int lane, float px, float py,
                                                const float (&W)[6])
@@ -1421,9 +1505,9 @@ struct PairExchange
 // One POI (queue index i) on one warp (kPoiWarps 1) or on the two warps of a pair
 // (kPoiWarps 2: this warp walks class `cls`, barrier `bar` joins the pair).  Same rules,
 // status codes and outputs as icgn_solve; class 0's lane 0 writes the record.
-template <int kPoiWarps>
+template <int kPoiWarps, int kSrc = kSrcTable>
 __device__ __forceinline__ void icgn_solve_pair(const IcgnParams& P, int64_t i, int lane, int cls,
-                                                PairExchange* xch, int bar)
+                                                PairExchange* xch, int bar, const PixelTile& T = PixelTile{})
 {
   dic_poi* poi = P.pois + i;
   const float px = poi->x, py = poi->y;
@@ -1453,18 +1537,31 @@ __device__ __forceinline__ void icgn_solve_pair(const IcgnParams& P, int64_t i, 
     ++it;
     float s[9];
     bool bad;
+    // pixel sampling: on the lattice, or every sample inside the window (warp-uniform)
+    bool fast = false, lat = false;
+    if constexpr (kSrc == kSrcPixels)
+    {
+      lat = on_lattice(W, px, py);
+      fast = !lat && window_covers(W, px, py, rx, ry, (float)(w - 2), (float)(h - 2), T, lane);
+    }
+    const auto class_sums = [&](int k, float(&out)[9]) {
+      if constexpr (kSrc == kSrcPixels)
+        return pair_class_sums_px(P, T, k, lane, px, py, cx, cy, t0, W, fast, lat, out);
+      else
+        return pair_class_sums(P, k, lane, px, py, cx, cy, t0, W, out);
+    };
     if constexpr (kPoiWarps == 1)
     {
       float s1[9];
-      bad = pair_class_sums(P, 0, lane, px, py, cx, cy, t0, W, s);
-      bad = pair_class_sums(P, 1, lane, px, py, cx, cy, t0, W, s1) || bad;
+      bad = class_sums(0, s);
+      bad = class_sums(1, s1) || bad;
 #pragma unroll
       for (int j = 0; j < 9; ++j) s[j] = __fadd_rn(s[j], s1[j]);
     }
     else
     {
       float mine[9];
-      const bool b = pair_class_sums(P, cls, lane, px, py, cx, cy, t0, W, mine);
+      const bool b = class_sums(cls, mine);
       float* slot = xch->sums[it & 1][cls];
       if (lane == 0)
       {
@@ -1805,10 +1902,14 @@ __host__ __device__ constexpr size_t px_window_bytes(int rx, int ry)
 // 7 % when both were compiled into one kernel).  Returns false when the TMA copy did not
 // arrive within P.wait_polls polls: bit 0 of err is set, lane 0 waits once more (bounded) for
 // the copy in flight, and the caller leaves.
-template <int kMode>
+//
+// kPoiWarps 2 (the two-warp pair walk): both warps of the POI bound the same window (from the
+// same record) and share it; warp cls 0 issues the copy, both wait for it and agree through
+// verdict[2] and the pair's barrier pair_bar whether it arrived; warp copies split the columns.
+template <int kMode, int kPoiWarps = 1>
 __device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lane, int win_f, uint32_t win,
                                          const CUtensorMap* map, uint32_t bar, uint32_t& parity, int* err,
-                                         PixelTile& T)
+                                         PixelTile& T, int cls = 0, int* verdict = nullptr, int pair_bar = 0)
 {
   constexpr int mode = kMode;
   const int rx = P.rx, ry = P.ry, w = P.w, h = P.h;
@@ -1844,7 +1945,7 @@ __device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lan
     if (fits)
     {
       fence_proxy_async_smem();   // this warp's reads of the previous window come first
-      if (mode == 2)
+      if (mode == 2 && cls == 0)
       {
         mbar_arrive_expect_tx(bar, (uint32_t)(bx * by * sizeof(float)));
         if (!P.wait_test) tma_load_2d(win, map, ox, oy, bar);
@@ -1864,9 +1965,16 @@ __device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lan
   {
     const bool done = mbar_wait_bounded(bar, parity, P.wait_polls);
     parity ^= 1u;
-    if (!__all_sync(kFull, done))
+    bool arrived = __all_sync(kFull, done);
+    if constexpr (kPoiWarps == 2)
     {
-      if (lane == 0)
+      if (lane == 0) verdict[cls] = arrived ? 1 : 0;
+      pair_sync(pair_bar);
+      arrived = verdict[0] != 0 && verdict[1] != 0;
+    }
+    if (!arrived)
+    {
+      if (lane == 0 && cls == 0)
       {
         atomicOr(err, 1);
         mbar_wait_bounded(bar, parity ^ 1u, P.wait_polls);   // the copy in flight, once more
@@ -1878,7 +1986,7 @@ __device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lan
   {
     // rows of the window by the whole warp, eight rows' loads in flight before their stores;
     // pixels outside the image as zero
-    for (int c = lane; c < bx; c += 32)
+    for (int c = lane + 32 * cls; c < bx; c += 32 * kPoiWarps)
     {
       const int gx = ox + c;
       const bool xin = gx >= 0 && gx < w;
@@ -1896,7 +2004,10 @@ __device__ __forceinline__ bool px_stage(const IcgnParams& P, int64_t i, int lan
           if (r0 + j < by) px_smem[win_f + (r0 + j) * bx + c] = v[j];
       }
     }
-    __syncwarp();
+    if constexpr (kPoiWarps == 2)
+      pair_sync(pair_bar);
+    else
+      __syncwarp();
   }
   T.bx = bx;
   T.by = by;
@@ -1938,6 +2049,61 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps
     if (!px_stage<kMode>(P, i, lane, win_f, win, &map, bar, parity, err, T)) return;
     icgn_solve<true, kSrcPixels, kPxRowUnroll, PixelTile>(P, i, lane, T);
     __syncwarp();   // every lane's reads of this window before the next copy overwrites it
+  }
+}
+
+// The POI fetch of the persistent pair-walk kernels: with two warps per POI the pair's class-0
+// warp takes the next index and shares it through `fetched` (double-buffered by fetch parity f,
+// the pair's barrier bar), which also orders both warps' reads of the previous POI's window
+// before the next copy.
+template <int kPoiWarps>
+__device__ __forceinline__ int64_t pair_fetch(unsigned long long* next, long long (&fetched)[2], unsigned f, int lane,
+                                              int cls, int bar)
+{
+  if constexpr (kPoiWarps == 1)
+  {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(next, 1ull);
+    return (int64_t)__shfl_sync(kFull, t, 0);
+  }
+  else
+  {
+    if (cls == 0 && lane == 0) fetched[f & 1] = (long long)atomicAdd(next, 1ull);
+    pair_sync(bar);
+    return (int64_t)fetched[f & 1];
+  }
+}
+
+// Pair walk (33 to 64 columns) under pixel sampling: k_icgn_pair_persistent's drain with
+// k_icgn_px's staged windows, one window per POI (shared by the two warps of a two-warp POI).
+// kMode as in k_icgn_px (2 TMA, 1 warp copies, 0 no windows).  Same bits for every kPoiWarps,
+// kWarps and kMode.
+template <int kPoiWarps, int kWarps, int kMode>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
+    k_icgn_pair_px(IcgnParams P, const __grid_constant__ CUtensorMap map, unsigned long long* next, int* err)
+{
+  constexpr int kSlots = kWarps / kPoiWarps;
+  __shared__ PairExchange xch[kSlots];
+  __shared__ long long fetched[kSlots][2];
+  __shared__ __align__(8) unsigned long long bars[kSlots];
+  __shared__ int verdict[kSlots][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = warp / kPoiWarps, cls = warp % kPoiWarps;
+  if (P.enable && *P.enable == 0) return;
+  uint32_t win = 0, parity = 0;
+  const int win_f = px_window(slot, px_window_bytes(P.rx, P.ry), win);
+  const uint32_t bar = smem_addr(&bars[slot]);
+  if (cls == 0 && lane == 0) mbar_init(bar, 1);
+  __syncthreads();   // the barrier's initialisation before the pair's other warp waits on it
+  for (unsigned f = 0;; ++f)
+  {
+    const int64_t i = pair_fetch<kPoiWarps>(next, fetched[slot], f, lane, cls, 1 + slot);
+    if (!queue_slot_active(P, i)) return;   // uniform over a pair
+    PixelTile T;
+    if (!px_stage<kMode, kPoiWarps>(P, i, lane, win_f, win, &map, bar, parity, err, T, cls, verdict[slot], 1 + slot))
+      return;
+    icgn_solve_pair<kPoiWarps, kSrcPixels>(P, i, lane, cls, &xch[slot], 1 + slot, T);
+    __syncwarp();
   }
 }
 
@@ -2109,6 +2275,56 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
     P.max_iter = max_iter;
     P.iter_sum = iter_sum;
     icgn_solve_pair<kPoiWarps>(P, k, lane, cls, &xch[slot], 1 + slot);
+  }
+}
+
+// The batch's pair-walk jobs under pixel sampling: k_icgn_batch_pair's drain with
+// k_icgn_pair_px's windows (each job's map in device memory, win_bytes the window of the
+// launch's largest radius).  kMode 2: TMA windows (every job has a map), 0: no windows.
+template <int kPoiWarps, int kWarps, int kMode>
+__global__ void __launch_bounds__(kWarps * 32, icgn_min_blocks(kWarps))
+    k_icgn_batch_pair_px(const BatchJob* __restrict__ jobs, int njobs, dic_poi* pois, const PoiRef* poi_ref,
+                         int64_t begin, int64_t end, unsigned long long* next, float conv, float max_iter,
+                         unsigned long long* iter_sum, uint32_t win_bytes, uint32_t wait_polls, int* err)
+{
+  constexpr int kSlots = kWarps / kPoiWarps;
+  __shared__ PairExchange xch[kSlots];
+  __shared__ long long fetched[kSlots][2];
+  __shared__ __align__(8) unsigned long long bars[kSlots];
+  __shared__ int verdict[kSlots][2];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int slot = warp / kPoiWarps, cls = warp % kPoiWarps;
+  uint32_t win = 0, parity = 0;
+  const int win_f = px_window(slot, win_bytes, win);
+  const uint32_t bar = smem_addr(&bars[slot]);
+  if (cls == 0 && lane == 0) mbar_init(bar, 1);
+  __syncthreads();
+  for (unsigned f = 0;; ++f)
+  {
+    const int64_t k = begin + pair_fetch<kPoiWarps>(next, fetched[slot], f, lane, cls, 1 + slot);
+    if (k >= end) return;
+    const BatchJob& J = jobs[batch_job_of(jobs, njobs, k)];
+    IcgnParams P;
+    P.coef = nullptr;
+    P.tar = J.tar;
+    P.ref_pack = J.ref_pack;
+    P.poi_ref = poi_ref;
+    P.slot = nullptr;
+    P.pois = pois;
+    P.n = end;
+    P.w = J.w;
+    P.h = J.h;
+    P.rx = J.rx;
+    P.ry = J.ry;
+    P.conv = conv;
+    P.max_iter = max_iter;
+    P.iter_sum = iter_sum;
+    P.wait_polls = wait_polls;
+    PixelTile T;
+    if (!px_stage<kMode, kPoiWarps>(P, k, lane, win_f, win, J.map, bar, parity, err, T, cls, verdict[slot], 1 + slot))
+      return;
+    icgn_solve_pair<kPoiWarps, kSrcPixels>(P, k, lane, cls, &xch[slot], 1 + slot, T);
+    __syncwarp();
   }
 }
 

@@ -299,11 +299,11 @@ class Engine:
         def shape(s):
             return {f: getattr(s, f) for f, _ in s._fields_}
         return {"icgn_flat": shape(t.icgn[0]), "icgn_column": shape(t.icgn[1]), "icgn_pair": shape(t.icgn[2]),
-                "icgn_column_px": shape(t.icgn[3]),
+                "icgn_column_px": shape(t.icgn[3]), "icgn_pair_px": shape(t.icgn[4]),
                 "batch_flat": shape(t.batch[0]), "batch_column": shape(t.batch[1]), "batch_pair": shape(t.batch[2]),
-                "batch_column_px": shape(t.batch[3])}
+                "batch_column_px": shape(t.batch[3]), "batch_pair_px": shape(t.batch[4])}
 
-    WALK_FLAT, WALK_COLUMN, WALK_PAIR, WALK_COLUMN_PX = 0, 1, 2, 3
+    WALK_FLAT, WALK_COLUMN, WALK_PAIR, WALK_COLUMN_PX, WALK_PAIR_PX = 0, 1, 2, 3, 4
 
     def set_sampling(self, mode: int) -> None:
         """How IC-GN reads the target (dic_set_sampling): DIC_SAMPLE_PIXELS (default; the
@@ -314,10 +314,11 @@ class Engine:
     def set_launch_shape(self, walk: int, warps_per_cta: int = 4, ctas_per_sm: int = 0, tile: int = 0,
                          warps_per_poi: int = 1) -> None:
         """Fixes the single-queue IC-GN launch of one subset walk (dic_set_launch_shape): walk 1
-        column (subsets up to 32 wide), 2 pair (33 to 64), 0 flat (wider), 3 column under pixel
-        sampling; ``tile`` 1 or 2 selects the TMA-staged coefficient tile forms (walk 1), with
-        walk 3 ``tile`` 1 stages pixel windows and 0 reads the global plane; ``warps_per_poi`` 2
-        the two-warp pair walk.  A bool walk is read as column (True) or flat (False)."""
+        column (subsets up to 32 wide), 2 pair (33 to 64), 0 flat (wider), 3 and 4 column and
+        pair under pixel sampling; ``tile`` 1 or 2 selects the TMA-staged coefficient tile forms
+        (walk 1), with walks 3 and 4 ``tile`` 1 stages pixel windows by TMA, 2 by warp copies and
+        0 reads the global plane; ``warps_per_poi`` 2 the two-warp pair walks.  A bool walk is
+        read as column (True) or flat (False)."""
         s = _lib.DicLaunchShape(warps_per_cta, ctas_per_sm, 0, 0.0, tile, warps_per_poi)
         self._call(self._L.dic_set_launch_shape(self._h, int(walk), ctypes.byref(s)))
 

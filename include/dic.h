@@ -296,28 +296,30 @@ typedef struct dic_launch_shape
                             1 (4 warps, 48x36 texels, 2 CTAs/SM) or 2 (8 warps, 64x40, 1 CTA/SM)
                             stage the block a chunk of consecutive POIs warps onto in shared memory
                             by TMA; warps_per_cta and ctas_per_sm then follow the tile kind */
-  int32_t warps_per_poi; /* pair walk: 1 (one warp walks both column classes) or 2 (one warp per
-                            class, class sums exchanged through shared memory); 1 elsewhere
-                            (0 is read as 1) */
+  int32_t warps_per_poi; /* pair walks (2 and 4): 1 (one warp walks both column classes) or 2
+                            (one warp per class, class sums exchanged through shared memory); 1
+                            elsewhere (0 is read as 1) */
 } dic_launch_shape;
 
 typedef struct dic_tuning
 {
-  dic_launch_shape icgn[4];    /* [0] flat walk, [1] column walk, [2] pair walk, [3] column walk with
-                                  pixel sampling (k_icgn_px, see dic_set_sampling) */
-  dic_launch_shape batch[4];   /* [3] the column walk under pixel sampling (k_icgn_batch_px) */
+  dic_launch_shape icgn[5];    /* [0] flat walk, [1] column walk, [2] pair walk, [3] column walk with
+                                  pixel sampling (k_icgn_px, see dic_set_sampling), [4] pair walk
+                                  with pixel sampling (k_icgn_pair_px) */
+  dic_launch_shape batch[5];   /* [3], [4]: the column and pair walks under pixel sampling
+                                  (k_icgn_batch_px, k_icgn_batch_pair_px) */
 } dic_tuning;
 
 int dic_set_autotune(dic_engine* engine, int32_t enabled);
 int dic_get_tuning(dic_engine* engine, dic_tuning* out);
 /* No reference counterpart: fixes the single-queue IC-GN launch shape of one subset walk
  * (walk 1: column walk, subsets at most 32 wide; 2: pair walk, 33 to 64; 0: flat walk,
- * wider; 3: the column walk under pixel sampling), e.g. to compare the gather and the
- * TMA-staged tile forms, or one and two warps per POI.  warps_per_cta in {2, 4, 8},
- * ctas_per_sm >= 0, tile in {0, 1, 2} (tile > 0 only with walks 1 and 3; with walk 3, tile
- * 1 stages each POI's pixel window in shared memory by TMA, 2 by warp copies, and 0 reads
- * the plane in global memory, ctas_per_sm 0 = full occupancy), warps_per_poi in {0, 1, 2}
- * (2 only with walk 2); tuned and ms are ignored.
+ * wider; 3 and 4: the column and pair walks under pixel sampling), e.g. to compare the
+ * gather and the TMA-staged tile forms, or one and two warps per POI.  warps_per_cta in
+ * {2, 4, 8}, ctas_per_sm >= 0, tile in {0, 1, 2} (tile > 0 only with walks 1, 3 and 4; with
+ * walks 3 and 4, tile 1 stages each POI's pixel window in shared memory by TMA, 2 by warp
+ * copies, and 0 reads the plane in global memory, ctas_per_sm 0 = full occupancy),
+ * warps_per_poi in {0, 1, 2} (2 only with walks 2 and 4); tuned and ms are ignored.
  * Results do not depend on the shape.  An enabled autotuner may replace it on the next large
  * queue. */
 int dic_set_launch_shape(dic_engine* engine, int32_t walk, const dic_launch_shape* shape);
@@ -328,8 +330,8 @@ int dic_set_launch_shape(dic_engine* engine, int32_t walk, const dic_launch_shap
  * sample).  DIC_SAMPLE_PIXELS (the default) evaluates the same polynomial regrouped by pixel,
  * sum_n wy[n] sum_m wx[m] I(iy-1+n, ix-1+m) with the B-spline weights of the BC matrix, from
  * the 4 x 4 pixels around the texel, each POI's window staged once in shared memory
- * (k_icgn_px) and no coefficient table built.  It applies to the column walk (subsets at
- * most 32 columns wide); wider subsets keep the table.  The two differ by float rounding
+ * (k_icgn_px, k_icgn_pair_px) and no coefficient table built.  It applies to the column and
+ * pair walks (subsets at most 64 columns wide); wider subsets keep the table.  The two differ by float rounding
  * only (both within the parity gate against the CPU; flags agree); samples on the pixel
  * lattice give the pixel itself either way.  Takes effect at the next solve. */
 #define DIC_SAMPLE_TABLE 0

@@ -142,5 +142,5 @@ def test_autotuner_keeps_results(dic):
             e.process_pair(qq)
             out.append(qq)
         np.testing.assert_array_equal(out[0].view(np.uint8), out[1].view(np.uint8))
-        key = "icgn_column_px" if r == 15 else "icgn_pair"
+        key = "icgn_column_px" if r == 15 else "icgn_pair_px"
         assert e2.tuning()[key]["tuned"] == 1, e2.tuning()

@@ -78,7 +78,8 @@ def test_autotuner_times_tile_forms(dic):
 def test_launch_shape_arguments(dic):
     e = dic.Engine(15)
     for kw in (dict(walk=1, tile=3), dict(walk=0, tile=1), dict(walk=2, tile=1),
-               dict(walk=1, warps_per_cta=3), dict(walk=1, ctas_per_sm=-1), dict(walk=4), dict(walk=3, tile=3),
+               dict(walk=1, warps_per_cta=3), dict(walk=1, ctas_per_sm=-1), dict(walk=5), dict(walk=3, tile=3),
+               dict(walk=4, tile=3), dict(walk=3, warps_per_poi=2), dict(walk=4, warps_per_poi=3),
                dict(walk=1, warps_per_poi=2), dict(walk=2, warps_per_poi=3)):
         with pytest.raises((ValueError, RuntimeError)):
             e.set_launch_shape(**kw)
@@ -86,6 +87,9 @@ def test_launch_shape_arguments(dic):
     assert e.tuning()["icgn_column"]["warps_per_cta"] == 2 and e.tuning()["icgn_column"]["tile"] == 0
     e.set_launch_shape(2, warps_per_cta=8, ctas_per_sm=4, warps_per_poi=2)
     assert e.tuning()["icgn_pair"]["warps_per_poi"] == 2 and e.tuning()["icgn_pair"]["warps_per_cta"] == 8
+    e.set_launch_shape(4, warps_per_cta=2, ctas_per_sm=0, tile=2, warps_per_poi=2)
+    t = e.tuning()["icgn_pair_px"]
+    assert t["warps_per_poi"] == 2 and t["warps_per_cta"] == 2 and t["tile"] == 2, t
     e.close()
 
 
