@@ -557,8 +557,8 @@ struct dic_engine
     {
       mark(kPhPoi, 0);
       const unsigned blocks = (unsigned)((n + kPrepPois - 1) / kPrepPois);
-      k_poi_prepare32<<<blocks, kPrepWarps * 32, 0, stream>>>(ref_pack.ptr, ref_f32.ptr, w, h, src, n,
-                                                              cfg.subset_radius_x, cfg.subset_radius_y, poi_ref.ptr);
+      k_poi_prepare32<<<blocks, kPrepWarps * 32, 0, stream>>>(ref_pack.ptr, w, h, src, n, cfg.subset_radius_x,
+                                                              cfg.subset_radius_y, poi_ref.ptr);
       check_launch("k_poi_prepare32");
       mark(kPhPoi, 1);
     }
@@ -1900,7 +1900,7 @@ struct dic_engine
       dic_poi* q = bq.ptr + b_first[k];
       DIC_CUDA(cudaMemcpyAsync(q, J.pois, sizeof(dic_poi) * J.count, in_kind, st));
       k_poi_prepare32<<<(unsigned)((J.count + kPrepPois - 1) / kPrepPois), kPrepWarps * 32, 0, st>>>(
-          M.ref_pack.ptr, M.ref_f32.ptr, J.width, J.height, q, J.count, r, r, bpoi.ptr + b_first[k]);
+          M.ref_pack.ptr, J.width, J.height, q, J.count, r, r, bpoi.ptr + b_first[k]);
       check_launch("k_poi_prepare32");
       FftccParams fp{M.ref_f32.ptr, M.tar_f32.ptr, q, J.count, J.width, J.height};
       fftcc_launch(fp, r, st);
@@ -3314,7 +3314,7 @@ extern "C" int dic_process_pair_noalloc(const dic_config* cfg, const void* d_ref
     }
     constexpr int wpb = 4;
     const unsigned blocks = (unsigned)((n + wpb - 1) / wpb);
-    k_poi_prepare<<<blocks, wpb * 32, 0, s>>>(ref_pack, ref_f32, w, h, d_pois, n, r, r, poi_ref);
+    k_poi_prepare<<<blocks, wpb * 32, 0, s>>>(ref_pack, w, h, d_pois, n, r, r, poi_ref);
     FftccParams fp{ref_f32, tar_f32, d_pois, n, w, h};
     switch (2 * r)
     {

@@ -346,25 +346,13 @@ struct PoiSums
 };
 
 // Entry test, mean (written to rec->t0), and the warp-reduced sums of one POI.  Returns false
-// (after writing valid = 0) when the reference subset leaves the image.  The mean pass reads
-// the grey levels from the float plane ref_plane (the same values as ref_pack's .x, 4 B per
-// sample instead of a 16-byte stride).  (Forming the means from precomputed horizontal window
-// sums instead saved 0.01 ms of the 0.60 ms prep on the 2048x2048 pair and cost 0.03 ms to
-// build the sums: dropped.)
-#ifndef DIC_PREP_MEAN_PLANE
-#define DIC_PREP_MEAN_PLANE 1
-#endif
-__device__ __forceinline__ float ref_grey(const float4* __restrict__ ref_pack, const float* __restrict__ ref_plane,
-                                         size_t o)
-{
-  if constexpr (DIC_PREP_MEAN_PLANE != 0)
-    return __ldg(ref_plane + o);
-  else
-    return __ldg(&ref_pack[o].x);
-}
-__device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, const float* __restrict__ ref_plane,
-                                         int w, int h, float px, float py, int rx, int ry, int lane,
-                                         PoiRef* __restrict__ rec, PoiSums& out_sums)
+// (after writing valid = 0) when the reference subset leaves the image.
+// (The mean pass re-reads the subset from ref_pack, whose lines the second pass then finds in
+// L1: reading the grey levels from the float plane instead, 4 B per sample, took 0.64 against
+// 0.60 ms on the 2048x2048 pair.  Forming the means from precomputed horizontal window sums
+// saved 0.01 ms and cost 0.03 ms to build the sums: dropped.)
+__device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, int w, int h, float px, float py,
+                                         int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums)
 {
   // Entry-test geometry of src/oc_icgn.cpp:184-185.
   if (!(py - ry >= 0 && px - rx >= 0 && py + ry <= h - 1 && px + rx <= w - 1))
@@ -381,10 +369,9 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, co
   for (int t = 0; t < 21; ++t) H[t] = 0.f;
   if (sw <= 32)
   {
-    const size_t col0 = (size_t)(cy - ry) * w + cx + (lane - rx);
-    const float4* col = ref_pack + col0;
+    const float4* col = ref_pack + (size_t)(cy - ry) * w + cx + (lane - rx);
     if (lane < sw)
-      for (int r = 0; r < 2 * ry + 1; ++r) sum += ref_grey(ref_pack, ref_plane, col0 + (size_t)r * w);
+      for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&col[(size_t)r * w].x);
     sum = warp_sum(sum);
     const float t0 = sum / (float)size;
     float Qxx[3] = {0.f, 0.f, 0.f}, Qyy[3] = {0.f, 0.f, 0.f}, Qxy[3] = {0.f, 0.f, 0.f};
@@ -443,14 +430,13 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, co
     // Pair walk (33 to 64 columns): column classes c = 2 lane + k, each walked like the
     // column walk and butterfly-reduced on its own, class totals added in class order --
     // the order in which the IC-GN pair walk forms its target-side sums.
-    const size_t base0 = (size_t)(cy - ry) * w + cx - rx;
-    const float4* base = ref_pack + base0;
+    const float4* base = ref_pack + (size_t)(cy - ry) * w + cx - rx;
 #pragma unroll
     for (int k = 0; k < 2; ++k)
     {
       const int c = pair_column(lane, k);
       if (c < sw)
-        for (int r = 0; r < 2 * ry + 1; ++r) sum += ref_grey(ref_pack, ref_plane, base0 + (size_t)r * w + c);
+        for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&base[(size_t)r * w + c].x);
     }
     sum = warp_sum(sum);
     const float t0 = sum / (float)size;
@@ -531,7 +517,7 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, co
   }
   else
   {
-    DIC_FOR_EACH_SAMPLE(lane, rx, ry, sum += ref_grey(ref_pack, ref_plane, (size_t)(cy + ly) * w + cx + lx);)
+    DIC_FOR_EACH_SAMPLE(lane, rx, ry, sum += __ldg(&ref_pack[(size_t)(cy + ly) * w + cx + lx].x);)
     sum = warp_sum(sum);
     const float t0 = sum / (float)size;
     DIC_FOR_EACH_SAMPLE(lane, rx, ry,
@@ -591,8 +577,7 @@ __device__ __forceinline__ void poi_write_sums(const PoiSums& q, int size, int l
   }
 }
 
-__global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ ref_pack,
-                                                     const float* __restrict__ ref_plane, int w, int h,
+__global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ ref_pack, int w, int h,
                                                      const dic_poi* __restrict__ pois, int64_t n,
                                                      int rx, int ry, PoiRef* __restrict__ out)
 {
@@ -601,7 +586,7 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
   if (i >= n) return;
   PoiRef* rec = out + i;
   PoiSums q;
-  if (!poi_sums(ref_pack, ref_plane, w, h, pois[i].x, pois[i].y, rx, ry, lane, rec, q)) return;
+  if (!poi_sums(ref_pack, w, h, pois[i].x, pois[i].y, rx, ry, lane, rec, q)) return;
   // Every lane holds the same sums (butterfly reductions), so the LU runs uniformly and
   // lane c < 6 solves and writes column c of the inverse.
   float hf[6][6];
@@ -630,8 +615,7 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
 // leaves through shared memory as one 144 B run per POI.
 // --------------------------------------------------------------------------------------
 constexpr int kPrepPois = 32, kPrepWarps = 4;   // (8 warps per 32 POIs: 0.72 against 0.60 ms at 2048^2)
-__global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4* __restrict__ ref_pack,
-                                                                  const float* __restrict__ ref_plane, int w,
+__global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4* __restrict__ ref_pack, int w,
                                                                   int h, const dic_poi* __restrict__ pois,
                                                                   int64_t n, int rx, int ry,
                                                                   PoiRef* __restrict__ out)
@@ -650,7 +634,7 @@ __global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4*
     if (i < n)
     {
       PoiSums q;
-      live = poi_sums(ref_pack, ref_plane, w, h, pois[i].x, pois[i].y, rx, ry, lane, out + i, q);
+      live = poi_sums(ref_pack, w, h, pois[i].x, pois[i].y, rx, ry, lane, out + i, q);
       if (live)
       {
         poi_write_sums(q, size, lane, out + i);
