@@ -345,6 +345,48 @@ struct PoiSums
   float nsq, src, S[6], G[6], H[21];
 };
 
+// The sums of one subset column that do not depend on the subset's mean, over the rows
+// ly = -ry..ry in order: the grey sum t, the gradient products' row moments
+// q = {xx, yy, xy} x ly^{0,1,2} (Qxx0 Qxx1 Qxx2 Qyy0 ... Qxy2) and S's terms s = {gx, gx ly,
+// gy, gy ly}.  Neighbouring POIs on one grid row share most of their columns, so
+// k_poi_prepare32 forms each image column's sums once per CTA (kColSums floats, in shared
+// memory) and every POI reads its columns from there; the per-POI path forms the same sums
+// with the same function, so both give the same bits.
+constexpr int kColSums = 14;
+struct ColSums
+{
+  float t, q[9], s[4];
+};
+__device__ __forceinline__ void col_sums_add(ColSums& c, const float4 v, float fly)
+{
+  c.t += v.x;
+  const float xx = __fmul_rn(v.y, v.y), yy = __fmul_rn(v.z, v.z), xy = __fmul_rn(v.y, v.z);
+  const float xxl = __fmul_rn(xx, fly), yyl = __fmul_rn(yy, fly), xyl = __fmul_rn(xy, fly);
+  c.q[0] = __fadd_rn(c.q[0], xx); c.q[1] = __fadd_rn(c.q[1], xxl); c.q[2] = __fmaf_rn(xxl, fly, c.q[2]);
+  c.q[3] = __fadd_rn(c.q[3], yy); c.q[4] = __fadd_rn(c.q[4], yyl); c.q[5] = __fmaf_rn(yyl, fly, c.q[5]);
+  c.q[6] = __fadd_rn(c.q[6], xy); c.q[7] = __fadd_rn(c.q[7], xyl); c.q[8] = __fmaf_rn(xyl, fly, c.q[8]);
+  c.s[0] = __fadd_rn(c.s[0], v.y); c.s[1] = __fmaf_rn(v.y, fly, c.s[1]);
+  c.s[2] = __fadd_rn(c.s[2], v.z); c.s[3] = __fmaf_rn(v.z, fly, c.s[3]);
+}
+// col: the column's texel in the subset's first row
+__device__ __forceinline__ ColSums col_sums(const float4* __restrict__ col, int w, int ry)
+{
+  ColSums c;
+  c.t = 0.f;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) c.q[k] = 0.f;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) c.s[k] = 0.f;
+  for (int r = 0; r < 2 * ry + 1; ++r) col_sums_add(c, __ldg(col + (size_t)r * w), (float)(r - ry));
+  return c;
+}
+// Column sums staged in shared memory, value-major: v[k * stride + j] is value k of column j.
+struct ColSumsShared
+{
+  const float* v;   // column 0 of the calling POI's subset
+  int stride;
+};
+
 // Entry test, mean (written to rec->t0), and the warp-reduced sums of one POI.  Returns false
 // (after writing valid = 0) when the reference subset leaves the image.
 // (The mean pass re-reads the subset from ref_pack, whose lines the second pass then finds in
@@ -352,7 +394,8 @@ struct PoiSums
 // 0.60 ms on the 2048x2048 pair.  Forming the means from precomputed horizontal window sums
 // saved 0.01 ms and cost 0.03 ms to build the sums: dropped.)
 __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, int w, int h, float px, float py,
-                                         int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums)
+                                         int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums,
+                                         ColSumsShared shared = ColSumsShared{nullptr, 0})
 {
   // Entry-test geometry of src/oc_icgn.cpp:184-185.
   if (!(py - ry >= 0 && px - rx >= 0 && py + ry <= h - 1 && px + rx <= w - 1))
@@ -370,13 +413,36 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
   if (sw <= 32)
   {
     const float4* col = ref_pack + (size_t)(cy - ry) * w + cx + (lane - rx);
-    if (lane < sw)
-      for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&col[(size_t)r * w].x);
-    sum = warp_sum(sum);
-    const float t0 = sum / (float)size;
-    float Qxx[3] = {0.f, 0.f, 0.f}, Qyy[3] = {0.f, 0.f, 0.f}, Qxy[3] = {0.f, 0.f, 0.f};
+    ColSums cs;
+    cs.t = 0.f;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) cs.q[k] = 0.f;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) cs.s[k] = 0.f;
     if (lane < sw)
     {
+      if (shared.v)
+      {
+        cs.t = shared.v[lane];
+#pragma unroll
+        for (int k = 0; k < 9; ++k) cs.q[k] = shared.v[(1 + k) * shared.stride + lane];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cs.s[k] = shared.v[(10 + k) * shared.stride + lane];
+      }
+      else
+        cs = col_sums(col, w, ry);
+    }
+    sum = warp_sum(cs.t);
+    const float t0 = sum / (float)size;
+    const float Qxx[3] = {cs.q[0], cs.q[1], cs.q[2]}, Qyy[3] = {cs.q[3], cs.q[4], cs.q[5]},
+                Qxy[3] = {cs.q[6], cs.q[7], cs.q[8]};
+    S[0] = cs.s[0];
+    S[2] = cs.s[1];
+    S[3] = cs.s[2];
+    S[5] = cs.s[3];
+    if (lane < sw)
+    {
+      // the sums that depend on the mean, per sample in the IC-GN walk's order
       for (int r = 0; r < 2 * ry + 1; ++r)
       {
         const float fly = (float)(r - ry);
@@ -389,15 +455,6 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
         G[2] = fmaf(grc, fly, G[2]);
         G[3] = __fadd_rn(G[3], hrc);
         G[5] = fmaf(hrc, fly, G[5]);
-        S[0] += v.y;
-        S[2] = fmaf(v.y, fly, S[2]);
-        S[3] += v.z;
-        S[5] = fmaf(v.z, fly, S[5]);
-        const float xx = v.y * v.y, yy = v.z * v.z, xy = v.y * v.z;
-        const float xxl = xx * fly, yyl = yy * fly, xyl = xy * fly;
-        Qxx[0] += xx; Qxx[1] += xxl; Qxx[2] = fmaf(xxl, fly, Qxx[2]);
-        Qyy[0] += yy; Qyy[1] += yyl; Qyy[2] = fmaf(yyl, fly, Qyy[2]);
-        Qxy[0] += xy; Qxy[1] += xyl; Qxy[2] = fmaf(xyl, fly, Qxy[2]);
       }
     }
     const float lx = (float)(lane - rx), lx2 = lx * lx;
@@ -427,32 +484,43 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
   }
   else if (sw <= kPairMaxWidth)
   {
-    // Pair walk (33 to 64 columns): column classes c = 2 lane + k, each walked like the
-    // column walk and butterfly-reduced on its own, class totals added in class order --
-    // the order in which the IC-GN pair walk forms its target-side sums.
+    // Pair walk (33 to 64 columns): column classes c = pair_column(lane, k), each walked like
+    // the column walk and butterfly-reduced on its own, class totals added in class order --
+    // the order in which the IC-GN pair walk forms its target-side sums.  The lane's two
+    // column grey sums are added in class order before the reduction.
     const float4* base = ref_pack + (size_t)(cy - ry) * w + cx - rx;
+    float tl = 0.f;
 #pragma unroll
     for (int k = 0; k < 2; ++k)
     {
       const int c = pair_column(lane, k);
       if (c < sw)
-        for (int r = 0; r < 2 * ry + 1; ++r) sum += __ldg(&base[(size_t)r * w + c].x);
+      {
+        float t = 0.f;
+        if (shared.v)
+          t = shared.v[c];
+        else
+          for (int r = 0; r < 2 * ry + 1; ++r) t += __ldg(&base[(size_t)r * w + c].x);
+        tl += t;
+      }
     }
-    sum = warp_sum(sum);
+    sum = warp_sum(tl);
     const float t0 = sum / (float)size;
 #pragma unroll 1
     for (int k = 0; k < 2; ++k)
     {
       const int c = pair_column(lane, k);
       float pn = 0.f, ps = 0.f, pS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, pG[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-      float Qxx[3] = {0.f, 0.f, 0.f}, Qyy[3] = {0.f, 0.f, 0.f}, Qxy[3] = {0.f, 0.f, 0.f};
+      ColSums cs;
+      cs.t = 0.f;
+#pragma unroll
+      for (int v = 0; v < 9; ++v) cs.q[v] = 0.f;
+#pragma unroll
+      for (int v = 0; v < 4; ++v) cs.s[v] = 0.f;
       if (c < sw)
       {
         const float4* col = base + c;
-        for (int r = 0; r < 2 * ry + 1; ++r)
-        {
-          const float fly = (float)(r - ry);
-          const float4 v = __ldg(&col[(size_t)r * w]);
+        const auto mean_sums = [&](const float4 v, float fly) {
           const float rc = v.x - t0;
           pn = fmaf(rc, rc, pn);
           ps += rc;
@@ -461,17 +529,30 @@ __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, in
           pG[2] = fmaf(grc, fly, pG[2]);
           pG[3] = __fadd_rn(pG[3], hrc);
           pG[5] = fmaf(hrc, fly, pG[5]);
-          pS[0] += v.y;
-          pS[2] = fmaf(v.y, fly, pS[2]);
-          pS[3] += v.z;
-          pS[5] = fmaf(v.z, fly, pS[5]);
-          const float xx = v.y * v.y, yy = v.z * v.z, xy = v.y * v.z;
-          const float xxl = xx * fly, yyl = yy * fly, xyl = xy * fly;
-          Qxx[0] += xx; Qxx[1] += xxl; Qxx[2] = fmaf(xxl, fly, Qxx[2]);
-          Qyy[0] += yy; Qyy[1] += yyl; Qyy[2] = fmaf(yyl, fly, Qyy[2]);
-          Qxy[0] += xy; Qxy[1] += xyl; Qxy[2] = fmaf(xyl, fly, Qxy[2]);
+        };
+        if (shared.v)
+        {
+#pragma unroll
+          for (int v = 0; v < 9; ++v) cs.q[v] = shared.v[(1 + v) * shared.stride + c];
+#pragma unroll
+          for (int v = 0; v < 4; ++v) cs.s[v] = shared.v[(10 + v) * shared.stride + c];
+          for (int r = 0; r < 2 * ry + 1; ++r) mean_sums(__ldg(&col[(size_t)r * w]), (float)(r - ry));
         }
+        else
+          for (int r = 0; r < 2 * ry + 1; ++r)
+          {
+            const float fly = (float)(r - ry);
+            const float4 v = __ldg(&col[(size_t)r * w]);
+            mean_sums(v, fly);
+            col_sums_add(cs, v, fly);
+          }
       }
+      pS[0] = cs.s[0];
+      pS[2] = cs.s[1];
+      pS[3] = cs.s[2];
+      pS[5] = cs.s[3];
+      const float Qxx[3] = {cs.q[0], cs.q[1], cs.q[2]}, Qyy[3] = {cs.q[3], cs.q[4], cs.q[5]},
+                  Qxy[3] = {cs.q[6], cs.q[7], cs.q[8]};
       const float lx = (float)(c - rx), lx2 = lx * lx;
       pG[1] = lx * pG[0];
       pG[4] = lx * pG[3];
@@ -613,8 +694,19 @@ __global__ void __launch_bounds__(128) k_poi_prepare(const float4* __restrict__ 
 // warp 0 factorises and inverts all 32 Hessians at once, one POI per lane (the same lu6 /
 // solve6_column code), instead of every warp running one uniform LU per POI.  The inverse
 // leaves through shared memory as one 144 B run per POI.
+//
+// Column sums shared across the CTA (column and pair walks): when the CTA's POIs lie on at most two
+// grid rows (one integer y each) and each row's subsets span at most kPrepCols image columns,
+// the CTA first forms every such column's ColSums once (one thread per column, the rows in
+// order) and the POIs read them from shared memory; only the sums that depend on a POI's mean
+// (norm, G) are formed per POI.  Any other set of POIs takes the per-POI path.  Same bits
+// either way.
 // --------------------------------------------------------------------------------------
 constexpr int kPrepPois = 32, kPrepWarps = 4;   // (8 warps per 32 POIs: 0.72 against 0.60 ms at 2048^2)
+constexpr int kPrepCols = 256;   // shared columns per grid row (32 POIs at step <= 7 for r 15, <= 6 for r 30)
+#ifndef DIC_PREP_SHARED_COLUMNS
+#define DIC_PREP_SHARED_COLUMNS 1
+#endif
 __global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4* __restrict__ ref_pack, int w,
                                                                   int h, const dic_poi* __restrict__ pois,
                                                                   int64_t n, int rx, int ry,
@@ -623,9 +715,65 @@ __global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4*
   __shared__ float sh_h[kPrepPois * 21];       // odd stride: lane p reads row p conflict-free
   __shared__ float sh_inv[kPrepPois * 37];
   __shared__ int sh_live[kPrepPois];
+  __shared__ float sh_col[2][kColSums][kPrepCols];
+  __shared__ int sh_row[2][3];                 // per grid row: cy, first column, columns
+  __shared__ int sh_shared;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int64_t base = (int64_t)blockIdx.x * kPrepPois;
   const int size = (2 * rx + 1) * (2 * ry + 1);
+  if (warp == 0)
+  {
+    // the POIs' rows and column spans (POIs whose subset leaves the image take no part)
+    const int64_t i = base + lane;
+    bool valid = false;
+    int pcx = 0, pcy = 0;
+    if (i < n)
+    {
+      const float px = pois[i].x, py = pois[i].y;
+      valid = py - ry >= 0 && px - rx >= 0 && py + ry <= h - 1 && px + rx <= w - 1;
+      pcx = (int)px;
+      pcy = (int)py;
+    }
+    const unsigned vm = __ballot_sync(kFull, valid);
+    const int cy0 = vm ? __shfl_sync(kFull, pcy, __ffs(vm) - 1) : 0;
+    const bool in0 = valid && pcy == cy0;
+    const unsigned rest = vm & ~__ballot_sync(kFull, in0);
+    const int cy1 = rest ? __shfl_sync(kFull, pcy, __ffs(rest) - 1) : 0;
+    const bool in1 = valid && !in0 && pcy == cy1;
+    const bool other = __any_sync(kFull, valid && !in0 && !in1);
+    const int lo0 = __reduce_min_sync(kFull, in0 ? pcx : INT_MAX), hi0 = __reduce_max_sync(kFull, in0 ? pcx : INT_MIN);
+    const int lo1 = __reduce_min_sync(kFull, in1 ? pcx : INT_MAX), hi1 = __reduce_max_sync(kFull, in1 ? pcx : INT_MIN);
+    const int n0 = vm ? hi0 - lo0 + 2 * rx + 1 : 0, n1 = rest ? hi1 - lo1 + 2 * rx + 1 : 0;
+    if (lane == 0)
+    {
+      sh_shared =
+          (DIC_PREP_SHARED_COLUMNS && 2 * rx + 1 <= kPairMaxWidth && vm && !other && n0 <= kPrepCols && n1 <= kPrepCols)
+              ? 1 : 0;
+      sh_row[0][0] = cy0;
+      sh_row[0][1] = lo0 - rx;
+      sh_row[0][2] = n0;
+      sh_row[1][0] = cy1;
+      sh_row[1][1] = lo1 - rx;
+      sh_row[1][2] = n1;
+    }
+  }
+  __syncthreads();
+  const bool shared = sh_shared != 0;
+  if (shared)
+  {
+    const int n0 = sh_row[0][2], total = n0 + sh_row[1][2];
+    for (int k = threadIdx.x; k < total; k += kPrepWarps * 32)
+    {
+      const int g = k < n0 ? 0 : 1, j = k < n0 ? k : k - n0;
+      const ColSums c = col_sums(ref_pack + (size_t)(sh_row[g][0] - ry) * w + sh_row[g][1] + j, w, ry);
+      sh_col[g][0][j] = c.t;
+#pragma unroll
+      for (int v = 0; v < 9; ++v) sh_col[g][1 + v][j] = c.q[v];
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sh_col[g][10 + v][j] = c.s[v];
+    }
+    __syncthreads();
+  }
   for (int k = 0; k < kPrepPois / kPrepWarps; ++k)
   {
     const int p = warp + kPrepWarps * k;
@@ -634,7 +782,14 @@ __global__ void __launch_bounds__(kPrepWarps * 32) k_poi_prepare32(const float4*
     if (i < n)
     {
       PoiSums q;
-      live = poi_sums(ref_pack, w, h, pois[i].x, pois[i].y, rx, ry, lane, out + i, q);
+      const float px = pois[i].x, py = pois[i].y;
+      ColSumsShared cols{nullptr, 0};
+      if (shared && py - ry >= 0 && px - rx >= 0 && py + ry <= h - 1 && px + rx <= w - 1)
+      {
+        const int g = (int)py == sh_row[0][0] ? 0 : 1;
+        cols = ColSumsShared{&sh_col[g][0][0] + ((int)px - rx - sh_row[g][1]), kPrepCols};
+      }
+      live = poi_sums(ref_pack, w, h, px, py, rx, ry, lane, out + i, q, cols);
       if (live)
       {
         poi_write_sums(q, size, lane, out + i);
