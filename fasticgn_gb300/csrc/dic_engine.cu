@@ -701,8 +701,11 @@ struct dic_engine
   // of its L1 wavefronts on the 2048² pair, 3.73 ms against 3.59 ms persistent with the
   // four-plane table); the autotuner still times both forms.  shape[0]: single queues,
   // shape[1]: batches.
-  IcgnShape shape[2][kWalks] = {{{4, 8, 0.f}, {4, 8, 0.f}, {4, 8, 0.f}, {4, 0, 0.f, 1}, {4, 0, 0.f, 1, 2}},
-                                {{4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {4, 0, 0.f, 0, 2}}};
+  // The pixel pair walk's default (2 warps per CTA, 2 per POI, TMA windows) is its fastest
+  // measured form on the 2048² pair at r 20 and 30 (5.84 and 8.05 ms; 4 warps per CTA 7.15 and
+  // 11.8, 8 warps 7.16 and 12.6, one warp per POI 6.9 and 17.1).
+  IcgnShape shape[2][kWalks] = {{{4, 8, 0.f}, {4, 8, 0.f}, {4, 8, 0.f}, {4, 0, 0.f, 1}, {2, 0, 0.f, 1, 2}},
+                                {{4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {4, 7, 0.f}, {2, 0, 0.f, 0, 2}}};
   bool tuned[2][kWalks] = {};
   DevBuf<dic_poi> tune_q;
   cudaEvent_t tune_ev[2] = {};

@@ -1490,8 +1490,19 @@ __global__ void __launch_bounds__(kWarps * 32, icgn_persistent_min_blocks(kWarps
 // on the warps per POI; k_poi_prepare forms the per-POI constants in the same class order,
 // which keeps the exact self-match.
 // --------------------------------------------------------------------------------------
-// barrier of the two warps of a pair (ids 1.., 0 is __syncthreads)
-__device__ __forceinline__ void pair_sync(int id) { asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory"); }
+// barrier of the two warps of a pair (ids 1..4, 0 is __syncthreads).  The id is an immediate
+// in every branch, so the kernel reserves only the barriers it names (a register id makes
+// ptxas reserve all 16 per CTA).
+__device__ __forceinline__ void pair_sync(int id)
+{
+  switch (id)
+  {
+    case 1: asm volatile("bar.sync 1, 64;" ::: "memory"); break;
+    case 2: asm volatile("bar.sync 2, 64;" ::: "memory"); break;
+    case 3: asm volatile("bar.sync 3, 64;" ::: "memory"); break;
+    default: asm volatile("bar.sync 4, 64;" ::: "memory"); break;
+  }
+}
 
 // The nine single-pass sums of column class k under warp W, butterfly-reduced (s: A0, A1,
 // A2, B0..B5).  Returns (warp-uniformly) whether a sample of the class failed the range test.
