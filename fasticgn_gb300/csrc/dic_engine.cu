@@ -1126,6 +1126,7 @@ struct dic_engine
     int64_t begin, end;
     unsigned long long* next;
     unsigned long long* iter_sum;
+    int rmax = 0;   // pixel sampling: the largest subset radius of the range (window size)
   };
   void launch_batch(const BatchLaunch& b, int walk, const IcgnShape& sh)
   {
@@ -1136,12 +1137,12 @@ struct dic_engine
     {
       // windows sized for the largest radius of the launch's jobs
       px_attributes();
-      const uint32_t win = (uint32_t)px_window_bytes(b_col_rmax, b_col_rmax);
+      const uint32_t win = (uint32_t)px_window_bytes(b.rmax, b.rmax);
       const size_t smem = 128 + (size_t)sh.warps * win;
       const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_batch_px(sh.warps, smem);
       const unsigned grid = (unsigned)(sms * ctas);
 #define DIC_BATCH_PX(W, M)                                                                                         \
-  k_icgn_batch_px<W, M><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,  \
+  k_icgn_batch_px<W, M><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,     \
                                                         cfg.conv_criterion, mi, b.iter_sum, win, wait_polls, wait_flag())
       if (b_col_maps)
       {
@@ -1164,12 +1165,12 @@ struct dic_engine
       // windows sized for the largest radius of the launch's jobs
       px_attributes();
       const int pw = sh.poi_warps == 2 ? 2 : 1;
-      const uint32_t win = (uint32_t)px_window_bytes(b_pair_rmax, b_pair_rmax);
+      const uint32_t win = (uint32_t)px_window_bytes(b.rmax, b.rmax);
       const size_t smem = b_col_maps ? pair_px_smem(sh.warps, pw, win) : 0;
       const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_pair_px(true, pw, sh.warps, smem);
       const unsigned grid = (unsigned)(sms * ctas);
 #define DIC_BATCH_PAIR_PX(PW, W, M)                                                                                  \
-  k_icgn_batch_pair_px<PW, W, M><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, \
+  k_icgn_batch_pair_px<PW, W, M><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end,    \
                                                                  b.next, cfg.conv_criterion, mi, b.iter_sum, win,     \
                                                                  wait_polls, wait_flag())
 #define DIC_BATCH_PAIR_PX_W(PW)                                \
@@ -1199,7 +1200,7 @@ struct dic_engine
     if (walk == kWalkPair)
     {
 #define DIC_BATCH_PAIR(PW, W)                                                                                      \
-  k_icgn_batch_pair<PW, W><<<grid, W * 32, 0, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next, \
+  k_icgn_batch_pair<PW, W><<<grid, W * 32, 0, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,    \
                                                        cfg.conv_criterion, mi, b.iter_sum)
       if (sh.poi_warps == 2)
       {
@@ -1219,7 +1220,7 @@ struct dic_engine
     }
     const bool column = walk == kWalkColumn;
 #define DIC_BATCH_LAUNCH(C, W)                                                                                     \
-  k_icgn_batch<C, W><<<grid, W * 32, 0, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,       \
+  k_icgn_batch<C, W><<<grid, W * 32, 0, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,          \
                                                   cfg.conv_criterion, mi, b.iter_sum)
     if (column)
     {
@@ -1310,16 +1311,21 @@ struct dic_engine
       for (int pw : {1, 2})
       {
         if (walk != kWalkPair && walk != kWalkPairPx && pw == 2) continue;
-        const int full =
-            walk == kWalkColumnPx
-                ? occupancy_batch_px(warps, 128 + (size_t)warps * px_window_bytes(b_col_rmax, b_col_rmax))
-            : walk == kWalkPairPx
-                ? occupancy_pair_px(true, pw, warps,
-                                    b_col_maps ? pair_px_smem(warps, pw, px_window_bytes(b_pair_rmax, b_pair_rmax)) : 0)
-            : walk == kWalkPair ? occupancy_pair(true, pw, warps)
-                                : occupancy(true, walk == kWalkColumn, warps);
-        for (int ctas : {full, std::max(1, (3 * full) / 4)})
+        // the pixel pair walk's drains run per window size, each at its own full occupancy
+        // (ctas_per_sm 0); the other drains try full and 3/4 occupancy
+        int cands[2] = {0, -1};
+        if (walk != kWalkPairPx)
         {
+          const int full = walk == kWalkColumnPx
+                               ? occupancy_batch_px(warps, 128 + (size_t)warps * px_window_bytes(b.rmax, b.rmax))
+                           : walk == kWalkPair ? occupancy_pair(true, pw, warps)
+                                               : occupancy(true, walk == kWalkColumn, warps);
+          cands[0] = full;
+          cands[1] = std::max(1, (3 * full) / 4);
+        }
+        for (int ctas : cands)
+        {
+          if (ctas < 0) continue;
           const IcgnShape sh{warps, ctas, 0.f, 0, pw};
           float t = INFINITY;
           for (int rep = 0; rep < 2; ++rep)
@@ -1743,6 +1749,19 @@ struct dic_engine
   int64_t b_total = 0, b_col_end = 0, b_pair_end = 0;
   int b_col_rmax = 0;                   // largest subset radius among the column-walk jobs
   int b_pair_rmax = 0;                  // and among the pair-walk jobs
+  // The pair-walk jobs' drains: one per subset radius under pixel sampling (queue range and
+  // radius), one for all of them under table sampling.
+  struct PairGroup
+  {
+    int64_t begin, end;
+    int rmax;
+  };
+  std::vector<PairGroup> b_pair_groups;
+#ifndef DIC_BATCH_PAIR_BY_RADIUS
+#define DIC_BATCH_PAIR_BY_RADIUS 1
+#endif
+  static constexpr bool kBatchPairByRadius = DIC_BATCH_PAIR_BY_RADIUS != 0;
+  static constexpr int kMaxPairGroups = kPairMaxWidth / 2 - 15;   // radii 16 .. (width - 1) / 2
   DevBuf<CUtensorMap> bmaps;            // the jobs' target-plane tensor maps (pixel sampling)
   bool b_col_maps = false;              // every pixel-sampled job has one (TMA windows), else warp copies / none
   std::vector<CUtensorMap> b_maps_host; // their host copy (kept alive for the asynchronous upload)
@@ -1759,18 +1778,24 @@ struct dic_engine
   {
     b_order.resize(nj);
     for (int j = 0; j < nj; ++j) b_order[j] = j;
-    // walk rank: column 0, pair 1, flat 2
+    // walk rank: column 0, pair 1, flat 2; pair-walk jobs by subset radius under pixel
+    // sampling, whose windows, and so the drain's residency, depend on it
     const auto rank = [&](int j) {
       const int wk = walk_of(jobs[j].subset_radius);
       return wk == kWalkColumn ? 0 : wk == kWalkPair ? 1 : 2;
     };
-    std::stable_sort(b_order.begin(), b_order.end(), [&](int a, int b) { return rank(a) < rank(b); });
+    const bool px_pairs = kBatchPairByRadius && sampling == DIC_SAMPLE_PIXELS;
+    std::stable_sort(b_order.begin(), b_order.end(), [&](int a, int b) {
+      if (rank(a) != rank(b)) return rank(a) < rank(b);
+      return px_pairs && rank(a) == 1 && jobs[a].subset_radius < jobs[b].subset_radius;
+    });
     b_first.assign(nj, 0);
     b_total = 0;
     b_col_end = 0;
     b_pair_end = 0;
     b_col_rmax = 0;
     b_pair_rmax = 0;
+    b_pair_groups.clear();
     for (int k = 0; k < nj; ++k)
     {
       const dic_job& J = jobs[b_order[k]];
@@ -1779,14 +1804,21 @@ struct dic_engine
       const int r = rank(b_order[k]);
       if (r == 0) b_col_end = b_total;
       if (r == 0) b_col_rmax = std::max(b_col_rmax, J.subset_radius);
-      if (r == 1) b_pair_rmax = std::max(b_pair_rmax, J.subset_radius);
+      if (r == 1)
+      {
+        b_pair_rmax = std::max(b_pair_rmax, J.subset_radius);
+        if (b_pair_groups.empty() || (px_pairs && b_pair_groups.back().rmax != J.subset_radius))
+          b_pair_groups.push_back(PairGroup{b_first[k], b_total, J.subset_radius});
+        b_pair_groups.back().end = b_total;
+        b_pair_groups.back().rmax = std::max(b_pair_groups.back().rmax, J.subset_radius);
+      }
       if (r <= 1) b_pair_end = b_total;
     }
     if ((int)jobs_mem.size() < nj) jobs_mem.resize(nj);
     bq.ensure((size_t)std::max<int64_t>(b_total, 1));
     bpoi.ensure((size_t)std::max<int64_t>(b_total, 1));
     bjobs.ensure((size_t)nj);
-    bnext.ensure(3);
+    bnext.ensure(2 + kMaxPairGroups);
     counters.ensure(1);
     std::vector<BatchJob> table(nj);
     for (int k = 0; k < nj; ++k)
@@ -1878,6 +1910,7 @@ struct dic_engine
     const cudaMemcpyKind in_kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     mark(kPhFrame, 0);
     DIC_CUDA(cudaMemsetAsync(counters.ptr, 0, sizeof(unsigned long long), stream));
+    DIC_CUDA(cudaMemsetAsync(bnext.ptr, 0, (2 + kMaxPairGroups) * sizeof(unsigned long long), stream));
     batch_lanes();
     DIC_CUDA(cudaEventRecord(b_fork, stream));
     for (int l = 0; l < kBatchLanes; ++l) DIC_CUDA(cudaStreamWaitEvent(b_lane[l], b_fork, 0));
@@ -1908,27 +1941,35 @@ struct dic_engine
       FftccParams fp{M.ref_f32.ptr, M.tar_f32.ptr, q, J.count, J.width, J.height};
       fftcc_launch(fp, r, st);
     }
+    BatchLaunch col{bjobs.ptr, nj, bq.ptr, bpoi.ptr, 0, b_col_end, bnext.ptr, counters.ptr, b_col_rmax};
+    BatchLaunch flat{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_pair_end, b_total, bnext.ptr + 1, counters.ptr};
+    std::vector<BatchLaunch> pairs;
+    for (size_t g = 0; g < b_pair_groups.size(); ++g)
+      pairs.push_back(BatchLaunch{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_pair_groups[g].begin, b_pair_groups[g].end,
+                                  bnext.ptr + 2 + g, counters.ptr, b_pair_groups[g].rmax});
+    // the pair walk is tuned on its largest drain
+    size_t pair_big = 0;
+    for (size_t g = 1; g < pairs.size(); ++g)
+      if (pairs[g].end - pairs[g].begin > pairs[pair_big].end - pairs[pair_big].begin) pair_big = g;
     for (int l = 0; l < kBatchLanes; ++l)
     {
       DIC_CUDA(cudaEventRecord(b_join[l], b_lane[l]));
       DIC_CUDA(cudaStreamWaitEvent(stream, b_join[l], 0));
     }
-    DIC_CUDA(cudaMemsetAsync(bnext.ptr, 0, 3 * sizeof(unsigned long long), stream));
-    BatchLaunch col{bjobs.ptr, nj, bq.ptr, bpoi.ptr, 0, b_col_end, bnext.ptr, counters.ptr};
-    BatchLaunch pair{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_col_end, b_pair_end, bnext.ptr + 2, counters.ptr};
-    BatchLaunch flat{bjobs.ptr, nj, bq.ptr, bpoi.ptr, b_pair_end, b_total, bnext.ptr + 1, counters.ptr};
     const bool cap = capturing();
     const int col_walk = sampling == DIC_SAMPLE_PIXELS ? kWalkColumnPx : kWalkColumn;
     const int pair_walk = sampling == DIC_SAMPLE_PIXELS ? kWalkPairPx : kWalkPair;
     if (autotune && !cap)
     {
       if (b_col_end >= kTuneMinPois && !tuned[1][col_walk]) tune_batch(col, col_walk, b_total);
-      if (b_pair_end - b_col_end >= kTuneMinPois && !tuned[1][pair_walk]) tune_batch(pair, pair_walk, b_total);
+      if (!pairs.empty() && pairs[pair_big].end - pairs[pair_big].begin >= kTuneMinPois && !tuned[1][pair_walk])
+        tune_batch(pairs[pair_big], pair_walk, b_total);
       if (b_total - b_pair_end >= kTuneMinPois && !tuned[1][kWalkFlat]) tune_batch(flat, kWalkFlat, b_total);
     }
     mark(kPhIcgn, 0);
     if (b_col_end > 0) launch_batch(col, col_walk, shape[1][col_walk]);
-    if (b_pair_end > b_col_end) launch_batch(pair, pair_walk, shape[1][pair_walk]);
+    for (const BatchLaunch& pl : pairs)
+      if (pl.end > pl.begin) launch_batch(pl, pair_walk, shape[1][pair_walk]);
     if (b_total > b_pair_end) launch_batch(flat, kWalkFlat, shape[1][kWalkFlat]);
     mark(kPhIcgn, 1);
     for (int k = 0; k < nj; ++k)
