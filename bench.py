@@ -1070,6 +1070,27 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def profile_pair(radius):
+    """One small, fixed launch sequence for an ncu capture: the bench's 2048x2048 pair at the
+    given subset radius, step 4, solved twice on one engine with the untuned launch shapes
+    (about 0.2 GB of planes and records on the device)."""
+    import fasticgn_gb300 as dic
+    ref, tar = load_pair()
+    h, w = ref.shape
+    q0 = dic.grid_queue(w, h, radius, 4)
+    e = dic.Engine(radius, radius, WORKLOAD["conv"], WORKLOAD["max_iter"])
+    e.set_autotune(False)
+    e.set_timing(True)
+    for _ in range(2):
+        q = q0.copy()
+        e.set_ref(ref)
+        e.set_tar(tar)
+        e.process_pair(q)
+    st = e.stats()
+    print(json.dumps({"radius": radius, "pois": len(q0), **{k: st[k] for k in st if k.startswith("ms_")}}))
+    e.close()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -1080,7 +1101,13 @@ def main():
     ap.add_argument("--skip-streams", action="store_true", help="do not measure the frame streams")
     ap.add_argument("--seed", choices=["fftcc", "learned"], default="fftcc",
                     help="seed method of the headline value (both are measured when the proposal weights exist)")
+    ap.add_argument("--profile-pair", type=int, default=0, metavar="R",
+                    help="profiling driver: solve the 2048x2048 pair at subset radius R (step 4, untuned default "
+                         "launch shapes) twice and print the second solve's kernel times; nothing else runs")
     args = ap.parse_args()
+    if args.profile_pair:
+        profile_pair(args.profile_pair)
+        return
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return

@@ -156,3 +156,34 @@ def test_pair_walk_pixels_match_table(dic, radius):
     assert np.abs(px["u"] - tb["u"])[ok].max() <= 1e-3 and np.abs(px["v"] - tb["v"])[ok].max() <= 1e-3
     assert np.median(np.abs(px["u"] - tb["u"])[ok]) <= 1e-5
     assert (C.failure_codes(px["zncc"]) == C.failure_codes(tb["zncc"])).mean() >= 0.999
+
+
+@pytest.mark.parametrize("width,dtype", [(418, np.uint16), (421, np.uint8), (403, np.float32)])
+def test_pair_walk_pixels_odd_widths_and_types(dic, width, dtype):
+    """Widths that are not a multiple of 4 (the padded-pitch plane under the TMA windows) and
+    12-bit / float input: the pixel pair walk's staged and unstaged forms give the same bits,
+    and match the table form to float rounding with identical flags."""
+    from fasticgn_gb300 import speckle
+    pr = speckle.pair_bumps(seed=700 + width, width=width, height=360, max_disp=6.0, max_strain=0.015)
+    scale = {np.uint8: 1.0, np.uint16: 16.0, np.float32: 1.0}[dtype]
+    ref = (pr.ref.astype(np.float32) * scale).astype(dtype)
+    tar = (pr.tar.astype(np.float32) * scale).astype(dtype)
+    radius = 22
+    outs = {}
+    for name, pixels, shape in (("tma", True, dict(warps_per_cta=2, warps_per_poi=2, tile=1)),
+                                ("none", True, dict(warps_per_cta=4, warps_per_poi=1, tile=0)),
+                                ("table", False, None)):
+        with _engine(dic, radius, pixels) as e:
+            if shape:
+                e.set_launch_shape(4, ctas_per_sm=0, **shape)
+            e.set_ref(ref)
+            e.set_tar(tar)
+            q = dic.grid_queue(width, 360, radius, 5)
+            e.process_pair(q)
+        outs[name] = q
+    assert outs["tma"].tobytes() == outs["none"].tobytes()
+    px, tb = outs["tma"], outs["table"]
+    ok = (px["zncc"] >= 0) & (tb["zncc"] >= 0)
+    assert ok.mean() > 0.9
+    assert np.abs(px["u"] - tb["u"])[ok].max() <= 1e-3 and np.abs(px["v"] - tb["v"])[ok].max() <= 1e-3
+    assert (C.failure_codes(px["zncc"]) == C.failure_codes(tb["zncc"])).mean() >= 0.999
