@@ -3258,70 +3258,78 @@ __device__ __forceinline__ int line_at(int line, int j)
   return kRows ? line * (M + 1) + j : j * (M + 1) + line;
 }
 
+// Work mapping of k_fftcc_big: thread -> line (or column) `line` = tid % M and part
+// `part` = tid / M of `parts` = kBigThreads / M; a thread walks its line's sub-transforms (or
+// rows) part, part + parts, ...  (A flat index per item, divided by M in every loop, made
+// integer arithmetic 61 % of the ALU pipe and the kernel instruction-bound.)  Threads past
+// parts * M only join the barriers and reductions.
+constexpr int kBigThreads = 128;
+
 // forward line transforms over all M lines: natural -> permuted
 template <int M, bool kRows>
-__device__ __forceinline__ void big_forward(float2* z)
+__device__ __forceinline__ void big_forward(float2* z, int line, int part, bool on)
 {
-  constexpr int N1 = big_n1(M), N2 = M / N1;
+  constexpr int N1 = big_n1(M), N2 = M / N1, kParts = kBigThreads / M;
   const float2* tw = c_tw + tw_offset(M);
-  for (int t = threadIdx.x; t < M * N2; t += blockDim.x)
-  {
-    const int line = t % M, n2 = t / M;
-    float2 a[N1], b[N1];
+  if (on)
+    for (int n2 = part; n2 < N2; n2 += kParts)
+    {
+      float2 a[N1], b[N1];
 #pragma unroll
-    for (int n1 = 0; n1 < N1; ++n1) a[n1] = z[line_at<M, kRows>(line, N2 * n1 + n2)];
-    Fft<N1>::run(a, b);
+      for (int n1 = 0; n1 < N1; ++n1) a[n1] = z[line_at<M, kRows>(line, N2 * n1 + n2)];
+      Fft<N1>::run(a, b);
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) z[line_at<M, kRows>(line, N2 * k1 + n2)] = k1 ? cmul(b[k1], tw[n2 * k1]) : b[k1];
-  }
+      for (int k1 = 0; k1 < N1; ++k1) z[line_at<M, kRows>(line, N2 * k1 + n2)] = k1 ? cmul(b[k1], tw[n2 * k1]) : b[k1];
+    }
   __syncthreads();
-  for (int t = threadIdx.x; t < M * N1; t += blockDim.x)
-  {
-    const int line = t % M, k1 = t / M;
-    float2 a[N2], b[N2];
+  if (on)
+    for (int k1 = part; k1 < N1; k1 += kParts)
+    {
+      float2 a[N2], b[N2];
 #pragma unroll
-    for (int n2 = 0; n2 < N2; ++n2) a[n2] = z[line_at<M, kRows>(line, N2 * k1 + n2)];
-    Fft<N2>::run(a, b);
+      for (int n2 = 0; n2 < N2; ++n2) a[n2] = z[line_at<M, kRows>(line, N2 * k1 + n2)];
+      Fft<N2>::run(a, b);
 #pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) z[line_at<M, kRows>(line, N2 * k1 + k2)] = b[k2];
-  }
+      for (int k2 = 0; k2 < N2; ++k2) z[line_at<M, kRows>(line, N2 * k1 + k2)] = b[k2];
+    }
   __syncthreads();
 }
 
 // forward-kernel transforms of permuted input over all M lines: permuted -> natural
 template <int M, bool kRows>
-__device__ __forceinline__ void big_from_permuted(float2* z)
+__device__ __forceinline__ void big_from_permuted(float2* z, int line, int part, bool on)
 {
-  constexpr int N1 = big_n1(M), N2 = M / N1;
+  constexpr int N1 = big_n1(M), N2 = M / N1, kParts = kBigThreads / M;
   const float2* tw = c_tw + tw_offset(M);
-  for (int t = threadIdx.x; t < M * N1; t += blockDim.x)
-  {
-    const int line = t % M, k1 = t / M;
-    float2 a[N2], b[N2];
+  if (on)
+    for (int k1 = part; k1 < N1; k1 += kParts)
+    {
+      float2 a[N2], b[N2];
 #pragma unroll
-    for (int k2 = 0; k2 < N2; ++k2) a[k2] = z[line_at<M, kRows>(line, N2 * k1 + k2)];
-    Fft<N2>::run(a, b);
+      for (int k2 = 0; k2 < N2; ++k2) a[k2] = z[line_at<M, kRows>(line, N2 * k1 + k2)];
+      Fft<N2>::run(a, b);
 #pragma unroll
-    for (int j = 0; j < N2; ++j) z[line_at<M, kRows>(line, N2 * k1 + j)] = k1 ? cmul(b[j], tw[j * k1]) : b[j];
-  }
+      for (int j = 0; j < N2; ++j) z[line_at<M, kRows>(line, N2 * k1 + j)] = k1 ? cmul(b[j], tw[j * k1]) : b[j];
+    }
   __syncthreads();
-  for (int t = threadIdx.x; t < M * N2; t += blockDim.x)
-  {
-    const int line = t % M, j = t / M;
-    float2 a[N1], b[N1];
+  if (on)
+    for (int j = part; j < N2; j += kParts)
+    {
+      float2 a[N1], b[N1];
 #pragma unroll
-    for (int k1 = 0; k1 < N1; ++k1) a[k1] = z[line_at<M, kRows>(line, N2 * k1 + j)];
-    Fft<N1>::run(a, b);
+      for (int k1 = 0; k1 < N1; ++k1) a[k1] = z[line_at<M, kRows>(line, N2 * k1 + j)];
+      Fft<N1>::run(a, b);
 #pragma unroll
-    for (int i = 0; i < N1; ++i) z[line_at<M, kRows>(line, N2 * i + j)] = b[i];
-  }
+      for (int i = 0; i < N1; ++i) z[line_at<M, kRows>(line, N2 * i + j)] = b[i];
+    }
   __syncthreads();
 }
 
 template <int M>
-__global__ void __launch_bounds__(128) k_fftcc_big(FftccParams P)
+__global__ void __launch_bounds__(kBigThreads) k_fftcc_big(FftccParams P)
 {
-  constexpr int N1 = big_n1(M), N2 = M / N1, S = M + 1, R = M / 2;
+  constexpr int N1 = big_n1(M), N2 = M / N1, S = M + 1, R = M / 2, kParts = kBigThreads / M;
+  static_assert(kParts >= 1, "one thread per line at least");
   extern __shared__ float2 zbig[];
   __shared__ float s_red[32];
   __shared__ int s_idx[32];
@@ -3334,67 +3342,77 @@ __global__ void __launch_bounds__(128) k_fftcc_big(FftccParams P)
       int(px + u_init) < R || int(px + u_init) >= w - R || int(py + v_init) < R ||
       int(py + v_init) >= h - R)
     return;
+  const int c = (int)threadIdx.x % M, part = (int)threadIdx.x / M;
+  const bool on = part < kParts;
+  // window columns: thread column c, rows part, part + kParts, ...
   float rsum = 0.f, tsum = 0.f;
-  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
+  if (on)
   {
-    const int r = t / M, c = t % M;
     const float fxr = __fsub_rn(__fadd_rn(px, (float)c), (float)R);
-    const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
-    const float rv = P.ref[(size_t)(int)fyr * w + (int)fxr];
-    const float tv = P.tar[(size_t)(int)__fadd_rn(fyr, v_init) * w + (int)__fadd_rn(fxr, u_init)];
-    zbig[r * S + c] = make_float2(rv, tv);
-    rsum += rv;
-    tsum += tv;
+    const int xr = (int)fxr, xt = (int)__fadd_rn(fxr, u_init);
+    for (int r = part; r < M; r += kParts)
+    {
+      const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
+      const float rv = P.ref[(size_t)(int)fyr * w + xr];
+      const float tv = P.tar[(size_t)(int)__fadd_rn(fyr, v_init) * w + xt];
+      zbig[r * S + c] = make_float2(rv, tv);
+      rsum += rv;
+      tsum += tv;
+    }
   }
   rsum = block_sum(rsum, s_red);
   tsum = block_sum(tsum, s_red);
   const float rmean = rsum / (float)(M * M), tmean = tsum / (float)(M * M);
   float rn = 0.f, tn = 0.f;
-  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
-  {
-    const int r = t / M, c = t % M;
-    float2 v = zbig[r * S + c];
-    v.x -= rmean;
-    v.y -= tmean;
-    rn += v.x * v.x;
-    tn += v.y * v.y;
-    zbig[r * S + c] = v;
-  }
+  if (on)
+    for (int r = part; r < M; r += kParts)
+    {
+      float2 v = zbig[r * S + c];
+      v.x -= rmean;
+      v.y -= tmean;
+      rn += v.x * v.x;
+      tn += v.y * v.y;
+      zbig[r * S + c] = v;
+    }
   rn = block_sum(rn, s_red);
   tn = block_sum(tn, s_red);
   __syncthreads();
-  big_forward<M, true>(zbig);    // rows
-  big_forward<M, false>(zbig);   // columns: Z[kr][kc] at (pos kr, pos kc)
+  big_forward<M, true>(zbig, c, part, on);    // rows (thread = row c)
+  big_forward<M, false>(zbig, c, part, on);   // columns (thread = column c): Z[kr][kc] at (pos kr, pos kc)
   // cross-power, conjugated for the inverse (conj(FFT(conj(.))) keeps the real part):
   // X(k) = conj(R(k)) T(k) with R, T recovered from Z[k] and Z[-k]; X(-k) = conj(X(k)).
-  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
+  if (on)
   {
-    const int pr = t / M, pc = t % M;
-    const int kr = pr / N2 + N1 * (pr % N2), kc = pc / N2 + N1 * (pc % N2);
-    const int mr = (M - kr) % M, mc = (M - kc) % M;
-    const int qr = N2 * (mr % N1) + mr / N1, qc = N2 * (mc % N1) + mc / N1;
-    const int p = pr * M + pc, q = qr * M + qc;
-    if (p > q) continue;
-    const float2 A = zbig[pr * S + pc];
-    const float2 zm = zbig[qr * S + qc];
-    const float2 B = make_float2(zm.x, -zm.y);
-    const float2 Rk = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y + B.y));
-    const float2 D = csub(A, B);
-    const float2 Tk = make_float2(0.5f * D.y, -0.5f * D.x);
-    const float2 X = make_float2(Rk.x * Tk.x + Rk.y * Tk.y, Rk.x * Tk.y - Rk.y * Tk.x);
-    zbig[pr * S + pc] = make_float2(X.x, -X.y);
-    if (q != p) zbig[qr * S + qc] = X;
+    const int pc = c, kc = pc / N2 + N1 * (pc % N2), mc = (M - kc) % M, qc = N2 * (mc % N1) + mc / N1;
+    for (int pr = part; pr < M; pr += kParts)
+    {
+      const int kr = pr / N2 + N1 * (pr % N2);
+      const int mr = (M - kr) % M;
+      const int qr = N2 * (mr % N1) + mr / N1;
+      const int p = pr * M + pc, q = qr * M + qc;
+      if (p > q) continue;
+      const float2 A = zbig[pr * S + pc];
+      const float2 zm = zbig[qr * S + qc];
+      const float2 B = make_float2(zm.x, -zm.y);
+      const float2 Rk = make_float2(0.5f * (A.x + B.x), 0.5f * (A.y + B.y));
+      const float2 D = csub(A, B);
+      const float2 Tk = make_float2(0.5f * D.y, -0.5f * D.x);
+      const float2 X = make_float2(Rk.x * Tk.x + Rk.y * Tk.y, Rk.x * Tk.y - Rk.y * Tk.x);
+      zbig[pr * S + pc] = make_float2(X.x, -X.y);
+      if (q != p) zbig[qr * S + qc] = X;
+    }
   }
   __syncthreads();
-  big_from_permuted<M, false>(zbig);   // columns back to natural rows
-  big_from_permuted<M, true>(zbig);    // rows back to natural columns: correlation in .x
+  big_from_permuted<M, false>(zbig, c, part, on);   // columns back to natural rows
+  big_from_permuted<M, true>(zbig, c, part, on);    // rows back to natural columns: correlation in .x
   float best = -2.f;
   int best_idx = 0;
-  for (int t = threadIdx.x; t < M * M; t += blockDim.x)
-  {
-    const float v = zbig[(t / M) * S + t % M].x;
-    if (v > best) { best = v; best_idx = t; }
-  }
+  if (on)
+    for (int r = part; r < M; r += kParts)   // increasing index: strict '>' keeps the lowest
+    {
+      const float v = zbig[r * S + c].x;
+      if (v > best) { best = v; best_idx = r * M + c; }
+    }
   block_argmax(best, best_idx, s_red, s_idx);
   if (threadIdx.x == 0)
   {

@@ -117,7 +117,7 @@ def test_fftcc_matches_oracle_r15(dic, oracle_mod, affine_pair):
     assert np.median(np.abs(q["u"] - ut)) < 1.0 and np.median(np.abs(q["v"] - vt)) < 1.0
 
 
-@pytest.mark.parametrize("radius", [3, 4, 5, 6, 7, 9, 10, 11, 12, 13, 14, 16, 17, 20, 25, 30, 31, 32])
+@pytest.mark.parametrize("radius", [3, 4, 5, 6, 7, 9, 10, 11, 12, 13, 14, 16, 17, 18, 20, 21, 22, 24, 25, 26, 27, 28, 30, 31, 32])
 def test_fftcc_matches_oracle_radii(dic, oracle_mod, radius):
     """Register FFT (2r <= 32) and the large-radius path against the oracle, shifted speckle.
     Every prime-factor split of k_fftcc2 is covered: 2r = 6, 10, 14, 18, 22, 26 (2 x odd),
