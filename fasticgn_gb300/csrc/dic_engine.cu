@@ -1144,7 +1144,7 @@ struct dic_engine
 #define DIC_BATCH_PX(W, M)                                                                                         \
   k_icgn_batch_px<W, M><<<grid, W * 32, smem, stream>>>(b.jobs, b.njobs, b.pois, b.poi_ref, b.begin, b.end, b.next,     \
                                                         cfg.conv_criterion, mi, b.iter_sum, win, wait_polls, wait_flag())
-      if (b_col_maps)
+      if (b_px_maps)
       {
         if (sh.warps == 2) DIC_BATCH_PX(2, 2);
         else if (sh.warps == 8) DIC_BATCH_PX(8, 2);
@@ -1166,7 +1166,7 @@ struct dic_engine
       px_attributes();
       const int pw = sh.poi_warps == 2 ? 2 : 1;
       const uint32_t win = (uint32_t)px_window_bytes(b.rmax, b.rmax);
-      const size_t smem = b_col_maps ? pair_px_smem(sh.warps, pw, win) : 0;
+      const size_t smem = b_px_maps ? pair_px_smem(sh.warps, pw, win) : 0;
       const int ctas = sh.ctas_per_sm > 0 ? sh.ctas_per_sm : occupancy_pair_px(true, pw, sh.warps, smem);
       const unsigned grid = (unsigned)(sms * ctas);
 #define DIC_BATCH_PAIR_PX(PW, W, M)                                                                                  \
@@ -1176,7 +1176,7 @@ struct dic_engine
 #define DIC_BATCH_PAIR_PX_W(PW)                                \
   do                                                           \
   {                                                            \
-    if (b_col_maps)                                            \
+    if (b_px_maps)                                            \
     {                                                          \
       if (sh.warps == 2) DIC_BATCH_PAIR_PX(PW, 2, 2);          \
       else if (sh.warps == 8) DIC_BATCH_PAIR_PX(PW, 8, 2);     \
@@ -1763,7 +1763,7 @@ struct dic_engine
   static constexpr bool kBatchPairByRadius = DIC_BATCH_PAIR_BY_RADIUS != 0;
   static constexpr int kMaxPairGroups = kPairMaxWidth / 2 - 15;   // radii 16 .. (width - 1) / 2
   DevBuf<CUtensorMap> bmaps;            // the jobs' target-plane tensor maps (pixel sampling)
-  bool b_col_maps = false;              // every pixel-sampled job has one (TMA windows), else warp copies / none
+  bool b_px_maps = false;              // every pixel-sampled job has one (TMA windows), else warp copies / none
   std::vector<CUtensorMap> b_maps_host; // their host copy (kept alive for the asynchronous upload)
   // pixel sampling covers the batch's column- and pair-walk jobs; the flat walk's sample the table
   bool job_table(int radius) const { return !pixel_radius(radius); }
@@ -1847,7 +1847,7 @@ struct dic_engine
     bmaps.ensure((size_t)nj);
     std::vector<TileMap> maps(nj);
     bool any_map = false;
-    b_col_maps = encode_tiled() != nullptr;
+    b_px_maps = encode_tiled() != nullptr;
     for (int k = 0; k < nj; ++k)
     {
       const dic_job& J = jobs[b_order[k]];
