@@ -2877,6 +2877,10 @@ __global__ void __launch_bounds__(128) k_fftcc(FftccParams P)
 // rule and outputs as k_fftcc (the results differ only in float rounding: columns are
 // transformed before rows, and without twiddles between coprime stages).
 // --------------------------------------------------------------------------------------
+#ifndef DIC_FFTCC_INT_ROWS
+#define DIC_FFTCC_INT_ROWS 1
+#endif
+constexpr bool kFftccIntRows = DIC_FFTCC_INT_ROWS != 0;
 template <int M>
 // (Register caps for 7 or 8 CTAs per SM spill: 0.93 against 0.67 ms at 2048^2.)
 __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
@@ -2922,16 +2926,32 @@ __global__ void __launch_bounds__(64) k_fftcc2(FftccParams P)
     {
       const float fxr = __fsub_rn(__fadd_rn(px, (float)lane), (float)R);
       const int xr = (int)fxr, xt = (int)__fadd_rn(fxr, ui);
-#pragma unroll
-      for (int r = 0; r < M; ++r)
+      if (kFftccIntRows && py == rintf(py) && vi == rintf(vi))
       {
-        const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
-        const int yr = (int)fyr, yt = (int)__fadd_rn(fyr, vi);
-        rv[r] = P.ref[(size_t)yr * w + xr];
-        tv[r] = P.tar[(size_t)yt * w + xt];
-        rsum += rv[r];
-        tsum += tv[r];
+        // whole-pixel row coordinate and seed (every grid queue): the CPU's float row
+        // coordinates py + r - R and + v are exact, so the rows are consecutive pointers
+        const float* rp = P.ref + (size_t)((int)py - R) * w + xr;
+        const float* tp = P.tar + (size_t)((int)py - R + (int)vi) * w + xt;
+#pragma unroll
+        for (int r = 0; r < M; ++r)
+        {
+          rv[r] = rp[(size_t)r * w];
+          tv[r] = tp[(size_t)r * w];
+          rsum += rv[r];
+          tsum += tv[r];
+        }
       }
+      else
+#pragma unroll
+        for (int r = 0; r < M; ++r)
+        {
+          const float fyr = __fsub_rn(__fadd_rn(py, (float)r), (float)R);
+          const int yr = (int)fyr, yt = (int)__fadd_rn(fyr, vi);
+          rv[r] = P.ref[(size_t)yr * w + xr];
+          tv[r] = P.tar[(size_t)yt * w + xt];
+          rsum += rv[r];
+          tsum += tv[r];
+        }
     }
     rsum = warp_sum(rsum);
     tsum = warp_sum(tsum);
