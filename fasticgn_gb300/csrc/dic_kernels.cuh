@@ -1180,12 +1180,6 @@ constexpr int kSrcTable = 0, kSrcCoefTile = 1, kSrcPixels = 2;
 #define DIC_ICGN_RESIDENT_WARPS 28
 #endif
 constexpr int kIcgnRowUnroll = DIC_ICGN_ROW_UNROLL;
-// Pixel walk: lattice iterations (integer translations) whose samples all lie in the window
-// read it without per-sample tests.
-#ifndef DIC_PX_LATTICE_FAST
-#define DIC_PX_LATTICE_FAST 1
-#endif
-constexpr bool kPxLatticeFast = DIC_PX_LATTICE_FAST != 0;
 
 // One POI (queue index i) on the calling warp; shared by the per-queue launch (k_icgn) and
 // the persistent multi-job launch (k_icgn_batch, which keeps one row in flight: its job
@@ -1235,13 +1229,9 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
     const bool lat = kSrc != kSrcCoefTile && (kSrc == kSrcPixels || P.lattice) && on_lattice(W, px, py);   // warp-uniform
     if constexpr (column_walk)
     {
-      bool fast = false, lat_fast = false;
+      bool fast = false;
       if constexpr (kSrc == kSrcPixels)
-      {
-        const bool covers = window_covers(W, px, py, rx, ry, xmax, ymax, T, lane);
-        fast = !lat && covers;
-        lat_fast = kPxLatticeFast && lat && covers;
-      }
+        fast = !lat && window_covers(W, px, py, rx, ry, xmax, ymax, T, lane);
       if (fast)
       {
         if constexpr (kSrc == kSrcPixels)
@@ -1262,35 +1252,6 @@ __device__ __forceinline__ void icgn_solve(const IcgnParams& P, int64_t i, int l
               const float gxp = px + fmaf(W[1], fly, ax);
               const float gyp = py + fmaf(W[4], fly, ay);
               const float t = sample_window(T, row, gxp, gyp);
-              const float tau = t - t0;
-              const float rc = cur.x - t0;
-              A0 += tau;
-              A1 = fmaf(tau, tau, A1);
-              A2 = fmaf(tau, rc, A2);
-              const float gt = __fmul_rn(cur.y, tau), ht = __fmul_rn(cur.z, tau);
-              B[0] = __fadd_rn(B[0], gt);
-              B[2] = fmaf(gt, fly, B[2]);
-              B[3] = __fadd_rn(B[3], ht);
-              B[5] = fmaf(ht, fly, B[5]);
-            }
-          }
-      }
-      else if (kSrc == kSrcPixels && lat_fast)
-      {
-        if constexpr (kSrc == kSrcPixels)
-          if (col_active)
-          {
-            // on the pixel lattice (an integer translation) with every sample in range and in
-            // the window: sample (r, lane) is the pixel (cx + u + lane - rx, cy + v + r - ry)
-            const int ix = (int)(px + fmaf(W[0], flx_col, W[2])), iy = (int)(py + fmaf(W[3], flx_col, W[5])) - ry;
-            const float* wp = px_smem + T.s + (iy - T.oy) * T.bx + (ix - T.ox);
-            const float4* rp = ref_col;
-            for (int r = 0; r < 2 * ry + 1; ++r)
-            {
-              const float4 cur = __ldg(rp);
-              rp += w;
-              const float fly = (float)(r - ry);
-              const float t = wp[r * T.bx];
               const float tau = t - t0;
               const float rc = cur.x - t0;
               A0 += tau;
