@@ -388,11 +388,13 @@ struct ColSumsShared
 };
 
 // Entry test, mean (written to rec->t0), and the warp-reduced sums of one POI.  Returns false
-// (after writing valid = 0) when the reference subset leaves the image.
-// (The mean pass re-reads the subset from ref_pack, whose lines the second pass then finds in
-// L1: reading the grey levels from the float plane instead, 4 B per sample, took 0.64 against
-// 0.60 ms on the 2048x2048 pair.  Forming the means from precomputed horizontal window sums
-// saved 0.01 ms and cost 0.03 ms to build the sums: dropped.)
+// (after writing valid = 0) when the reference subset leaves the image.  `shared`: the POI's
+// column sums as k_poi_prepare32 staged them (column and pair walks); otherwise col_sums forms
+// them here, and a second pass over the subset forms the sums that depend on the mean.
+// (Before the column sums were shared, the mean pass read ref_pack, whose lines the second
+// pass then found in L1; reading the grey levels from the float plane instead, 4 B per
+// sample, took 0.64 against 0.60 ms on the 2048x2048 pair.  Forming the means from
+// precomputed horizontal window sums saved 0.01 ms and cost 0.03 ms to build them: dropped.)
 __device__ __forceinline__ bool poi_sums(const float4* __restrict__ ref_pack, int w, int h, float px, float py,
                                          int rx, int ry, int lane, PoiRef* __restrict__ rec, PoiSums& out_sums,
                                          ColSumsShared shared = ColSumsShared{nullptr, 0})
