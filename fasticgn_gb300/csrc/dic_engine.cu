@@ -1748,7 +1748,6 @@ struct dic_engine
   std::vector<int64_t> b_first;
   int64_t b_total = 0, b_col_end = 0, b_pair_end = 0;
   int b_col_rmax = 0;                   // largest subset radius among the column-walk jobs
-  int b_pair_rmax = 0;                  // and among the pair-walk jobs
   // The pair-walk jobs' drains: one per subset radius under pixel sampling (queue range and
   // radius), one for all of them under table sampling.
   struct PairGroup
@@ -1794,7 +1793,6 @@ struct dic_engine
     b_col_end = 0;
     b_pair_end = 0;
     b_col_rmax = 0;
-    b_pair_rmax = 0;
     b_pair_groups.clear();
     for (int k = 0; k < nj; ++k)
     {
@@ -1806,7 +1804,6 @@ struct dic_engine
       if (r == 0) b_col_rmax = std::max(b_col_rmax, J.subset_radius);
       if (r == 1)
       {
-        b_pair_rmax = std::max(b_pair_rmax, J.subset_radius);
         if (b_pair_groups.empty() || (px_pairs && b_pair_groups.back().rmax != J.subset_radius))
           b_pair_groups.push_back(PairGroup{b_first[k], b_total, J.subset_radius});
         b_pair_groups.back().end = b_total;
