@@ -245,12 +245,14 @@ void dic_host_free(void* ptr);
 
 /* Uneven batch: several image pairs of different sizes, each with its own subset radius
  * (square, 1..32) and POI queue, solved together (FFTCC seed + IC-GN).  No single call of
- * the reference does this; the CLI loops over pairs.  Per pair the prep and FFTCC launches
- * run back to back on the engine stream; all POIs of all pairs then go through one
- * persistent IC-GN launch per code path (subsets up to 32 columns wide, and wider) whose
- * warps take POIs from a shared atomic counter, so pairs with many POIs or slow-converging
- * POIs do not leave SMs idle.  Results are written back into each job's queue.  The
- * engine's conv_criterion and max_iteration apply to all jobs. */
+ * the reference does this; the CLI loops over pairs.  The pairs' prep and FFTCC chains run
+ * side by side on four streams of the engine; all POIs of all pairs then go through one
+ * persistent IC-GN launch per subset walk (column walk up to 32 columns, pair walk up to 64
+ * -- under pixel sampling one per subset radius, whose windows set the residency -- and the
+ * flat walk beyond) whose warps take POIs from a shared atomic counter, so pairs with many
+ * POIs or slow-converging POIs do not leave SMs idle.  Results are written back into each
+ * job's queue, bit-identical to the job solved alone.  The engine's conv_criterion and
+ * max_iteration apply to all jobs. */
 typedef struct dic_job
 {
   const void* ref;
